@@ -1,0 +1,201 @@
+/*
+ * mdgb.h: C ABI of the GB300 (sm_103a) MD step engine (libmdgb.so).
+ *
+ * Drop-in for the step loop of vakuras/moleculardynamics' cpumd
+ * (cpu/cpumd/Host.cpp:114-195): neighbour-list build, Lennard-Jones and
+ * bond-order forces, Gear predictor-corrector, energy/virial reduction.
+ *
+ * Two layers, both plain C (pointers and sizes only):
+ *
+ *  1. Engine API (md_*): a context that owns the state on the device and runs
+ *     whole steps there.  Host arrays use the reference's layouts: positions
+ *     real4 = (x, y, z, type), vectors real3, real = double
+ *     (common/Global.h:58-72).  Every call returns an md_status; nothing
+ *     exits the process (the reference exits on any error, Global.h:116-117).
+ *     One context per host thread; a context is not re-entrant.
+ *
+ *  2. Reference-signature API (mdgb_*): the functions of cpu/common/Device.h,
+ *     common/NeighborList.h and common/DebugCalculations.h with the same
+ *     arguments and meaning, operating on host arrays (each call copies in,
+ *     computes on the GPU, copies out).  A C++ file that forwards the
+ *     reference names to these is all cpumd needs.  They
+ *     return void like the reference; mdgb_last_status() reports failures.
+ *
+ * Units are the reference's: angstrom, femtosecond, g/mol, energy 1e7 J/mol.
+ */
+#ifndef MDGB_H
+#define MDGB_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum md_status {
+  MD_OK = 0,
+  MD_BAD_CONFIG = 1,     /* invalid configuration value */
+  MD_LIST_OVERFLOW = 2,  /* caller buffer too small for the neighbour list */
+  MD_NONFINITE = 3,      /* NaN/inf in positions, velocities or forces */
+  MD_TIMEOUT = 4,        /* a bounded device wait gave up */
+  MD_CUDA_ERROR = 5,     /* CUDA runtime error (see md_last_error) */
+  MD_BAD_ARGUMENT = 6,   /* NULL pointer, bad index or size */
+  MD_NO_DEVICE = 7,      /* no usable CUDA device */
+  MD_OUT_OF_MEMORY = 8,  /* device allocation failed */
+  MD_CELL_OVERFLOW = 9   /* cell grid out of range (atoms far outside the box) */
+} md_status;
+
+enum { MD_PREC_FP64 = 0, MD_PREC_MIXED = 1 };
+enum { MD_SPECIES_NEON = 0, MD_SPECIES_ARGON = 1 };
+
+/* Configuration.  The first block is the subset of the reference's
+ * `configuration` (common/Global.h:75-104, keys in common/Loader.h:25-51)
+ * that the step uses; the second block are extensions whose zero value is
+ * the reference's behaviour. */
+typedef struct md_config {
+  int n_lj;                /* "Lennard Jones Particles" */
+  int n_mb;                /* "Many Body Particles": atoms [0, n_mb) are many-body */
+  float dt;                /* "DT" */
+  int timesteps;           /* "Timesteps" */
+  float lj_rs, lj_rcut;    /* "LennardJonesRS", "LennardJonesRCUT" */
+  float mb_rs, mb_rcut;    /* "ManyBodyRS", "ManyBodyRCUT" */
+  int use_lj, use_mb;      /* "UseLennardJones", "UseManyBody" */
+  int output_timesteps;    /* "OutputTimesteps" (<= 0: no records) */
+  float energy_loss;       /* "EnergyLoss"; its square root is used (Host.cpp:73) */
+  /* extensions */
+  int periodic;            /* 1: periodic cubic box of edge `box`, no walls */
+  double box;
+  int precision;           /* MD_PREC_FP64 (plain) or MD_PREC_MIXED (FP32 pairs) */
+  int species;             /* MD_SPECIES_NEON (reference table) or _ARGON (NG = argon) */
+  int device;              /* CUDA device ordinal */
+  int reference_energy;    /* 1: records use the reference's all-pairs energy
+                              (DebugCalculations.cpp:129-270, O(N^2)/O(N^3)) */
+} md_config;
+
+/* One output record.  The first 11 doubles are the reference's `results`
+ * (common/Results.h:15-28) in the same order; eu is the potential energy
+ * (list energy, or the all-pairs one with reference_energy). */
+typedef struct md_thermo {
+  double time, temperature, e, ek, eu;
+  double com_x, com_y, com_z;
+  double momentum_x, momentum_y, momentum_z;
+  double e_lj;             /* LJ energy over the force's pairs (within rcut) */
+  double e_lj_shifted;     /* same, each pair shifted by its value at rcut */
+  double e_mb;             /* bond-order energy over the force's pairs */
+  double virial;           /* W = 1/2 sum r_ij.f_ij (LJ) + sum r_i.F_i (bond order) */
+  double step;
+} md_thermo;
+
+typedef struct md_stats {
+  long long steps;
+  long long list_builds;
+  long long list_trips;    /* steps that walked full rows (skin exceeded) */
+  long long wall_hits;     /* steps with a wall reflection (Device.cpp:86-118) */
+  long long missing_xi;    /* pass-2 reads of an xi pass 1 did not make */
+  long long launches;      /* kernels launched by this context */
+  int lj_max_row;          /* longest compact LJ row at the last build */
+  int lj_nlargest;         /* longest full LJ candidate row (nlargestsize) */
+  int mb_nlargest;
+  int lj_cells, mb_cells;
+} md_stats;
+
+typedef struct md_ctx md_ctx;
+
+/* ---- engine API ---- */
+md_status md_create(const md_config* cfg, md_ctx** out);
+void md_destroy(md_ctx* ctx);
+const char* md_status_string(md_status s);
+const char* md_last_error(const md_ctx* ctx);
+
+/* Positions (n x real4) and velocities (n x real3), n = n_lj + n_mb.
+ * Replaces readInput into posArray/velocityArray (common/Loader.cpp:125). */
+md_status md_upload(md_ctx* ctx, const double* pos4, const double* vel3);
+/* Full Gear state in/out (checkpoint): acc, b, c as n x real3; any may be NULL. */
+md_status md_upload_state(md_ctx* ctx, const double* pos4, const double* vel3,
+                          const double* acc3, const double* b3, const double* c3);
+md_status md_download(md_ctx* ctx, double* pos4, double* vel3);
+md_status md_download_state(md_ctx* ctx, double* acc3, double* b3, double* c3,
+                            double* force3);
+
+/* Start of one vxcm pass of hostMain (cpu/cpumd/Host.cpp:86-138): zero the
+ * Gear derivatives, clamp into the box (or wrap, periodic), add vxcm to vx,
+ * build the lists, initial forces and a = F/m, record t = 0. */
+md_status md_begin(md_ctx* ctx, float vxcm);
+/* nsteps iterations of the step loop (cpu/cpumd/Host.cpp:141-195). */
+md_status md_step(md_ctx* ctx, int nsteps);
+
+/* Output records collected at t = 0 and every output step. */
+int md_record_count(const md_ctx* ctx);
+md_status md_get_records(md_ctx* ctx, md_thermo* out, int max_records);
+/* performOutput (common/DebugCalculations.cpp:14-41) on the current state. */
+md_status md_thermo_now(md_ctx* ctx, md_thermo* out);
+/* calculatePotentional (common/DebugCalculations.cpp:129-270) on the device. */
+md_status md_reference_potential(md_ctx* ctx, double* vib_lj, double* vib_mb);
+/* Forces at the current positions as Host.cpp:132-135 computes them, plus
+ * [E_lj, E_lj_shifted, W_lj, E_mb, W_mb] (energy5 may be NULL). */
+md_status md_compute_forces(md_ctx* ctx, double* force3, double* energy5);
+/* Neighbour list in the reference layout (NeighborList.cpp:119-177): which =
+ * 0 (LJ) or 1 (many-body); rows[i * nlistsize + k], -1 padded; images
+ * (optional, same shape, periodic image (ix+1)*9+(iy+1)*3+(iz+1), 13 = none).
+ * capacity is the number of ints rows can hold. */
+md_status md_neighbor_list(md_ctx* ctx, int which, int* rows, signed char* images,
+                           long long capacity, int* nlistsize, int* nlargest);
+md_status md_get_stats(const md_ctx* ctx, md_stats* out);
+/* Per-kernel device timing with CUDA events on the engine's stream.
+ * kernel: 0 = LJ force, 1 = bond order, 2 = predict, 3 = correct, 4 = list build. */
+md_status md_set_timing(md_ctx* ctx, int on);
+md_status md_kernel_time(const md_ctx* ctx, int kernel, double* total_ms, long long* launches);
+/* Wait for all work of the context; returns the first deferred error. */
+md_status md_synchronize(md_ctx* ctx);
+
+/* ---- reference-signature API ---- */
+typedef struct mdgb_list_settings { /* common/NeighborList.h:19-28 listSettings */
+  float maxnlmove, maxnlmovesq, rcut, rs, rcutsq;
+  int nlistsize, nlargestsize;
+} mdgb_list_settings;
+
+/* cpu/common/Device.h:19 predict */
+void mdgb_predict(double* r4, double* v3, double* a3, double* b3, double* c3, double dt,
+                  int nop);
+/* cpu/common/Device.h:20 correct; *flag set to 1 on a wall hit */
+void mdgb_correct(double* r4, double* v3, const double* f3, double* a3, double* b3,
+                  double* c3, double dt, int nop, double npos, int* flag, float energy_loss);
+/* cpu/common/Device.h:21 lennardJonesForces (list in the reference layout) */
+void mdgb_lennard_jones_forces(const double* pos4, double* f3, int n, int nlargestsize,
+                               int nlistsize, const int* list, double rcutsq);
+/* cpu/common/Device.h:22 manyBodyForces */
+void mdgb_many_body_forces(const double* pos4, double* f3, int n, int nlargestsize,
+                           int nlistsize, const int* list, double rcutsq, int ljexist);
+/* cpu/common/Device.h:23 calculateAccelerations */
+void mdgb_calculate_accelerations(const double* pos4, double* a3, const double* f3, int n);
+/* common/NeighborList.h:30 buildNeighborList; returns a malloc'd list that
+ * the caller frees with mdgb_free (the reference returns new int[]) */
+int* mdgb_build_neighbor_list(const double* pos4, mdgb_list_settings* s, double box,
+                              int buckets, int n);
+void mdgb_free(void* p);
+/* common/DebugCalculations.h:18 PerformCalculations */
+void mdgb_perform_calculations(const double* pos4, const double* vel3, int n, double* com_x,
+                               double* com_y, double* com_z, double* kinetic,
+                               double* mom_x, double* mom_y, double* mom_z, double* temp);
+/* common/DebugCalculations.h:20 calculatePotentional */
+void mdgb_calculate_potential(const double* pos4, double* vib_lj, double* vib_mb, int n);
+/* species table of the mdgb_* layer: MD_SPECIES_NEON (default, the reference's) */
+void mdgb_set_species(int species);
+/* status of the last mdgb_* call on this thread (MD_OK or the failure) */
+int mdgb_last_status(void);
+
+/* ---- configuration and results files (common/ConfigParser, Loader, Results) ---- */
+/* Reads a reference config file (key=value, '//' comments, keys case-
+ * insensitive; the 25 mandatory keys of common/Loader.cpp:49-82) into cfg;
+ * strings (Input, Output, Filename, AnimationData) into 4 slots of 512 bytes;
+ * extra[0..5] = Temperature, VXCMFROM, VXCMTO, VXCMSTEP, CUDA Blocks, AnimationTimesteps.
+ * Optional extension keys: Periodic, Box, Precision, Species, Device. */
+md_status md_read_config(const char* path, md_config* cfg, char* strings, double* extra,
+                         char* err, int err_len);
+/* Writes the .dat/.txt result pair of common/Results.cpp:120-229. */
+md_status md_write_results(const char* filename, const md_config* cfg, float vxcm,
+                           float elapsed_ms, const md_thermo* records, int nrec,
+                           const double* pos4);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,800 @@
+// The step engine behind the md_* C ABI (include/mdgb.h).
+//
+// One context owns one system on one GPU: the Gear state in the reference's
+// AoS layouts (real4 positions, real3 vectors, real = double), the LJ and
+// bond-order neighbour lists, and the scratch of the force kernels.  md_step
+// replays the body of cpu/cpumd/Host.cpp:141-195 on the device:
+//   list rebuild when scheduled (readyList + buildList, Host.cpp:143-152)
+//   predict -> LJ forces -> bond-order forces -> correct (Host.cpp:155-166)
+//   wall hit: forces and a = F/m again (Host.cpp:168-178)
+//   record at output steps (performOutput, Host.cpp:181-185)
+// Host synchronisation happens only at list builds (the schedule needs the
+// largest speed, Host.cpp:289), after a correct in the reference's wall mode
+// (the wall flag, as the reference's CUDA host also reads it every step) and
+// at the end of md_step.  The periodic mode has no walls and no per-step
+// host round trip.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/mdgb.h"
+#include "md_forces.h"
+#include "md_integrate.h"
+#include "md_neighbor.cuh"
+
+using namespace mdgb;
+
+namespace {
+
+Species species_table(int which) {
+  // common/Constants.h:36-43,55-57; the argon table replaces the NG slot
+  Species s;
+  s.sig[0] = 3.015f;  // NG-N
+  s.sig[1] = 2.835f;  // NG-O
+  s.eps[0] = 0.328e-4f;
+  s.eps[1] = 0.447e-4f;
+  s.mass[0] = 14.00674f;
+  s.mass[1] = 15.9994f;
+  if (which == MD_SPECIES_ARGON) {
+    s.sig[2] = 3.405f;
+    s.eps[2] = 9.960172e-5f;
+    s.mass[2] = 39.948f;
+  } else {
+    s.sig[2] = 2.72f;
+    s.eps[2] = 0.391e-4f;
+    s.mass[2] = 20.1797f;
+  }
+  return s;
+}
+
+// cpu/cpumd/Host.cpp:57-61
+void list_settings(float rs, float rcut, float& maxnlmove, float& rcutsq) {
+  maxnlmove = (rs - rcut) * 0.5f;
+  rcutsq = (float)pow((double)rcut, 2);
+}
+
+// cpu/cpumd/Host.cpp:289-290; vmax = 0 or an out-of-range quotient is "never"
+int next_build(float maxnlmove, double vmax, double dt, int t) {
+  double q = ((double)maxnlmove / vmax) / fabs(dt);
+  if (!(q < 2147483647.0) || q != q) return 2147483647;
+  long long nb = (long long)(int)q + t;
+  return nb > 2147483647LL ? 2147483647 : (int)nb;
+}
+
+constexpr int kKernels = 5;  // timing ids of md_kernel_time
+
+__global__ void k_begin(md_double4* pos, double* vel, int n, double half_box, int clamp,
+                        double vxcm) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  md_double4 p = pos[i];
+  if (clamp) {
+    // cpu/cpumd/Host.cpp:94-104
+    if (fabs(p.x) > half_box) p.x = __dmul_rn(half_box, __ddiv_rn(p.x, fabs(p.x)));
+    if (fabs(p.y) > half_box) p.y = __dmul_rn(half_box, __ddiv_rn(p.y, fabs(p.y)));
+    if (fabs(p.z) > half_box) p.z = __dmul_rn(half_box, __ddiv_rn(p.z, fabs(p.z)));
+    pos[i] = p;
+  }
+  vel[3 * i] = __dadd_rn(vel[3 * i], vxcm);
+}
+
+}  // namespace
+
+struct md_ctx {
+  md_config cfg{};
+  int n = 0;
+  std::string err;
+  cudaStream_t st = nullptr;
+  Species sp{};
+  GearCoef gear{};
+  double box_size = 0;  // cpu/cpumd/Host.cpp:31, the wall half-width of correct
+  float energy_loss = 1.f;
+  float lj_maxnlmove = 0, lj_rcutsq = 0, mb_maxnlmove = 0, mb_rcutsq = 0;
+  // state
+  md_double4* pos = nullptr;
+  double *vel = nullptr, *acc = nullptr, *b = nullptr, *c = nullptr, *f3 = nullptr,
+         *f3_tmp = nullptr;
+  float4* posf = nullptr;
+  NeighborList lj, mb;
+  // bond-order scratch
+  uint32_t* mb_sl = nullptr;
+  int* mb_slen = nullptr;
+  void *xsi = nullptr, *xsj = nullptr, *va = nullptr;
+  long long mb_elems = 0;
+  // flags and reductions
+  int* status = nullptr;
+  int* wall_flag = nullptr;
+  int* missing = nullptr;
+  Scratch sc;
+  double* epart = nullptr;
+  long long epart_cap = 0;
+  double* dsc = nullptr;  // device scalars: th8[0..7] elj[8..10] emb[11..13] ref[14..15]
+  double* rec = nullptr;
+  int rec_cap = 0, nrec = 0;
+  // schedule
+  int t = 0, lj_next = 0, mb_next = 0, printout = 0;
+  bool begun = false;
+  md_stats stats{};
+  // timing
+  bool timing = false;
+  std::vector<cudaEvent_t> ev_pool;
+  std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> pending;
+  double kt_ms[kKernels] = {0, 0, 0, 0, 0};
+  long long kt_n[kKernels] = {0, 0, 0, 0, 0};
+
+  bool mixed() const { return cfg.precision == MD_PREC_MIXED; }
+  bool walls() const { return !cfg.periodic; }
+};
+
+namespace {
+
+md_status fail(md_ctx* c, md_status s, const std::string& msg) {
+  c->err = msg;
+  return s;
+}
+
+md_status cuda_fail(md_ctx* c, cudaError_t e, const char* where) {
+  c->err = std::string(where) + ": " + cudaGetErrorString(e);
+  return e == cudaErrorMemoryAllocation ? MD_OUT_OF_MEMORY : MD_CUDA_ERROR;
+}
+
+#define CK(expr, where)                                  \
+  do {                                                   \
+    cudaError_t e_ = (expr);                             \
+    if (e_ != cudaSuccess) return cuda_fail(c, e_, where); \
+  } while (0)
+
+cudaEvent_t take_event(md_ctx* c) {
+  if (!c->ev_pool.empty()) {
+    cudaEvent_t e = c->ev_pool.back();
+    c->ev_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e;
+  cudaEventCreate(&e);
+  return e;
+}
+
+struct Timed {
+  md_ctx* c;
+  int id;
+  cudaEvent_t a = nullptr, b = nullptr;
+  Timed(md_ctx* c_, int id_) : c(c_), id(id_) {
+    if (c->timing) {
+      a = take_event(c);
+      b = take_event(c);
+      cudaEventRecord(a, c->st);
+    }
+  }
+  ~Timed() {
+    if (c->timing) {
+      cudaEventRecord(b, c->st);
+      c->pending.push_back({id, {a, b}});
+    }
+  }
+};
+
+void resolve_timing(md_ctx* c) {
+  for (auto& p : c->pending) {
+    float ms = 0;
+    if (cudaEventElapsedTime(&ms, p.second.first, p.second.second) == cudaSuccess) {
+      c->kt_ms[p.first] += ms;
+      c->kt_n[p.first]++;
+    }
+    c->ev_pool.push_back(p.second.first);
+    c->ev_pool.push_back(p.second.second);
+  }
+  c->pending.clear();
+}
+
+md_status ensure_epart(md_ctx* c, long long need) {
+  if (need <= c->epart_cap) return MD_OK;
+  if (c->epart) cudaFree(c->epart);
+  c->epart = nullptr;
+  CK(cudaMalloc(&c->epart, sizeof(double) * (size_t)need), "epart");
+  c->epart_cap = need;
+  return MD_OK;
+}
+
+md_status ensure_mb_scratch(md_ctx* c) {
+  long long need = (long long)c->mb.cap * (c->cfg.n_mb > 0 ? c->cfg.n_mb : 1);
+  if (need <= c->mb_elems && c->mb_sl) return MD_OK;
+  for (void** p : {(void**)&c->mb_sl, &c->xsi, &c->xsj, &c->va})
+    if (*p) {
+      cudaFree(*p);
+      *p = nullptr;
+    }
+  size_t es = sizeof(double);
+  CK(cudaMalloc(&c->mb_sl, sizeof(uint32_t) * (size_t)need), "mb short list");
+  CK(cudaMalloc(&c->xsi, es * (size_t)need), "mb xi");
+  CK(cudaMalloc(&c->xsj, es * (size_t)need), "mb xi");
+  CK(cudaMalloc(&c->va, es * (size_t)need), "mb va");
+  c->mb_elems = need;
+  return MD_OK;
+}
+
+ForceArgs lj_args(md_ctx* c, double* f3, double* epart) {
+  ForceArgs a;
+  a.pos = c->pos;
+  a.posf = c->posf;
+  a.f3 = f3;
+  a.n = c->n;
+  a.list = c->lj.list;
+  a.len = c->lj.len;
+  a.walker = make_walker(c->lj);
+  a.status = c->status;
+  a.rcutsq = (double)c->lj_rcutsq;
+  a.sp = c->sp;
+  a.epart = epart;
+  return a;
+}
+
+MbArgs mb_args(md_ctx* c, double* f3, int ljexist) {
+  MbArgs a;
+  a.pos = c->pos;
+  a.posf = c->posf;
+  a.f3 = f3;
+  a.n = c->cfg.n_mb;
+  a.list = c->mb.list;
+  a.len = c->mb.len;
+  a.grid = c->mb.grid;
+  a.cell3 = c->mb.cell3;
+  a.ref_rows = nullptr;
+  a.ref_nls = 0;
+  a.ref_nlargest = 0;
+  a.rcutsq = (double)c->mb_rcutsq;
+  a.ljexist = ljexist;
+  a.sl = c->mb_sl;
+  a.slen = c->mb_slen;
+  a.xsi = c->xsi;
+  a.xsj = c->xsj;
+  a.va = c->va;
+  a.missing = c->missing;
+  a.epart1 = nullptr;
+  a.epart2 = nullptr;
+  return a;
+}
+
+// Host.cpp:132-135 / :157-161: LJ over all atoms (overwrites), bond order
+// over the first n_mb atoms (accumulates when LJ is on).
+md_status forces(md_ctx* c, double* f3) {
+  if (c->cfg.use_lj) {
+    Timed tm(c, 0);
+    launch_lj(lj_args(c, f3, nullptr), c->mixed(), false, c->st);
+    c->stats.launches++;
+  }
+  if (c->cfg.use_mb && c->cfg.n_mb > 0) {
+    Timed tm(c, 1);
+    launch_mb(mb_args(c, f3, c->cfg.use_lj), c->mixed(), false, c->st);
+    c->stats.launches += 3;
+  }
+  return MD_OK;
+}
+
+GearArgs gear_args(md_ctx* c) {
+  GearArgs g;
+  g.pos = c->pos;
+  g.vel = c->vel;
+  g.acc = c->acc;
+  g.b = c->b;
+  g.c = c->c;
+  g.f3 = c->f3;
+  g.n = c->n;
+  g.k = c->gear;
+  g.sp = c->sp;
+  g.posf = c->mixed() ? c->posf : nullptr;
+  const bool skin = c->cfg.use_lj && c->lj.compact && c->lj.pos_build;
+  g.pos_build = skin ? c->lj.pos_build : nullptr;
+  g.trip2 = skin ? (float)(c->lj.trip_dist * c->lj.trip_dist) : 0.f;
+  if (skin && c->lj.trip_dist <= 0) g.trip2 = -1.f;  // skin too thin: always walk full rows
+  g.status = c->status;
+  g.npos = c->box_size;
+  g.energy_loss = c->energy_loss;
+  g.walls = c->walls();
+  g.wall_flag = c->wall_flag;
+  return g;
+}
+
+md_status check_status(md_ctx* c) {
+  int s = 0;
+  CK(cudaMemcpyAsync(&s, c->status, sizeof(int), cudaMemcpyDeviceToHost, c->st), "status");
+  int miss = 0;
+  CK(cudaMemcpyAsync(&miss, c->missing, sizeof(int), cudaMemcpyDeviceToHost, c->st), "status");
+  CK(cudaStreamSynchronize(c->st), "step");
+  CK(cudaGetLastError(), "step");
+  c->stats.missing_xi = miss;
+  if (s & ST_NONFINITE) return fail(c, MD_NONFINITE, "non-finite position or velocity");
+  if (s & ST_CELL_OVERFLOW) return fail(c, MD_CELL_OVERFLOW, "cell grid out of range");
+  return MD_OK;
+}
+
+// readyList + buildList for the lists due at step t (Host.cpp:143-152)
+md_status rebuild(md_ctx* c, int t) {
+  Timed tm(c, 4);
+  unsigned long long um[2];
+  launch_ready(c->pos, c->vel, c->n, c->sc.umax, c->status, c->st);
+  CK(cudaMemcpyAsync(um, c->sc.umax, sizeof(um), cudaMemcpyDeviceToHost, c->st), "ready");
+  int s = 0;
+  CK(cudaMemcpyAsync(&s, c->status, sizeof(int), cudaMemcpyDeviceToHost, c->st), "ready");
+  CK(cudaStreamSynchronize(c->st), "ready");
+  c->stats.launches += 1;
+  if (s & ST_NONFINITE) return fail(c, MD_NONFINITE, "non-finite position or velocity");
+  double vmax, maxabs;
+  memcpy(&vmax, &um[0], 8);
+  memcpy(&maxabs, &um[1], 8);
+  const double box_list = maxabs * 2;
+  const bool both = c->cfg.periodic != 0;
+  const double dt = (double)c->cfg.dt;
+  bool did_lj = false;
+  if (c->cfg.use_lj && (c->lj_next == t || both)) {
+    if (s & ST_LIST_TRIP) c->stats.list_trips++;
+    CK(cudaMemsetAsync(c->status, 0, sizeof(int), c->st), "status");
+    Grid g = c->cfg.periodic ? make_grid_periodic(c->cfg.box, c->cfg.lj_rs)
+                             : make_grid_reference(box_list, c->cfg.lj_rs);
+    std::string e;
+    int r = list_build(c->lj, c->pos, c->n, g, 1, c->cfg.lj_rs, sqrt((double)c->lj_rcutsq),
+                       c->sc, c->status, c->st, e);
+    c->stats.launches += 9;
+    if (r != 0) {
+      if (r == -1) return fail(c, e.find("non-finite") != std::string::npos ? MD_NONFINITE : MD_CELL_OVERFLOW, e);
+      return cuda_fail(c, (cudaError_t)r, "LJ list build");
+    }
+    c->lj_next = next_build(c->lj_maxnlmove, vmax, dt, t);
+    c->stats.list_builds++;
+    c->stats.lj_max_row = c->lj.max_len;
+    c->stats.lj_nlargest = c->lj.nlargest;
+    c->stats.lj_cells = c->lj.grid.cells;
+    did_lj = true;
+  }
+  if (c->cfg.use_mb && c->cfg.n_mb > 0 && (c->mb_next == t || both)) {
+    Grid g = c->cfg.periodic ? make_grid_periodic(c->cfg.box, c->cfg.mb_rs)
+                             : make_grid_reference(box_list, c->cfg.mb_rs);
+    std::string e;
+    if (!did_lj) {
+      // keep a set skin bit of the LJ list, clear the rest
+      CK(cudaMemsetAsync(c->status, 0, sizeof(int), c->st), "status");
+      if (s & ST_LIST_TRIP) {
+        int v = ST_LIST_TRIP;
+        CK(cudaMemcpyAsync(c->status, &v, sizeof(int), cudaMemcpyHostToDevice, c->st), "status");
+        CK(cudaStreamSynchronize(c->st), "status");
+      }
+    }
+    int r = list_build(c->mb, c->pos, c->cfg.n_mb, g, 0, 0.f, sqrt((double)c->mb_rcutsq), c->sc,
+                       c->status, c->st, e);
+    c->stats.launches += 9;
+    if (r != 0) {
+      if (r == -1) return fail(c, e.find("non-finite") != std::string::npos ? MD_NONFINITE : MD_CELL_OVERFLOW, e);
+      return cuda_fail(c, (cudaError_t)r, "many-body list build");
+    }
+    if (!c->mb_slen) CK(cudaMalloc(&c->mb_slen, sizeof(int) * (size_t)c->cfg.n_mb), "mb slen");
+    md_status ms = ensure_mb_scratch(c);
+    if (ms != MD_OK) return ms;
+    c->mb_next = next_build(c->mb_maxnlmove, vmax, dt, t);
+    c->stats.list_builds++;
+    c->stats.mb_nlargest = c->mb.nlargest;
+    c->stats.mb_cells = c->mb.grid.cells;
+  }
+  if (both) {
+    // periodic box: both lists are rebuilt together (positions wrap at a build)
+    int m = 2147483647;
+    if (c->cfg.use_lj && c->lj_next < m) m = c->lj_next;
+    if (c->cfg.use_mb && c->mb_next < m) m = c->mb_next;
+    if (c->cfg.use_lj) c->lj_next = m;
+    if (c->cfg.use_mb) c->mb_next = m;
+  }
+  if (c->mixed()) {
+    launch_posf(c->pos, c->posf, c->n, c->st);
+    c->stats.launches++;
+  }
+  return MD_OK;
+}
+
+// thermo + energies of the current state into a 16-double record at rec16
+md_status make_record(md_ctx* c, int t, double* rec16) {
+  double* th8 = c->dsc;
+  double* elj = c->dsc + 8;
+  double* emb = c->dsc + 11;
+  double* ref = c->dsc + 14;
+  launch_thermo(c->pos, c->vel, c->n, c->sp, c->sc.dpart, th8, c->st);
+  c->stats.launches += 5;
+  CK(cudaMemsetAsync(elj, 0, sizeof(double) * 8, c->st), "record");
+  if (c->cfg.use_lj) {
+    int B = lj_blocks(c->n);
+    md_status s = ensure_epart(c, 3LL * B);
+    if (s != MD_OK) return s;
+    launch_lj(lj_args(c, c->f3_tmp, c->epart), c->mixed(), true, c->st);
+    launch_sum_partials(c->epart, B, 3, elj, c->st);
+    c->stats.launches += 2;
+  }
+  if (c->cfg.use_mb && c->cfg.n_mb > 0) {
+    int B = mb_blocks(c->cfg.n_mb);
+    md_status s = ensure_epart(c, 3LL * B);
+    if (s != MD_OK) return s;
+    MbArgs a = mb_args(c, c->f3_tmp, 0);
+    a.epart1 = c->epart;
+    a.epart2 = c->epart + 2LL * B;
+    launch_mb(a, c->mixed(), true, c->st);
+    launch_sum_partials(a.epart1, B, 2, emb, c->st);
+    launch_sum_partials(a.epart2, B, 1, emb + 2, c->st);
+    c->stats.launches += 5;
+  }
+  if (c->cfg.reference_energy) {
+    md_status s = ensure_epart(c, 2LL * c->n);
+    if (s != MD_OK) return s;
+    launch_ref_potential(c->pos, c->n, c->sp, c->epart, ref, c->st);
+    c->stats.launches += 2;
+  }
+  launch_record(th8, elj, emb, ref, c->cfg.reference_energy, (double)t * (double)c->cfg.dt,
+                (double)t, rec16, c->st);
+  c->stats.launches++;
+  return MD_OK;
+}
+
+md_status push_record(md_ctx* c, int t) {
+  if (c->nrec >= c->rec_cap) {
+    int cap = c->rec_cap ? 2 * c->rec_cap : 64;
+    double* nr = nullptr;
+    CK(cudaMalloc(&nr, sizeof(double) * 16 * (size_t)cap), "records");
+    if (c->rec) {
+      CK(cudaMemcpyAsync(nr, c->rec, sizeof(double) * 16 * (size_t)c->nrec,
+                         cudaMemcpyDeviceToDevice, c->st), "records");
+      CK(cudaStreamSynchronize(c->st), "records");
+      cudaFree(c->rec);
+    }
+    c->rec = nr;
+    c->rec_cap = cap;
+  }
+  md_status s = make_record(c, t, c->rec + 16 * (size_t)c->nrec);
+  if (s == MD_OK) c->nrec++;
+  return s;
+}
+
+md_status step_once(md_ctx* c) {
+  const int t = c->t;
+  if ((c->cfg.use_lj && c->lj_next == t) || (c->cfg.use_mb && c->mb_next == t)) {
+    md_status s = rebuild(c, t);
+    if (s != MD_OK) return s;
+  }
+  GearArgs g = gear_args(c);
+  {
+    Timed tm(c, 2);
+    launch_predict(g, c->st);
+    c->stats.launches++;
+  }
+  forces(c, c->f3);
+  if (c->walls()) CK(cudaMemsetAsync(c->wall_flag, 0, sizeof(int), c->st), "wall flag");
+  {
+    Timed tm(c, 3);
+    launch_correct(g, c->st);
+    c->stats.launches++;
+  }
+  if (c->walls()) {
+    int flag = 0;
+    CK(cudaMemcpyAsync(&flag, c->wall_flag, sizeof(int), cudaMemcpyDeviceToHost, c->st), "wall");
+    CK(cudaStreamSynchronize(c->st), "wall");
+    if (flag) {
+      c->stats.wall_hits++;
+      forces(c, c->f3);
+      launch_accel(c->pos, c->acc, c->f3, c->n, c->sp, c->st);
+      c->stats.launches++;
+    }
+  }
+  if (c->cfg.output_timesteps > 0 && c->printout == t) {
+    md_status s = push_record(c, t);
+    if (s != MD_OK) return s;
+    c->printout += c->cfg.output_timesteps;
+  }
+  c->t++;
+  c->stats.steps++;
+  return MD_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* md_status_string(md_status s) {
+  switch (s) {
+    case MD_OK: return "ok";
+    case MD_BAD_CONFIG: return "bad configuration";
+    case MD_LIST_OVERFLOW: return "neighbour list does not fit the buffer";
+    case MD_NONFINITE: return "non-finite value";
+    case MD_TIMEOUT: return "device wait timed out";
+    case MD_CUDA_ERROR: return "CUDA error";
+    case MD_BAD_ARGUMENT: return "bad argument";
+    case MD_NO_DEVICE: return "no CUDA device";
+    case MD_OUT_OF_MEMORY: return "out of device memory";
+    case MD_CELL_OVERFLOW: return "cell grid out of range";
+  }
+  return "unknown status";
+}
+
+const char* md_last_error(const md_ctx* c) { return c ? c->err.c_str() : "no context"; }
+
+md_status md_create(const md_config* cfg, md_ctx** out) {
+  if (!cfg || !out) return MD_BAD_ARGUMENT;
+  *out = nullptr;
+  const long long n = (long long)cfg->n_lj + cfg->n_mb;
+  if (cfg->n_lj < 0 || cfg->n_mb < 0 || n < 1 || n > kMaxAtoms) return MD_BAD_CONFIG;
+  if (!(cfg->dt == cfg->dt) || cfg->dt == 0.f) return MD_BAD_CONFIG;
+  if (cfg->use_lj && !(cfg->lj_rcut > 0.f && cfg->lj_rs > cfg->lj_rcut)) return MD_BAD_CONFIG;
+  if (cfg->use_mb && !(cfg->mb_rcut > 0.f && cfg->mb_rs >= cfg->mb_rcut &&
+                       cfg->mb_rcut < MD_CUTOFF_RIJ))
+    return MD_BAD_CONFIG;
+  if (cfg->precision != MD_PREC_FP64 && cfg->precision != MD_PREC_MIXED) return MD_BAD_CONFIG;
+  if (cfg->species != MD_SPECIES_NEON && cfg->species != MD_SPECIES_ARGON) return MD_BAD_CONFIG;
+  if (cfg->periodic) {
+    double rsmax = 0;
+    if (cfg->use_lj) rsmax = fmax(rsmax, cfg->lj_rs);
+    if (cfg->use_mb) rsmax = fmax(rsmax, cfg->mb_rs);
+    if (!(cfg->box > 2.0 * rsmax)) return MD_BAD_CONFIG;
+    // the bond-order third-body pass needs distinct stencil cells
+    if (cfg->use_mb && floor(cfg->box / (double)cfg->mb_rs) < 3) return MD_BAD_CONFIG;
+  }
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= cfg->device || cfg->device < 0)
+    return MD_NO_DEVICE;
+  md_ctx* c = new md_ctx();
+  c->cfg = *cfg;
+  c->n = (int)n;
+  c->sp = species_table(cfg->species);
+  c->gear = gear_coef((double)cfg->dt);
+  c->box_size = pow((double)n, 1.0 / 3.0) * 52.8;  // Host.cpp:31
+  c->energy_loss = sqrtf(cfg->energy_loss);        // Host.cpp:73
+  if (cfg->use_lj) list_settings(cfg->lj_rs, cfg->lj_rcut, c->lj_maxnlmove, c->lj_rcutsq);
+  if (cfg->use_mb) list_settings(cfg->mb_rs, cfg->mb_rcut, c->mb_maxnlmove, c->mb_rcutsq);
+  auto bail = [&](cudaError_t e, const char* w) {
+    md_status s = cuda_fail(c, e, w);
+    md_destroy(c);
+    return s;
+  };
+  cudaError_t e;
+  if ((e = cudaSetDevice(cfg->device)) != cudaSuccess) return bail(e, "cudaSetDevice");
+  if ((e = cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking)) != cudaSuccess)
+    return bail(e, "stream");
+  const size_t N = (size_t)n;
+  if ((e = cudaMalloc(&c->pos, sizeof(md_double4) * N)) != cudaSuccess) return bail(e, "pos");
+  double** vecs[] = {&c->vel, &c->acc, &c->b, &c->c, &c->f3, &c->f3_tmp};
+  for (double** p : vecs)
+    if ((e = cudaMalloc(p, sizeof(double) * 3 * N)) != cudaSuccess) return bail(e, "state");
+  if ((e = cudaMalloc(&c->posf, sizeof(float4) * N)) != cudaSuccess) return bail(e, "posf");
+  if ((e = cudaMalloc(&c->status, sizeof(int) * 4)) != cudaSuccess) return bail(e, "flags");
+  c->wall_flag = c->status + 1;
+  c->missing = c->status + 2;
+  if ((e = cudaMemset(c->status, 0, sizeof(int) * 4)) != cudaSuccess) return bail(e, "flags");
+  if ((e = cudaMalloc(&c->sc.dpart, sizeof(double) * (8 * 1024 + 64))) != cudaSuccess)
+    return bail(e, "scratch");
+  if ((e = cudaMalloc(&c->sc.umax, sizeof(unsigned long long) * 4)) != cudaSuccess)
+    return bail(e, "scratch");
+  if ((e = cudaMalloc(&c->sc.counts, sizeof(int) * 4)) != cudaSuccess) return bail(e, "scratch");
+  if ((e = cudaMalloc(&c->dsc, sizeof(double) * 32)) != cudaSuccess) return bail(e, "scratch");
+  cudaMemsetAsync(c->dsc, 0, sizeof(double) * 32, c->st);
+  *out = c;
+  return MD_OK;
+}
+
+void md_destroy(md_ctx* c) {
+  if (!c) return;
+  if (c->st) cudaStreamSynchronize(c->st);
+  list_free(c->lj);
+  list_free(c->mb);
+  void* ptrs[] = {c->pos, c->vel, c->acc, c->b, c->c, c->f3, c->f3_tmp, c->posf, c->mb_sl,
+                  c->mb_slen, c->xsi, c->xsj, c->va, c->status, c->epart, c->dsc, c->rec,
+                  c->sc.dpart, c->sc.umax, c->sc.counts, c->sc.block_sums};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  for (auto& p : c->pending) {
+    cudaEventDestroy(p.second.first);
+    cudaEventDestroy(p.second.second);
+  }
+  for (auto e : c->ev_pool) cudaEventDestroy(e);
+  if (c->st) cudaStreamDestroy(c->st);
+  delete c;
+}
+
+md_status md_upload(md_ctx* c, const double* pos4, const double* vel3) {
+  return md_upload_state(c, pos4, vel3, nullptr, nullptr, nullptr);
+}
+
+md_status md_upload_state(md_ctx* c, const double* pos4, const double* vel3, const double* a3,
+                          const double* b3, const double* c3) {
+  if (!c) return MD_BAD_ARGUMENT;
+  const size_t N = (size_t)c->n;
+  if (pos4)
+    CK(cudaMemcpyAsync(c->pos, pos4, sizeof(double) * 4 * N, cudaMemcpyHostToDevice, c->st), "upload");
+  if (vel3)
+    CK(cudaMemcpyAsync(c->vel, vel3, sizeof(double) * 3 * N, cudaMemcpyHostToDevice, c->st), "upload");
+  if (a3) CK(cudaMemcpyAsync(c->acc, a3, sizeof(double) * 3 * N, cudaMemcpyHostToDevice, c->st), "upload");
+  if (b3) CK(cudaMemcpyAsync(c->b, b3, sizeof(double) * 3 * N, cudaMemcpyHostToDevice, c->st), "upload");
+  if (c3) CK(cudaMemcpyAsync(c->c, c3, sizeof(double) * 3 * N, cudaMemcpyHostToDevice, c->st), "upload");
+  if (c->mixed() && pos4) launch_posf(c->pos, c->posf, c->n, c->st);
+  CK(cudaStreamSynchronize(c->st), "upload");
+  return MD_OK;
+}
+
+md_status md_download(md_ctx* c, double* pos4, double* vel3) {
+  if (!c) return MD_BAD_ARGUMENT;
+  const size_t N = (size_t)c->n;
+  if (pos4)
+    CK(cudaMemcpyAsync(pos4, c->pos, sizeof(double) * 4 * N, cudaMemcpyDeviceToHost, c->st), "download");
+  if (vel3)
+    CK(cudaMemcpyAsync(vel3, c->vel, sizeof(double) * 3 * N, cudaMemcpyDeviceToHost, c->st), "download");
+  CK(cudaStreamSynchronize(c->st), "download");
+  return MD_OK;
+}
+
+md_status md_download_state(md_ctx* c, double* a3, double* b3, double* c3, double* f3) {
+  if (!c) return MD_BAD_ARGUMENT;
+  const size_t B = sizeof(double) * 3 * (size_t)c->n;
+  if (a3) CK(cudaMemcpyAsync(a3, c->acc, B, cudaMemcpyDeviceToHost, c->st), "download");
+  if (b3) CK(cudaMemcpyAsync(b3, c->b, B, cudaMemcpyDeviceToHost, c->st), "download");
+  if (c3) CK(cudaMemcpyAsync(c3, c->c, B, cudaMemcpyDeviceToHost, c->st), "download");
+  if (f3) CK(cudaMemcpyAsync(f3, c->f3, B, cudaMemcpyDeviceToHost, c->st), "download");
+  CK(cudaStreamSynchronize(c->st), "download");
+  return MD_OK;
+}
+
+md_status md_begin(md_ctx* c, float vxcm) {
+  if (!c) return MD_BAD_ARGUMENT;
+  const size_t B = sizeof(double) * 3 * (size_t)c->n;
+  CK(cudaMemsetAsync(c->acc, 0, B, c->st), "begin");
+  CK(cudaMemsetAsync(c->b, 0, B, c->st), "begin");
+  CK(cudaMemsetAsync(c->c, 0, B, c->st), "begin");
+  CK(cudaMemsetAsync(c->status, 0, sizeof(int) * 4, c->st), "begin");
+  k_begin<<<(c->n + 255) / 256, 256, 0, c->st>>>(c->pos, c->vel, c->n, c->box_size / 2,
+                                                  c->walls(), (double)vxcm);
+  c->stats = md_stats{};
+  c->stats.launches = 1;
+  c->t = 0;
+  c->lj_next = c->mb_next = 0;
+  c->printout = c->cfg.output_timesteps;
+  c->nrec = 0;
+  c->begun = true;
+  md_status s = rebuild(c, 0);
+  if (s != MD_OK) return s;
+  if (c->cfg.output_timesteps > 0) {
+    s = push_record(c, 0);
+    if (s != MD_OK) return s;
+  }
+  forces(c, c->f3);
+  launch_accel(c->pos, c->acc, c->f3, c->n, c->sp, c->st);
+  c->stats.launches++;
+  return check_status(c);
+}
+
+md_status md_step(md_ctx* c, int nsteps) {
+  if (!c || nsteps < 0) return MD_BAD_ARGUMENT;
+  if (!c->begun) return fail(c, MD_BAD_ARGUMENT, "md_begin has not been called");
+  for (int s = 0; s < nsteps; s++) {
+    md_status r = step_once(c);
+    if (r != MD_OK) return r;
+  }
+  md_status r = check_status(c);
+  if (c->timing) resolve_timing(c);
+  return r;
+}
+
+int md_record_count(const md_ctx* c) { return c ? c->nrec : 0; }
+
+md_status md_get_records(md_ctx* c, md_thermo* out, int max_records) {
+  if (!c || (!out && max_records > 0)) return MD_BAD_ARGUMENT;
+  int n = c->nrec < max_records ? c->nrec : max_records;
+  static_assert(sizeof(md_thermo) == 16 * sizeof(double), "md_thermo layout");
+  if (n > 0)
+    CK(cudaMemcpyAsync(out, c->rec, sizeof(md_thermo) * (size_t)n, cudaMemcpyDeviceToHost, c->st), "records");
+  CK(cudaStreamSynchronize(c->st), "records");
+  return MD_OK;
+}
+
+md_status md_thermo_now(md_ctx* c, md_thermo* out) {
+  if (!c || !out) return MD_BAD_ARGUMENT;
+  if (!c->begun) return fail(c, MD_BAD_ARGUMENT, "md_begin has not been called");
+  double* tmp = c->dsc + 16;
+  md_status s = make_record(c, c->t, tmp);
+  if (s != MD_OK) return s;
+  CK(cudaMemcpyAsync(out, tmp, sizeof(md_thermo), cudaMemcpyDeviceToHost, c->st), "thermo");
+  CK(cudaStreamSynchronize(c->st), "thermo");
+  return MD_OK;
+}
+
+md_status md_reference_potential(md_ctx* c, double* vib_lj, double* vib_mb) {
+  if (!c) return MD_BAD_ARGUMENT;
+  md_status s = ensure_epart(c, 2LL * c->n);
+  if (s != MD_OK) return s;
+  launch_ref_potential(c->pos, c->n, c->sp, c->epart, c->dsc + 14, c->st);
+  double r[2];
+  CK(cudaMemcpyAsync(r, c->dsc + 14, sizeof(r), cudaMemcpyDeviceToHost, c->st), "potential");
+  CK(cudaStreamSynchronize(c->st), "potential");
+  if (vib_lj) *vib_lj = r[0];
+  if (vib_mb) *vib_mb = r[1];
+  return MD_OK;
+}
+
+md_status md_compute_forces(md_ctx* c, double* f3, double* energy5) {
+  if (!c) return MD_BAD_ARGUMENT;
+  if (!c->begun) return fail(c, MD_BAD_ARGUMENT, "md_begin has not been called");
+  double e[16];
+  md_status s = make_record(c, c->t, c->dsc + 16);
+  if (s != MD_OK) return s;
+  CK(cudaMemcpyAsync(e, c->dsc, sizeof(double) * 16, cudaMemcpyDeviceToHost, c->st), "forces");
+  // forces of the same evaluation as Host.cpp:132-135 (f3_tmp holds LJ then
+  // bond order written by the energy kernels without accumulation; redo it)
+  forces(c, c->f3_tmp);
+  if (f3)
+    CK(cudaMemcpyAsync(f3, c->f3_tmp, sizeof(double) * 3 * (size_t)c->n, cudaMemcpyDeviceToHost, c->st), "forces");
+  CK(cudaStreamSynchronize(c->st), "forces");
+  if (energy5) {
+    energy5[0] = e[8];
+    energy5[1] = e[9];
+    energy5[2] = e[10];
+    energy5[3] = e[11];
+    energy5[4] = e[12] + e[13];
+  }
+  return check_status(c);
+}
+
+md_status md_neighbor_list(md_ctx* c, int which, int* rows, signed char* images,
+                           long long capacity, int* nlistsize, int* nlargest) {
+  if (!c || (which != 0 && which != 1)) return MD_BAD_ARGUMENT;
+  NeighborList& nl = which == 0 ? c->lj : c->mb;
+  if (!nl.cell3) return fail(c, MD_BAD_ARGUMENT, "list not built (call md_begin)");
+  if (nlistsize) *nlistsize = nl.nlistsize;
+  if (nlargest) *nlargest = nl.nlargest;
+  const long long need = (long long)nl.nlistsize * nl.n;
+  if (!rows) return MD_OK;
+  if (capacity < need) return fail(c, MD_LIST_OVERFLOW, "rows buffer too small");
+  if (need == 0) return MD_OK;
+  int* d_rows = nullptr;
+  signed char* d_img = nullptr;
+  CK(cudaMalloc(&d_rows, sizeof(int) * (size_t)need), "list rows");
+  if (images && cudaMalloc(&d_img, (size_t)need) != cudaSuccess) {
+    cudaFree(d_rows);
+    return fail(c, MD_OUT_OF_MEMORY, "list images");
+  }
+  list_reference_rows(nl, c->pos, d_rows, d_img, c->st);
+  cudaError_t e = cudaMemcpyAsync(rows, d_rows, sizeof(int) * (size_t)need, cudaMemcpyDeviceToHost, c->st);
+  if (e == cudaSuccess && images)
+    e = cudaMemcpyAsync(images, d_img, (size_t)need, cudaMemcpyDeviceToHost, c->st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
+  cudaFree(d_rows);
+  if (d_img) cudaFree(d_img);
+  if (e != cudaSuccess) return cuda_fail(c, e, "list rows");
+  return MD_OK;
+}
+
+md_status md_get_stats(const md_ctx* c, md_stats* out) {
+  if (!c || !out) return MD_BAD_ARGUMENT;
+  *out = c->stats;
+  return MD_OK;
+}
+
+md_status md_set_timing(md_ctx* c, int on) {
+  if (!c) return MD_BAD_ARGUMENT;
+  cudaStreamSynchronize(c->st);
+  resolve_timing(c);
+  c->timing = on != 0;
+  for (int k = 0; k < kKernels; k++) {
+    c->kt_ms[k] = 0;
+    c->kt_n[k] = 0;
+  }
+  return MD_OK;
+}
+
+md_status md_kernel_time(const md_ctx* cc, int kernel, double* total_ms, long long* launches) {
+  md_ctx* c = const_cast<md_ctx*>(cc);
+  if (!c || kernel < 0 || kernel >= kKernels) return MD_BAD_ARGUMENT;
+  cudaStreamSynchronize(c->st);
+  resolve_timing(c);
+  if (total_ms) *total_ms = c->kt_ms[kernel];
+  if (launches) *launches = c->kt_n[kernel];
+  return MD_OK;
+}
+
+md_status md_synchronize(md_ctx* c) {
+  if (!c) return MD_BAD_ARGUMENT;
+  return check_status(c);
+}
+
+}  // extern "C"

@@ -1,0 +1,633 @@
+// Force kernels: Lennard-Jones (cpu/common/LennardJones.h) and the bond-order
+// many-body term (cpu/common/BondOrderFuncs.h).
+//
+// LJ, FP64 ("plain"): one thread per atom walks its compact row in the
+// reference's candidate order and evaluates every in-range pair with the
+// reference's roundings (no FMA contraction), so that forces are bit-identical
+// to the reference on the same positions and list.
+// LJ, FP32 (precision form): same rows; pair arithmetic in FP32 from the FP32
+// position copy; pairs within 1e-5 of the cutoff are re-tested in FP64 so the
+// pair set equals the FP64 one; per-atom sums are FP32 chunks of 16 pairs
+// folded into a compensated (Kahan) FP32 pair (hi, lo), stored as FP64.
+// Bond order: a short list per atom (candidates within rcut now), then
+//   pass 1: one warp per atom i, one lane per pair (i, j); the lane loops over
+//           the third bodies m of i's short list (BondOrderFuncs.h:12-143,
+//           242-278) and stores xi_ij, xi_ji and Va_ij per (i, slot);
+//   pass 2: one warp per atom k, one lane per i of k's short list; the lane
+//           loops over j of i's short list that lie in k's candidate row and
+//           adds k's third-body force (BondOrderFuncs.h:148-237, 339-393).
+// Lane sums are combined with warp shuffles.
+#include <cmath>
+
+#include "md_forces.h"
+#include "md_neighbor.cuh"
+#include "md_potential.cuh"
+
+namespace mdgb {
+
+namespace {
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Sum of NV doubles over the block, written to out[NV * blockIdx.x + k].
+template <int NV>
+__device__ __forceinline__ void block_partial(double (&v)[NV], double* out) {
+  __shared__ double sm[NV][32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int k = 0; k < NV; k++) {
+    double x = warp_sum(v[k]);
+    if (lane == 0) sm[k][warp] = x;
+  }
+  __syncthreads();
+  if (warp == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; k++) {
+      double x = lane < nw ? sm[k][lane] : 0.0;
+      x = warp_sum(x);
+      if (lane == 0) out[NV * blockIdx.x + k] = x;
+    }
+  }
+}
+
+// ------------------------------------------------------------------ LJ FP64
+template <bool ENERGY>
+__global__ void __launch_bounds__(128)
+    k_lj_fp64(const md_double4* __restrict__ pos, double* __restrict__ f3, int n,
+              const uint32_t* __restrict__ list, const int* __restrict__ len, RowWalker w,
+              const int* __restrict__ status, double rcutsq, Species sp,
+              double* __restrict__ epart) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double ev[3] = {0.0, 0.0, 0.0};
+  if (i < n) {
+    const md_double4 pi = pos[i];
+    const int ti = (int)pi.w;
+    const double box = w.g.box;
+    double fx = 0.0, fy = 0.0, fz = 0.0;
+    auto visit = [&](int j, int ix, int iy, int iz, bool img) {
+      const md_double4 pj = pos[j];
+      double xj = pj.x, yj = pj.y, zj = pj.z;
+      if (img) {
+        xj = xadd(xj, (double)ix * box);
+        yj = xadd(yj, (double)iy * box);
+        zj = xadd(zj, (double)iz * box);
+      }
+      const double ijx = xsub(pi.x, xj), ijy = xsub(pi.y, yj), ijz = xsub(pi.z, zj);
+      const double r2 = norm2_exact(ijx, ijy, ijz);
+      if (r2 >= rcutsq) return;
+      const int tj = (int)pj.w;
+      if (tj == SP_NG || ti == SP_NG) {
+        const int sel = lj_select(ti, tj);
+        const double sig = sp.sig[sel], eps = sp.eps[sel];
+        const double fij = lj_pair_exact(fx, fy, fz, __dsqrt_rn(r2), ijx, ijy, ijz, sig, eps);
+        if (ENERGY) {
+          // common/DebugCalculations.cpp:199-201 per ordered pair, restricted
+          // to the force's pairs; shifted by its value at the cutoff
+          double sr2 = xdiv(xmul(sig, sig), r2);
+          double sr6 = xmul(xmul(sr2, sr2), sr2);
+          double e = xmul(xmul(2.0, eps), xsub(xmul(sr6, sr6), sr6));
+          double src2 = xdiv(xmul(sig, sig), rcutsq);
+          double src6 = xmul(xmul(src2, src2), src2);
+          ev[0] += e;
+          ev[1] += e - xmul(xmul(2.0, eps), xsub(xmul(src6, src6), src6));
+          ev[2] += 0.5 * (ijx * (ijx * fij) + ijy * (ijy * fij) + ijz * (ijz * fij));
+        }
+      }
+    };
+    if (!(*status & ST_LIST_TRIP)) {
+      const int L = len[i];
+      for (int k = 0; k < L; k++) {
+        const uint32_t e = list[(size_t)k * n + i];
+        visit(entry_index(e), entry_img(e, 0), entry_img(e, 1), entry_img(e, 2), (e >> 26) != 0);
+      }
+    } else {
+      walk_row(w, pos, i, [&](int m, int ix, int iy, int iz) {
+        visit(m, ix, iy, iz, w.g.periodic && (ix | iy | iz));
+      });
+    }
+    f3[3 * i] = fx;
+    f3[3 * i + 1] = fy;
+    f3[3 * i + 2] = fz;
+  }
+  if (ENERGY) block_partial<3>(ev, epart);
+}
+
+// ------------------------------------------------------------------ LJ FP32
+__device__ __forceinline__ void kahan(float& hi, float& lo, float x) {
+  float y = x - lo;
+  float t = hi + y;
+  lo = (t - hi) - y;
+  hi = t;
+}
+
+template <bool ENERGY>
+__global__ void __launch_bounds__(128)
+    k_lj_fp32(const float4* __restrict__ posf, const md_double4* __restrict__ pos,
+              double* __restrict__ f3, int n, const uint32_t* __restrict__ list,
+              const int* __restrict__ len, RowWalker w, const int* __restrict__ status,
+              double rcutsq, Species sp, double* __restrict__ epart) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double ev[3] = {0.0, 0.0, 0.0};
+  if (i < n) {
+    const float4 pi = posf[i];
+    const int ti = __float_as_int(pi.w);
+    const float rc2 = (float)rcutsq;
+    const float band = 1e-5f * rc2;
+    const float Lf = w.g.box_f, Llo = w.g.box_lo;
+    float hx = 0.f, hy = 0.f, hz = 0.f, lx = 0.f, ly = 0.f, lz = 0.f;
+    float cx = 0.f, cy = 0.f, cz = 0.f;
+    int inchunk = 0;
+    auto visit = [&](int j, int ix, int iy, int iz, bool img) {
+      const float4 pj = posf[j];
+      float dx, dy, dz;
+      if (!img) {
+        dx = pi.x - pj.x;
+        dy = pi.y - pj.y;
+        dz = pi.z - pj.z;
+      } else {
+        dx = (pi.x - fmaf((float)ix, Lf, pj.x)) - (float)ix * Llo;
+        dy = (pi.y - fmaf((float)iy, Lf, pj.y)) - (float)iy * Llo;
+        dz = (pi.z - fmaf((float)iz, Lf, pj.z)) - (float)iz * Llo;
+      }
+      const float r2 = dx * dx + dy * dy + dz * dz;
+      if (r2 >= rc2 + band) return;
+      if (r2 > rc2 - band) {
+        // borderline: decide inclusion exactly as the FP64 path does
+        const md_double4 a = pos[i], b = pos[j];
+        double xj = b.x, yj = b.y, zj = b.z;
+        if (img) {
+          xj = xadd(xj, (double)ix * w.g.box);
+          yj = xadd(yj, (double)iy * w.g.box);
+          zj = xadd(zj, (double)iz * w.g.box);
+        }
+        if (norm2_exact(xsub(a.x, xj), xsub(a.y, yj), xsub(a.z, zj)) >= rcutsq) return;
+      }
+      const int tj = __float_as_int(pj.w);
+      if (tj != SP_NG && ti != SP_NG) return;
+      const int sel = lj_select(ti, tj);
+      const float sig = sp.sig[sel], eps = sp.eps[sel];
+      const float inv = 1.0f / r2;
+      const float sr2 = sig * sig * inv;
+      const float sr6 = sr2 * sr2 * sr2;
+      const float fij = (24.0f * eps) * inv * sr6 * (2.0f * sr6 - 1.0f);
+      cx = fmaf(dx, fij, cx);
+      cy = fmaf(dy, fij, cy);
+      cz = fmaf(dz, fij, cz);
+      if (ENERGY) {
+        const float src2 = sig * sig / rc2;
+        const float src6 = src2 * src2 * src2;
+        const float e = 2.0f * eps * (sr6 * sr6 - sr6);
+        ev[0] += (double)e;
+        ev[1] += (double)e - (double)(2.0f * eps * (src6 * src6 - src6));
+        ev[2] += 0.5 * (double)(r2 * fij);
+      }
+      if (++inchunk == 16) {
+        kahan(hx, lx, cx);
+        kahan(hy, ly, cy);
+        kahan(hz, lz, cz);
+        cx = cy = cz = 0.f;
+        inchunk = 0;
+      }
+    };
+    if (!(*status & ST_LIST_TRIP)) {
+      const int L = len[i];
+      for (int k = 0; k < L; k++) {
+        const uint32_t e = list[(size_t)k * n + i];
+        visit(entry_index(e), entry_img(e, 0), entry_img(e, 1), entry_img(e, 2), (e >> 26) != 0);
+      }
+    } else {
+      walk_row(w, pos, i, [&](int m, int ix, int iy, int iz) {
+        visit(m, ix, iy, iz, w.g.periodic && (ix | iy | iz));
+      });
+    }
+    kahan(hx, lx, cx);
+    kahan(hy, ly, cy);
+    kahan(hz, lz, cz);
+    f3[3 * i] = (double)hx - (double)lx;
+    f3[3 * i + 1] = (double)hy - (double)ly;
+    f3[3 * i + 2] = (double)hz - (double)lz;
+  }
+  if (ENERGY) block_partial<3>(ev, epart);
+}
+
+// --------------------------------------------------------------- bond order
+template <typename T>
+struct PosT;
+template <>
+struct PosT<double> {
+  static __device__ __forceinline__ void load(const md_double4* pos, const float4*, int j,
+                                              double& x, double& y, double& z, int& t) {
+    md_double4 p = pos[j];
+    x = p.x;
+    y = p.y;
+    z = p.z;
+    t = (int)p.w;
+  }
+  // image position: p + img * L, exactly as the oracle forms it
+  static __device__ __forceinline__ void image(double& x, double& y, double& z, uint32_t e,
+                                               const Grid& g) {
+    if (e >> 26) image3(x, y, z, entry_img(e, 0), entry_img(e, 1), entry_img(e, 2), g);
+  }
+  static __device__ __forceinline__ void image3(double& x, double& y, double& z, int ix,
+                                                int iy, int iz, const Grid& g) {
+    x = xadd(x, (double)ix * g.box);
+    y = xadd(y, (double)iy * g.box);
+    z = xadd(z, (double)iz * g.box);
+  }
+};
+template <>
+struct PosT<float> {
+  static __device__ __forceinline__ void load(const md_double4*, const float4* posf, int j,
+                                              float& x, float& y, float& z, int& t) {
+    float4 p = posf[j];
+    x = p.x;
+    y = p.y;
+    z = p.z;
+    t = __float_as_int(p.w);
+  }
+  static __device__ __forceinline__ void image(float& x, float& y, float& z, uint32_t e,
+                                               const Grid& g) {
+    if (e >> 26) image3(x, y, z, entry_img(e, 0), entry_img(e, 1), entry_img(e, 2), g);
+  }
+  static __device__ __forceinline__ void image3(float& x, float& y, float& z, int ix, int iy,
+                                                int iz, const Grid& g) {
+    x = fmaf((float)ix, g.box_f, x) + (float)ix * g.box_lo;
+    y = fmaf((float)iy, g.box_f, y) + (float)iy * g.box_lo;
+    z = fmaf((float)iz, g.box_f, z) + (float)iz * g.box_lo;
+  }
+};
+
+// short list: candidates within rcut at the current positions, row order
+template <typename T>
+__global__ void __launch_bounds__(128)
+    k_mb_short(const md_double4* __restrict__ pos, const float4* __restrict__ posf, int n,
+               const uint32_t* __restrict__ list, const int* __restrict__ len, Grid g,
+               double rcutsq, uint32_t* __restrict__ sl, int* __restrict__ slen) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  T xi, yi, zi;
+  int ti;
+  PosT<T>::load(pos, posf, i, xi, yi, zi, ti);
+  const T rc2 = (T)rcutsq;
+  const T band = (T)1e-5 * rc2;
+  int cnt = 0;
+  const int L = len[i];
+  for (int k = 0; k < L; k++) {
+    const uint32_t e = list[(size_t)k * n + i];
+    const int j = entry_index(e);
+    T xj, yj, zj;
+    int tj;
+    PosT<T>::load(pos, posf, j, xj, yj, zj, tj);
+    PosT<T>::image(xj, yj, zj, e, g);
+    T r2;
+    if (sizeof(T) == 8)
+      r2 = (T)norm2_exact((double)(xi - xj), (double)(yi - yj), (double)(zi - zj));
+    else
+      r2 = (xi - xj) * (xi - xj) + (yi - yj) * (yi - yj) + (zi - zj) * (zi - zj);
+    bool keep = r2 < rc2;
+    if (sizeof(T) == 4 && r2 > rc2 - band && r2 < rc2 + band) {
+      double a[3], b[3];
+      int t0;
+      PosT<double>::load(pos, posf, i, a[0], a[1], a[2], t0);
+      PosT<double>::load(pos, posf, j, b[0], b[1], b[2], t0);
+      PosT<double>::image(b[0], b[1], b[2], e, g);
+      keep = norm2_exact(xsub(a[0], b[0]), xsub(a[1], b[1]), xsub(a[2], b[2])) < rcutsq;
+    }
+    if (keep) sl[(size_t)(cnt++) * n + i] = e;
+  }
+  slen[i] = cnt;
+}
+
+template <typename T, bool ENERGY>
+__global__ void __launch_bounds__(128)
+    k_mb_pass1(const md_double4* __restrict__ pos, const float4* __restrict__ posf,
+               double* __restrict__ f3, int n, const uint32_t* __restrict__ sl,
+               const int* __restrict__ slen, Grid g, int ljexist, T* __restrict__ xsi_s,
+               T* __restrict__ xsj_s, T* __restrict__ va_s, double* __restrict__ epart) {
+  const int warps = blockDim.x >> 5;
+  const int i = blockIdx.x * warps + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  double ev[2] = {0.0, 0.0};
+  if (i < n) {
+    T xi, yi, zi;
+    int ti;
+    PosT<T>::load(pos, posf, i, xi, yi, zi, ti);
+    const int S = slen[i];
+    T fx = 0, fy = 0, fz = 0;
+    const T cut_rijsq = (T)MD_CUTOFF_RIJSQ;
+    const T nanv = (T)NAN;
+    for (int s = lane; s < S; s += 32) {
+      const uint32_t e = sl[(size_t)s * n + i];
+      const int j = entry_index(e);
+      T xj, yj, zj;
+      int tj;
+      PosT<T>::load(pos, posf, j, xj, yj, zj, tj);
+      PosT<T>::image(xj, yj, zj, e, g);
+      const size_t slot = (size_t)s * n + i;
+      const T ijx = xi - xj, ijy = yi - yj, ijz = zi - zj;
+      T rij = ijx * ijx + ijy * ijy + ijz * ijz;
+      if (tj == SP_NG || rij > cut_rijsq) {
+        xsi_s[slot] = nanv;
+        xsj_s[slot] = nanv;
+        va_s[slot] = 0;
+        continue;
+      }
+      rij = md_sqrt(rij);
+      // BondOrderFuncs.h:242-278 bondForces
+      T va = 0, dva = 0, vr = 0, dvr = 0, vdw, dvdw, bo = 0;
+      T dbx = 0, dby = 0, dbz = 0;
+      T fcut, dfcut;
+      cutoff<T>(rij / 10, fcut, dfcut);
+      T xs_i = nanv, xs_j = nanv;
+      if (fcut > 0) {
+        const T de = get_de<T>(ti, tj), re = get_re<T>(ti, tj), beta = get_beta<T>(ti, tj);
+        attractive<T>(va, dva, rij, de, beta, re);
+        repulsive<T>(vr, dvr, rij, de, beta, re);
+        // BondOrderFuncs.h:12-143 bondOrder1
+        const T drijx = ijx / rij, drijy = ijy / rij, drijz = ijz / rij;
+        const T E = md_exp((T)MD_LAMDA3 * (rij - re));
+        T xsi = 0, xsj = 0;
+        T dxsix = 0, dxsiy = 0, dxsiz = 0, dxsjx = 0, dxsjy = 0, dxsjz = 0;
+        for (int m = 0; m < S; m++) {
+          const uint32_t em = sl[(size_t)m * n + i];
+          const int mp = entry_index(em);
+          T xm, ym, zm;
+          int tm;
+          PosT<T>::load(pos, posf, mp, xm, ym, zm, tm);
+          if (tm == SP_NG || mp == j) continue;
+          PosT<T>::image(xm, ym, zm, em, g);
+          const T imx = xi - xm, imy = yi - ym, imz = zi - zm;
+          const T rim = md_sqrt(imx * imx + imy * imy + imz * imz);
+          const T jmx = xj - xm, jmy = yj - ym, jmz = zj - zm;
+          const T rjm = md_sqrt(jmx * jmx + jmy * jmy + jmz * jmz);
+          T fci, dfci, fcj, dfcj;
+          cutoff<T>(rim, fci, dfci);
+          cutoff<T>(rjm, fcj, dfcj);
+          const T drimx = imx / rim, drimy = imy / rim, drimz = imz / rim;
+          if (fci > 0) {
+            const T num2 = rij * rij + rim * rim - rjm * rjm;
+            const T icos = num2 / (2.0f * rij * rim);
+            T gth, gpre;
+            angular<T>(icos, gth, gpre);
+            xsi += fci * gth * E;
+            const T den = 4.0f * rij * rij * rim * rim;
+            const T dcx = ((2.0f * rij * drijx + 2.0f * rim * drimx) * 2.0f * rij * rim -
+                           (2.0f * rim * drijx + 2.0f * rij * drimx) * num2) / den;
+            const T dcy = ((2.0f * rij * drijy + 2.0f * rim * drimy) * 2.0f * rij * rim -
+                           (2.0f * rim * drijy + 2.0f * rij * drimy) * num2) / den;
+            const T dcz = ((2.0f * rij * drijz + 2.0f * rim * drimz) * 2.0f * rij * rim -
+                           (2.0f * rim * drijz + 2.0f * rij * drimz) * num2) / den;
+            dxsix += dfci * drimx * gth * E + fci * (gpre * dcx) * E + fci * gth * MD_LAMDA3 * E * drijx;
+            dxsiy += dfci * drimy * gth * E + fci * (gpre * dcy) * E + fci * gth * MD_LAMDA3 * E * drijy;
+            dxsiz += dfci * drimz * gth * E + fci * (gpre * dcz) * E + fci * gth * MD_LAMDA3 * E * drijz;
+          }
+          if (fcj > 0) {
+            const T num2 = rij * rij + rjm * rjm - rim * rim;
+            const T jcos = num2 / (2.0f * rij * rjm);
+            T gth, gpre;
+            angular<T>(jcos, gth, gpre);
+            xsj += fcj * gth * E;
+            const T den = 4.0f * rij * rij * rjm * rjm;
+            const T dcx = ((2.0f * rij * drijx - 2.0f * rim * drimx) * 2.0f * rij * rjm -
+                           2.0f * rjm * drijx * num2) / den;
+            const T dcy = ((2.0f * rij * drijy - 2.0f * rim * drimy) * 2.0f * rij * rjm -
+                           2.0f * rjm * drijy * num2) / den;
+            const T dcz = ((2.0f * rij * drijz - 2.0f * rim * drimz) * 2.0f * rij * rjm -
+                           2.0f * rjm * drijz * num2) / den;
+            dxsjx += fcj * ((gpre * dcx) * E + MD_LAMDA3 * E * drijx * gth);
+            dxsjy += fcj * ((gpre * dcy) * E + MD_LAMDA3 * E * drijy * gth);
+            dxsjz += fcj * ((gpre * dcz) * E + MD_LAMDA3 * E * drijz * gth);
+          }
+        }
+        xs_i = xsi;
+        xs_j = xsj;
+        const T bij = 1.0f / (1.0f + xsi), pbi = 1.0f / ((1.0f + xsi) * (1.0f + xsi));
+        const T bji = 1.0f / (1.0f + xsj), pbj = 1.0f / ((1.0f + xsj) * (1.0f + xsj));
+        bo = 0.5f * (bij + bji);
+        dbx = 0.5f * (pbi * dxsix + pbj * dxsjx);
+        dby = 0.5f * (pbi * dxsiy + pbj * dxsjy);
+        dbz = 0.5f * (pbi * dxsiz + pbj * dxsjz);
+      }
+      xsi_s[slot] = xs_i;
+      xsj_s[slot] = xs_j;
+      va_s[slot] = va;
+      vander_waals<T>(vdw, dvdw, rij, get_r0v<T>(ti, tj));
+      const T fij = dvr - bo * dva + dvdw;
+      fx += fij * ijx / rij - dbx * va;
+      fy += fij * ijy / rij - dby * va;
+      fz += fij * ijz / rij - dbz * va;
+      if (ENERGY) ev[0] += (double)(0.5f * ((vr - bo * va) + vdw));
+    }
+    double sx = warp_sum((double)fx), sy = warp_sum((double)fy), sz = warp_sum((double)fz);
+    if (lane == 0) {
+      if (ljexist) {
+        f3[3 * i] += sx;
+        f3[3 * i + 1] += sy;
+        f3[3 * i + 2] += sz;
+      } else {
+        f3[3 * i] = sx;
+        f3[3 * i + 1] = sy;
+        f3[3 * i + 2] = sz;
+      }
+      if (ENERGY) {
+        const md_double4 p = pos[i];
+        ev[1] = p.x * sx + p.y * sy + p.z * sz;
+      }
+    }
+  }
+  if (ENERGY) block_partial<2>(ev, epart);
+}
+
+template <typename T, bool ENERGY>
+__global__ void __launch_bounds__(128)
+    k_mb_pass2(const md_double4* __restrict__ pos, const float4* __restrict__ posf,
+               double* __restrict__ f3, int n, const uint32_t* __restrict__ sl,
+               const int* __restrict__ slen, Grid g, const int* __restrict__ cell3,
+               const int* __restrict__ ref_rows, int ref_nls, int ref_nlargest,
+               double rcutsq, const T* __restrict__ xsi_s, const T* __restrict__ xsj_s,
+               const T* __restrict__ va_s, int* __restrict__ missing,
+               double* __restrict__ epart) {
+  const int warps = blockDim.x >> 5;
+  const int k = blockIdx.x * warps + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  double ev[1] = {0.0};
+  if (k < n) {
+    T xk, yk, zk;
+    int tk;
+    PosT<T>::load(pos, posf, k, xk, yk, zk, tk);
+    const int Sk = slen[k];
+    const T cut_rijsq = (T)MD_CUTOFF_RIJSQ;
+    const T rc2 = (T)rcutsq;
+    T fx = 0, fy = 0, fz = 0;
+    int miss = 0;
+    for (int s = lane; s < Sk; s += 32) {
+      const uint32_t ei = sl[(size_t)s * n + k];
+      const int ip = entry_index(ei);
+      T xi, yi, zi;
+      int ti;
+      PosT<T>::load(pos, posf, ip, xi, yi, zi, ti);
+      PosT<T>::image(xi, yi, zi, ei, g);
+      const T ikx = xk - xi, iky = yk - yi, ikz = zk - zi;
+      const T rik = md_sqrt(ikx * ikx + iky * iky + ikz * ikz);
+      T fci, dfci;
+      cutoff<T>(rik, fci, dfci);
+      const T drikx = ikx / rik, driky = iky / rik, drikz = ikz / rik;
+      const int Si = slen[ip];
+      for (int sj = 0; sj < Si; sj++) {
+        const size_t q = (size_t)sj * n + ip;
+        const uint32_t ej = sl[q];
+        const int jp = entry_index(ej);
+        if (jp == k) continue;
+        int im[3] = {0, 0, 0};
+        if (ref_rows) {
+          // caller-supplied rows (no periodic box): is jp in row k?
+          const int* row = ref_rows + (size_t)k * ref_nls;
+          bool found = false;
+          for (int q2 = 0; q2 < ref_nlargest && row[q2] != -1; q2++)
+            if (row[q2] == jp) {
+              found = true;
+              break;
+            }
+          if (!found) continue;
+        } else if (!in_row(cell3, g, k, jp, im)) {
+          continue;
+        }
+        // j at its image in k's row, as BondOrderFuncs.h:367-369 sees it
+        T xj, yj, zj;
+        int tj;
+        PosT<T>::load(pos, posf, jp, xj, yj, zj, tj);
+        if (im[0] | im[1] | im[2]) PosT<T>::image3(xj, yj, zj, im[0], im[1], im[2], g);
+        const T ijx = xi - xj, ijy = yi - yj, ijz = zi - zj;
+        T rij = ijx * ijx + ijy * ijy + ijz * ijz;
+        if (rij >= rc2 || rij > cut_rijsq) continue;
+        T xs_i = xsi_s[q], xs_j = xsj_s[q];
+        if (xs_i != xs_i || tj == SP_NG) {
+          miss++;
+          xs_i = 0;
+          xs_j = 0;
+        }
+        rij = md_sqrt(rij);
+        const T va = va_s[q];
+        const T re = get_re<T>(ti, tj);
+        const T pjx = xj, pjy = yj, pjz = zj;
+        // BondOrderFuncs.h:148-237 bondOrder2 (k third body of pair ip, jp)
+        const T jkx = pjx - xk, jky = pjy - yk, jkz = pjz - zk;
+        const T rjk = md_sqrt(jkx * jkx + jky * jky + jkz * jkz);
+        const T drjkx = -jkx / rjk, drjky = -jky / rjk, drjkz = -jkz / rjk;
+        T fcj, dfcj;
+        cutoff<T>(rjk, fcj, dfcj);
+        const T E = md_exp((T)MD_LAMDA3 * (rij - re));
+        T dbx = 0, dby = 0, dbz = 0;
+        if (fci > 0) {
+          const T num2 = rij * rij + rik * rik - rjk * rjk;
+          const T icos = num2 / (2.0f * rij * rik);
+          T gth, gpre;
+          angular<T>(icos, gth, gpre);
+          const T den = 4.0f * rij * rij * rik * rik;
+          const T dcx = ((2.0f * rik * drikx - 2.0f * rjk * drjkx) * 2.0f * rij * rik - (2.0f * rij * drikx) * num2) / den;
+          const T dcy = ((2.0f * rik * driky - 2.0f * rjk * drjky) * 2.0f * rij * rik - (2.0f * rij * driky) * num2) / den;
+          const T dcz = ((2.0f * rik * drikz - 2.0f * rjk * drjkz) * 2.0f * rij * rik - (2.0f * rij * drikz) * num2) / den;
+          const T p = 1.0f / ((1.0f + xs_i) * (1.0f + xs_i));
+          dbx += 0.5f * (p * (dfci * drikx * gth * E + fci * (gpre * dcx) * E));
+          dby += 0.5f * (p * (dfci * driky * gth * E + fci * (gpre * dcy) * E));
+          dbz += 0.5f * (p * (dfci * drikz * gth * E + fci * (gpre * dcz) * E));
+        }
+        if (fcj > 0) {
+          const T num2 = rij * rij + rjk * rjk - rik * rik;
+          const T jcos = num2 / (2.0f * rij * rjk);
+          T gth, gpre;
+          angular<T>(jcos, gth, gpre);
+          const T den = 4.0f * rij * rij * rjk * rjk;
+          const T dcx = ((2.0f * rjk * drjkx - 2.0f * rik * drikx) * 2.0f * rij * rjk - (2.0f * rij * drjkx) * num2) / den;
+          const T dcy = ((2.0f * rjk * drjky - 2.0f * rik * driky) * 2.0f * rij * rjk - (2.0f * rij * drjky) * num2) / den;
+          const T dcz = ((2.0f * rjk * drjkz - 2.0f * rik * drikz) * 2.0f * rij * rjk - (2.0f * rij * drjkz) * num2) / den;
+          const T p = 1.0f / ((1.0f + xs_j) * (1.0f + xs_j));
+          dbx += 0.5f * (p * (dfcj * drjkx * gth * E + fcj * (gpre * dcx) * E));
+          dby += 0.5f * (p * (dfcj * drjky * gth * E + fcj * (gpre * dcy) * E));
+          dbz += 0.5f * (p * (dfcj * drjkz * gth * E + fcj * (gpre * dcz) * E));
+        }
+        fx -= 0.5f * dbx * va;
+        fy -= 0.5f * dby * va;
+        fz -= 0.5f * dbz * va;
+      }
+    }
+    double sx = warp_sum((double)fx), sy = warp_sum((double)fy), sz = warp_sum((double)fz);
+    int m = __reduce_add_sync(0xffffffffu, miss);
+    if (lane == 0) {
+      f3[3 * k] += sx;
+      f3[3 * k + 1] += sy;
+      f3[3 * k + 2] += sz;
+      if (m) atomicAdd(missing, m);
+      if (ENERGY) {
+        const md_double4 p = pos[k];
+        ev[0] = p.x * sx + p.y * sy + p.z * sz;
+      }
+    }
+  }
+  if (ENERGY) block_partial<1>(ev, epart);
+}
+
+inline int nblk(long long n, int t) { return (int)((n + t - 1) / t); }
+
+}  // namespace
+
+void launch_lj(const ForceArgs& a, bool fp32, bool energy, cudaStream_t st) {
+  const int T = 128;
+  const int B = nblk(a.n, T);
+  if (B == 0) return;
+  if (!fp32) {
+    if (energy)
+      k_lj_fp64<true><<<B, T, 0, st>>>(a.pos, a.f3, a.n, a.list, a.len, a.walker, a.status,
+                                       a.rcutsq, a.sp, a.epart);
+    else
+      k_lj_fp64<false><<<B, T, 0, st>>>(a.pos, a.f3, a.n, a.list, a.len, a.walker, a.status,
+                                        a.rcutsq, a.sp, a.epart);
+  } else {
+    if (energy)
+      k_lj_fp32<true><<<B, T, 0, st>>>(a.posf, a.pos, a.f3, a.n, a.list, a.len, a.walker,
+                                       a.status, a.rcutsq, a.sp, a.epart);
+    else
+      k_lj_fp32<false><<<B, T, 0, st>>>(a.posf, a.pos, a.f3, a.n, a.list, a.len, a.walker,
+                                        a.status, a.rcutsq, a.sp, a.epart);
+  }
+}
+
+int lj_blocks(int n) { return nblk(n, 128); }
+int mb_blocks(int n) { return nblk(n, 4); }
+
+template <typename T>
+static void launch_mb_t(const MbArgs& a, bool energy, cudaStream_t st) {
+  if (a.n <= 0) return;
+  k_mb_short<T><<<nblk(a.n, 128), 128, 0, st>>>(a.pos, a.posf, a.n, a.list, a.len, a.grid,
+                                                a.rcutsq, a.sl, a.slen);
+  const int B = nblk(a.n, 4);
+  T* xsi = (T*)a.xsi;
+  T* xsj = (T*)a.xsj;
+  T* va = (T*)a.va;
+  if (energy) {
+    k_mb_pass1<T, true><<<B, 128, 0, st>>>(a.pos, a.posf, a.f3, a.n, a.sl, a.slen, a.grid,
+                                           a.ljexist, xsi, xsj, va, a.epart1);
+    k_mb_pass2<T, true><<<B, 128, 0, st>>>(a.pos, a.posf, a.f3, a.n, a.sl, a.slen, a.grid,
+                                           a.cell3, a.ref_rows, a.ref_nls, a.ref_nlargest, a.rcutsq, xsi, xsj, va,
+                                           a.missing, a.epart2);
+  } else {
+    k_mb_pass1<T, false><<<B, 128, 0, st>>>(a.pos, a.posf, a.f3, a.n, a.sl, a.slen, a.grid,
+                                            a.ljexist, xsi, xsj, va, nullptr);
+    k_mb_pass2<T, false><<<B, 128, 0, st>>>(a.pos, a.posf, a.f3, a.n, a.sl, a.slen, a.grid,
+                                            a.cell3, a.ref_rows, a.ref_nls, a.ref_nlargest, a.rcutsq, xsi, xsj,
+                                            va, a.missing, nullptr);
+  }
+}
+
+void launch_mb(const MbArgs& a, bool fp32, bool energy, cudaStream_t st) {
+  if (fp32)
+    launch_mb_t<float>(a, energy, st);
+  else
+    launch_mb_t<double>(a, energy, st);
+}
+
+}  // namespace mdgb

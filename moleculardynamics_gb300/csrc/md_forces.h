@@ -1,0 +1,50 @@
+// Launch interface of the force kernels (md_forces.cu).
+#pragma once
+#include "md_internal.h"
+
+namespace mdgb {
+
+struct ForceArgs {
+  const md_double4* pos;
+  const float4* posf;   // FP32 copy (precision form)
+  double* f3;
+  int n;
+  const uint32_t* list;
+  const int* len;
+  RowWalker walker;     // full rows, used when the list is tripped
+  const int* status;
+  double rcutsq;
+  Species sp;
+  double* epart;        // 3 doubles per block when energy is requested
+};
+
+struct MbArgs {
+  const md_double4* pos;
+  const float4* posf;
+  double* f3;
+  int n;                // many-body atoms [0, n)
+  const uint32_t* list; // full candidate rows
+  const int* len;
+  Grid grid;
+  const int* cell3;     // build-time cells of the many-body list
+  const int* ref_rows;  // or: rows in the reference layout (membership by scan)
+  int ref_nls;
+  int ref_nlargest;
+  double rcutsq;
+  int ljexist;          // accumulate onto F (BondOrderFuncs.h:325-336)
+  uint32_t* sl;         // short list scratch (cap x n)
+  int* slen;
+  void* xsi;            // per (i, slot), T
+  void* xsj;
+  void* va;
+  int* missing;
+  double* epart1;       // 2 doubles per pass-1 block
+  double* epart2;       // 1 double per pass-2 block
+};
+
+void launch_lj(const ForceArgs& a, bool fp32, bool energy, cudaStream_t st);
+void launch_mb(const MbArgs& a, bool fp32, bool energy, cudaStream_t st);
+int lj_blocks(int n);
+int mb_blocks(int n);
+
+}  // namespace mdgb

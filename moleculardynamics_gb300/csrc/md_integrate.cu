@@ -1,0 +1,414 @@
+// Gear predictor-corrector, accelerations, readyList, thermo reductions and
+// the reference's all-pairs potential energy.
+//
+// predict/correct/accelerations follow cpu/common/Device.cpp:17-133 with the
+// reference's roundings (no FMA contraction), so one FP64 step on the GPU
+// returns the same bits as the reference on the same forces.  Reductions are
+// deterministic: per-block partials in a fixed grid, then one block that sums
+// them in a fixed order.
+#include <cmath>
+
+#include "md_integrate.h"
+#include "md_potential.cuh"
+
+namespace mdgb {
+
+GearCoef gear_coef(double dt) {
+  GearCoef k;
+  k.c1 = dt;
+  k.c2 = k.c1 * dt / 2.0f;
+  k.c3 = k.c2 * dt / 3.0f;
+  k.c4 = k.c3 * dt / 4.0f;
+  k.cr = MD_GEAR1 * k.c2;
+  k.cv = MD_GEAR2 * k.c2 / k.c1;
+  k.cb = MD_GEAR3 * k.c2 / k.c3;
+  k.cc = MD_GEAR4 * k.c2 / k.c4;
+  return k;
+}
+
+namespace {
+
+__device__ __forceinline__ double mass_of(int type, const Species& sp) {
+  return type == SP_N ? (double)sp.mass[0] : (type == SP_O ? (double)sp.mass[1] : (double)sp.mass[2]);
+}
+
+__device__ __forceinline__ void skin_check(const GearArgs& a, int i, double x, double y,
+                                           double z, int type) {
+  if (a.posf) a.posf[i] = make_float4((float)x, (float)y, (float)z, __int_as_float(type));
+  if (a.pos_build) {
+    float4 pb = a.pos_build[i];
+    float dx = (float)x - pb.x, dy = (float)y - pb.y, dz = (float)z - pb.z;
+    if (dx * dx + dy * dy + dz * dz > a.trip2) atomicOr(a.status, ST_LIST_TRIP);
+  }
+}
+
+// cpu/common/Device.cpp:17-39
+__global__ void k_predict(GearArgs a) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  const GearCoef k = a.k;
+  md_double4 r = a.pos[i];
+  double v[3], ac[3], b[3], c[3];
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    v[d] = a.vel[3 * i + d];
+    ac[d] = a.acc[3 * i + d];
+    b[d] = a.b[3 * i + d];
+    c[d] = a.c[3 * i + d];
+  }
+  double rr[3] = {r.x, r.y, r.z};
+#pragma unroll
+  for (int d = 0; d < 3; d++)
+    rr[d] = xadd(xadd(xadd(xadd(rr[d], xmul(k.c1, v[d])), xmul(k.c2, ac[d])), xmul(k.c3, b[d])),
+                 xmul(k.c4, c[d]));
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    double nv = xadd(xadd(xadd(v[d], xmul(k.c1, ac[d])), xmul(k.c2, b[d])), xmul(k.c3, c[d]));
+    double na = xadd(xadd(ac[d], xmul(k.c1, b[d])), xmul(k.c2, c[d]));
+    double nb = xadd(b[d], xmul(k.c1, c[d]));
+    a.vel[3 * i + d] = nv;
+    a.acc[3 * i + d] = na;
+    a.b[3 * i + d] = nb;
+  }
+  r.x = rr[0];
+  r.y = rr[1];
+  r.z = rr[2];
+  a.pos[i] = r;
+  skin_check(a, i, rr[0], rr[1], rr[2], (int)r.w);
+}
+
+// cpu/common/Device.cpp:44-120
+__global__ void k_correct(GearArgs a) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  const GearCoef k = a.k;
+  md_double4 r = a.pos[i];
+  const double mass = mass_of((int)r.w, a.sp);
+  double rr[3] = {r.x, r.y, r.z}, v[3], ac[3], corr[3];
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    ac[d] = xdiv(a.f3[3 * i + d], mass);
+    corr[d] = xsub(ac[d], a.acc[3 * i + d]);
+    rr[d] = xadd(rr[d], xmul(k.cr, corr[d]));
+    v[d] = xadd(a.vel[3 * i + d], xmul(k.cv, corr[d]));
+    a.acc[3 * i + d] = ac[d];
+    a.b[3 * i + d] = xadd(a.b[3 * i + d], xmul(k.cb, corr[d]));
+    a.c[3 * i + d] = xadd(a.c[3 * i + d], xmul(k.cc, corr[d]));
+  }
+  if (a.walls) {
+    const double np = a.npos;
+    bool hit = false;
+    if (rr[0] > np && rr[1] > 0) { hit = true; v[0] = xmul(-v[0], (double)a.energy_loss); rr[0] = np; }
+    if (rr[0] > np && rr[1] < 0) { hit = true; rr[0] = -np; }
+    if (rr[0] < -np) { hit = true; v[0] = -v[0]; rr[0] = -np; }
+    if (fabs(rr[1]) > np) { hit = true; v[1] = -v[1]; rr[1] = xmul(np, xdiv(rr[1], fabs(rr[1]))); }
+    if (fabs(rr[2]) > np) { hit = true; v[2] = -v[2]; rr[2] = xmul(np, xdiv(rr[2], fabs(rr[2]))); }
+    if (hit) atomicOr(a.wall_flag, 1);
+  }
+#pragma unroll
+  for (int d = 0; d < 3; d++) a.vel[3 * i + d] = v[d];
+  r.x = rr[0];
+  r.y = rr[1];
+  r.z = rr[2];
+  a.pos[i] = r;
+  if (!(isfinite(rr[0]) && isfinite(rr[1]) && isfinite(rr[2]) && isfinite(v[0]) &&
+        isfinite(v[1]) && isfinite(v[2])))
+    atomicOr(a.status, ST_NONFINITE);
+  skin_check(a, i, rr[0], rr[1], rr[2], (int)r.w);
+}
+
+// cpu/common/Device.cpp:125-133
+__global__ void k_accel(const md_double4* __restrict__ pos, double* __restrict__ acc,
+                        const double* __restrict__ f3, int n, Species sp) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double mass = mass_of((int)pos[i].w, sp);
+#pragma unroll
+  for (int d = 0; d < 3; d++) acc[3 * i + d] = xdiv(f3[3 * i + d], mass);
+}
+
+__global__ void k_posf(const md_double4* __restrict__ pos, float4* __restrict__ posf, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  md_double4 p = pos[i];
+  posf[i] = make_float4((float)p.x, (float)p.y, (float)p.z, __int_as_float((int)p.w));
+}
+
+__device__ __forceinline__ unsigned long long warp_umax(unsigned long long v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    unsigned long long y = __shfl_xor_sync(0xffffffffu, v, o);
+    v = y > v ? y : v;
+  }
+  return v;
+}
+
+// cpu/cpumd/Host.cpp:245-271 (max over atoms is exact in any order)
+__global__ void k_ready(const md_double4* __restrict__ pos, const double* __restrict__ vel,
+                        int n, unsigned long long* umax, int* status) {
+  unsigned long long vm = 0, bm = 0;
+  bool bad = false;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double vx = vel[3 * i], vy = vel[3 * i + 1], vz = vel[3 * i + 2];
+    double s = sqrt(norm2_exact(vx, vy, vz));
+    md_double4 p = pos[i];
+    double b = fmax(fabs(p.x), fmax(fabs(p.y), fabs(p.z)));
+    if (!(isfinite(s) && isfinite(b))) {
+      bad = true;
+      continue;
+    }
+    unsigned long long us = __double_as_longlong(s), ub = __double_as_longlong(b);
+    vm = us > vm ? us : vm;
+    bm = ub > bm ? ub : bm;
+  }
+  vm = warp_umax(vm);
+  bm = warp_umax(bm);
+  if ((threadIdx.x & 31) == 0) {
+    atomicMax(&umax[0], vm);
+    atomicMax(&umax[1], bm);
+  }
+  if (bad) atomicOr(status, ST_NONFINITE);
+}
+
+constexpr int kRedBlocks = 1024;
+constexpr int kRedThreads = 256;
+
+template <int NV>
+__device__ __forceinline__ void block_store(double (&v)[NV], double* out) {
+  __shared__ double sm[NV][kRedThreads / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < NV; k++) {
+    double x = v[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    if (lane == 0) sm[k][warp] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x < NV) {
+    double s = 0;
+    for (int w = 0; w < kRedThreads / 32; w++) s += sm[threadIdx.x][w];
+    out[NV * blockIdx.x + threadIdx.x] = s;
+  }
+}
+
+// common/DebugCalculations.cpp:81-110
+__global__ void k_thermo1(const md_double4* __restrict__ pos, const double* __restrict__ vel,
+                          int n, Species sp, double* part) {
+  double v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    md_double4 p = pos[i];
+    const double m = mass_of((int)p.w, sp);
+    const double vx = vel[3 * i], vy = vel[3 * i + 1], vz = vel[3 * i + 2];
+    v[0] += m * norm2_exact(vx, vy, vz);
+    v[1] += m * vx;
+    v[2] += m * vy;
+    v[3] += m * vz;
+    v[4] += m;
+    v[5] += m * p.x;
+    v[6] += m * p.y;
+    v[7] += m * p.z;
+  }
+  block_store<8>(v, part);
+}
+
+// common/DebugCalculations.cpp:124-141 (needs the momentum sums)
+__global__ void k_thermo2(const md_double4* __restrict__ pos, const double* __restrict__ vel,
+                          int n, Species sp, const double* __restrict__ s8, double* part) {
+  const double tot = s8[4];
+  const double cx = s8[1] / tot, cy = s8[2] / tot, cz = s8[3] / tot;
+  double v[1] = {0};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double m = mass_of((int)pos[i].w, sp);
+    const double dx = vel[3 * i] - cx, dy = vel[3 * i + 1] - cy, dz = vel[3 * i + 2] - cz;
+    v[0] += m * norm2_exact(dx, dy, dz);
+  }
+  block_store<1>(v, part);
+}
+
+__global__ void k_thermo_final(const double* __restrict__ s8, const double* __restrict__ t1,
+                               int n, double* out) {
+  if (threadIdx.x || blockIdx.x) return;
+  const double tot = s8[4];
+  out[0] = s8[5] / tot;
+  out[1] = s8[6] / tot;
+  out[2] = s8[7] / tot;
+  out[3] = s8[0] / 2;
+  out[4] = s8[1];
+  out[5] = s8[2];
+  out[6] = s8[3];
+  out[7] = t1[0] / (3.0f * ((double)n) * MD_KB);
+}
+
+__global__ void k_sum_partials(const double* __restrict__ part, int nblocks, int nv,
+                               double* out) {
+  __shared__ double sm[kRedThreads];
+  for (int k = 0; k < nv; k++) {
+    double s = 0;
+    for (int b = threadIdx.x; b < nblocks; b += blockDim.x) s += part[(size_t)nv * b + k];
+    sm[threadIdx.x] = s;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+      if (threadIdx.x < w) sm[threadIdx.x] += sm[threadIdx.x + w];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) out[k] = sm[0];
+    __syncthreads();
+  }
+}
+
+// common/DebugCalculations.cpp:129-270: one block per atom i
+__global__ void k_ref_potential(const md_double4* __restrict__ pos, int n, Species sp,
+                                double* part) {
+  const int i = blockIdx.x;
+  const md_double4 pi = pos[i];
+  const int ti = (int)pi.w;
+  double v[2] = {0, 0};
+  for (int j = threadIdx.x; j < n; j += blockDim.x) {
+    if (j == i) continue;
+    const md_double4 pj = pos[j];
+    const int tj = (int)pj.w;
+    const double ijx = pi.x - pj.x, ijy = pi.y - pj.y, ijz = pi.z - pj.z;
+    const double rijsq = norm2_exact(ijx, ijy, ijz);
+    if (tj == SP_NG || ti == SP_NG) {
+      const int sel = lj_select(ti, tj);
+      const double sig = sp.sig[sel], eps = sp.eps[sel];
+      double sr2 = sig * sig / rijsq;
+      double sr6 = sr2 * sr2 * sr2;
+      v[0] += 2.0f * eps * (sr6 * sr6 - sr6);
+    } else {
+      double va = 0, dva, vr = 0, dvr, vdw, dvdw, bo = 0;
+      const double rij = sqrt(rijsq);
+      if (rij > MD_CUTOFF_RIJ) continue;
+      double fcut, dfcut;
+      cutoff<double>(rij / 10, fcut, dfcut);
+      if (fcut > 0) {
+        const double de = get_de<double>(ti, tj), re = get_re<double>(ti, tj),
+                     beta = get_beta<double>(ti, tj);
+        attractive<double>(va, dva, rij, de, beta, re);
+        repulsive<double>(vr, dvr, rij, de, beta, re);
+        const double E = exp(MD_LAMDA3 * (rij - re));
+        double xsi = 0, xsj = 0;
+        for (int m = 0; m < n; m++) {
+          const md_double4 pm = pos[m];
+          if ((int)pm.w == SP_NG || m == j || m == i) continue;
+          const double imx = pi.x - pm.x, imy = pi.y - pm.y, imz = pi.z - pm.z;
+          const double rim = sqrt(norm2_exact(imx, imy, imz));
+          const double jmx = pj.x - pm.x, jmy = pj.y - pm.y, jmz = pj.z - pm.z;
+          const double rjm = sqrt(norm2_exact(jmx, jmy, jmz));
+          double fci, dfci, fcj, dfcj;
+          cutoff<double>(rim, fci, dfci);
+          cutoff<double>(rjm, fcj, dfcj);
+          if (fci > 0) {
+            double g, gp;
+            angular<double>((rij * rij + rim * rim - rjm * rjm) / (2.0f * rij * rim), g, gp);
+            xsi += fci * g * E;
+          }
+          if (fcj > 0) {
+            double g, gp;
+            angular<double>((rij * rij + rjm * rjm - rim * rim) / (2.0f * rij * rjm), g, gp);
+            xsj += fcj * g * E;
+          }
+        }
+        bo = 0.5f * (1.0f / (1.0f + xsi) + 1.0f / (1.0f + xsj));
+      }
+      vander_waals<double>(vdw, dvdw, rij, get_r0v<double>(ti, tj));
+      v[1] += 0.5f * ((vr - bo * va) + vdw);
+    }
+  }
+  __shared__ double sm[2][4];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int k = 0; k < 2; k++) {
+    double x = v[k];
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    if (lane == 0) sm[k][warp] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x < 2) {
+    double s = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) s += sm[threadIdx.x][w];
+    part[2 * i + threadIdx.x] = s;
+  }
+}
+
+__global__ void k_record(const double* __restrict__ th8, const double* __restrict__ elj,
+                         const double* __restrict__ emb, const double* __restrict__ ref2,
+                         int use_ref, double time, double step, double* rec) {
+  if (threadIdx.x || blockIdx.x) return;
+  // common/DebugCalculations.cpp:41-50
+  const double eu = use_ref ? (ref2[1] + ref2[0]) : (emb[0] + elj[0]);
+  rec[0] = time;
+  rec[1] = th8[7];
+  rec[2] = th8[3] + eu;
+  rec[3] = th8[3];
+  rec[4] = eu;
+  rec[5] = th8[0];
+  rec[6] = th8[1];
+  rec[7] = th8[2];
+  rec[8] = th8[4];
+  rec[9] = th8[5];
+  rec[10] = th8[6];
+  rec[11] = elj[0];
+  rec[12] = elj[1];
+  rec[13] = emb[0];
+  rec[14] = elj[2] + emb[1] + emb[2];
+  rec[15] = step;
+}
+
+inline int nblk(long long n, int t) { return (int)((n + t - 1) / t); }
+
+}  // namespace
+
+void launch_predict(const GearArgs& a, cudaStream_t st) {
+  if (a.n > 0) k_predict<<<nblk(a.n, 256), 256, 0, st>>>(a);
+}
+void launch_correct(const GearArgs& a, cudaStream_t st) {
+  if (a.n > 0) k_correct<<<nblk(a.n, 256), 256, 0, st>>>(a);
+}
+void launch_accel(const md_double4* pos, double* acc, const double* f3, int n, Species sp,
+                  cudaStream_t st) {
+  if (n > 0) k_accel<<<nblk(n, 256), 256, 0, st>>>(pos, acc, f3, n, sp);
+}
+void launch_posf(const md_double4* pos, float4* posf, int n, cudaStream_t st) {
+  if (n > 0) k_posf<<<nblk(n, 256), 256, 0, st>>>(pos, posf, n);
+}
+void launch_ready(const md_double4* pos, const double* vel, int n, unsigned long long* umax,
+                  int* status, cudaStream_t st) {
+  cudaMemsetAsync(umax, 0, 2 * sizeof(unsigned long long), st);
+  int B = nblk(n, 256);
+  if (B > kRedBlocks) B = kRedBlocks;
+  if (B > 0) k_ready<<<B, 256, 0, st>>>(pos, vel, n, umax, status);
+}
+void launch_thermo(const md_double4* pos, const double* vel, int n, Species sp, double* part,
+                   double* out, cudaStream_t st) {
+  int B = nblk(n, kRedThreads);
+  if (B > kRedBlocks) B = kRedBlocks;
+  if (B < 1) B = 1;
+  double* s8 = part + 8 * kRedBlocks;
+  double* t1 = s8 + 8;
+  k_thermo1<<<B, kRedThreads, 0, st>>>(pos, vel, n, sp, part);
+  k_sum_partials<<<1, kRedThreads, 0, st>>>(part, B, 8, s8);
+  k_thermo2<<<B, kRedThreads, 0, st>>>(pos, vel, n, sp, s8, part);
+  k_sum_partials<<<1, kRedThreads, 0, st>>>(part, B, 1, t1);
+  k_thermo_final<<<1, 32, 0, st>>>(s8, t1, n, out);
+}
+void launch_sum_partials(const double* part, int nblocks, int nv, double* out,
+                         cudaStream_t st) {
+  k_sum_partials<<<1, kRedThreads, 0, st>>>(part, nblocks, nv, out);
+}
+void launch_ref_potential(const md_double4* pos, int n, Species sp, double* part, double* out,
+                          cudaStream_t st) {
+  if (n <= 0) {
+    cudaMemsetAsync(out, 0, 2 * sizeof(double), st);
+    return;
+  }
+  k_ref_potential<<<n, 128, 0, st>>>(pos, n, sp, part);
+  k_sum_partials<<<1, kRedThreads, 0, st>>>(part, n, 2, out);
+}
+void launch_record(const double* th8, const double* e_lj3, const double* e_mb3,
+                   const double* ref2, int use_ref, double time, double step, double* rec16,
+                   cudaStream_t st) {
+  k_record<<<1, 32, 0, st>>>(th8, e_lj3, e_mb3, ref2, use_ref, time, step, rec16);
+}
+
+}  // namespace mdgb

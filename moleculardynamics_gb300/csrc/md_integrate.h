@@ -1,0 +1,60 @@
+// Launch interface of the integrator and reduction kernels (md_integrate.cu).
+#pragma once
+#include "md_internal.h"
+
+namespace mdgb {
+
+// Gear coefficients of cpu/common/Device.cpp:19-22 and :49-56
+struct GearCoef {
+  double c1, c2, c3, c4, cr, cv, cb, cc;
+};
+GearCoef gear_coef(double dt);
+
+struct GearArgs {
+  md_double4* pos;
+  double* vel;
+  double* acc;
+  double* b;
+  double* c;
+  const double* f3;
+  int n;
+  GearCoef k;
+  Species sp;
+  float4* posf;            // FP32 copy written after the update (may be NULL)
+  const float4* pos_build; // skin reference positions (may be NULL)
+  float trip2;             // squared skin displacement
+  int* status;
+  // correct only
+  double npos;
+  float energy_loss;
+  int walls;
+  int* wall_flag;
+};
+
+void launch_predict(const GearArgs& a, cudaStream_t st);
+void launch_correct(const GearArgs& a, cudaStream_t st);
+void launch_accel(const md_double4* pos, double* acc, const double* f3, int n, Species sp,
+                  cudaStream_t st);
+void launch_posf(const md_double4* pos, float4* posf, int n, cudaStream_t st);
+// max |v| and max |coordinate| (cpu/cpumd/Host.cpp:245-271) into umax[0..1]
+// as the bit patterns of non-negative doubles; sets ST_NONFINITE.
+void launch_ready(const md_double4* pos, const double* vel, int n, unsigned long long* umax,
+                  int* status, cudaStream_t st);
+// PerformCalculations (common/DebugCalculations.cpp:46-124) into out[0..7]:
+// com x,y,z, kinetic, momentum x,y,z, temperature.  part: >= 8 * 1024 doubles.
+void launch_thermo(const md_double4* pos, const double* vel, int n, Species sp, double* part,
+                   double* out, cudaStream_t st);
+// Deterministic sum of nv-vectors over nblocks partials: out[k] = sum_b part[nv*b + k].
+void launch_sum_partials(const double* part, int nblocks, int nv, double* out,
+                         cudaStream_t st);
+// calculatePotentional (common/DebugCalculations.cpp:129-270) into out[0..1].
+// part: >= 2 * n doubles.
+void launch_ref_potential(const md_double4* pos, int n, Species sp, double* part, double* out,
+                          cudaStream_t st);
+// Assembles an md_thermo record (as 16 doubles) from device scalars:
+// th8 from launch_thermo, e_lj3 = (E, E_shifted, W), e_mb3 = (E, W1, W2).
+void launch_record(const double* th8, const double* e_lj3, const double* e_mb3,
+                   const double* ref2, int use_ref, double time, double step,
+                   double* rec16, cudaStream_t st);
+
+}  // namespace mdgb

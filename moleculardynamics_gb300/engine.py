@@ -1,0 +1,349 @@
+"""Python binding of the engine's C ABI (include/mdgb.h) over ctypes.
+
+This mirrors the two C layers for tests and benchmarks:
+
+* ``Engine``: the device-resident step engine (md_create / md_upload /
+  md_begin / md_step / md_download ...), the drop-in for the step loop of
+  cpu/cpumd/Host.cpp;
+* ``Shim``: the reference-signature functions (mdgb_predict, mdgb_correct,
+  mdgb_lennard_jones_forces, ...) with the reference's arguments.
+
+There is no CPU fallback: loading fails with an error when libmdgb.so has
+not been built (``moleculardynamics_gb300.build.build()``), and every call
+that fails on the device raises ``EngineError``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "libmdgb.so")
+
+PREC_FP64, PREC_MIXED = 0, 1
+SPECIES_NEON, SPECIES_ARGON = 0, 1
+KERNEL_LJ, KERNEL_MB, KERNEL_PREDICT, KERNEL_CORRECT, KERNEL_LIST = range(5)
+
+
+class EngineError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{msg} (md_status {status})")
+        self.status = status
+
+
+class MdConfig(C.Structure):
+    _fields_ = [("n_lj", C.c_int), ("n_mb", C.c_int), ("dt", C.c_float), ("timesteps", C.c_int),
+                ("lj_rs", C.c_float), ("lj_rcut", C.c_float), ("mb_rs", C.c_float),
+                ("mb_rcut", C.c_float), ("use_lj", C.c_int), ("use_mb", C.c_int),
+                ("output_timesteps", C.c_int), ("energy_loss", C.c_float), ("periodic", C.c_int),
+                ("box", C.c_double), ("precision", C.c_int), ("species", C.c_int),
+                ("device", C.c_int), ("reference_energy", C.c_int)]
+
+
+THERMO_FIELDS = ["time", "temperature", "e", "ek", "eu", "com_x", "com_y", "com_z",
+                 "momentum_x", "momentum_y", "momentum_z", "e_lj", "e_lj_shifted", "e_mb",
+                 "virial", "step"]
+
+
+class MdThermo(C.Structure):
+    _fields_ = [(k, C.c_double) for k in THERMO_FIELDS]
+
+
+class MdStats(C.Structure):
+    _fields_ = [("steps", C.c_longlong), ("list_builds", C.c_longlong),
+                ("list_trips", C.c_longlong), ("wall_hits", C.c_longlong),
+                ("missing_xi", C.c_longlong), ("launches", C.c_longlong),
+                ("lj_max_row", C.c_int), ("lj_nlargest", C.c_int), ("mb_nlargest", C.c_int),
+                ("lj_cells", C.c_int), ("mb_cells", C.c_int)]
+
+
+class ListSettings(C.Structure):
+    _fields_ = [("maxnlmove", C.c_float), ("maxnlmovesq", C.c_float), ("rcut", C.c_float),
+                ("rs", C.c_float), ("rcutsq", C.c_float), ("nlistsize", C.c_int),
+                ("nlargestsize", C.c_int)]
+
+
+_dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+_ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+_lib = None
+
+# every exported symbol of include/mdgb.h
+EXPORTS = ["md_create", "md_destroy", "md_status_string", "md_last_error", "md_upload",
+           "md_upload_state", "md_download", "md_download_state", "md_begin", "md_step",
+           "md_record_count", "md_get_records", "md_thermo_now", "md_reference_potential",
+           "md_compute_forces", "md_neighbor_list", "md_get_stats", "md_set_timing",
+           "md_kernel_time", "md_synchronize", "mdgb_predict", "mdgb_correct",
+           "mdgb_lennard_jones_forces", "mdgb_many_body_forces", "mdgb_calculate_accelerations",
+           "mdgb_build_neighbor_list", "mdgb_free", "mdgb_perform_calculations",
+           "mdgb_calculate_potential", "mdgb_set_species", "mdgb_last_status", "md_read_config",
+           "md_write_results"]
+
+
+def load(path: str | None = None) -> C.CDLL:
+    """Loads libmdgb.so (raises if it was not built)."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise FileNotFoundError(f"{p} not built: run moleculardynamics_gb300.build.build()")
+    L = C.CDLL(p)
+    P = C.POINTER
+    L.md_create.argtypes = [P(MdConfig), P(C.c_void_p)]
+    L.md_destroy.argtypes = [C.c_void_p]
+    L.md_status_string.restype = C.c_char_p
+    L.md_status_string.argtypes = [C.c_int]
+    L.md_last_error.restype = C.c_char_p
+    L.md_last_error.argtypes = [C.c_void_p]
+    L.md_upload.argtypes = [C.c_void_p, _dp, _dp]
+    L.md_upload_state.argtypes = [C.c_void_p] + [C.c_void_p] * 5
+    L.md_download.argtypes = [C.c_void_p, _dp, _dp]
+    L.md_download_state.argtypes = [C.c_void_p] + [C.c_void_p] * 4
+    L.md_begin.argtypes = [C.c_void_p, C.c_float]
+    L.md_step.argtypes = [C.c_void_p, C.c_int]
+    L.md_record_count.argtypes = [C.c_void_p]
+    L.md_get_records.argtypes = [C.c_void_p, C.c_void_p, C.c_int]
+    L.md_thermo_now.argtypes = [C.c_void_p, P(MdThermo)]
+    L.md_reference_potential.argtypes = [C.c_void_p, P(C.c_double), P(C.c_double)]
+    L.md_compute_forces.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+    L.md_neighbor_list.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_longlong,
+                                   P(C.c_int), P(C.c_int)]
+    L.md_get_stats.argtypes = [C.c_void_p, P(MdStats)]
+    L.md_set_timing.argtypes = [C.c_void_p, C.c_int]
+    L.md_kernel_time.argtypes = [C.c_void_p, C.c_int, P(C.c_double), P(C.c_longlong)]
+    L.md_synchronize.argtypes = [C.c_void_p]
+    L.mdgb_predict.argtypes = [_dp, _dp, _dp, _dp, _dp, C.c_double, C.c_int]
+    L.mdgb_correct.argtypes = [_dp, _dp, _dp, _dp, _dp, _dp, C.c_double, C.c_int, C.c_double,
+                               P(C.c_int), C.c_float]
+    L.mdgb_lennard_jones_forces.argtypes = [_dp, _dp, C.c_int, C.c_int, C.c_int, _ip, C.c_double]
+    L.mdgb_many_body_forces.argtypes = [_dp, _dp, C.c_int, C.c_int, C.c_int, _ip, C.c_double,
+                                        C.c_int]
+    L.mdgb_calculate_accelerations.argtypes = [_dp, _dp, _dp, C.c_int]
+    L.mdgb_build_neighbor_list.restype = P(C.c_int)
+    L.mdgb_build_neighbor_list.argtypes = [_dp, P(ListSettings), C.c_double, C.c_int, C.c_int]
+    L.mdgb_free.argtypes = [C.c_void_p]
+    L.mdgb_perform_calculations.argtypes = [_dp, _dp, C.c_int] + [P(C.c_double)] * 8
+    L.mdgb_calculate_potential.argtypes = [_dp, P(C.c_double), P(C.c_double), C.c_int]
+    L.mdgb_set_species.argtypes = [C.c_int]
+    L.mdgb_last_status.restype = C.c_int
+    L.md_read_config.argtypes = [C.c_char_p, P(MdConfig), C.c_char_p, P(C.c_double),
+                                 C.c_char_p, C.c_int]
+    L.md_write_results.argtypes = [C.c_char_p, P(MdConfig), C.c_float, C.c_float,
+                                   C.c_void_p, C.c_int, C.c_void_p]
+    if path is None:
+        _lib = L
+    return L
+
+
+def make_config(n_lj=0, n_mb=0, dt=2.0, timesteps=0, lj_rs=9.534, lj_rcut=8.5125, mb_rs=3.5,
+                mb_rcut=3.0, use_lj=1, use_mb=0, output_timesteps=0, energy_loss=1.0,
+                periodic=0, box=0.0, precision=PREC_FP64, species=SPECIES_ARGON, device=0,
+                reference_energy=0) -> MdConfig:
+    return MdConfig(n_lj, n_mb, dt, timesteps, lj_rs, lj_rcut, mb_rs, mb_rcut, use_lj, use_mb,
+                    output_timesteps, energy_loss, periodic, box, precision, species, device,
+                    reference_energy)
+
+
+class Engine:
+    """One md_ctx: a system on the GPU, stepped by the engine."""
+
+    def __init__(self, cfg: MdConfig):
+        self.lib = load()
+        self.cfg = cfg
+        self.n = cfg.n_lj + cfg.n_mb
+        h = C.c_void_p()
+        s = self.lib.md_create(C.byref(cfg), C.byref(h))
+        if s != 0:
+            raise EngineError(s, "md_create: " + self.lib.md_status_string(s).decode())
+        self.h = h
+
+    def _ck(self, s: int, what: str):
+        if s != 0:
+            raise EngineError(s, f"{what}: {self.lib.md_last_error(self.h).decode()}")
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.md_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def upload(self, pos4: np.ndarray, vel3: np.ndarray):
+        self._ck(self.lib.md_upload(self.h, np.ascontiguousarray(pos4, np.float64),
+                                    np.ascontiguousarray(vel3, np.float64)), "md_upload")
+
+    def upload_state(self, pos4, vel3, acc=None, b=None, c=None):
+        keep = [np.ascontiguousarray(x, np.float64) if x is not None else None
+                for x in (pos4, vel3, acc, b, c)]
+        ptrs = [x.ctypes.data if x is not None else None for x in keep]
+        self._ck(self.lib.md_upload_state(self.h, *ptrs), "md_upload_state")
+
+    def download(self):
+        pos = np.zeros((self.n, 4))
+        vel = np.zeros((self.n, 3))
+        self._ck(self.lib.md_download(self.h, pos, vel), "md_download")
+        return pos, vel
+
+    def download_state(self):
+        arrs = [np.zeros((self.n, 3)) for _ in range(4)]
+        self._ck(self.lib.md_download_state(self.h, *[a.ctypes.data for a in arrs]),
+                 "md_download_state")
+        return dict(acc=arrs[0], b=arrs[1], c=arrs[2], force=arrs[3])
+
+    def begin(self, vxcm: float = 0.0):
+        self._ck(self.lib.md_begin(self.h, vxcm), "md_begin")
+
+    def step(self, nsteps: int):
+        self._ck(self.lib.md_step(self.h, nsteps), "md_step")
+
+    def records(self) -> np.ndarray:
+        n = self.lib.md_record_count(self.h)
+        out = (MdThermo * max(n, 1))()
+        self._ck(self.lib.md_get_records(self.h, out, n), "md_get_records")
+        return np.array([[getattr(r, k) for k in THERMO_FIELDS] for r in out[:n]]).reshape(n, 16)
+
+    def thermo_now(self) -> dict:
+        t = MdThermo()
+        self._ck(self.lib.md_thermo_now(self.h, C.byref(t)), "md_thermo_now")
+        return {k: getattr(t, k) for k in THERMO_FIELDS}
+
+    def reference_potential(self):
+        a, b = C.c_double(), C.c_double()
+        self._ck(self.lib.md_reference_potential(self.h, C.byref(a), C.byref(b)),
+                 "md_reference_potential")
+        return a.value, b.value
+
+    def compute_forces(self):
+        f = np.zeros((self.n, 3))
+        e = np.zeros(5)
+        self._ck(self.lib.md_compute_forces(self.h, f.ctypes.data, e.ctypes.data),
+                 "md_compute_forces")
+        return f, e
+
+    def neighbor_list(self, which: int = 0, images: bool = False):
+        nls, nl = C.c_int(), C.c_int()
+        self._ck(self.lib.md_neighbor_list(self.h, which, None, None, 0, C.byref(nls),
+                                           C.byref(nl)), "md_neighbor_list")
+        rows_n = self.cfg.n_mb if which == 1 else self.n
+        rows = np.zeros((rows_n, nls.value), np.int32)
+        img = np.zeros((rows_n, nls.value), np.int8) if images else None
+        self._ck(self.lib.md_neighbor_list(self.h, which, rows.ctypes.data,
+                                           img.ctypes.data if images else None, rows.size,
+                                           C.byref(nls), C.byref(nl)), "md_neighbor_list")
+        return (rows, nls.value, nl.value) + ((img,) if images else ())
+
+    def stats(self) -> dict:
+        s = MdStats()
+        self._ck(self.lib.md_get_stats(self.h, C.byref(s)), "md_get_stats")
+        return {k: getattr(s, k) for k, _ in MdStats._fields_}
+
+    def set_timing(self, on: bool):
+        self._ck(self.lib.md_set_timing(self.h, int(on)), "md_set_timing")
+
+    def kernel_time(self, kernel: int):
+        ms, n = C.c_double(), C.c_longlong()
+        self._ck(self.lib.md_kernel_time(self.h, kernel, C.byref(ms), C.byref(n)),
+                 "md_kernel_time")
+        return ms.value, n.value
+
+    def synchronize(self):
+        self._ck(self.lib.md_synchronize(self.h), "md_synchronize")
+
+
+class Shim:
+    """The reference-signature functions (mdgb_*), host arrays in and out."""
+
+    def __init__(self, species: int = SPECIES_NEON):
+        self.lib = load()
+        self.lib.mdgb_set_species(species)
+
+    def _ck(self, what):
+        s = self.lib.mdgb_last_status()
+        if s != 0:
+            raise EngineError(s, what)
+
+    def predict(self, r4, v, a, b, c, dt):
+        self.lib.mdgb_predict(r4, v, a, b, c, dt, len(r4))
+        self._ck("mdgb_predict")
+
+    def correct(self, r4, v, f, a, b, c, dt, npos, energy_loss=1.0):
+        flag = C.c_int()
+        self.lib.mdgb_correct(r4, v, f, a, b, c, dt, len(r4), npos, C.byref(flag), energy_loss)
+        self._ck("mdgb_correct")
+        return flag.value
+
+    def lennard_jones_forces(self, pos4, rows, nlargest, rcutsq):
+        f = np.zeros((len(pos4), 3))
+        rows = np.ascontiguousarray(rows, np.int32)
+        self.lib.mdgb_lennard_jones_forces(pos4, f, len(pos4), nlargest, rows.shape[1], rows,
+                                           rcutsq)
+        self._ck("mdgb_lennard_jones_forces")
+        return f
+
+    def many_body_forces(self, pos4, rows, nlargest, mbp, rcutsq, f_init=None, ljexist=False):
+        f = np.zeros((len(pos4), 3)) if f_init is None else np.ascontiguousarray(f_init).copy()
+        rows = np.ascontiguousarray(rows, np.int32)
+        self.lib.mdgb_many_body_forces(pos4, f, mbp, nlargest, rows.shape[1], rows, rcutsq,
+                                       int(ljexist))
+        self._ck("mdgb_many_body_forces")
+        return f
+
+    def calculate_accelerations(self, pos4, f):
+        a = np.zeros((len(pos4), 3))
+        self.lib.mdgb_calculate_accelerations(pos4, a, np.ascontiguousarray(f), len(pos4))
+        self._ck("mdgb_calculate_accelerations")
+        return a
+
+    def build_neighbor_list(self, pos4, rs, rcut, box, n=None):
+        n = len(pos4) if n is None else n
+        s = ListSettings(0, 0, rcut, rs, 0, 0, 0)
+        p = self.lib.mdgb_build_neighbor_list(pos4, C.byref(s), box, 3 * len(pos4), n)
+        self._ck("mdgb_build_neighbor_list")
+        nls = s.nlistsize
+        rows = np.ctypeslib.as_array(p, shape=(n * nls,)).reshape(n, nls).copy() if n * nls \
+            else np.zeros((n, 0), np.int32)
+        self.lib.mdgb_free(p)
+        return rows, nls, s.nlargestsize
+
+    def perform_calculations(self, pos4, vel3):
+        vals = [C.c_double() for _ in range(8)]
+        self.lib.mdgb_perform_calculations(pos4, vel3, len(pos4), *[C.byref(v) for v in vals])
+        self._ck("mdgb_perform_calculations")
+        return np.array([v.value for v in vals])
+
+    def calculate_potential(self, pos4):
+        a, b = C.c_double(), C.c_double()
+        self.lib.mdgb_calculate_potential(pos4, C.byref(a), C.byref(b), len(pos4))
+        self._ck("mdgb_calculate_potential")
+        return a.value, b.value
+
+
+def read_config(path: str):
+    """md_read_config: returns (MdConfig, strings dict, extras dict) or raises."""
+    L = load()
+    cfg = MdConfig()
+    strs = C.create_string_buffer(2048)
+    extra = (C.c_double * 6)()
+    err = C.create_string_buffer(512)
+    s = L.md_read_config(path.encode(), C.byref(cfg), strs, extra, err, 512)
+    if s != 0:
+        raise EngineError(s, err.value.decode())
+    raw = strs.raw
+    names = ["Input", "Output", "Filename", "AnimationData"]
+    strings = {k: raw[512 * i:512 * (i + 1)].split(b"\0")[0].decode() for i, k in enumerate(names)}
+    extras = dict(zip(["Temperature", "VXCMFROM", "VXCMTO", "VXCMSTEP", "CUDA Blocks",
+                       "AnimationTimesteps"], list(extra)))
+    return cfg, strings, extras

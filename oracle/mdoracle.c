@@ -1030,10 +1030,14 @@ int orc_run(const orc_run_params* p, double* pos4, double* vel3, double* acc3, d
       /* periodic box: positions are wrapped at a build, which would stale
        * the image codes of the other list, so both lists are rebuilt
        * together at the earlier of their two schedules */
-      int both = p->periodic;
-      if (p->use_lj && (lj_next == t || both)) BUILD(lj, ljl, lj_mv, p->lj_rs, n, lj_next);
-      if (p->use_mb && (mb_next == t || both)) BUILD(mb, mbl, mb_mv, p->mb_rs, p->n_mb, mb_next);
-      if (both) sync_schedule(p, &lj_next, &mb_next);
+      int due_lj = p->use_lj && lj_next == t, due_mb = p->use_mb && mb_next == t;
+      if (p->periodic && (due_lj || due_mb)) {
+        due_lj = p->use_lj;
+        due_mb = p->use_mb;
+      }
+      if (due_lj) BUILD(lj, ljl, lj_mv, p->lj_rs, n, lj_next);
+      if (due_mb) BUILD(mb, mbl, mb_mv, p->mb_rs, p->n_mb, mb_next);
+      if (p->periodic) sync_schedule(p, &lj_next, &mb_next);
     }
     orc_predict(pos4, vel3, acc3, b3, c3, p->dt, n);
     if (p->use_lj) orc_lj_forces(pos4, f3, n, ljl, lj_rc2, &sp, NULL);
