@@ -1,0 +1,405 @@
+#!/usr/bin/env python3
+"""Throughput benchmark of the GB300 MD step engine.
+
+Workload (default "lj1m"): 1,048,576 argon atoms on an FCC lattice of 64^3
+cubic cells at reduced density 0.8442 in a periodic box (L = 366.0 A),
+Maxwell-Boltzmann velocities at 94.4 K from a fixed seed with the momentum
+zeroed, LJ cutoff 2.5 sigma, neighbour cells of 2.8 sigma (skin 0.3 sigma),
+Gear 5th order with dt = 2 fs, precision form (FP32 pair arithmetic, FP64
+Gear state and reductions).  One bench step is 100 MD steps, list rebuilds
+included on the reference's schedule (cpu/cpumd/Host.cpp:289).  The state
+(176 MB) plus the list (330 MB) exceed the 129 MB L2, so no L2 flush is
+needed between steps.
+
+The JSON line also carries the plain FP64 GPU path on the same workload (the
+speedup of the chosen form is measured against it), the force RMS error and
+energy drift of the chosen form, the roofline of the LJ force kernel and the
+CPU oracle timed on the host cores.
+
+--impl reference times the reference's CPU implementation of the step on the
+host cores (the compiled reference where it exists, else its C restatement
+in oracle/, with all host threads) on the same workload and metric.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+SIGMA = 3.405
+EPS_K = 119.8
+KB = 8.314e-7
+EPS = EPS_K * KB
+MD_PER_BENCH_STEP = 100
+METRIC = "atom-steps/s on 1 GB300, chosen form vs plain FP64 GPU, at stated drift/RMS error"
+
+WORKLOADS = {
+    # name: (fcc cells per edge, temperature K, precision)
+    "lj1m": (64, 94.4, "mixed"),
+    "lj864": (6, 94.4, "mixed"),
+    "lj256k": (40, 94.4, "mixed"),
+}
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class Dist:
+    """Barrier and max over ranks (gloo on the host; the data path has no
+    collective: the ranks run independent replicas)."""
+
+    def __init__(self, world):
+        self.world = world
+        self.pg = None
+        if world > 1:
+            import torch.distributed as td
+            td.init_process_group("gloo")
+            self.td = td
+
+    def barrier(self):
+        if self.world > 1:
+            self.td.barrier()
+
+    def max(self, x: float) -> float:
+        if self.world == 1:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64)
+        self.td.all_reduce(t, op=self.td.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.world > 1:
+            self.td.destroy_process_group()
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        with open(self.path) as fh:
+            for line in fh:
+                f = [x.strip() for x in line.split(",")]
+                if len(f) >= 9:
+                    rows.append(f)
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({n for r in rows for n, v in zip(names, r[5:9]) if v.lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(rows)}
+
+
+def make_workload(name: str, seed: int = 2024):
+    from moleculardynamics_gb300 import lattice as lat
+    ncell, temp, prec = WORKLOADS[name]
+    pos, vel, L = lat.make_system("fcc", ncell, temp, seed=seed)
+    return pos, vel, L, prec
+
+
+def engine_for(eng, n, L, precision, device, output=MD_PER_BENCH_STEP):
+    cfg = eng.make_config(n_lj=n, dt=2.0, lj_rs=2.8 * SIGMA, lj_rcut=2.5 * SIGMA, periodic=1,
+                          box=L, precision=precision, species=eng.SPECIES_ARGON, device=device,
+                          output_timesteps=output)
+    return eng.Engine(cfg)
+
+
+def drift_per_1000(recs: np.ndarray, n: int, first_step: int) -> float:
+    """(E_end - E_start) / N / eps per 1000 MD steps, E = KE + shifted LJ energy."""
+    sel = recs[recs[:, 15] >= first_step]
+    if len(sel) < 2:
+        return float("nan")
+    e = sel[:, 3] + sel[:, 12]
+    steps = sel[-1, 15] - sel[0, 15]
+    return float((e[-1] - e[0]) / n / EPS / steps * 1000.0)
+
+
+def roofline_traffic(workload: str):
+    """dram bytes per launch of the LJ kernel from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", f"lj_force_{workload}.md")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        if line.startswith("traffic_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+def measured_peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        return {}
+
+
+def cpu_baseline(pos, vel, L, steps: int, threads: int):
+    """The CPU oracle on a bounded sample of the same workload (host cores)."""
+    from oracle.oracle import load_oracle, load_reference
+    O = load_oracle()
+    p = dict(n_lj=len(pos), n_mb=0, timesteps=steps, use_lj=1, use_mb=0, output_timesteps=0,
+             dt=2.0, lj_rs=2.8 * SIGMA, lj_rcut=2.5 * SIGMA, mb_rs=3.5, mb_rcut=3.0,
+             energy_loss=1.0, vxcm=0.0, periodic=1, box=L, species=1, threads=threads)
+    r = O.run(p, pos, vel)
+    kind = "port"
+    return r["elapsed_ms"], kind
+
+
+def run_reference_arm(args, rank, world):
+    if rank != 0:
+        return 0
+    from moleculardynamics_gb300 import lattice as lat  # noqa: F401
+    from oracle.oracle import build_oracle
+    build_oracle()
+    pos, vel, L, _ = make_workload(args.workload)
+    n = len(pos)
+    threads = os.cpu_count() or 1
+    per = args.ref_md_steps
+    # warm-up run (list build + W bench steps), then the timed run
+    cpu_baseline(pos, vel, L, per * args.warmup, threads)
+    ms, kind = cpu_baseline(pos, vel, L, per * args.steps, threads)
+    value = n * per * args.steps / (ms / 1e3)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "atom-steps/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"{args.workload}: {n} argon atoms FCC, periodic, dt 2 fs",
+                   "md_steps_per_bench_step": per, "form": "reference CPU path (FP64)"},
+        "cpu_baseline": {"value": value, "unit": "atom-steps/s", "cores": threads, "kind": kind,
+                         "sample": f"{n} atoms, {per * args.steps} MD steps after the list build, "
+                                   f"{threads} OpenMP threads of the C restatement of the "
+                                   "reference step (oracle/mdoracle.c)"},
+        "e2e": {"value": value, "unit": "atom-steps/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_gb300(args, rank, world):
+    from moleculardynamics_gb300 import build as b
+    from moleculardynamics_gb300 import engine as eng
+    if rank == 0:
+        b.build()
+    dist = Dist(world)
+    dist.barrier()
+    b.build()
+    eng.load()
+    device = int(os.environ.get("LOCAL_RANK", "0"))
+    pos, vel, L, prec_name = make_workload(args.workload)
+    n = len(pos)
+    precision = eng.PREC_MIXED if prec_name == "mixed" else eng.PREC_FP64
+    e = engine_for(eng, n, L, precision, device)
+    e.upload(pos, vel)
+    e.begin(0.0)
+    for _ in range(args.warmup):
+        e.step(MD_PER_BENCH_STEP)
+    warm_steps = args.warmup * MD_PER_BENCH_STEP
+    e.synchronize()
+    e.set_timing(True)
+    s0 = e.stats()
+    clocks = Clocks(device)
+    dist.barrier()
+    clocks.start()
+    for _ in range(args.steps):
+        e.step(MD_PER_BENCH_STEP)
+    e.synchronize()
+    ck = clocks.stop()
+    dist.barrier()
+    step_ms, _ = e.kernel_time(eng.KERNEL_STEP)
+    lj_ms, lj_n = e.kernel_time(eng.KERNEL_LJ)
+    pr_ms, pr_n = e.kernel_time(eng.KERNEL_PREDICT)
+    co_ms, co_n = e.kernel_time(eng.KERNEL_CORRECT)
+    li_ms, li_n = e.kernel_time(eng.KERNEL_LIST)
+    s1 = e.stats()
+    e.set_timing(False)
+    t_max = dist.max(step_ms)
+    md_steps = args.steps * MD_PER_BENCH_STEP
+    value = world * n * md_steps / (t_max / 1e3)
+    recs = e.records()
+    drift = drift_per_1000(recs, n, warm_steps)
+
+    # end to end through the C ABI: the caller owns the Gear state in pinned
+    # host memory; every bench step copies it in, runs, and copies it back
+    hp = eng.pinned((n, 4))
+    hv = eng.pinned((n, 3))
+    ha, hb, hc = (eng.pinned((n, 3)) for _ in range(3))
+    p0, v0 = e.download()
+    st = e.download_state()
+    hp[:], hv[:], ha[:], hb[:], hc[:] = p0, v0, st["acc"], st["b"], st["c"]
+    dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e.upload_state(hp, hv, ha, hb, hc)
+        e.step(MD_PER_BENCH_STEP)
+        e.lib.md_download(e.h, hp, hv)
+        e.lib.md_download_state(e.h, ha.ctypes.data, hb.ctypes.data, hc.ctypes.data, None)
+    e.synchronize()
+    e2e_s = dist.max(time.perf_counter() - t0)
+    e2e_value = world * n * md_steps / e2e_s
+    h2d = n * (32 + 24 + 3 * 24)   # pos4, vel3, acc3, b3, c3 in
+    d2h = n * (32 + 24 + 3 * 24)   # the same out
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "atom-steps/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32" if precision == eng.PREC_MIXED else "f64",
+        "data": "synthetic",
+        "config": {"workload": f"{args.workload}: {n} argon atoms, FCC {WORKLOADS[args.workload][0]}^3 "
+                               f"cells at rho*=0.8442, periodic L={L:.1f} A, T=94.4 K, rc=2.5 sigma, "
+                               "skin 0.3 sigma, dt=2 fs, Gear 5th order",
+                   "form": "precision: FP32 pairs, compensated FP32 sums, FP64 Gear state "
+                           "and reductions" if precision == eng.PREC_MIXED else "plain FP64",
+                   "md_steps_per_bench_step": MD_PER_BENCH_STEP, "atoms": n,
+                   "parallelism": f"replicas x{world}" if world > 1 else "1 GPU",
+                   "l2": "inputs larger than L2 (state 176 MB + list 330 MB), no flush"},
+        "gpu_launches": s1["launches"] - s0["launches"],
+        "clocks": ck,
+        "e2e": {"value": e2e_value, "unit": "atom-steps/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "list": {"builds_in_timed_region": s1["list_builds"] - s0["list_builds"],
+                 "skin_trips": s1["list_trips"], "mean_compact_row": s1["lj_list_entries"] / n,
+                 "cells_per_edge": s1["lj_cells"]},
+        "kernel_ms_per_md_step": {
+            "lj_force": lj_ms / max(lj_n, 1), "predict": pr_ms / max(pr_n, 1),
+            "correct": co_ms / max(co_n, 1),
+            "list_build_amortised": li_ms / md_steps},
+        "accuracy": {"energy_drift_eps_per_atom_per_1000_steps": drift},
+    }
+    peaks = measured_peaks()
+    if lj_n:
+        entries = s1["lj_list_entries"]
+        pos_b = 16 if precision == eng.PREC_MIXED else 32
+        bytes_alg = n * (pos_b + 4 + 24) + 4 * entries
+        avg_s = lj_ms / lj_n / 1e3
+        achieved = bytes_alg / avg_s / 1e9
+        peak = peaks.get("hbm_gbs")
+        traffic = roofline_traffic(args.workload)
+        line["roofline"] = {"kernel": "k_lj_fp32" if precision == eng.PREC_MIXED else "k_lj_fp64",
+                            "bound": "hbm", "achieved": achieved,
+                            "peak": peak if peak else 6800.0, "unit": "GB/s",
+                            "frac": achieved / (peak if peak else 6800.0),
+                            "peak_source": "measured" if peak else "fallback",
+                            "traffic": traffic,
+                            "bytes_alg_per_launch": bytes_alg,
+                            "avg_launch_ms": lj_ms / lj_n}
+
+    if rank == 0 and not args.no_compare:
+        # plain FP64 GPU path on the same workload (fewer steps: it is slow)
+        f64 = engine_for(eng, n, L, eng.PREC_FP64, device)
+        f64.upload(pos, vel)
+        f64.begin(0.0)
+        f64.step(20)
+        f64.synchronize()
+        f64.set_timing(True)
+        k64 = max(1, args.fp64_steps)
+        f64.step(k64)
+        f64.synchronize()
+        ms64, _ = f64.kernel_time(eng.KERNEL_STEP)
+        lj64_ms, lj64_n = f64.kernel_time(eng.KERNEL_LJ)
+        v64 = n * k64 / (ms64 / 1e3)
+        # force error of the chosen form at the same positions
+        pnow, vnow = e.download()
+        f64.upload(pnow, vnow)
+        f64.begin(0.0)
+        fa, _ = f64.compute_forces()
+        fb, _ = e.compute_forces()
+        f64.close()
+        rms = float(np.sqrt(((fb - fa) ** 2).sum(1).mean()) / np.sqrt((fa ** 2).sum(1).mean()))
+        line["plain_fp64"] = {"value": v64, "unit": "atom-steps/s", "md_steps": k64,
+                              "lj_force_ms": lj64_ms / max(lj64_n, 1)}
+        line["speedup_vs_plain_fp64"] = value / world / v64
+        line["accuracy"]["force_rms_rel_vs_fp64"] = rms
+    if rank == 0 and world == 1 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        csteps = args.cpu_md_steps
+        ms, kind = cpu_baseline(pos, vel, L, csteps, threads)
+        line["cpu_baseline"] = {"value": n * csteps / (ms / 1e3), "unit": "atom-steps/s",
+                                "cores": threads, "kind": kind,
+                                "sample": f"{n} atoms, {csteps} MD steps after the list build, "
+                                          f"{threads} OpenMP threads, C restatement of the "
+                                          "reference step (oracle/mdoracle.c)"}
+    e.close()
+    dist.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="lj1m", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-compare", action="store_true", help="skip the plain FP64 leg")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    ap.add_argument("--fp64-steps", type=int, default=100)
+    ap.add_argument("--cpu-md-steps", type=int, default=5)
+    ap.add_argument("--ref-md-steps", type=int, default=2)
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    rank, world, _ = dist_env()
+    if args.impl == "reference":
+        return run_reference_arm(args, rank, world)
+    return run_gb300(args, rank, world)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -26,6 +26,8 @@
 #ifndef MDGB_H
 #define MDGB_H
 
+#include <stddef.h>
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -95,6 +97,7 @@ typedef struct md_stats {
   int lj_nlargest;         /* longest full LJ candidate row (nlargestsize) */
   int mb_nlargest;
   int lj_cells, mb_cells;
+  long long lj_list_entries; /* entries of the compact LJ list at the last build */
 } md_stats;
 
 typedef struct md_ctx md_ctx;
@@ -140,11 +143,15 @@ md_status md_neighbor_list(md_ctx* ctx, int which, int* rows, signed char* image
                            long long capacity, int* nlistsize, int* nlargest);
 md_status md_get_stats(const md_ctx* ctx, md_stats* out);
 /* Per-kernel device timing with CUDA events on the engine's stream.
- * kernel: 0 = LJ force, 1 = bond order, 2 = predict, 3 = correct, 4 = list build. */
+ * kernel: 0 = LJ force, 1 = bond order, 2 = predict, 3 = correct, 4 = list build,
+ * 5 = whole md_step calls (first launch to last). */
 md_status md_set_timing(md_ctx* ctx, int on);
 md_status md_kernel_time(const md_ctx* ctx, int kernel, double* total_ms, long long* launches);
 /* Wait for all work of the context; returns the first deferred error. */
 md_status md_synchronize(md_ctx* ctx);
+/* Page-locked host memory for fast md_upload/md_download (NULL on failure). */
+void* md_host_alloc(size_t bytes);
+void md_host_free(void* p);
 
 /* ---- reference-signature API ---- */
 typedef struct mdgb_list_settings { /* common/NeighborList.h:19-28 listSettings */

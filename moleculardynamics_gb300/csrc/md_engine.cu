@@ -63,7 +63,7 @@ int next_build(float maxnlmove, double vmax, double dt, int t) {
   return nb > 2147483647LL ? 2147483647 : (int)nb;
 }
 
-constexpr int kKernels = 5;  // timing ids of md_kernel_time
+constexpr int kKernels = 6;  // timing ids of md_kernel_time
 
 __global__ void k_begin(md_double4* pos, double* vel, int n, double half_box, int clamp,
                         double vxcm) {
@@ -121,8 +121,8 @@ struct md_ctx {
   bool timing = false;
   std::vector<cudaEvent_t> ev_pool;
   std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> pending;
-  double kt_ms[kKernels] = {0, 0, 0, 0, 0};
-  long long kt_n[kKernels] = {0, 0, 0, 0, 0};
+  double kt_ms[kKernels] = {0, 0, 0, 0, 0, 0};
+  long long kt_n[kKernels] = {0, 0, 0, 0, 0, 0};
 
   bool mixed() const { return cfg.precision == MD_PREC_MIXED; }
   bool walls() const { return !cfg.periodic; }
@@ -346,6 +346,7 @@ md_status rebuild(md_ctx* c, int t) {
     c->stats.lj_max_row = c->lj.max_len;
     c->stats.lj_nlargest = c->lj.nlargest;
     c->stats.lj_cells = c->lj.grid.cells;
+    c->stats.lj_list_entries = c->lj.entries;
     did_lj = true;
   }
   if (c->cfg.use_mb && c->cfg.n_mb > 0 && (c->mb_next == t || both)) {
@@ -568,7 +569,7 @@ md_status md_create(const md_config* cfg, md_ctx** out) {
     return bail(e, "scratch");
   if ((e = cudaMalloc(&c->sc.umax, sizeof(unsigned long long) * 4)) != cudaSuccess)
     return bail(e, "scratch");
-  if ((e = cudaMalloc(&c->sc.counts, sizeof(int) * 4)) != cudaSuccess) return bail(e, "scratch");
+  if ((e = cudaMalloc(&c->sc.counts, sizeof(int) * 8)) != cudaSuccess) return bail(e, "scratch");
   if ((e = cudaMalloc(&c->dsc, sizeof(double) * 32)) != cudaSuccess) return bail(e, "scratch");
   cudaMemsetAsync(c->dsc, 0, sizeof(double) * 32, c->st);
   *out = c;
@@ -667,9 +668,12 @@ md_status md_begin(md_ctx* c, float vxcm) {
 md_status md_step(md_ctx* c, int nsteps) {
   if (!c || nsteps < 0) return MD_BAD_ARGUMENT;
   if (!c->begun) return fail(c, MD_BAD_ARGUMENT, "md_begin has not been called");
-  for (int s = 0; s < nsteps; s++) {
-    md_status r = step_once(c);
-    if (r != MD_OK) return r;
+  {
+    Timed whole(c, 5);
+    for (int s = 0; s < nsteps; s++) {
+      md_status r = step_once(c);
+      if (r != MD_OK) return r;
+    }
   }
   md_status r = check_status(c);
   if (c->timing) resolve_timing(c);
@@ -795,6 +799,16 @@ md_status md_kernel_time(const md_ctx* cc, int kernel, double* total_ms, long lo
 md_status md_synchronize(md_ctx* c) {
   if (!c) return MD_BAD_ARGUMENT;
   return check_status(c);
+}
+
+void* md_host_alloc(size_t bytes) {
+  void* p = nullptr;
+  if (cudaMallocHost(&p, bytes) != cudaSuccess) return nullptr;
+  return p;
+}
+
+void md_host_free(void* p) {
+  if (p) cudaFreeHost(p);
 }
 
 }  // extern "C"

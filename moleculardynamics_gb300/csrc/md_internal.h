@@ -47,6 +47,7 @@ struct NeighborList {
   double trip_dist = 0;        // an atom displaced by more than this trips the list
   // host copies of the last build's sizes
   int maxcell = 0, nlargest = 0, nlistsize = 0, max_len = 0;
+  long long entries = 0;         // total kept entries
   int n_alloc = 0;
 };
 

@@ -16,6 +16,7 @@
 // the full row (same candidates, same order as the reference).
 #include <cmath>
 #include <cstdio>
+#include <cstring>
 
 #include "md_neighbor.cuh"
 
@@ -199,6 +200,7 @@ __global__ void k_rows(RowWalker w, const md_double4* __restrict__ pos,
     len[i] = kept;
     atomicMax(&counters[1], full);
     atomicMax(&counters[2], kept);
+    atomicAdd((unsigned long long*)(counters + 4), (unsigned long long)kept);
   }
 }
 
@@ -338,7 +340,7 @@ int list_build(NeighborList& nl, md_double4* pos, int n, const Grid& g, int comp
   cudaMemsetAsync(nl.table.keys, 0xFF, sizeof(unsigned long long) * (size_t)cap, st);
   cudaMemsetAsync(nl.table.count, 0, sizeof(int) * (size_t)cap, st);
   cudaMemsetAsync(nl.table.fill, 0, sizeof(int) * (size_t)cap, st);
-  cudaMemsetAsync(sc.counts, 0, sizeof(int) * 4, st);
+  cudaMemsetAsync(sc.counts, 0, sizeof(int) * 8, st);
   const int T = 256;
   if (n > 0) {
     k_cell_assign<<<blocks(n, T), T, 0, st>>>(pos, n, g, nl.cell3, nl.table.keys, nl.table.count,
@@ -361,7 +363,7 @@ int list_build(NeighborList& nl, md_double4* pos, int n, const Grid& g, int comp
   if (n > 0)
     k_rows<0><<<blocks(n, 128), 128, 0, st>>>(w, pos, nl.pos_build, compact, rv2, g.box_f,
                                               nullptr, nl.len, n, sc.counts);
-  int hc[4] = {0, 0, 0, 0};
+  int hc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   int status = 0;
   cudaMemcpyAsync(hc, sc.counts, sizeof(hc), cudaMemcpyDeviceToHost, st);
   cudaMemcpyAsync(&status, d_status, sizeof(int), cudaMemcpyDeviceToHost, st);
@@ -373,6 +375,11 @@ int list_build(NeighborList& nl, md_double4* pos, int n, const Grid& g, int comp
   }
   nl.maxcell = hc[0];
   nl.nlargest = hc[1];
+  {
+    unsigned long long ent;
+    memcpy(&ent, hc + 4, sizeof(ent));
+    nl.entries = (long long)ent;
+  }
   long long nls = (long long)hc[0] * 27;
   if (nls > n - 1) nls = n - 1;
   if (nls < 0) nls = 0;

@@ -87,7 +87,7 @@ bool shim_ready(long long n) {
     if (cudaMalloc(&s.flags, sizeof(int) * 4) != cudaSuccess) return false;
     if (cudaMalloc(&s.sc.dpart, sizeof(double) * (8 * 1024 + 64)) != cudaSuccess) return false;
     if (cudaMalloc(&s.sc.umax, sizeof(unsigned long long) * 4) != cudaSuccess) return false;
-    if (cudaMalloc(&s.sc.counts, sizeof(int) * 4) != cudaSuccess) return false;
+    if (cudaMalloc(&s.sc.counts, sizeof(int) * 8) != cudaSuccess) return false;
     if (cudaMalloc(&s.out, sizeof(double) * 16) != cudaSuccess) return false;
     s.init = true;
   }

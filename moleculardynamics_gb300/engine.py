@@ -25,7 +25,7 @@ LIB_PATH = os.path.join(PKG, "libmdgb.so")
 
 PREC_FP64, PREC_MIXED = 0, 1
 SPECIES_NEON, SPECIES_ARGON = 0, 1
-KERNEL_LJ, KERNEL_MB, KERNEL_PREDICT, KERNEL_CORRECT, KERNEL_LIST = range(5)
+KERNEL_LJ, KERNEL_MB, KERNEL_PREDICT, KERNEL_CORRECT, KERNEL_LIST, KERNEL_STEP = range(6)
 
 
 class EngineError(RuntimeError):
@@ -57,7 +57,7 @@ class MdStats(C.Structure):
                 ("list_trips", C.c_longlong), ("wall_hits", C.c_longlong),
                 ("missing_xi", C.c_longlong), ("launches", C.c_longlong),
                 ("lj_max_row", C.c_int), ("lj_nlargest", C.c_int), ("mb_nlargest", C.c_int),
-                ("lj_cells", C.c_int), ("mb_cells", C.c_int)]
+                ("lj_cells", C.c_int), ("mb_cells", C.c_int), ("lj_list_entries", C.c_longlong)]
 
 
 class ListSettings(C.Structure):
@@ -79,7 +79,7 @@ EXPORTS = ["md_create", "md_destroy", "md_status_string", "md_last_error", "md_u
            "mdgb_lennard_jones_forces", "mdgb_many_body_forces", "mdgb_calculate_accelerations",
            "mdgb_build_neighbor_list", "mdgb_free", "mdgb_perform_calculations",
            "mdgb_calculate_potential", "mdgb_set_species", "mdgb_last_status", "md_read_config",
-           "md_write_results"]
+           "md_write_results", "md_host_alloc", "md_host_free"]
 
 
 def load(path: str | None = None) -> C.CDLL:
@@ -115,6 +115,9 @@ def load(path: str | None = None) -> C.CDLL:
     L.md_set_timing.argtypes = [C.c_void_p, C.c_int]
     L.md_kernel_time.argtypes = [C.c_void_p, C.c_int, P(C.c_double), P(C.c_longlong)]
     L.md_synchronize.argtypes = [C.c_void_p]
+    L.md_host_alloc.restype = C.c_void_p
+    L.md_host_alloc.argtypes = [C.c_size_t]
+    L.md_host_free.argtypes = [C.c_void_p]
     L.mdgb_predict.argtypes = [_dp, _dp, _dp, _dp, _dp, C.c_double, C.c_int]
     L.mdgb_correct.argtypes = [_dp, _dp, _dp, _dp, _dp, _dp, C.c_double, C.c_int, C.c_double,
                                P(C.c_int), C.c_float]
@@ -329,6 +332,31 @@ class Shim:
         self.lib.mdgb_calculate_potential(pos4, C.byref(a), C.byref(b), len(pos4))
         self._ck("mdgb_calculate_potential")
         return a.value, b.value
+
+
+def pinned(shape, dtype=np.float64):
+    """A numpy array over page-locked host memory (md_host_alloc); the memory
+    lives as long as the returned array."""
+    L = load()
+    nbytes = int(np.prod(shape)) * np.dtype(dtype).itemsize
+    p = L.md_host_alloc(max(nbytes, 1))
+    if not p:
+        raise EngineError(8, "md_host_alloc failed")
+    buf = (C.c_char * max(nbytes, 1)).from_address(p)
+    arr = np.frombuffer(buf, dtype=dtype, count=int(np.prod(shape))).reshape(shape)
+
+    class _Owner:
+        def __del__(self, p=p, L=L):
+            L.md_host_free(p)
+    arr_owner = _Owner()
+    # keep the owner alive with the array
+    out = arr.view(_PinnedArray)
+    out._owner = arr_owner
+    return out
+
+
+class _PinnedArray(np.ndarray):
+    pass
 
 
 def read_config(path: str):
