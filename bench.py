@@ -314,7 +314,7 @@ def run_gb300(args, rank, world):
                 "d2h_bytes_per_step": d2h},
         "list": {"builds_in_timed_region": s1["list_builds"] - s0["list_builds"],
                  "skin_trips": s1["list_trips"], "mean_compact_row": s1["lj_list_entries"] / n,
-                 "cells_per_edge": s1["lj_cells"]},
+                 "cells_per_edge": s1["lj_cells"], "tma": s1["lj_tma"]},
         "kernel_ms_per_md_step": {
             "lj_force": lj_ms / max(lj_n, 1), "predict": pr_ms / max(pr_n, 1),
             "correct": co_ms / max(co_n, 1),

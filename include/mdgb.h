@@ -98,6 +98,7 @@ typedef struct md_stats {
   int mb_nlargest;
   int lj_cells, mb_cells;
   long long lj_list_entries; /* entries of the compact LJ list at the last build */
+  int lj_tma;              /* 1: the LJ list is streamed by TMA (precision form) */
 } md_stats;
 
 typedef struct md_ctx md_ctx;

@@ -74,6 +74,10 @@ __host__ __device__ __forceinline__ int entry_img(uint32_t e, int axis) {
   return (f ^ 2) - 2;
 }
 
+// TMA tile of a compact neighbour list: 128 atoms x 16 slots of uint32.
+constexpr int kListTileAtoms = 128;
+constexpr int kListTileSlots = 16;
+
 // Cell-grid geometry of one list build.
 struct Grid {
   int periodic;   // 0: reference box (NeighborList.cpp:19-27), 1: periodic cube

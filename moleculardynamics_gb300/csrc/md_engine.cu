@@ -116,6 +116,8 @@ struct md_ctx {
   // schedule
   int t = 0, lj_next = 0, mb_next = 0, printout = 0;
   bool begun = false;
+  bool predicted = false;  // the state already holds the prediction for step t
+  int all_ng = 0;          // every atom is of the NG species (set at upload)
   md_stats stats{};
   // timing
   bool timing = false;
@@ -223,8 +225,16 @@ ForceArgs lj_args(md_ctx* c, double* f3, double* epart) {
   a.n = c->n;
   a.list = c->lj.list;
   a.len = c->lj.len;
-  a.walker = make_walker(c->lj);
+  a.ld = c->lj.ld;
+  a.tmap = c->lj.tmap_ok ? &c->lj.tmap : nullptr;
+  a.all_ng = c->all_ng;
   a.status = c->status;
+  a.walker = make_walker(c->lj);
+  a.skin = c->lj.skin;
+  a.parity = c->t & 1;
+  a.cap = c->lj.cap;
+  a.rv2 = c->lj.rv2_keep;
+  a.pos_build = c->lj.pos_build;
   a.rcutsq = (double)c->lj_rcutsq;
   a.sp = c->sp;
   a.epart = epart;
@@ -239,6 +249,7 @@ MbArgs mb_args(md_ctx* c, double* f3, int ljexist) {
   a.n = c->cfg.n_mb;
   a.list = c->mb.list;
   a.len = c->mb.len;
+  a.ld = c->mb.ld;
   a.grid = c->mb.grid;
   a.cell3 = c->mb.cell3;
   a.ref_rows = nullptr;
@@ -273,7 +284,7 @@ md_status forces(md_ctx* c, double* f3) {
   return MD_OK;
 }
 
-GearArgs gear_args(md_ctx* c) {
+GearArgs gear_args(md_ctx* c, int parity) {
   GearArgs g;
   g.pos = c->pos;
   g.vel = c->vel;
@@ -289,7 +300,10 @@ GearArgs gear_args(md_ctx* c) {
   g.pos_build = skin ? c->lj.pos_build : nullptr;
   g.trip2 = skin ? (float)(c->lj.trip_dist * c->lj.trip_dist) : 0.f;
   if (skin && c->lj.trip_dist <= 0) g.trip2 = -1.f;  // skin too thin: always walk full rows
+  g.trip = skin ? c->lj.skin + (parity & 1) : nullptr;
   g.status = c->status;
+  g.exact = !c->mixed();
+  for (int k = 0; k < 3; k++) g.inv_mass[k] = 1.0 / (double)c->sp.mass[k];
   g.npos = c->box_size;
   g.energy_loss = c->energy_loss;
   g.walls = c->walls();
@@ -307,6 +321,7 @@ md_status check_status(md_ctx* c) {
   c->stats.missing_xi = miss;
   if (s & ST_NONFINITE) return fail(c, MD_NONFINITE, "non-finite position or velocity");
   if (s & ST_CELL_OVERFLOW) return fail(c, MD_CELL_OVERFLOW, "cell grid out of range");
+  if (s & ST_TMA_TIMEOUT) return fail(c, MD_TIMEOUT, "a TMA transfer did not complete in time");
   return MD_OK;
 }
 
@@ -329,7 +344,13 @@ md_status rebuild(md_ctx* c, int t) {
   const double dt = (double)c->cfg.dt;
   bool did_lj = false;
   if (c->cfg.use_lj && (c->lj_next == t || both)) {
-    if (s & ST_LIST_TRIP) c->stats.list_trips++;
+    if (c->lj.skin) {
+      int sk[4];
+      CK(cudaMemcpy(sk, c->lj.skin, sizeof(sk), cudaMemcpyDeviceToHost), "skin");
+      c->stats.list_trips += sk[3];
+      if (sk[2]) c->lj.headroom *= 1.5f;  // a refreshed row did not fit: more room
+      CK(cudaMemsetAsync(c->lj.skin + 3, 0, sizeof(int), c->st), "skin");
+    }
     CK(cudaMemsetAsync(c->status, 0, sizeof(int), c->st), "status");
     Grid g = c->cfg.periodic ? make_grid_periodic(c->cfg.box, c->cfg.lj_rs)
                              : make_grid_reference(box_list, c->cfg.lj_rs);
@@ -347,21 +368,14 @@ md_status rebuild(md_ctx* c, int t) {
     c->stats.lj_nlargest = c->lj.nlargest;
     c->stats.lj_cells = c->lj.grid.cells;
     c->stats.lj_list_entries = c->lj.entries;
+    c->stats.lj_tma = c->lj.tmap_ok;
     did_lj = true;
   }
   if (c->cfg.use_mb && c->cfg.n_mb > 0 && (c->mb_next == t || both)) {
     Grid g = c->cfg.periodic ? make_grid_periodic(c->cfg.box, c->cfg.mb_rs)
                              : make_grid_reference(box_list, c->cfg.mb_rs);
     std::string e;
-    if (!did_lj) {
-      // keep a set skin bit of the LJ list, clear the rest
-      CK(cudaMemsetAsync(c->status, 0, sizeof(int), c->st), "status");
-      if (s & ST_LIST_TRIP) {
-        int v = ST_LIST_TRIP;
-        CK(cudaMemcpyAsync(c->status, &v, sizeof(int), cudaMemcpyHostToDevice, c->st), "status");
-        CK(cudaStreamSynchronize(c->st), "status");
-      }
-    }
+    if (!did_lj) CK(cudaMemsetAsync(c->status, 0, sizeof(int), c->st), "status");
     int r = list_build(c->mb, c->pos, c->cfg.n_mb, g, 0, 0.f, sqrt((double)c->mb_rcutsq), c->sc,
                        c->status, c->st, e);
     c->stats.launches += 9;
@@ -452,23 +466,39 @@ md_status push_record(md_ctx* c, int t) {
   return s;
 }
 
-md_status step_once(md_ctx* c) {
+bool due(const md_ctx* c, int t) {
+  return (c->cfg.use_lj && c->lj_next == t) || (c->cfg.use_mb && c->mb_next == t);
+}
+
+// One iteration of cpu/cpumd/Host.cpp:141-195.  In the precision form with a
+// periodic box, correct(t) and predict(t+1) run as one kernel unless step
+// t+1 rebuilds a list, step t records output, or this is the last step of
+// the call (the state between calls is always the corrected one).
+md_status step_once(md_ctx* c, bool last) {
   const int t = c->t;
-  if ((c->cfg.use_lj && c->lj_next == t) || (c->cfg.use_mb && c->mb_next == t)) {
+  if (due(c, t)) {
     md_status s = rebuild(c, t);
     if (s != MD_OK) return s;
   }
-  GearArgs g = gear_args(c);
-  {
+  if (!c->predicted) {
+    GearArgs g = gear_args(c, t);
     Timed tm(c, 2);
     launch_predict(g, c->st);
     c->stats.launches++;
   }
+  c->predicted = false;
   forces(c, c->f3);
   if (c->walls()) CK(cudaMemsetAsync(c->wall_flag, 0, sizeof(int), c->st), "wall flag");
+  const bool output = c->cfg.output_timesteps > 0 && c->printout == t;
+  const bool fuse = c->mixed() && !c->walls() && !last && !output && !due(c, t + 1);
   {
     Timed tm(c, 3);
-    launch_correct(g, c->st);
+    if (fuse) {
+      launch_correct_predict(gear_args(c, t + 1), c->st);
+      c->predicted = true;
+    } else {
+      launch_correct(gear_args(c, t), c->st);
+    }
     c->stats.launches++;
   }
   if (c->walls()) {
@@ -482,7 +512,7 @@ md_status step_once(md_ctx* c) {
       c->stats.launches++;
     }
   }
-  if (c->cfg.output_timesteps > 0 && c->printout == t) {
+  if (output) {
     md_status s = push_record(c, t);
     if (s != MD_OK) return s;
     c->printout += c->cfg.output_timesteps;
@@ -603,8 +633,12 @@ md_status md_upload_state(md_ctx* c, const double* pos4, const double* vel3, con
                           const double* b3, const double* c3) {
   if (!c) return MD_BAD_ARGUMENT;
   const size_t N = (size_t)c->n;
-  if (pos4)
+  if (pos4) {
+    int all = 1;
+    for (size_t i = 0; i < N && all; i++) all = (int)pos4[4 * i + 3] == SP_NG;
+    c->all_ng = all;
     CK(cudaMemcpyAsync(c->pos, pos4, sizeof(double) * 4 * N, cudaMemcpyHostToDevice, c->st), "upload");
+  }
   if (vel3)
     CK(cudaMemcpyAsync(c->vel, vel3, sizeof(double) * 3 * N, cudaMemcpyHostToDevice, c->st), "upload");
   if (a3) CK(cudaMemcpyAsync(c->acc, a3, sizeof(double) * 3 * N, cudaMemcpyHostToDevice, c->st), "upload");
@@ -653,6 +687,7 @@ md_status md_begin(md_ctx* c, float vxcm) {
   c->printout = c->cfg.output_timesteps;
   c->nrec = 0;
   c->begun = true;
+  c->predicted = false;
   md_status s = rebuild(c, 0);
   if (s != MD_OK) return s;
   if (c->cfg.output_timesteps > 0) {
@@ -671,7 +706,7 @@ md_status md_step(md_ctx* c, int nsteps) {
   {
     Timed whole(c, 5);
     for (int s = 0; s < nsteps; s++) {
-      md_status r = step_once(c);
+      md_status r = step_once(c, s == nsteps - 1);
       if (r != MD_OK) return r;
     }
   }
@@ -771,6 +806,14 @@ md_status md_neighbor_list(md_ctx* c, int which, int* rows, signed char* images,
 md_status md_get_stats(const md_ctx* c, md_stats* out) {
   if (!c || !out) return MD_BAD_ARGUMENT;
   *out = c->stats;
+  if (c->lj.skin) {
+    // skin refreshes since the last list build are still on the device
+    int sk[4];
+    if (cudaStreamSynchronize(c->st) != cudaSuccess ||
+        cudaMemcpy(sk, c->lj.skin, sizeof(sk), cudaMemcpyDeviceToHost) != cudaSuccess)
+      return MD_CUDA_ERROR;
+    out->list_trips += sk[3];
+  }
   return MD_OK;
 }
 

@@ -22,10 +22,18 @@
 #include "md_forces.h"
 #include "md_neighbor.cuh"
 #include "md_potential.cuh"
+#include "md_tma.cuh"
 
 namespace mdgb {
 
 namespace {
+
+// current FP32 position of atom j (the FP32 copy when there is one)
+__device__ __forceinline__ float4 cur_pos(const md_double4* pos, const float4* posf, int j) {
+  if (posf) return posf[j];
+  const md_double4 p = pos[j];
+  return make_float4((float)p.x, (float)p.y, (float)p.z, __int_as_float((int)p.w));
+}
 
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
@@ -57,10 +65,10 @@ __device__ __forceinline__ void block_partial(double (&v)[NV], double* out) {
 // ------------------------------------------------------------------ LJ FP64
 template <bool ENERGY>
 __global__ void __launch_bounds__(128)
-    k_lj_fp64(const md_double4* __restrict__ pos, double* __restrict__ f3, int n,
-              const uint32_t* __restrict__ list, const int* __restrict__ len, RowWalker w,
-              const int* __restrict__ status, double rcutsq, Species sp,
-              double* __restrict__ epart) {
+    k_lj_fp64(const md_double4* __restrict__ pos, double* __restrict__ f3, int n, int ld,
+              uint32_t* __restrict__ list, int* __restrict__ len, RowWalker w, int* skin,
+              int parity, int cap, float rv2, float4* __restrict__ pos_build, double rcutsq,
+              Species sp, double* __restrict__ epart) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   double ev[3] = {0.0, 0.0, 0.0};
   if (i < n) {
@@ -98,17 +106,36 @@ __global__ void __launch_bounds__(128)
         }
       }
     };
-    if (!(*status & ST_LIST_TRIP)) {
+    const bool tripped = (skin[parity] | skin[2]) != 0;
+    if (!tripped) {
       const int L = len[i];
       for (int k = 0; k < L; k++) {
-        const uint32_t e = list[(size_t)k * n + i];
+        const uint32_t e = list[(size_t)k * ld + i];
         visit(entry_index(e), entry_img(e, 0), entry_img(e, 1), entry_img(e, 2), (e >> 26) != 0);
       }
     } else {
+      // skin exceeded: walk the full candidate row (the reference's row,
+      // same order) and refresh this atom's compact row at the current
+      // positions, so that the following steps use the compact row again
+      const float4 pc = cur_pos(pos, (const float4*)nullptr, i);
+      int kept = 0;
       walk_row(w, pos, i, [&](int m, int ix, int iy, int iz) {
         visit(m, ix, iy, iz, w.g.periodic && (ix | iy | iz));
+        const float4 pm = cur_pos(pos, (const float4*)nullptr, m);
+        const float dx = pc.x - (pm.x + (float)ix * w.g.box_f);
+        const float dy = pc.y - (pm.y + (float)iy * w.g.box_f);
+        const float dz = pc.z - (pm.z + (float)iz * w.g.box_f);
+        if (dx * dx + dy * dy + dz * dz < rv2) {
+          if (kept < cap) list[(size_t)kept * ld + i] = pack_entry(m, ix, iy, iz);
+          kept++;
+        }
       });
+      if (kept > cap) atomicOr(&skin[2], 1);
+      len[i] = kept < cap ? kept : cap;
+      pos_build[i] = pc;
+      if (i == 0) atomicAdd(&skin[3], 1);
     }
+    if (i == 0) skin[parity ^ 1] = 0;  // the next step's flag starts clear
     f3[3 * i] = fx;
     f3[3 * i + 1] = fy;
     f3[3 * i + 2] = fz;
@@ -124,94 +151,275 @@ __device__ __forceinline__ void kahan(float& hi, float& lo, float x) {
   hi = t;
 }
 
+// Is the FP32 pair (i, j) inside rcut?  Pairs within a relative 1e-5 band of
+// the cutoff are decided in FP64 exactly as the FP64 path decides them.
+__device__ __forceinline__ bool lj_inside(float r2, float rc_lo, float rc_hi,
+                                          const md_double4* pos, int i, int j, bool img,
+                                          int ix, int iy, int iz, const Grid& g,
+                                          double rcutsq) {
+  if (r2 >= rc_hi) return false;
+  if (r2 <= rc_lo) return true;
+  const md_double4 a = pos[i], b = pos[j];
+  double xj = b.x, yj = b.y, zj = b.z;
+  if (img) {
+    xj = xadd(xj, (double)ix * g.box);
+    yj = xadd(yj, (double)iy * g.box);
+    zj = xadd(zj, (double)iz * g.box);
+  }
+  return norm2_exact(xsub(a.x, xj), xsub(a.y, yj), xsub(a.z, zj)) < rcutsq;
+}
+
+// One atom of the FP32 LJ force: the compact row, or (skin tripped) the full
+// candidate row with a refresh of the compact row.  ev: E, E_shifted, W.
+template <bool ENERGY>
+__device__ __forceinline__ void lj32_atom(int i, const float4* __restrict__ posf,
+                                          const md_double4* __restrict__ pos,
+                                          double* __restrict__ f3, int ld,
+                                          uint32_t* __restrict__ list, int* __restrict__ len,
+                                          const RowWalker& w, bool tripped, int* skin, int cap,
+                                          float rv2, float4* __restrict__ pos_build,
+                                          double rcutsq, const Species& sp, double* ev) {
+  const float4 pi = posf[i];
+  const int ti = __float_as_int(pi.w);
+  const float rc2 = (float)rcutsq;
+  const float rc_lo = rc2 * (1.0f - 1e-5f), rc_hi = rc2 * (1.0f + 1e-5f);
+  const float Lf = w.g.box_f, Llo = w.g.box_lo;
+  float hx = 0.f, hy = 0.f, hz = 0.f, lx = 0.f, ly = 0.f, lz = 0.f;
+  float cx = 0.f, cy = 0.f, cz = 0.f;
+  int inchunk = 0;
+  auto visit = [&](int j, int ix, int iy, int iz, bool img) {
+    const float4 pj = posf[j];
+    float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+    if (img) {
+      dx = (pi.x - fmaf((float)ix, Lf, pj.x)) - (float)ix * Llo;
+      dy = (pi.y - fmaf((float)iy, Lf, pj.y)) - (float)iy * Llo;
+      dz = (pi.z - fmaf((float)iz, Lf, pj.z)) - (float)iz * Llo;
+    }
+    const float r2 = dx * dx + dy * dy + dz * dz;
+    if (!lj_inside(r2, rc_lo, rc_hi, pos, i, j, img, ix, iy, iz, w.g, rcutsq)) return;
+    const int tj = __float_as_int(pj.w);
+    if (tj != SP_NG && ti != SP_NG) return;
+    const int sel = lj_select(ti, tj);
+    const float sig = sp.sig[sel], eps = sp.eps[sel];
+    const float inv = 1.0f / r2;
+    const float sr2 = sig * sig * inv;
+    const float sr6 = sr2 * sr2 * sr2;
+    const float fij = (24.0f * eps) * inv * sr6 * (2.0f * sr6 - 1.0f);
+    cx = fmaf(dx, fij, cx);
+    cy = fmaf(dy, fij, cy);
+    cz = fmaf(dz, fij, cz);
+    if (ENERGY) {
+      const float src2 = sig * sig / rc2;
+      const float src6 = src2 * src2 * src2;
+      const float e = 2.0f * eps * (sr6 * sr6 - sr6);
+      ev[0] += (double)e;
+      ev[1] += (double)e - (double)(2.0f * eps * (src6 * src6 - src6));
+      ev[2] += 0.5 * (double)(r2 * fij);
+    }
+    if (++inchunk == 16) {
+      kahan(hx, lx, cx);
+      kahan(hy, ly, cy);
+      kahan(hz, lz, cz);
+      cx = cy = cz = 0.f;
+      inchunk = 0;
+    }
+  };
+  if (!tripped) {
+    const int L = len[i];
+    for (int k = 0; k < L; k++) {
+      const uint32_t e = list[(size_t)k * ld + i];
+      visit(entry_index(e), entry_img(e, 0), entry_img(e, 1), entry_img(e, 2), (e >> 26) != 0);
+    }
+  } else {
+    // skin exceeded: walk the full candidate row (the reference's row, same
+    // order) and refresh this atom's compact row at the current positions
+    const float4 pc = pi;
+    int kept = 0;
+    walk_row(w, pos, i, [&](int m, int ix, int iy, int iz) {
+      visit(m, ix, iy, iz, w.g.periodic && (ix | iy | iz));
+      const float4 pm = posf[m];
+      const float dx = pc.x - (pm.x + (float)ix * w.g.box_f);
+      const float dy = pc.y - (pm.y + (float)iy * w.g.box_f);
+      const float dz = pc.z - (pm.z + (float)iz * w.g.box_f);
+      if (dx * dx + dy * dy + dz * dz < rv2) {
+        if (kept < cap) list[(size_t)kept * ld + i] = pack_entry(m, ix, iy, iz);
+        kept++;
+      }
+    });
+    if (kept > cap) atomicOr(&skin[2], 1);
+    len[i] = kept < cap ? kept : cap;
+    pos_build[i] = pc;
+  }
+  kahan(hx, lx, cx);
+  kahan(hy, ly, cy);
+  kahan(hz, lz, cz);
+  f3[3 * i] = (double)hx - (double)lx;
+  f3[3 * i + 1] = (double)hy - (double)ly;
+  f3[3 * i + 2] = (double)hz - (double)lz;
+}
+
+// out-of-line copy of the tripped path for the TMA kernel (keeps its
+// register allocation free of the rarely used full-row walk)
+__device__ __noinline__ void lj32_atom_tripped(int i, const float4* posf, const md_double4* pos,
+                                              double* f3, int ld, uint32_t* list, int* len,
+                                              const RowWalker& w, int* skin, int cap, float rv2,
+                                              float4* pos_build, double rcutsq,
+                                              const Species& sp) {
+  double ev[3];
+  lj32_atom<false>(i, posf, pos, f3, ld, list, len, w, true, skin, cap, rv2, pos_build, rcutsq,
+                   sp, ev);
+}
+
 template <bool ENERGY>
 __global__ void __launch_bounds__(128)
     k_lj_fp32(const float4* __restrict__ posf, const md_double4* __restrict__ pos,
-              double* __restrict__ f3, int n, const uint32_t* __restrict__ list,
-              const int* __restrict__ len, RowWalker w, const int* __restrict__ status,
-              double rcutsq, Species sp, double* __restrict__ epart) {
+              double* __restrict__ f3, int n, int ld, uint32_t* __restrict__ list,
+              int* __restrict__ len, RowWalker w, int* skin, int parity, int cap, float rv2,
+              float4* __restrict__ pos_build, double rcutsq, Species sp,
+              double* __restrict__ epart) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   double ev[3] = {0.0, 0.0, 0.0};
-  if (i < n) {
-    const float4 pi = posf[i];
-    const int ti = __float_as_int(pi.w);
-    const float rc2 = (float)rcutsq;
-    const float band = 1e-5f * rc2;
-    const float Lf = w.g.box_f, Llo = w.g.box_lo;
-    float hx = 0.f, hy = 0.f, hz = 0.f, lx = 0.f, ly = 0.f, lz = 0.f;
+  const bool tripped = (skin[parity] | skin[2]) != 0;
+  if (i < n)
+    lj32_atom<ENERGY>(i, posf, pos, f3, ld, list, len, w, tripped, skin, cap, rv2, pos_build,
+                      rcutsq, sp, ev);
+  if (tripped && i == 0) atomicAdd(&skin[3], 1);
+  if (i == 0) skin[parity ^ 1] = 0;  // the next step's flag starts clear
+  if (ENERGY) block_partial<3>(ev, epart);
+}
+
+// The FP32 LJ force with the compact list streamed through shared memory by
+// TMA: each block of 128 atoms walks its list in tiles of 16 slots x 128
+// atoms (8 KB), double-buffered and synchronised with mbarriers, so that
+// list traffic is bulk and in flight while the pairs of the previous tile
+// are computed.  Positions are gathered through L1.  Each tile's FP32 sums
+// are folded into a compensated (Kahan) FP32 pair.  ALL_NG: every atom is of
+// the NG species (one parameter set, no type tests).
+template <bool ALL_NG>
+__global__ void __launch_bounds__(kListTileAtoms, 8)
+    k_lj_tma(const __grid_constant__ CUtensorMap tmap, const float4* __restrict__ posf,
+             const md_double4* __restrict__ pos, double* __restrict__ f3, int n, int ld,
+             uint32_t* __restrict__ list, int* __restrict__ len, RowWalker w, int* skin,
+             int parity, int cap, float rv2, float4* __restrict__ pos_build, double rcutsq,
+             Species sp, int* status) {
+  __shared__ __align__(128) uint32_t tile[2][kListTileSlots][kListTileAtoms];
+  __shared__ __align__(8) uint64_t bar[2];
+  __shared__ int s_max[kListTileAtoms / 32];
+  const int tid = threadIdx.x;
+  const int i = blockIdx.x * kListTileAtoms + tid;
+  const bool tripped = (skin[parity] | skin[2]) != 0;
+  if (tripped) {
+    if (i < n)
+      lj32_atom_tripped(i, posf, pos, f3, ld, list, len, w, skin, cap, rv2, pos_build, rcutsq,
+                        sp);
+    if (i == 0) {
+      atomicAdd(&skin[3], 1);
+      skin[parity ^ 1] = 0;
+    }
+    return;
+  }
+  const int L = i < n ? len[i] : 0;
+  int m = L;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((tid & 31) == 0) s_max[tid >> 5] = m;
+  if (tid == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  int maxlen = s_max[0];
+#pragma unroll
+  for (int k = 1; k < kListTileAtoms / 32; k++) maxlen = max(maxlen, s_max[k]);
+  const int T = (maxlen + kListTileSlots - 1) / kListTileSlots;
+  constexpr uint32_t kTileBytes = kListTileSlots * kListTileAtoms * 4;
+  const int x0 = blockIdx.x * kListTileAtoms;
+  if (tid == 0) {
+    for (int t = 0; t < 2 && t < T; t++) {
+      mbar_expect_tx(&bar[t], kTileBytes);
+      tma_load_2d(&tile[t][0][0], &tmap, x0, t * kListTileSlots, &bar[t]);
+    }
+  }
+  const float4 pi = i < n ? posf[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+  const int ti = __float_as_int(pi.w);
+  const float rc2 = (float)rcutsq;
+  const float rc_lo = rc2 * (1.0f - 1e-5f), rc_hi = rc2 * (1.0f + 1e-5f);
+  const float Lf = w.g.box_f, Llo = w.g.box_lo;
+  // NG-NG parameters, and the two cross parameter sets for mixed systems
+  const float s2_ng = sp.sig[2] * sp.sig[2], c_ng = 24.0f * sp.eps[2];
+  const float s2_n = sp.sig[0] * sp.sig[0], c_n = 24.0f * sp.eps[0];
+  const float s2_o = sp.sig[1] * sp.sig[1], c_o = 24.0f * sp.eps[1];
+  float hx = 0.f, hy = 0.f, hz = 0.f, lx = 0.f, ly = 0.f, lz = 0.f;
+  bool ok = true;
+  for (int t = 0; t < T; t++) {
+    const int b = t & 1;
+    if (!mbar_wait(&bar[b], (uint32_t)((t >> 1) & 1), status)) {
+      ok = false;
+      break;
+    }
+    const int kmax = min(kListTileSlots, L - t * kListTileSlots);
     float cx = 0.f, cy = 0.f, cz = 0.f;
-    int inchunk = 0;
-    auto visit = [&](int j, int ix, int iy, int iz, bool img) {
-      const float4 pj = posf[j];
-      float dx, dy, dz;
-      if (!img) {
-        dx = pi.x - pj.x;
-        dy = pi.y - pj.y;
-        dz = pi.z - pj.z;
-      } else {
-        dx = (pi.x - fmaf((float)ix, Lf, pj.x)) - (float)ix * Llo;
-        dy = (pi.y - fmaf((float)iy, Lf, pj.y)) - (float)iy * Llo;
-        dz = (pi.z - fmaf((float)iz, Lf, pj.z)) - (float)iz * Llo;
+    // every slot is evaluated by every lane (no divergence); slots past the
+    // atom's row read the atom itself and contribute zero
+#pragma unroll 4
+    for (int kk = 0; kk < kListTileSlots; kk++) {
+      const bool valid = kk < kmax;
+      const uint32_t e = valid ? tile[b][kk][tid] : (uint32_t)(i < n ? i : 0);
+      const int j = entry_index(e);
+      const float4 pj = __ldg(&posf[j]);
+      float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+      if (e >> 26) {  // periodic image (rare: boundary cells only)
+        const float fx = (float)entry_img(e, 0), fy = (float)entry_img(e, 1),
+                    fz = (float)entry_img(e, 2);
+        dx = (pi.x - fmaf(fx, Lf, pj.x)) - fx * Llo;
+        dy = (pi.y - fmaf(fy, Lf, pj.y)) - fy * Llo;
+        dz = (pi.z - fmaf(fz, Lf, pj.z)) - fz * Llo;
       }
-      const float r2 = dx * dx + dy * dy + dz * dz;
-      if (r2 >= rc2 + band) return;
-      if (r2 > rc2 - band) {
-        // borderline: decide inclusion exactly as the FP64 path does
-        const md_double4 a = pos[i], b = pos[j];
-        double xj = b.x, yj = b.y, zj = b.z;
-        if (img) {
-          xj = xadd(xj, (double)ix * w.g.box);
-          yj = xadd(yj, (double)iy * w.g.box);
-          zj = xadd(zj, (double)iz * w.g.box);
-        }
-        if (norm2_exact(xsub(a.x, xj), xsub(a.y, yj), xsub(a.z, zj)) >= rcutsq) return;
+      const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+      float s2 = s2_ng, c24 = c_ng;
+      bool use = valid;
+      if (!ALL_NG) {
+        const int tj = __float_as_int(pj.w);
+        use = use && (tj == SP_NG || ti == SP_NG);
+        const int sel = lj_select(ti, tj);
+        s2 = sel == SP_N ? s2_n : (sel == SP_O ? s2_o : s2_ng);
+        c24 = sel == SP_N ? c_n : (sel == SP_O ? c_o : c_ng);
       }
-      const int tj = __float_as_int(pj.w);
-      if (tj != SP_NG && ti != SP_NG) return;
-      const int sel = lj_select(ti, tj);
-      const float sig = sp.sig[sel], eps = sp.eps[sel];
-      const float inv = 1.0f / r2;
-      const float sr2 = sig * sig * inv;
+      const float inv = rcp_approx(r2);
+      const float sr2 = s2 * inv;
       const float sr6 = sr2 * sr2 * sr2;
-      const float fij = (24.0f * eps) * inv * sr6 * (2.0f * sr6 - 1.0f);
+      float fij = c24 * inv * sr6 * fmaf(2.0f, sr6, -1.0f);
+      bool in = r2 <= rc_lo;
+      if (use && !in && r2 < rc_hi)  // within 1e-5 of the cutoff: decide in FP64
+        in = lj_inside(r2, rc_lo, rc_hi, pos, i, j, (e >> 26) != 0, entry_img(e, 0),
+                       entry_img(e, 1), entry_img(e, 2), w.g, rcutsq);
+      fij = (use && in) ? fij : 0.0f;
       cx = fmaf(dx, fij, cx);
       cy = fmaf(dy, fij, cy);
       cz = fmaf(dz, fij, cz);
-      if (ENERGY) {
-        const float src2 = sig * sig / rc2;
-        const float src6 = src2 * src2 * src2;
-        const float e = 2.0f * eps * (sr6 * sr6 - sr6);
-        ev[0] += (double)e;
-        ev[1] += (double)e - (double)(2.0f * eps * (src6 * src6 - src6));
-        ev[2] += 0.5 * (double)(r2 * fij);
-      }
-      if (++inchunk == 16) {
-        kahan(hx, lx, cx);
-        kahan(hy, ly, cy);
-        kahan(hz, lz, cz);
-        cx = cy = cz = 0.f;
-        inchunk = 0;
-      }
-    };
-    if (!(*status & ST_LIST_TRIP)) {
-      const int L = len[i];
-      for (int k = 0; k < L; k++) {
-        const uint32_t e = list[(size_t)k * n + i];
-        visit(entry_index(e), entry_img(e, 0), entry_img(e, 1), entry_img(e, 2), (e >> 26) != 0);
-      }
-    } else {
-      walk_row(w, pos, i, [&](int m, int ix, int iy, int iz) {
-        visit(m, ix, iy, iz, w.g.periodic && (ix | iy | iz));
-      });
     }
     kahan(hx, lx, cx);
     kahan(hy, ly, cy);
     kahan(hz, lz, cz);
+    __syncthreads();  // everyone is done with buffer b
+    if (tid == 0 && t + 2 < T) {
+      fence_proxy_async();
+      mbar_expect_tx(&bar[b], kTileBytes);
+      tma_load_2d(&tile[b][0][0], &tmap, x0, (t + 2) * kListTileSlots, &bar[b]);
+    }
+  }
+  if (!ok) {
+    // give copies still in flight a bounded chance to land, then leave
+    for (int t = 0; t < 2 && t < T; t++) mbar_wait(&bar[t], 0, status);
+    return;
+  }
+  if (i < n) {
     f3[3 * i] = (double)hx - (double)lx;
     f3[3 * i + 1] = (double)hy - (double)ly;
     f3[3 * i + 2] = (double)hz - (double)lz;
   }
-  if (ENERGY) block_partial<3>(ev, epart);
+  if (i == 0) skin[parity ^ 1] = 0;  // the next step's flag starts clear
 }
 
 // --------------------------------------------------------------- bond order
@@ -265,7 +473,7 @@ struct PosT<float> {
 template <typename T>
 __global__ void __launch_bounds__(128)
     k_mb_short(const md_double4* __restrict__ pos, const float4* __restrict__ posf, int n,
-               const uint32_t* __restrict__ list, const int* __restrict__ len, Grid g,
+               int ld, const uint32_t* __restrict__ list, const int* __restrict__ len, Grid g,
                double rcutsq, uint32_t* __restrict__ sl, int* __restrict__ slen) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -277,7 +485,7 @@ __global__ void __launch_bounds__(128)
   int cnt = 0;
   const int L = len[i];
   for (int k = 0; k < L; k++) {
-    const uint32_t e = list[(size_t)k * n + i];
+    const uint32_t e = list[(size_t)k * ld + i];
     const int j = entry_index(e);
     T xj, yj, zj;
     int tj;
@@ -581,18 +789,34 @@ void launch_lj(const ForceArgs& a, bool fp32, bool energy, cudaStream_t st) {
   if (B == 0) return;
   if (!fp32) {
     if (energy)
-      k_lj_fp64<true><<<B, T, 0, st>>>(a.pos, a.f3, a.n, a.list, a.len, a.walker, a.status,
-                                       a.rcutsq, a.sp, a.epart);
+      k_lj_fp64<true><<<B, T, 0, st>>>(a.pos, a.f3, a.n, a.ld, a.list, a.len, a.walker, a.skin,
+                                       a.parity, a.cap, a.rv2, a.pos_build, a.rcutsq, a.sp,
+                                       a.epart);
     else
-      k_lj_fp64<false><<<B, T, 0, st>>>(a.pos, a.f3, a.n, a.list, a.len, a.walker, a.status,
-                                        a.rcutsq, a.sp, a.epart);
+      k_lj_fp64<false><<<B, T, 0, st>>>(a.pos, a.f3, a.n, a.ld, a.list, a.len, a.walker, a.skin,
+                                        a.parity, a.cap, a.rv2, a.pos_build, a.rcutsq, a.sp,
+                                        a.epart);
+  } else if (!energy && a.tmap) {
+    const int TB = nblk(a.n, kListTileAtoms);
+    if (a.all_ng)
+      k_lj_tma<true><<<TB, kListTileAtoms, 0, st>>>(*a.tmap, a.posf, a.pos, a.f3, a.n, a.ld,
+                                                    a.list, a.len, a.walker, a.skin, a.parity,
+                                                    a.cap, a.rv2, a.pos_build, a.rcutsq, a.sp,
+                                                    a.status);
+    else
+      k_lj_tma<false><<<TB, kListTileAtoms, 0, st>>>(*a.tmap, a.posf, a.pos, a.f3, a.n, a.ld,
+                                                     a.list, a.len, a.walker, a.skin, a.parity,
+                                                     a.cap, a.rv2, a.pos_build, a.rcutsq, a.sp,
+                                                     a.status);
   } else {
     if (energy)
-      k_lj_fp32<true><<<B, T, 0, st>>>(a.posf, a.pos, a.f3, a.n, a.list, a.len, a.walker,
-                                       a.status, a.rcutsq, a.sp, a.epart);
+      k_lj_fp32<true><<<B, T, 0, st>>>(a.posf, a.pos, a.f3, a.n, a.ld, a.list, a.len, a.walker,
+                                       a.skin, a.parity, a.cap, a.rv2, a.pos_build, a.rcutsq,
+                                       a.sp, a.epart);
     else
-      k_lj_fp32<false><<<B, T, 0, st>>>(a.posf, a.pos, a.f3, a.n, a.list, a.len, a.walker,
-                                        a.status, a.rcutsq, a.sp, a.epart);
+      k_lj_fp32<false><<<B, T, 0, st>>>(a.posf, a.pos, a.f3, a.n, a.ld, a.list, a.len, a.walker,
+                                        a.skin, a.parity, a.cap, a.rv2, a.pos_build, a.rcutsq,
+                                        a.sp, a.epart);
   }
 }
 
@@ -602,7 +826,7 @@ int mb_blocks(int n) { return nblk(n, 4); }
 template <typename T>
 static void launch_mb_t(const MbArgs& a, bool energy, cudaStream_t st) {
   if (a.n <= 0) return;
-  k_mb_short<T><<<nblk(a.n, 128), 128, 0, st>>>(a.pos, a.posf, a.n, a.list, a.len, a.grid,
+  k_mb_short<T><<<nblk(a.n, 128), 128, 0, st>>>(a.pos, a.posf, a.n, a.ld, a.list, a.len, a.grid,
                                                 a.rcutsq, a.sl, a.slen);
   const int B = nblk(a.n, 4);
   T* xsi = (T*)a.xsi;

@@ -9,10 +9,18 @@ struct ForceArgs {
   const float4* posf;   // FP32 copy (precision form)
   double* f3;
   int n;
-  const uint32_t* list;
-  const int* len;
-  RowWalker walker;     // full rows, used when the list is tripped
-  const int* status;
+  uint32_t* list;       // compact rows (rewritten per atom after a skin trip)
+  int* len;
+  int ld;               // list[k * ld + i]
+  const CUtensorMap* tmap;  // TMA descriptor of the list (NULL: no TMA kernel)
+  int all_ng;           // every atom is of the NG species
+  int* status;
+  RowWalker walker;     // full rows, walked when the skin is tripped
+  int* skin;            // NeighborList::skin
+  int parity;           // step parity: skin[parity] is this step's trip flag
+  int cap;              // compact row capacity
+  float rv2;            // compact filter radius squared
+  float4* pos_build;    // skin reference positions
   double rcutsq;
   Species sp;
   double* epart;        // 3 doubles per block when energy is requested
@@ -23,8 +31,9 @@ struct MbArgs {
   const float4* posf;
   double* f3;
   int n;                // many-body atoms [0, n)
-  const uint32_t* list; // full candidate rows
+  const uint32_t* list; // full candidate rows, list[k * ld + i]
   const int* len;
+  int ld;
   Grid grid;
   const int* cell3;     // build-time cells of the many-body list
   const int* ref_rows;  // or: rows in the reference layout (membership by scan)

@@ -38,17 +38,23 @@ __device__ __forceinline__ void skin_check(const GearArgs& a, int i, double x, d
   if (a.pos_build) {
     float4 pb = a.pos_build[i];
     float dx = (float)x - pb.x, dy = (float)y - pb.y, dz = (float)z - pb.z;
-    if (dx * dx + dy * dy + dz * dz > a.trip2) atomicOr(a.status, ST_LIST_TRIP);
+    if (dx * dx + dy * dy + dz * dz > a.trip2) *a.trip = 1;
   }
 }
 
-// cpu/common/Device.cpp:17-39
-__global__ void k_predict(GearArgs a) {
+enum { G_PREDICT = 0, G_CORRECT = 1, G_CORRECT_PREDICT = 2 };
+
+// cpu/common/Device.cpp:17-39 (predict) and :44-120 (correct).  EXACT keeps
+// every rounding of the reference; otherwise products fuse into FMAs and
+// F/m becomes F * (1/m) (the precision form, still FP64 state).
+template <int MODE, bool EXACT>
+__global__ void __launch_bounds__(256) k_gear(GearArgs a) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.n) return;
   const GearCoef k = a.k;
   md_double4 r = a.pos[i];
-  double v[3], ac[3], b[3], c[3];
+  const int type = (int)r.w;
+  double rr[3] = {r.x, r.y, r.z}, v[3], ac[3], b[3], c[3];
 #pragma unroll
   for (int d = 0; d < 3; d++) {
     v[d] = a.vel[3 * i + d];
@@ -56,65 +62,74 @@ __global__ void k_predict(GearArgs a) {
     b[d] = a.b[3 * i + d];
     c[d] = a.c[3 * i + d];
   }
-  double rr[3] = {r.x, r.y, r.z};
+  if (MODE != G_PREDICT) {
+    const double mass = mass_of(type, a.sp);
+    const double im = type == SP_N ? a.inv_mass[0] : (type == SP_O ? a.inv_mass[1] : a.inv_mass[2]);
 #pragma unroll
-  for (int d = 0; d < 3; d++)
-    rr[d] = xadd(xadd(xadd(xadd(rr[d], xmul(k.c1, v[d])), xmul(k.c2, ac[d])), xmul(k.c3, b[d])),
-                 xmul(k.c4, c[d]));
-#pragma unroll
-  for (int d = 0; d < 3; d++) {
-    double nv = xadd(xadd(xadd(v[d], xmul(k.c1, ac[d])), xmul(k.c2, b[d])), xmul(k.c3, c[d]));
-    double na = xadd(xadd(ac[d], xmul(k.c1, b[d])), xmul(k.c2, c[d]));
-    double nb = xadd(b[d], xmul(k.c1, c[d]));
-    a.vel[3 * i + d] = nv;
-    a.acc[3 * i + d] = na;
-    a.b[3 * i + d] = nb;
+    for (int d = 0; d < 3; d++) {
+      const double f = a.f3[3 * i + d];
+      if (EXACT) {
+        const double ai = xdiv(f, mass);
+        const double corr = xsub(ai, ac[d]);
+        rr[d] = xadd(rr[d], xmul(k.cr, corr));
+        v[d] = xadd(v[d], xmul(k.cv, corr));
+        ac[d] = ai;
+        b[d] = xadd(b[d], xmul(k.cb, corr));
+        c[d] = xadd(c[d], xmul(k.cc, corr));
+      } else {
+        const double ai = f * im;
+        const double corr = ai - ac[d];
+        rr[d] = fma(k.cr, corr, rr[d]);
+        v[d] = fma(k.cv, corr, v[d]);
+        ac[d] = ai;
+        b[d] = fma(k.cb, corr, b[d]);
+        c[d] = fma(k.cc, corr, c[d]);
+      }
+    }
+    if (MODE == G_CORRECT && a.walls) {
+      const double np = a.npos;
+      bool hit = false;
+      if (rr[0] > np && rr[1] > 0) { hit = true; v[0] = xmul(-v[0], (double)a.energy_loss); rr[0] = np; }
+      if (rr[0] > np && rr[1] < 0) { hit = true; rr[0] = -np; }
+      if (rr[0] < -np) { hit = true; v[0] = -v[0]; rr[0] = -np; }
+      if (fabs(rr[1]) > np) { hit = true; v[1] = -v[1]; rr[1] = xmul(np, xdiv(rr[1], fabs(rr[1]))); }
+      if (fabs(rr[2]) > np) { hit = true; v[2] = -v[2]; rr[2] = xmul(np, xdiv(rr[2], fabs(rr[2]))); }
+      if (hit) atomicOr(a.wall_flag, 1);
+    }
+    if (!(isfinite(rr[0]) && isfinite(rr[1]) && isfinite(rr[2]) && isfinite(v[0]) &&
+          isfinite(v[1]) && isfinite(v[2])))
+      atomicOr(a.status, ST_NONFINITE);
   }
-  r.x = rr[0];
-  r.y = rr[1];
-  r.z = rr[2];
-  a.pos[i] = r;
-  skin_check(a, i, rr[0], rr[1], rr[2], (int)r.w);
-}
-
-// cpu/common/Device.cpp:44-120
-__global__ void k_correct(GearArgs a) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= a.n) return;
-  const GearCoef k = a.k;
-  md_double4 r = a.pos[i];
-  const double mass = mass_of((int)r.w, a.sp);
-  double rr[3] = {r.x, r.y, r.z}, v[3], ac[3], corr[3];
+  if (MODE != G_CORRECT) {
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+      if (EXACT) {
+        rr[d] = xadd(xadd(xadd(xadd(rr[d], xmul(k.c1, v[d])), xmul(k.c2, ac[d])),
+                          xmul(k.c3, b[d])),
+                     xmul(k.c4, c[d]));
+        v[d] = xadd(xadd(xadd(v[d], xmul(k.c1, ac[d])), xmul(k.c2, b[d])), xmul(k.c3, c[d]));
+        ac[d] = xadd(xadd(ac[d], xmul(k.c1, b[d])), xmul(k.c2, c[d]));
+        b[d] = xadd(b[d], xmul(k.c1, c[d]));
+      } else {
+        rr[d] = fma(k.c4, c[d], fma(k.c3, b[d], fma(k.c2, ac[d], fma(k.c1, v[d], rr[d]))));
+        v[d] = fma(k.c3, c[d], fma(k.c2, b[d], fma(k.c1, ac[d], v[d])));
+        ac[d] = fma(k.c2, c[d], fma(k.c1, b[d], ac[d]));
+        b[d] = fma(k.c1, c[d], b[d]);
+      }
+    }
+  }
 #pragma unroll
   for (int d = 0; d < 3; d++) {
-    ac[d] = xdiv(a.f3[3 * i + d], mass);
-    corr[d] = xsub(ac[d], a.acc[3 * i + d]);
-    rr[d] = xadd(rr[d], xmul(k.cr, corr[d]));
-    v[d] = xadd(a.vel[3 * i + d], xmul(k.cv, corr[d]));
+    a.vel[3 * i + d] = v[d];
     a.acc[3 * i + d] = ac[d];
-    a.b[3 * i + d] = xadd(a.b[3 * i + d], xmul(k.cb, corr[d]));
-    a.c[3 * i + d] = xadd(a.c[3 * i + d], xmul(k.cc, corr[d]));
+    a.b[3 * i + d] = b[d];
+    if (MODE != G_PREDICT) a.c[3 * i + d] = c[d];
   }
-  if (a.walls) {
-    const double np = a.npos;
-    bool hit = false;
-    if (rr[0] > np && rr[1] > 0) { hit = true; v[0] = xmul(-v[0], (double)a.energy_loss); rr[0] = np; }
-    if (rr[0] > np && rr[1] < 0) { hit = true; rr[0] = -np; }
-    if (rr[0] < -np) { hit = true; v[0] = -v[0]; rr[0] = -np; }
-    if (fabs(rr[1]) > np) { hit = true; v[1] = -v[1]; rr[1] = xmul(np, xdiv(rr[1], fabs(rr[1]))); }
-    if (fabs(rr[2]) > np) { hit = true; v[2] = -v[2]; rr[2] = xmul(np, xdiv(rr[2], fabs(rr[2]))); }
-    if (hit) atomicOr(a.wall_flag, 1);
-  }
-#pragma unroll
-  for (int d = 0; d < 3; d++) a.vel[3 * i + d] = v[d];
   r.x = rr[0];
   r.y = rr[1];
   r.z = rr[2];
   a.pos[i] = r;
-  if (!(isfinite(rr[0]) && isfinite(rr[1]) && isfinite(rr[2]) && isfinite(v[0]) &&
-        isfinite(v[1]) && isfinite(v[2])))
-    atomicOr(a.status, ST_NONFINITE);
-  skin_check(a, i, rr[0], rr[1], rr[2], (int)r.w);
+  skin_check(a, i, rr[0], rr[1], rr[2], type);
 }
 
 // cpu/common/Device.cpp:125-133
@@ -360,10 +375,25 @@ inline int nblk(long long n, int t) { return (int)((n + t - 1) / t); }
 }  // namespace
 
 void launch_predict(const GearArgs& a, cudaStream_t st) {
-  if (a.n > 0) k_predict<<<nblk(a.n, 256), 256, 0, st>>>(a);
+  if (a.n <= 0) return;
+  if (a.exact)
+    k_gear<G_PREDICT, true><<<nblk(a.n, 256), 256, 0, st>>>(a);
+  else
+    k_gear<G_PREDICT, false><<<nblk(a.n, 256), 256, 0, st>>>(a);
 }
 void launch_correct(const GearArgs& a, cudaStream_t st) {
-  if (a.n > 0) k_correct<<<nblk(a.n, 256), 256, 0, st>>>(a);
+  if (a.n <= 0) return;
+  if (a.exact)
+    k_gear<G_CORRECT, true><<<nblk(a.n, 256), 256, 0, st>>>(a);
+  else
+    k_gear<G_CORRECT, false><<<nblk(a.n, 256), 256, 0, st>>>(a);
+}
+void launch_correct_predict(const GearArgs& a, cudaStream_t st) {
+  if (a.n <= 0) return;
+  if (a.exact)
+    k_gear<G_CORRECT_PREDICT, true><<<nblk(a.n, 256), 256, 0, st>>>(a);
+  else
+    k_gear<G_CORRECT_PREDICT, false><<<nblk(a.n, 256), 256, 0, st>>>(a);
 }
 void launch_accel(const md_double4* pos, double* acc, const double* f3, int n, Species sp,
                   cudaStream_t st) {

@@ -23,7 +23,10 @@ struct GearArgs {
   float4* posf;            // FP32 copy written after the update (may be NULL)
   const float4* pos_build; // skin reference positions (may be NULL)
   float trip2;             // squared skin displacement
+  int* trip;               // trip flag set when an atom exceeds the skin
   int* status;
+  int exact;               // 1: the reference's roundings; 0: FMA and 1/m
+  double inv_mass[3];
   // correct only
   double npos;
   float energy_loss;
@@ -33,6 +36,8 @@ struct GearArgs {
 
 void launch_predict(const GearArgs& a, cudaStream_t st);
 void launch_correct(const GearArgs& a, cudaStream_t st);
+// correct for this step and predict for the next in one pass (no walls)
+void launch_correct_predict(const GearArgs& a, cudaStream_t st);
 void launch_accel(const md_double4* pos, double* acc, const double* f3, int n, Species sp,
                   cudaStream_t st);
 void launch_posf(const md_double4* pos, float4* posf, int n, cudaStream_t st);

@@ -1,5 +1,6 @@
 // Internal host-side interfaces shared by the engine's translation units.
 #pragma once
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -11,11 +12,11 @@ namespace mdgb {
 
 // Device status word bits (set by kernels, read by the host).
 enum : int {
-  ST_LIST_TRIP = 1,       // an atom moved beyond the compact list's skin
   ST_NONFINITE = 2,       // NaN/inf seen in positions or forces
   ST_CELL_OVERFLOW = 4,   // hash table full or cell coordinate out of range
   ST_XI_MISSING = 8,      // bond-order pass 2 needed a xi pass 1 did not make
   ST_WALL_HIT = 16,       // a wall reflection happened (cpu/common/Device.cpp:86-118)
+  ST_TMA_TIMEOUT = 32,    // a bounded wait on a TMA transfer ran out
 };
 
 // Cell structure of one list build (open-addressing table of cells).
@@ -39,12 +40,20 @@ struct NeighborList {
   int* sorted = nullptr;       // atoms grouped by slot, ascending inside a cell
   uint32_t* list = nullptr;
   int* len = nullptr;
+  int ld = 0;                  // leading dimension: list[k * ld + i], ld = n rounded up to 32
   int cap = 0;                 // slots per row allocated
+  CUtensorMap tmap;            // TMA descriptor of the list (compact lists)
+  int tmap_ok = 0;
   long long list_elems = 0;    // allocated list entries
   float4* pos_build = nullptr; // FP32 positions at build time (skin check)
   int compact = 0;             // 1: rows filtered at radius rv; 0: full candidate rows
   float rv = 0.f;
   double trip_dist = 0;        // an atom displaced by more than this trips the list
+  float rv2_keep = 0.f;        // squared filter radius (rv plus FP32 margin)
+  float headroom = 1.25f;      // compact row capacity / longest row at build
+  // skin flags: [0], [1] trip flag of even / odd steps, [2] refresh overflow
+  // (sticky until the next build), [3] refreshes done
+  int* skin = nullptr;
   // host copies of the last build's sizes
   int maxcell = 0, nlargest = 0, nlistsize = 0, max_len = 0;
   long long entries = 0;         // total kept entries

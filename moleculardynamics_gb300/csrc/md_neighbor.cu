@@ -239,6 +239,43 @@ inline int blocks(long long n, int t) { return (int)((n + t - 1) / t); }
 
 }  // namespace
 
+// cuTensorMapEncodeTiled from the driver, looked up once through the runtime
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                                  const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                  const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encode_fn() {
+  static EncodeTiledFn fn = nullptr;
+  static bool tried = false;
+  if (!tried) {
+    tried = true;
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (EncodeTiledFn)p;
+  }
+  return fn;
+}
+
+// TMA descriptor of a compact list: a 2-D uint32 tensor of n atoms (x) by
+// cap slots (y), row stride ld * 4 bytes; tiles of kListTileAtoms x
+// kListTileSlots.  Out-of-range atoms and slots read as zero.
+int encode_list_map(NeighborList& nl) {
+  EncodeTiledFn fn = encode_fn();
+  if (!fn || (nl.ld * 4) % 16 != 0) return 0;
+  cuuint64_t dims[2] = {(cuuint64_t)nl.n, (cuuint64_t)nl.cap};
+  cuuint64_t strides[1] = {(cuuint64_t)nl.ld * 4};
+  cuuint32_t box[2] = {kListTileAtoms, kListTileSlots};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = fn(&nl.tmap, CU_TENSOR_MAP_DATA_TYPE_UINT32, 2, nl.list, dims, strides, box, estr,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                  CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? 1 : 0;
+}
+
 Grid make_grid_reference(double box_list, float rs) {
   Grid g{};
   g.periodic = 0;
@@ -386,14 +423,20 @@ int list_build(NeighborList& nl, md_double4* pos, int n, const Grid& g, int comp
   nl.nlistsize = (int)nls;
   nl.max_len = hc[2];
   int need_cap = hc[2] > 0 ? hc[2] : 1;
-  long long elems = (long long)need_cap * (n > 0 ? n : 1);
+  if (compact) need_cap = (int)(need_cap * nl.headroom) + 8;  // room for skin refreshes
+  nl.ld = ((n > 0 ? n : 1) + 31) / 32 * 32;
+  long long elems = (long long)need_cap * nl.ld;
   if ((e = grow(nl.list, nl.list_elems, elems)) != cudaSuccess) return e;
   nl.cap = need_cap;
+  nl.tmap_ok = compact && n > 0 ? encode_list_map(nl) : 0;
   if (n > 0)
     k_rows<1><<<blocks(n, 128), 128, 0, st>>>(w, pos, nl.pos_build, compact, rv2, g.box_f,
-                                              nl.list, nl.len, n, sc.counts);
+                                              nl.list, nl.len, nl.ld, sc.counts);
   double rc = rcut;
   nl.trip_dist = compact ? 0.5 * ((double)rv - rc) - (double)margin : 1e300;
+  nl.rv2_keep = rv2;
+  if (!nl.skin && (e = cudaMalloc(&nl.skin, sizeof(int) * 4)) != cudaSuccess) return e;
+  cudaMemsetAsync(nl.skin, 0, sizeof(int) * 3, st);
   return (int)cudaGetLastError();
 }
 
@@ -409,7 +452,7 @@ void list_free(NeighborList& nl) {
   for (void* p : {(void*)nl.table.keys, (void*)nl.table.count, (void*)nl.table.start,
                   (void*)nl.table.fill, (void*)nl.atom_slot, (void*)nl.cell3,
                   (void*)nl.unsorted, (void*)nl.sorted, (void*)nl.list, (void*)nl.len,
-                  (void*)nl.pos_build})
+                  (void*)nl.pos_build, (void*)nl.skin})
     if (p) cudaFree(p);
   nl = NeighborList();
 }

@@ -194,6 +194,7 @@ void mdgb_predict(double* r4, double* v3, double* a3, double* b3, double* c3, do
   g.k = gear_coef(dt);
   g.sp = shim_species(s.species);
   g.status = s.flags;
+  g.exact = 1;
   launch_predict(g, s.st);
   SHIM_CK(down(r4, s.pos, 32 * N) && down(v3, s.v[0], 24 * N) && down(a3, s.v[1], 24 * N) &&
               down(b3, s.v[2], 24 * N) && finish(),
@@ -228,6 +229,7 @@ void mdgb_correct(double* r4, double* v3, const double* f3, double* a3, double* 
   g.energy_loss = energy_loss;
   g.walls = 1;
   g.wall_flag = s.flags + 1;
+  g.exact = 1;
   launch_correct(g, s.st);
   int fl[2] = {0, 0};
   SHIM_CK(down(r4, s.pos, 32 * N) && down(v3, s.v[0], 24 * N) && down(a3, s.v[1], 24 * N) &&
@@ -287,6 +289,7 @@ void mdgb_many_body_forces(const double* pos4, double* f3, int n, int nlargestsi
   a.n = n;
   a.list = s.ell;
   a.len = s.len;
+  a.ld = n;
   a.grid = Grid{};
   a.cell3 = nullptr;
   a.ref_rows = s.rows;

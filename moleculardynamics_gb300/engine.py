@@ -57,7 +57,8 @@ class MdStats(C.Structure):
                 ("list_trips", C.c_longlong), ("wall_hits", C.c_longlong),
                 ("missing_xi", C.c_longlong), ("launches", C.c_longlong),
                 ("lj_max_row", C.c_int), ("lj_nlargest", C.c_int), ("mb_nlargest", C.c_int),
-                ("lj_cells", C.c_int), ("mb_cells", C.c_int), ("lj_list_entries", C.c_longlong)]
+                ("lj_cells", C.c_int), ("mb_cells", C.c_int), ("lj_list_entries", C.c_longlong),
+                ("lj_tma", C.c_int)]
 
 
 class ListSettings(C.Structure):

@@ -317,3 +317,47 @@ def test_large_list_checksum(eng, oracle):
     nl = oracle.build_list(pos.copy(), RS, L, periodic=True)
     assert np.array_equal(rows, nl.rows) and np.array_equal(img, nl.code)
     oracle.free_list(nl)
+
+
+def test_skin_trip_refresh_keeps_trajectory_exact(eng, oracle):
+    """Atoms at 1 K on a lattice with 0.5 A noise: the largest speed at the
+    build is tiny, so the reference's schedule (Host.cpp:289) waits long, while
+    the noise accelerates atoms past the list's skin.  The engine then walks
+    the full candidate rows and refreshes the compact rows; the trajectory must
+    still equal the oracle's, which always walks the full rows."""
+    pos, vel, L = argon_fcc(6, temperature=1.0, seed=4, noise=0.5)
+    n = len(pos)
+    rs, rc = RS, RC
+    with _engine(eng, n_lj=n, lj_rs=rs, lj_rcut=rc, periodic=1, box=L) as e:
+        e.upload(pos, vel)
+        e.begin(0.0)
+        e.step(200)
+        gp, gv = e.download()
+        st = e.stats()
+    ref = oracle.run(run_params(n_lj=n, timesteps=200, lj_rs=rs, lj_rcut=rc, periodic=1, box=L),
+                     pos, vel)
+    assert st["list_trips"] > 0
+    assert st["list_builds"] == ref["builds"]
+    assert np.array_equal(gp, ref["pos"]) and np.array_equal(gv, ref["vel"])
+
+
+def test_precision_form_trips_and_tma_path(eng):
+    """Precision form through the TMA kernel, with skin trips: forces stay
+    within 1e-4 of the FP64 path at the same positions."""
+    pos, vel, L = argon_fcc(10, temperature=300.0, seed=6, noise=0.1)
+    n = len(pos)
+    rs, rc = 8.7, 8.5125
+    with _engine(eng, n_lj=n, lj_rs=rs, lj_rcut=rc, periodic=1, box=L,
+                 precision=eng.PREC_MIXED) as e:
+        e.upload(pos, vel)
+        e.begin(0.0)
+        e.step(150)
+        st = e.stats()
+        p, v = e.download()
+        fm, _ = e.compute_forces()
+    with _engine(eng, n_lj=n, lj_rs=rs, lj_rcut=rc, periodic=1, box=L) as e:
+        e.upload(p, v)
+        e.begin(0.0)
+        f64, _ = e.compute_forces()
+    assert st["list_trips"] > 0
+    assert rel_rms(fm, f64) < 1e-4
