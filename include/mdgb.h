@@ -185,6 +185,25 @@ void mdgb_perform_calculations(const double* pos4, const double* vel3, int n, do
                                double* mom_x, double* mom_y, double* mom_z, double* temp);
 /* common/DebugCalculations.h:20 calculatePotentional */
 void mdgb_calculate_potential(const double* pos4, double* vib_lj, double* vib_mb, int n);
+/* Bond-order forces as mdgb_many_body_forces computes them, on DEVICE arrays,
+ * without allocating any GPU memory.  No counterpart in the reference: it is
+ * for callers that may not allocate device memory themselves, such as a host
+ * application that hands out all GPU memory from its own pool and forbids
+ * direct cudaMalloc/cudaFree, or a time-critical loop that cannot take the
+ * synchronisation an allocation may cause.  Inputs and the output are the
+ * caller's device arrays: d_pos4 (n x real4, 32-byte aligned), d_list (rows in
+ * the reference layout), d_f3 (n x real3, accumulated into when ljexist).
+ * Scratch lives in one fixed array of about 33 MB inside the library, held on
+ * every GPU that loads it until the process exits; sizes above 16384 atoms or
+ * 1048576 atom x row-slot pairs (n * nlargestsize) are rejected with
+ * MD_BAD_ARGUMENT and a message in err.  The first call on a device looks up
+ * the array's address; make that first call before any stream capture.  All
+ * calls share the array: calls that overlap on the GPU race, so serialise
+ * them.  stream is a cudaStream_t (NULL: the default stream); the work is
+ * queued on it and the function returns without waiting.  Returns md_status. */
+int mdgb_many_body_forces_static(const double* d_pos4, double* d_f3, int n, int nlargestsize,
+                                 int nlistsize, const int* d_list, double rcutsq, int ljexist,
+                                 void* stream, char* err, int err_len);
 /* species table of the mdgb_* layer: MD_SPECIES_NEON (default, the reference's) */
 void mdgb_set_species(int species);
 /* status of the last mdgb_* call on this thread (MD_OK or the failure) */

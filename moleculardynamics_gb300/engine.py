@@ -80,7 +80,8 @@ EXPORTS = ["md_create", "md_destroy", "md_status_string", "md_last_error", "md_u
            "mdgb_lennard_jones_forces", "mdgb_many_body_forces", "mdgb_calculate_accelerations",
            "mdgb_build_neighbor_list", "mdgb_free", "mdgb_perform_calculations",
            "mdgb_calculate_potential", "mdgb_set_species", "mdgb_last_status", "md_read_config",
-           "md_write_results", "md_host_alloc", "md_host_free"]
+           "md_write_results", "md_host_alloc", "md_host_free",
+           "mdgb_many_body_forces_static"]
 
 
 def load(path: str | None = None) -> C.CDLL:
@@ -132,6 +133,10 @@ def load(path: str | None = None) -> C.CDLL:
     L.mdgb_perform_calculations.argtypes = [_dp, _dp, C.c_int] + [P(C.c_double)] * 8
     L.mdgb_calculate_potential.argtypes = [_dp, P(C.c_double), P(C.c_double), C.c_int]
     L.mdgb_set_species.argtypes = [C.c_int]
+    L.mdgb_many_body_forces_static.restype = C.c_int
+    L.mdgb_many_body_forces_static.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int,
+                                               C.c_int, C.c_void_p, C.c_double, C.c_int,
+                                               C.c_void_p, C.c_char_p, C.c_int]
     L.mdgb_last_status.restype = C.c_int
     L.md_read_config.argtypes = [C.c_char_p, P(MdConfig), C.c_char_p, P(C.c_double),
                                  C.c_char_p, C.c_int]
