@@ -148,10 +148,10 @@ def make_workload(name: str, seed: int = 2024):
     return pos, vel, L, prec
 
 
-def engine_for(eng, n, L, precision, device, output=MD_PER_BENCH_STEP):
+def engine_for(eng, n, L, precision, device, output=MD_PER_BENCH_STEP, lj_kernel=0):
     cfg = eng.make_config(n_lj=n, dt=2.0, lj_rs=2.8 * SIGMA, lj_rcut=2.5 * SIGMA, periodic=1,
                           box=L, precision=precision, species=eng.SPECIES_ARGON, device=device,
-                          output_timesteps=output)
+                          output_timesteps=output, lj_kernel=lj_kernel)
     return eng.Engine(cfg)
 
 
@@ -165,9 +165,9 @@ def drift_per_1000(recs: np.ndarray, n: int, first_step: int) -> float:
     return float((e[-1] - e[0]) / n / EPS / steps * 1000.0)
 
 
-def roofline_traffic(workload: str):
+def roofline_traffic(workload: str, kernel: str = "lj_force"):
     """dram bytes per launch of the LJ kernel from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", f"lj_force_{workload}.md")
+    path = os.path.join(ROOT, "profiles", f"{kernel}_{workload}.md")
     if not os.path.exists(path):
         return None
     for line in open(path):
@@ -243,9 +243,11 @@ def run_gb300(args, rank, world):
     pos, vel, L, prec_name = make_workload(args.workload)
     n = len(pos)
     precision = eng.PREC_MIXED if prec_name == "mixed" else eng.PREC_FP64
-    e = engine_for(eng, n, L, precision, device)
+    lj_kernel = {"auto": eng.LJ_AUTO, "rows": eng.LJ_ROWS, "cluster": eng.LJ_CLUSTER}[args.lj_kernel]
+    e = engine_for(eng, n, L, precision, device, lj_kernel=lj_kernel)
     e.upload(pos, vel)
     e.begin(0.0)
+    tune = e.autotune(3) if not args.no_tune else None
     for _ in range(args.warmup):
         e.step(MD_PER_BENCH_STEP)
     warm_steps = args.warmup * MD_PER_BENCH_STEP
@@ -265,6 +267,7 @@ def run_gb300(args, rank, world):
     pr_ms, pr_n = e.kernel_time(eng.KERNEL_PREDICT)
     co_ms, co_n = e.kernel_time(eng.KERNEL_CORRECT)
     li_ms, li_n = e.kernel_time(eng.KERNEL_LIST)
+    fu_ms, fu_n = e.kernel_time(eng.KERNEL_FUSED)
     s1 = e.stats()
     e.set_timing(False)
     t_max = dist.max(step_ms)
@@ -307,30 +310,60 @@ def run_gb300(args, rank, world):
                            "and reductions" if precision == eng.PREC_MIXED else "plain FP64",
                    "md_steps_per_bench_step": MD_PER_BENCH_STEP, "atoms": n,
                    "parallelism": f"replicas x{world}" if world > 1 else "1 GPU",
-                   "l2": "inputs larger than L2 (state 176 MB + list 330 MB), no flush"},
+                   "lj_kernel": "cluster" if s1["lj_cluster"] else "rows",
+                   "autotune": tune,
+                   "l2": "inputs larger than L2 (Gear state 176 MB + list >= 160 MB), no flush"},
         "gpu_launches": s1["launches"] - s0["launches"],
         "clocks": ck,
         "e2e": {"value": e2e_value, "unit": "atom-steps/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
         "list": {"builds_in_timed_region": s1["list_builds"] - s0["list_builds"],
                  "skin_trips": s1["list_trips"], "mean_compact_row": s1["lj_list_entries"] / n,
-                 "cells_per_edge": s1["lj_cells"], "tma": s1["lj_tma"]},
+                 "cells_per_edge": s1["lj_cells"], "tma": s1["lj_tma"],
+                 "cluster_segments": s1["cluster_segments"],
+                 "cluster_max_staged": s1["cluster_max_staged"]},
         "kernel_ms_per_md_step": {
             "lj_force": lj_ms / max(lj_n, 1), "predict": pr_ms / max(pr_n, 1),
             "correct": co_ms / max(co_n, 1),
+            "fused_force_gear": fu_ms / max(fu_n, 1),
             "list_build_amortised": li_ms / md_steps},
+        "kernel_launches": {"lj_force": lj_n, "predict": pr_n, "correct": co_n,
+                            "fused_force_gear": fu_n, "list_build": li_n},
         "accuracy": {"energy_drift_eps_per_atom_per_1000_steps": drift},
     }
     peaks = measured_peaks()
-    if lj_n:
+    if fu_n:
+        # the fused kernel: float4 position, 16-bit row length and entries,
+        # FP64 position in and out, float4 next position out, vel/acc/b/c in
+        # and out (FP64), float4 build position in
         entries = s1["lj_list_entries"]
-        pos_b = 16 if precision == eng.PREC_MIXED else 32
-        bytes_alg = n * (pos_b + 4 + 24) + 4 * entries
+        bytes_alg = n * (16 + 2 + 32 + 32 + 16 + 96 + 96 + 16) + 2 * entries
+        avg_s = fu_ms / fu_n / 1e3
+        achieved = bytes_alg / avg_s / 1e9
+        peak = peaks.get("hbm_gbs")
+        line["roofline"] = {"kernel": "k_lj_cl<fused Gear>", "bound": "hbm", "achieved": achieved,
+                            "peak": peak if peak else 6800.0, "unit": "GB/s",
+                            "frac": achieved / (peak if peak else 6800.0),
+                            "peak_source": "measured" if peak else "fallback",
+                            "traffic": roofline_traffic(args.workload, "lj_cluster_fused"),
+                            "bytes_alg_per_launch": bytes_alg,
+                            "avg_launch_ms": fu_ms / fu_n}
+    elif lj_n:
+        entries = s1["lj_list_entries"]
+        if s1["lj_cluster"]:
+            # float4 position, 16-bit row length and entries, FP64 force out
+            bytes_alg = n * (16 + 2 + 24) + 2 * entries
+            kname = "k_lj_cl"
+            traffic = roofline_traffic(args.workload, "lj_cluster")
+        else:
+            pos_b = 16 if precision == eng.PREC_MIXED else 32
+            bytes_alg = n * (pos_b + 4 + 24) + 4 * entries
+            kname = "k_lj_tma" if precision == eng.PREC_MIXED else "k_lj_fp64"
+            traffic = roofline_traffic(args.workload)
         avg_s = lj_ms / lj_n / 1e3
         achieved = bytes_alg / avg_s / 1e9
         peak = peaks.get("hbm_gbs")
-        traffic = roofline_traffic(args.workload)
-        line["roofline"] = {"kernel": "k_lj_fp32" if precision == eng.PREC_MIXED else "k_lj_fp64",
+        line["roofline"] = {"kernel": kname,
                             "bound": "hbm", "achieved": achieved,
                             "peak": peak if peak else 6800.0, "unit": "GB/s",
                             "frac": achieved / (peak if peak else 6800.0),
@@ -393,6 +426,8 @@ def main():
     ap.add_argument("--fp64-steps", type=int, default=100)
     ap.add_argument("--cpu-md-steps", type=int, default=5)
     ap.add_argument("--ref-md-steps", type=int, default=2)
+    ap.add_argument("--lj-kernel", default="auto", choices=["auto", "rows", "cluster"])
+    ap.add_argument("--no-tune", action="store_true", help="skip the cluster autotuner")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world, _ = dist_env()

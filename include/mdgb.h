@@ -70,7 +70,19 @@ typedef struct md_config {
   int device;              /* CUDA device ordinal */
   int reference_energy;    /* 1: records use the reference's all-pairs energy
                               (DebugCalculations.cpp:129-270, O(N^2)/O(N^3)) */
+  int lj_kernel;           /* MD_LJ_AUTO, MD_LJ_ROWS or MD_LJ_CLUSTER (precision form) */
+  int cluster_cells;       /* cells per segment of the cluster kernel (0: default) */
+  int cluster_threads;     /* threads per segment block (0: default; multiple of 32, <= 224) */
 } md_config;
+
+/* LJ kernel of the precision form.  ROWS: compact rows of packed atom
+ * indices streamed by TMA, positions gathered from L2.  CLUSTER (periodic,
+ * LJ only): atoms sorted by cell, each block stages the positions of a
+ * segment's neighbour cells in shared memory and rows hold 16-bit offsets
+ * into it; the state is kept in that order on the device and mapped back to
+ * the caller's numbering at every download.  AUTO picks CLUSTER where it
+ * applies. */
+enum { MD_LJ_AUTO = 0, MD_LJ_ROWS = 1, MD_LJ_CLUSTER = 2 };
 
 /* One output record.  The first 11 doubles are the reference's `results`
  * (common/Results.h:15-28) in the same order; eu is the potential energy
@@ -99,6 +111,9 @@ typedef struct md_stats {
   int lj_cells, mb_cells;
   long long lj_list_entries; /* entries of the compact LJ list at the last build */
   int lj_tma;              /* 1: the LJ list is streamed by TMA (precision form) */
+  int lj_cluster;          /* 1: the cluster kernel computes LJ (precision form) */
+  int cluster_segments;    /* segment blocks of the cluster kernel */
+  int cluster_max_staged;  /* largest staged neighbourhood (atoms) */
 } md_stats;
 
 typedef struct md_ctx md_ctx;
@@ -145,9 +160,22 @@ md_status md_neighbor_list(md_ctx* ctx, int which, int* rows, signed char* image
 md_status md_get_stats(const md_ctx* ctx, md_stats* out);
 /* Per-kernel device timing with CUDA events on the engine's stream.
  * kernel: 0 = LJ force, 1 = bond order, 2 = predict, 3 = correct, 4 = list build,
- * 5 = whole md_step calls (first launch to last). */
+ * 5 = whole md_step calls (first launch to last), 6 = cluster force kernel with the
+ * Gear correct + predict fused in (precision form, periodic). */
 md_status md_set_timing(md_ctx* ctx, int on);
 md_status md_kernel_time(const md_ctx* ctx, int kernel, double* total_ms, long long* launches);
+/* Autotuner of the cluster kernel (precision form, periodic): times `evals`
+ * force evaluations on the current state for each candidate block size and
+ * staged-atom cap per segment, keeps the fastest and rebuilds the list with
+ * it.  Forces do not depend on the choice (same pairs, same order).  No-op
+ * for the other kernels.  Call after md_begin. */
+typedef struct md_tune_result {
+  int threads;             /* threads per segment block */
+  int stage_cap;           /* staged atoms per segment (cap of the column cut) */
+  int candidates;          /* configurations timed */
+  double best_ms;          /* force evaluation time of the choice */
+} md_tune_result;
+md_status md_autotune(md_ctx* ctx, int evals, md_tune_result* out);
 /* Wait for all work of the context; returns the first deferred error. */
 md_status md_synchronize(md_ctx* ctx);
 /* Page-locked host memory for fast md_upload/md_download (NULL on failure). */

@@ -1,0 +1,1126 @@
+// Cell-cluster neighbour build and the shared-memory-staged FP32 LJ force of
+// the precision form in periodic boxes (md_cluster.h has the layout).
+//
+// Build, per list rebuild (replaces common/NeighborList.cpp:14-156 for the
+// periodic precision form; cell arithmetic as md_neighbor.cu's periodic grid):
+//   1. wrap each position into its box and find its dense cell; count;
+//   2. exclusive scan of the counts; scatter; rank each cell's atoms by
+//      original index; permute the state into that order;
+//   3. cut every z-column greedily into segments of at most one block of
+//      atoms; per segment, the staged pieces of its 9 neighbour columns;
+//   4. per atom, the compact row: staged offsets of the candidates within
+//      the list radius, in candidate order (counted, then written).
+// Force: one block per segment stages its neighbourhood (FP32 positions with
+// periodic images applied) while TMA streams the segment's rows in tiles of
+// 16 slots (double-buffered, mbarrier-completed); every atom of the segment
+// then walks its compact row against shared memory.  Pair arithmetic and the
+// cutoff band rule are those of md_forces.cu's FP32 kernels.  When the skin
+// flag is up, the block walks full candidate rows from shared memory and
+// refreshes the compact rows.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "md_cluster.h"
+#include "md_gear.cuh"
+#include "md_neighbor.cuh"
+#include "md_potential.cuh"
+#include "md_tma.cuh"
+
+namespace mdgb {
+
+cudaError_t scan_exclusive(const int* in, int* out, int n, Scratch& sc, cudaStream_t st);
+
+namespace {
+
+constexpr int kOffW = kClusterMaxZ + 3;  // z slots of the per-segment offset table
+
+// replica holding atom / cell / column i (the *0 fields ascend)
+template <int ClusterReplica::*F>
+__device__ __forceinline__ int find_rep(const ClusterReplica* reps, int nrep, int i) {
+  int lo = 0, hi = nrep - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (reps[mid].*F <= i) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+__host__ __device__ __forceinline__ int cid(const ClusterReplica& r, int cx, int cy, int cz) {
+  return r.cell0 + (cx * r.G + cy) * r.G + cz;
+}
+
+__device__ __forceinline__ int wrapc(int c, int G, int& img) {
+  img = 0;
+  if (c < 0) { c += G; img = -1; }
+  if (c >= G) { c -= G; img = 1; }
+  return c;
+}
+
+__device__ __forceinline__ int zimg(int z, int G) { return z < 0 ? -1 : (z >= G ? 1 : 0); }
+
+// 1. wrap into [-L/2, L/2) and find the dense cell (the arithmetic of
+// md_neighbor.cu's periodic grid: x - L floor((x + L/2) / L), then
+// (int)((x + L/2) / cs) clamped to the grid); count atoms per cell
+__global__ void k_cl_assign(md_double4* __restrict__ pos, int n, const ClusterReplica* reps,
+                            int nrep, int* __restrict__ cell, int* __restrict__ count,
+                            int* __restrict__ counters, int* __restrict__ status) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const ClusterReplica r = reps[find_rep<&ClusterReplica::atom0>(reps, nrep, i)];
+  md_double4 p = pos[i];
+  double x[3] = {p.x, p.y, p.z};
+  const double h = r.L * 0.5;
+  int c[3];
+  bool bad = false;
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    const double q = floor(xdiv(xadd(x[d], h), r.L));
+    x[d] = xsub(x[d], xmul(q, r.L));
+    double s = xdiv(xadd(x[d], h), r.cs);
+    if (!(s >= 0.0 && s < 2.0e9)) {
+      bad = true;
+      s = 0.0;
+    }
+    const int cc = __double2int_rz(s);
+    c[d] = cc >= r.G ? r.G - 1 : cc;
+  }
+  if (bad) atomicOr(status, ST_NONFINITE);
+  p.x = x[0];
+  p.y = x[1];
+  p.z = x[2];
+  pos[i] = p;
+  const int id = r.G == 1 ? r.cell0 : cid(r, c[0], c[1], c[2]);
+  cell[i] = id;
+  const int old = atomicAdd(&count[id], 1);
+  atomicMax(&counters[4], old + 1);
+}
+
+__global__ void k_cl_scatter(const int* __restrict__ cell, int n, const int* __restrict__ start,
+                             int* __restrict__ fill, int* __restrict__ unsorted) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int c = cell[i];
+  unsorted[start[c] + atomicAdd(&fill[c], 1)] = i;
+}
+
+// members of each cell in ascending original index
+__global__ void k_cl_rank(const int* __restrict__ unsorted, const int* __restrict__ cell,
+                          const int* __restrict__ orig, int n, const int* __restrict__ start,
+                          int* __restrict__ perm) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  const int a = unsorted[q];
+  const int c = cell[a];
+  const int lo = start[c], hi = start[c + 1];
+  const int key = orig[a];
+  int rank = 0;
+  for (int k = lo; k < hi; k++) rank += orig[unsorted[k]] < key;
+  perm[lo + rank] = a;
+}
+
+template <typename T>
+__global__ void k_gather(const T* __restrict__ src, T* __restrict__ dst,
+                         const int* __restrict__ perm, int n) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p < n) dst[p] = src[perm[p]];
+}
+
+__global__ void k_gather3(const double* __restrict__ src, double* __restrict__ dst,
+                          const int* __restrict__ perm, int n) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  const int a = perm[p];
+#pragma unroll
+  for (int d = 0; d < 3; d++) dst[3 * p + d] = src[3 * a + d];
+}
+
+__global__ void k_cl_posf(const md_double4* __restrict__ pos, float4* __restrict__ pb,
+                          float4* __restrict__ posf, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const md_double4 p = pos[i];
+  const float4 v = make_float4((float)p.x, (float)p.y, (float)p.z, __int_as_float((int)p.w));
+  pb[i] = v;
+  posf[i] = v;
+}
+
+// 3a. greedy cut of each z-column: a segment starts at z = 0 and wherever
+// the next cell would take it past `cap_atoms` own atoms, `cap_staged`
+// staged atoms (its 9 neighbour columns over cz0-1 .. cz1+1) or `zmax` cells
+__global__ void k_seg_flags(const ClusterReplica* __restrict__ reps, int nrep, int ncols,
+                            int ncells, const int* __restrict__ count, int* __restrict__ flag,
+                            int cap_atoms, int cap_staged, int zmax) {
+  const int col = blockIdx.x * blockDim.x + threadIdx.x;
+  if (col == 0) flag[ncells] = 0;
+  if (col >= ncols) return;
+  const ClusterReplica r = reps[find_rep<&ClusterReplica::col0>(reps, nrep, col)];
+  if (r.G == 1) {
+    flag[r.cell0] = 1;
+    return;
+  }
+  const int G = r.G;
+  const int local = col - r.col0;
+  const int cx = local / G, cy = local % G;
+  int nbase[9];  // first cell of each neighbour column
+  for (int g = 0; g < 9; g++) {
+    int ix, iy;
+    nbase[g] = cid(r, wrapc(cx + g / 3 - 1, G, ix), wrapc(cy + g % 3 - 1, G, iy), 0);
+  }
+  // atoms of the 9 neighbour columns at z (periodic in z)
+  auto layer = [&](int z) {
+    z = z < 0 ? z + G : (z >= G ? z - G : z);
+    int s = 0;
+    for (int g = 0; g < 9; g++) s += count[nbase[g] + z];
+    return s;
+  };
+  const int base = nbase[4];
+  int acc = 0, cells = 0, staged = 0;
+  for (int z = 0; z < G; z++) {
+    const int c = count[base + z];
+    const bool cut = z == 0 || cells == zmax || (acc > 0 && acc + c > cap_atoms) ||
+                     staged + layer(z + 1) > cap_staged;
+    flag[base + z] = cut ? 1 : 0;
+    if (cut) {
+      acc = c;
+      cells = 1;
+      staged = layer(z - 1) + layer(z) + layer(z + 1);
+    } else {
+      acc += c;
+      cells++;
+      staged += layer(z + 1);
+    }
+  }
+}
+
+// 3b. segment geometry at its scanned index
+__global__ void k_seg_emit(const ClusterReplica* __restrict__ reps, int nrep, int ncells,
+                           const int* __restrict__ flag, const int* __restrict__ segidx,
+                           ClusterSegment* __restrict__ seg) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncells || !flag[c]) return;
+  const int k = find_rep<&ClusterReplica::cell0>(reps, nrep, c);
+  const ClusterReplica r = reps[k];
+  ClusterSegment& S = seg[segidx[c]];
+  S.rep = k;
+  if (r.G == 1) {
+    S.cx = S.cy = S.cz0 = S.cz1 = 0;
+    return;
+  }
+  const int local = c - r.cell0;
+  const int cz = local % r.G;
+  int z = cz + 1;
+  while (z < r.G && !flag[c - cz + z]) z++;
+  S.cx = local / (r.G * r.G);
+  S.cy = (local / r.G) % r.G;
+  S.cz0 = cz;
+  S.cz1 = z - 1;
+}
+
+// 3c. pieces of each segment: for each (dx, dy) group the z range
+// cz0-1 .. cz1+1, split where the periodic image changes
+__global__ void k_cl_segments(ClusterSegment* __restrict__ seg, const int* __restrict__ nseg_dev,
+                              const ClusterReplica* __restrict__ reps,
+                              const int* __restrict__ start, int* __restrict__ counters) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= *nseg_dev) return;
+  ClusterSegment& S = seg[s];
+  const ClusterReplica r = reps[S.rep];
+  if (r.G == 1) {
+    ClusterPiece pc;
+    pc.src = start[r.cell0];
+    pc.count = start[r.cell0 + 1] - pc.src;
+    pc.dst = 0;
+    pc.ix = pc.iy = pc.iz = pc.pad = 0;
+    S.p0 = pc.src;
+    S.p1 = pc.src + pc.count;
+    S.piece[0] = pc;
+    for (int g = 0; g < 10; g++) S.group[g] = g == 9 ? 1 : 0;
+    S.npieces = 1;
+    S.staged = pc.count;
+    atomicMax(&counters[0], S.staged);
+    return;
+  }
+  const int G = r.G;
+  S.p0 = start[cid(r, S.cx, S.cy, S.cz0)];
+  S.p1 = start[cid(r, S.cx, S.cy, S.cz1) + 1];
+  int np = 0, dst = 0;
+  for (int dx = -1; dx < 2; dx++)
+    for (int dy = -1; dy < 2; dy++) {
+      S.group[(dx + 1) * 3 + (dy + 1)] = np;
+      int ix, iy;
+      const int cx = wrapc(S.cx + dx, G, ix), cy = wrapc(S.cy + dy, G, iy);
+      const int zend = S.cz1 + 1;
+      for (int z = S.cz0 - 1; z <= zend;) {
+        const int iz = zimg(z, G);
+        int zb = z;
+        while (zb + 1 <= zend && zimg(zb + 1, G) == iz) zb++;
+        ClusterPiece pc;
+        pc.src = start[cid(r, cx, cy, z - iz * G)];
+        pc.count = start[cid(r, cx, cy, zb - iz * G) + 1] - pc.src;
+        pc.dst = dst;
+        pc.ix = (signed char)ix;
+        pc.iy = (signed char)iy;
+        pc.iz = (signed char)iz;
+        pc.pad = 0;
+        S.piece[np++] = pc;
+        dst += pc.count;
+        z = zb + 1;
+      }
+    }
+  S.group[9] = np;
+  S.npieces = np;
+  S.staged = dst;
+  atomicMax(&counters[0], dst);
+}
+
+// ---- per-block segment context in shared memory ----
+struct SegShared {
+  ClusterSegment S;
+  ClusterReplica r;
+  int self0;          // staged offset of the segment's first own atom
+  int off[9][kOffW];  // staged offset of z slot w (cell cz0-1+w) of each group; w = zspan: end
+};
+
+__device__ __forceinline__ void load_segment(SegShared& sh, const ClusterSegment* seg,
+                                             const ClusterReplica* reps) {
+  const int* src = (const int*)&seg[blockIdx.x];
+  int* dst = (int*)&sh.S;
+  for (int k = threadIdx.x; k < (int)(sizeof(ClusterSegment) / 4); k += blockDim.x)
+    dst[k] = src[k];
+  __syncthreads();
+  const int* rs = (const int*)&reps[sh.S.rep];
+  int* rd = (int*)&sh.r;
+  for (int k = threadIdx.x; k < (int)(sizeof(ClusterReplica) / 4); k += blockDim.x) rd[k] = rs[k];
+  if (threadIdx.x == 0) {
+    // own cells cz0..cz1 lie in the image-free piece of the (0, 0) group
+    int s0 = 0;
+    if (reps[sh.S.rep].G > 1)
+      for (int k = sh.S.group[4]; k < sh.S.group[5]; k++)
+        if (sh.S.piece[k].iz == 0) s0 = sh.S.piece[k].dst + (sh.S.p0 - sh.S.piece[k].src);
+    sh.self0 = s0;
+  }
+}
+
+// staged copy of positions with the pieces' periodic images applied
+__device__ __forceinline__ void stage(const SegShared& sh, const float4* __restrict__ src,
+                                      float4* st) {
+  const ClusterSegment& S = sh.S;
+  const float Lf = sh.r.Lf, Llo = sh.r.Llo;
+  for (int k = 0; k < S.npieces; k++) {
+    const ClusterPiece pc = S.piece[k];
+    const float sx = (float)pc.ix, sy = (float)pc.iy, sz = (float)pc.iz;
+    const bool img = (pc.ix | pc.iy | pc.iz) != 0;
+    for (int q = threadIdx.x; q < pc.count; q += blockDim.x) {
+      float4 v = src[pc.src + q];
+      if (img) {
+        v.x = fmaf(sx, Lf, v.x) + sx * Llo;
+        v.y = fmaf(sy, Lf, v.y) + sy * Llo;
+        v.z = fmaf(sz, Lf, v.z) + sz * Llo;
+      }
+      st[pc.dst + q] = v;
+    }
+  }
+}
+
+// The same staging by bulk copies: thread 0 issues one cp.async.bulk per
+// piece, all completing on `bar` (phase 0); after the wait the image pieces
+// are shifted in place.  Returns false (uniformly) if the bounded wait ran
+// out; the caller then leaves after the copies land or time out.
+__device__ __forceinline__ bool stage_bulk(const SegShared& sh, const float4* __restrict__ src,
+                                           float4* st, uint64_t* bar, int* status) {
+  const ClusterSegment& S = sh.S;
+  if (threadIdx.x == 0) {
+    mbar_expect_tx(bar, (uint32_t)S.staged * (uint32_t)sizeof(float4));
+    for (int k = 0; k < S.npieces; k++) {
+      const ClusterPiece& pc = S.piece[k];
+      if (pc.count > 0)
+        bulk_load(st + pc.dst, src + pc.src, (uint32_t)pc.count * (uint32_t)sizeof(float4), bar);
+    }
+  }
+  const bool got = mbar_wait(bar, 0u, status);
+  if (!__syncthreads_and(got)) {
+    if (threadIdx.x == 0) mbar_wait(bar, 0u, status);
+    return false;
+  }
+  const float Lf = sh.r.Lf, Llo = sh.r.Llo;
+  for (int k = 0; k < S.npieces; k++) {
+    const ClusterPiece& pc = S.piece[k];
+    if ((pc.ix | pc.iy | pc.iz) == 0) continue;
+    const float sx = (float)pc.ix, sy = (float)pc.iy, sz = (float)pc.iz;
+    for (int q = threadIdx.x; q < pc.count; q += blockDim.x) {
+      float4 v = st[pc.dst + q];
+      v.x = fmaf(sx, Lf, v.x) + sx * Llo;
+      v.y = fmaf(sy, Lf, v.y) + sy * Llo;
+      v.z = fmaf(sz, Lf, v.z) + sz * Llo;
+      st[pc.dst + q] = v;
+    }
+  }
+  return true;
+}
+
+__device__ __forceinline__ void fill_offsets(SegShared& sh, const int* __restrict__ start) {
+  const ClusterSegment& S = sh.S;
+  const ClusterReplica& r = sh.r;
+  if (r.G == 1) return;
+  const int zspan = S.cz1 - S.cz0 + 3;
+  for (int k = threadIdx.x; k < 9 * (zspan + 1); k += blockDim.x) {
+    const int g = k / (zspan + 1), w = k % (zspan + 1);
+    const int pe = S.group[g + 1];
+    int v;
+    if (w == zspan) {
+      v = S.piece[pe - 1].dst + S.piece[pe - 1].count;
+    } else {
+      int ix, iy;
+      const int cx = wrapc(S.cx + g / 3 - 1, r.G, ix), cy = wrapc(S.cy + g % 3 - 1, r.G, iy);
+      const int z = S.cz0 - 1 + w, iz = zimg(z, r.G);
+      v = 0;
+      for (int p = S.group[g]; p < pe; p++)
+        if (S.piece[p].iz == iz) {
+          v = S.piece[p].dst + (start[cid(r, cx, cy, z - iz * r.G)] - S.piece[p].src);
+          break;
+        }
+    }
+    sh.off[g][w] = v;
+  }
+}
+
+// staged offset of the segment's own atom p
+__device__ __forceinline__ int self_offset(const SegShared& sh, int p) {
+  return sh.self0 + (p - sh.S.p0);
+}
+
+// visit(q) for every staged candidate of atom p's 27-cell row, in row order
+template <typename F>
+__device__ __forceinline__ void walk_staged(const SegShared& sh, int self, F&& visit) {
+  if (sh.r.G == 1) {
+    for (int q = 0; q < sh.S.staged; q++)
+      if (q != self) visit(q);
+    return;
+  }
+  const int zspan = sh.S.cz1 - sh.S.cz0 + 3;
+  int w = 1;
+  while (w < zspan - 2 && sh.off[4][w + 1] <= self) w++;
+  const int u = w - 1;
+  for (int g = 0; g < 9; g++) {
+    const int a = sh.off[g][u], b = sh.off[g][u + 3];
+    for (int q = a; q < b; q++)
+      if (q != self) visit(q);
+  }
+}
+
+// staged offset -> (sorted index, image)
+__device__ __forceinline__ int staged_source(const ClusterSegment& S, int q, int& ix, int& iy,
+                                             int& iz) {
+  for (int k = 0; k < S.npieces; k++) {
+    const ClusterPiece& pc = S.piece[k];
+    if (q >= pc.dst && q < pc.dst + pc.count) {
+      ix = pc.ix;
+      iy = pc.iy;
+      iz = pc.iz;
+      return pc.src + (q - pc.dst);
+    }
+  }
+  ix = iy = iz = 0;
+  return S.p0;
+}
+
+__device__ __forceinline__ float min_img(float d, float Lf, float invL) {
+  return d - Lf * rintf(d * invL);
+}
+
+// 4. compact rows from the build-time positions (MODE 0: count, 1: write)
+template <int MODE>
+__global__ void __launch_bounds__(256)
+    k_cl_rows(const ClusterSegment* __restrict__ seg, const ClusterReplica* __restrict__ reps,
+              const int* __restrict__ start, const float4* __restrict__ pb, float rv2,
+              uint16_t* __restrict__ rows, uint16_t* __restrict__ len, int ld, int cap,
+              int* __restrict__ counters) {
+  extern __shared__ float4 st[];
+  __shared__ SegShared sh;
+  load_segment(sh, seg, reps);
+  __syncthreads();
+  stage(sh, pb, st);
+  fill_offsets(sh, start);
+  __syncthreads();
+  const bool minimg = sh.r.G == 1;
+  const float Lf = sh.r.Lf, invL = 1.0f / sh.r.Lf;
+  int mx = 0;
+  unsigned long long tot = 0;
+  for (int p = sh.S.p0 + threadIdx.x; p < sh.S.p1; p += blockDim.x) {
+    const int self = self_offset(sh, p);
+    const float4 pi = st[self];
+    int kept = 0;
+    walk_staged(sh, self, [&](int q) {
+      const float4 pj = st[q];
+      float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+      if (minimg) {
+        dx = min_img(dx, Lf, invL);
+        dy = min_img(dy, Lf, invL);
+        dz = min_img(dz, Lf, invL);
+      }
+      if (dx * dx + dy * dy + dz * dz < rv2) {
+        if (MODE == 1 && kept < cap) rows[(size_t)kept * ld + p] = (uint16_t)q;
+        kept++;
+      }
+    });
+    if (MODE == 0) {
+      len[p] = (uint16_t)min(kept, 65535);
+      mx = max(mx, kept);
+      tot += (unsigned long long)kept;
+    }
+  }
+  if (MODE == 0) {
+    atomicMax(&counters[1], mx);
+    atomicAdd((unsigned long long*)(counters + 2), tot);
+  }
+}
+
+__device__ __forceinline__ void kahan_add(float& hi, float& lo, float x) {
+  const float y = x - lo;
+  const float t = hi + y;
+  lo = (t - hi) - y;
+  hi = t;
+}
+
+template <int NV>
+__device__ __forceinline__ void block_sums(double (&v)[NV], double* out) {
+  __shared__ double sm[NV][32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int k = 0; k < NV; k++) {
+    double x = v[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    if (lane == 0) sm[k][warp] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x < NV) {
+    double s = 0;
+    for (int w = 0; w < nw; w++) s += sm[threadIdx.x][w];
+    out[NV * blockIdx.x + threadIdx.x] = s;
+  }
+}
+
+// Pair (p, q) within 1e-5 of the cutoff: decided in FP64 as the FP64 path
+// decides it (same image, same roundings).
+__device__ __noinline__ bool band_inside(const SegShared& sh, const md_double4* pos, int p,
+                                         int q, double rcutsq) {
+  int ix, iy, iz;
+  const int j = staged_source(sh.S, q, ix, iy, iz);
+  const md_double4 a = pos[p], b = pos[j];
+  const double L = sh.r.L;
+  if (sh.r.G == 1) {
+    ix = min_image(a.x, b.x, L);
+    iy = min_image(a.y, b.y, L);
+    iz = min_image(a.z, b.z, L);
+  }
+  double xj = b.x, yj = b.y, zj = b.z;
+  if (ix | iy | iz) {
+    xj = xadd(xj, (double)ix * L);
+    yj = xadd(yj, (double)iy * L);
+    zj = xadd(zj, (double)iz * L);
+  }
+  return norm2_exact(xsub(a.x, xj), xsub(a.y, yj), xsub(a.z, zj)) < rcutsq;
+}
+
+// Arguments of the segment force kernel (device copy of ClusterForceArgs).
+struct ClStep {
+  const ClusterSegment* seg;
+  const ClusterReplica* reps;
+  const int* start;
+  const float4* posf;
+  const md_double4* pos;
+  double* f3;
+  uint16_t* rows;
+  uint16_t* len;
+  int ld, cap;
+  float rv2;
+  float4* pos_build;
+  int* skin;
+  int flag_read, flag_set, flag_clear;
+  double rcutsq;
+  Species sp;
+  double* epart;
+  int* status;
+  ClusterGearArgs g;
+};
+
+// FP32 LJ force of one segment.  ev: E, E_shifted, W (as md_forces.cu).
+// GEAR: the Gear correct of this step and predict of the next follow for each
+// atom in the same thread (cpu/common/Device.cpp:17-85 in FP64 with FMAs).
+// Dynamic shared memory: two row tiles [16][blockDim + 8] of uint16 (TMA
+// destinations), then the staged positions.
+template <bool ENERGY, bool ALL_NG, bool GEAR>
+__global__ void __launch_bounds__(256)
+    k_lj_cl(const __grid_constant__ CUtensorMap rmap, const ClStep a) {
+  extern __shared__ __align__(128) unsigned char dyn[];
+  const int tid = threadIdx.x;
+  const int BX = blockDim.x + 8;
+  uint16_t* tiles = (uint16_t*)dyn;
+  float4* st = (float4*)(dyn + 2 * kClusterTileSlots * BX * sizeof(uint16_t));
+  __shared__ SegShared sh;
+  __shared__ __align__(8) uint64_t bar[3];  // two row tiles, staging
+  __shared__ int s_max[8];
+  __shared__ int s_trip;
+  if (tid == 0) {
+    s_trip = (a.skin[a.flag_read] | a.skin[3]) != 0;
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    mbar_init(&bar[2], 1);
+    fence_mbar_init();
+  }
+  load_segment(sh, a.seg, a.reps);
+  __syncthreads();
+  const bool tripped = s_trip != 0;
+  if (!stage_bulk(sh, a.posf, st, &bar[2], a.status)) return;
+  if (tripped) fill_offsets(sh, a.start);
+  __syncthreads();
+  const bool minimg = sh.r.G == 1;
+  const float Lf = sh.r.Lf, invL = 1.0f / sh.r.Lf;
+  const float rc2 = (float)a.rcutsq;
+  const float rc_lo = rc2 * (1.0f - 1e-5f), rc_hi = rc2 * (1.0f + 1e-5f);
+  const float s2_ng = a.sp.sig[2] * a.sp.sig[2], c_ng = 24.0f * a.sp.eps[2];
+  const float s2_n = a.sp.sig[0] * a.sp.sig[0], c_n = 24.0f * a.sp.eps[0];
+  const float s2_o = a.sp.sig[1] * a.sp.sig[1], c_o = 24.0f * a.sp.eps[1];
+  const uint32_t tile_elems = kClusterTileSlots * BX;
+  const uint32_t tile_bytes = tile_elems * sizeof(uint16_t);
+  uint32_t phase = 0u;       // bit b: parity to wait for on bar[b]
+  uint32_t inflight = 0u;    // bit b: a copy into buffer b is in flight (issuing thread)
+  double ev[3] = {0.0, 0.0, 0.0};
+  bool trip_next = false;
+  const int p0 = sh.S.p0, p1 = sh.S.p1;
+  for (int base = p0; base < p1; base += blockDim.x) {
+    const int p = base + tid;
+    const bool live = p < p1;
+    const int self = live ? self_offset(sh, p) : 0;
+    const float4 pi = st[self];
+    const int ti = __float_as_int(pi.w);
+    float hx = 0.f, hy = 0.f, hz = 0.f, lx = 0.f, ly = 0.f, lz = 0.f;
+    // candidate q into the running sums (cx, cy, cz); `valid` false
+    // evaluates a harmless dummy (no branch)
+    auto pair = [&](int q, bool valid, float& cx, float& cy, float& cz) {
+      const float4 pj = st[q];
+      float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+      if (minimg) {
+        dx = min_img(dx, Lf, invL);
+        dy = min_img(dy, Lf, invL);
+        dz = min_img(dz, Lf, invL);
+      }
+      const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+      float s2 = s2_ng, c24 = c_ng;
+      bool use = valid;
+      if (!ALL_NG) {
+        const int tj = __float_as_int(pj.w);
+        use = use && (tj == SP_NG || ti == SP_NG);
+        const int sel = lj_select(ti, tj);
+        s2 = sel == SP_N ? s2_n : (sel == SP_O ? s2_o : s2_ng);
+        c24 = sel == SP_N ? c_n : (sel == SP_O ? c_o : c_ng);
+      }
+      const float inv = rcp_approx(r2);
+      const float sr2 = s2 * inv;
+      const float sr6 = sr2 * sr2 * sr2;
+      float fij = c24 * inv * sr6 * fmaf(2.0f, sr6, -1.0f);
+      bool in = r2 <= rc_lo;
+      if (use && !in && r2 < rc_hi) in = band_inside(sh, a.pos, p, q, a.rcutsq);
+      in = in && use;
+      fij = in ? fij : 0.0f;
+      cx = fmaf(dx, fij, cx);
+      cy = fmaf(dy, fij, cy);
+      cz = fmaf(dz, fij, cz);
+      if (ENERGY && in) {
+        const float src2 = s2 / rc2;
+        const float src6 = src2 * src2 * src2;
+        const float eps = c24 * (1.0f / 24.0f);
+        const float e = 2.0f * eps * (sr6 * sr6 - sr6);
+        ev[0] += (double)e;
+        ev[1] += (double)e - (double)(2.0f * eps * (src6 * src6 - src6));
+        ev[2] += 0.5 * (double)(r2 * fij);
+      }
+    };
+    if (!tripped) {
+      const int L = live ? (int)a.len[p] : 0;
+      int wmax = L;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) wmax = max(wmax, __shfl_xor_sync(0xffffffffu, wmax, o));
+      if ((tid & 31) == 0) s_max[tid >> 5] = wmax;
+      __syncthreads();
+      int maxl = 0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); w++) maxl = max(maxl, s_max[w]);
+      __syncthreads();  // s_max is rewritten by the next pass
+      const int T = (maxl + kClusterTileSlots - 1) / kClusterTileSlots;
+      const int x0 = base & ~7;  // 16-byte aligned start of the tile
+      const int col = live ? p - x0 : tid;
+      if (tid == 0) {
+        for (int t = 0; t < 2 && t < T; t++) {
+          fence_proxy_async();
+          mbar_expect_tx(&bar[t], tile_bytes);
+          tma_load_2d(tiles + t * tile_elems, &rmap, x0, t * kClusterTileSlots, &bar[t]);
+          inflight |= 1u << t;
+        }
+      }
+      bool failed = false;
+      for (int t = 0; t < T; t++) {
+        const int b = t & 1;
+        const bool got = mbar_wait(&bar[b], (phase >> b) & 1u, a.status);
+        const int wrem = wmax - t * kClusterTileSlots;  // warp-uniform
+        if (got) {
+          phase ^= 1u << b;
+          inflight &= ~(1u << b);
+          if (wrem > 0) {
+            const int rem = L - t * kClusterTileSlots;
+            const uint16_t* tl = tiles + b * tile_elems + col;
+            float cx = 0.f, cy = 0.f, cz = 0.f;
+#pragma unroll
+            for (int kk = 0; kk < kClusterTileSlots; kk++) {
+              if (kk < wrem) {
+                const bool valid = kk < rem;
+                const int q = valid ? (int)tl[kk * BX] : self;
+                pair(q, valid, cx, cy, cz);
+              }
+            }
+            kahan_add(hx, lx, cx);
+            kahan_add(hy, ly, cy);
+            kahan_add(hz, lz, cz);
+          }
+        }
+        // everyone is done with buffer b (and every wait succeeded)
+        if (!__syncthreads_and(got)) {
+          failed = true;
+          break;
+        }
+        if (tid == 0 && t + 2 < T) {
+          fence_proxy_async();
+          mbar_expect_tx(&bar[b], tile_bytes);
+          tma_load_2d(tiles + b * tile_elems, &rmap, x0, (t + 2) * kClusterTileSlots, &bar[b]);
+          inflight |= 1u << b;
+        }
+      }
+      if (failed) {
+        // a bounded wait ran out: give copies still in flight a bounded
+        // chance to land in this block's shared memory, then leave
+        if (tid == 0)
+          for (int b = 0; b < 2; b++)
+            if ((inflight >> b) & 1u) mbar_wait(&bar[b], (phase >> b) & 1u, a.status);
+        return;
+      }
+    } else if (live) {
+      // skin exceeded: the full candidate row from shared memory, and a
+      // fresh compact row at the current positions
+      int kept = 0, inchunk = 0;
+      float cx = 0.f, cy = 0.f, cz = 0.f;
+      walk_staged(sh, self, [&](int q) {
+        pair(q, true, cx, cy, cz);
+        if (++inchunk == kClusterTileSlots) {
+          kahan_add(hx, lx, cx);
+          kahan_add(hy, ly, cy);
+          kahan_add(hz, lz, cz);
+          cx = cy = cz = 0.f;
+          inchunk = 0;
+        }
+        const float4 pj = st[q];
+        float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+        if (minimg) {
+          dx = min_img(dx, Lf, invL);
+          dy = min_img(dy, Lf, invL);
+          dz = min_img(dz, Lf, invL);
+        }
+        if (dx * dx + dy * dy + dz * dz < a.rv2) {
+          if (kept < a.cap) a.rows[(size_t)kept * a.ld + p] = (uint16_t)q;
+          kept++;
+        }
+      });
+      kahan_add(hx, lx, cx);
+      kahan_add(hy, ly, cy);
+      kahan_add(hz, lz, cz);
+      if (kept > a.cap) atomicOr(&a.skin[3], 1);
+      a.len[p] = (uint16_t)(kept < a.cap ? kept : a.cap);
+      a.pos_build[p] = a.posf[p];
+    }
+    if (live) {
+      const double f[3] = {(double)hx - (double)lx, (double)hy - (double)ly,
+                           (double)hz - (double)lz};
+      if (!GEAR) {
+        a.f3[3 * p] = f[0];
+        a.f3[3 * p + 1] = f[1];
+        a.f3[3 * p + 2] = f[2];
+      } else {
+        const md_double4 r = a.pos[p];
+        const int type = (int)r.w;
+        GearAtom s;
+        s.r[0] = r.x;
+        s.r[1] = r.y;
+        s.r[2] = r.z;
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+          s.v[d] = a.g.vel[3 * p + d];
+          s.a[d] = a.g.acc[3 * p + d];
+          s.b[d] = a.g.b[3 * p + d];
+          s.c[d] = a.g.c[3 * p + d];
+        }
+        const double im = type == SP_N ? a.g.inv_mass[0]
+                                       : (type == SP_O ? a.g.inv_mass[1] : a.g.inv_mass[2]);
+        gear_correct_fma(s, f, im, a.g.k);
+        if (!gear_finite(s)) atomicOr(a.status, ST_NONFINITE);
+        gear_predict_fma(s, a.g.k);
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+          a.g.vel[3 * p + d] = s.v[d];
+          a.g.acc[3 * p + d] = s.a[d];
+          a.g.b[3 * p + d] = s.b[d];
+          a.g.c[3 * p + d] = s.c[d];
+        }
+        md_double4 rn;
+        rn.x = s.r[0];
+        rn.y = s.r[1];
+        rn.z = s.r[2];
+        rn.w = r.w;
+        a.g.pos_next[p] = rn;
+        const float4 pf = make_float4((float)s.r[0], (float)s.r[1], (float)s.r[2],
+                                      __int_as_float(type));
+        a.g.posf_next[p] = pf;
+        const float4 pb = a.pos_build[p];
+        const float ddx = pf.x - pb.x, ddy = pf.y - pb.y, ddz = pf.z - pb.z;
+        trip_next |= ddx * ddx + ddy * ddy + ddz * ddz > a.g.trip2;
+      }
+    }
+  }
+  if (GEAR && trip_next) a.skin[a.flag_set] = 1;
+  if (blockIdx.x == 0 && tid == 0) {
+    if (tripped) atomicAdd(&a.skin[4], 1);
+    a.skin[a.flag_clear] = 0;  // flag of step t + 2 starts clear
+  }
+  if (ENERGY) block_sums<3>(ev, a.epart);
+}
+
+// reference-layout rows, original numbering (single replica)
+__global__ void __launch_bounds__(256)
+    k_cl_ref_rows(const ClusterSegment* __restrict__ seg, const ClusterReplica* __restrict__ reps,
+                  const int* __restrict__ start, const int* __restrict__ orig,
+                  const md_double4* __restrict__ pos, int nls, int* __restrict__ out,
+                  signed char* __restrict__ img, int* __restrict__ nlargest) {
+  __shared__ SegShared sh;
+  load_segment(sh, seg, reps);
+  __syncthreads();
+  fill_offsets(sh, start);
+  __syncthreads();
+  const double L = sh.r.L;
+  for (int p = sh.S.p0 + threadIdx.x; p < sh.S.p1; p += blockDim.x) {
+    const int self = self_offset(sh, p);
+    const size_t o = (size_t)orig[p] * nls;
+    const md_double4 a = pos[p];
+    int k = 0;
+    walk_staged(sh, self, [&](int q) {
+      int ix, iy, iz;
+      const int j = staged_source(sh.S, q, ix, iy, iz);
+      if (sh.r.G == 1) {
+        const md_double4 b = pos[j];
+        ix = min_image(a.x, b.x, L);
+        iy = min_image(a.y, b.y, L);
+        iz = min_image(a.z, b.z, L);
+      }
+      if (out && k < nls) {
+        out[o + k] = orig[j];
+        if (img) img[o + k] = (signed char)((ix + 1) * 9 + (iy + 1) * 3 + (iz + 1));
+      }
+      k++;
+    });
+    atomicMax(nlargest, k);
+    if (!out) continue;
+    for (; k < nls; k++) {
+      out[o + k] = -1;
+      if (img) img[o + k] = 13;
+    }
+  }
+}
+
+__global__ void k_unpermute(const double* __restrict__ in, double* __restrict__ out,
+                            const int* __restrict__ orig, int n, int width) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  const size_t o = (size_t)orig[p];
+  for (int d = 0; d < width; d++) out[width * o + d] = in[(size_t)width * p + d];
+}
+
+__global__ void k_permute_in(const double* __restrict__ in, double* __restrict__ out,
+                             const int* __restrict__ orig, int n, int width) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  const size_t o = (size_t)orig[p];
+  for (int d = 0; d < width; d++) out[(size_t)width * p + d] = in[width * o + d];
+}
+
+__global__ void k_iota(int* __restrict__ a, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) a[i] = i;
+}
+
+inline int nb(long long n, int t) { return (int)((n + t - 1) / t); }
+
+template <typename T>
+cudaError_t realloc_dev(T*& p, size_t count) {
+  if (p) cudaFree(p);
+  p = nullptr;
+  return cudaMalloc(&p, sizeof(T) * (count > 0 ? count : 1));
+}
+
+size_t stage_bytes(int staged) { return sizeof(float4) * (size_t)std::max(staged, 1); }
+
+template <typename K>
+void allow_smem(K kern) {
+  cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)(sizeof(float4) * kClusterMaxStaged +
+                             2 * kClusterTileSlots * 256 * sizeof(uint16_t)));
+}
+
+}  // namespace
+
+int cluster_blocks(const ClusterList& cl) { return cl.nseg; }
+
+int cluster_build(ClusterList& cl, const std::vector<ClusterReplica>& reps_in, float rv,
+                  double rcut, md_double4** pos, double** v3[5], float4* posf, Scratch& sc,
+                  int* d_status, cudaStream_t st, std::string& err) {
+  cudaError_t e;
+  if (cl.block < 32 || cl.block > 248 || cl.block % 32) {
+    err = "cluster block size must be a multiple of 32 up to 224";
+    return -1;
+  }
+  // replica geometry (host): cells and columns
+  std::vector<ClusterReplica> reps = reps_in;
+  int natoms = 0, cell0 = 0, col0 = 0;
+  for (auto& r : reps) {
+    if (!(r.L > 2.0 * (double)rv)) {
+      err = "periodic box must exceed twice the list radius";
+      return -1;
+    }
+    r.atom0 = natoms;
+    natoms += r.n;
+    int G = (int)floor(r.L / (double)rv);
+    if (G < 3) G = 1;
+    r.G = G;
+    r.pad = 0;
+    r.cs = r.L / G;
+    r.Lf = (float)r.L;
+    r.Llo = (float)(r.L - (double)r.Lf);
+    r.cell0 = cell0;
+    r.col0 = col0;
+    cell0 += G == 1 ? 1 : G * G * G;
+    col0 += G == 1 ? 1 : G * G;
+  }
+  if (natoms > kMaxAtoms) {
+    err = "too many atoms";
+    return -1;
+  }
+  const int n = natoms;
+  const bool new_geometry = cl.h_rep.size() != reps.size() || !cl.rep ||
+                            memcmp(cl.h_rep.data(), reps.data(),
+                                   sizeof(ClusterReplica) * reps.size()) != 0;
+  cl.nrep = (int)reps.size();
+  cl.natoms = n;
+  cl.h_rep = reps;
+  cl.ncells = cell0;
+  cl.ncols = col0;
+  if (new_geometry) {
+    if ((e = realloc_dev(cl.rep, reps.size())) != cudaSuccess) return e;
+    if ((e = cudaMemcpyAsync(cl.rep, reps.data(), sizeof(ClusterReplica) * reps.size(),
+                             cudaMemcpyHostToDevice, st)) != cudaSuccess)
+      return e;
+    // the copy reads cl.h_rep, which stays alive; no wait needed
+  }
+  if (cl.ncells + 1 > cl.cells_alloc) {
+    for (int** p : {&cl.count, &cl.start, &cl.fill, &cl.segidx})
+      if ((e = realloc_dev(*p, (size_t)cl.ncells + 1)) != cudaSuccess) return e;
+    if ((e = realloc_dev(cl.seg, (size_t)cl.ncells)) != cudaSuccess) return e;
+    cl.cells_alloc = cl.ncells + 1;
+    cl.seg_alloc = cl.ncells;
+  }
+  if (n > cl.n_alloc) {
+    for (int** p : {&cl.cell, &cl.unsorted, &cl.perm, &cl.itmp})
+      if ((e = realloc_dev(*p, (size_t)n)) != cudaSuccess) return e;
+    if ((e = realloc_dev(cl.orig, (size_t)n)) != cudaSuccess) return e;
+    k_iota<<<nb(n, 256), 256, 0, st>>>(cl.orig, n);  // first build: identity
+    if ((e = realloc_dev(cl.len, (size_t)n)) != cudaSuccess) return e;
+    if ((e = realloc_dev(cl.pos_build, (size_t)n)) != cudaSuccess) return e;
+    if ((e = realloc_dev(cl.pos_tmp, (size_t)n)) != cudaSuccess) return e;
+    for (int k = 0; k < 5; k++)
+      if (v3[k] && *v3[k] && (e = realloc_dev(cl.v3_tmp[k], 3 * (size_t)n)) != cudaSuccess)
+        return e;
+    cl.n_alloc = n;
+  }
+  if (!cl.skin) {
+    if ((e = cudaMalloc(&cl.skin, sizeof(int) * 8)) != cudaSuccess) return e;
+    cudaMemsetAsync(cl.skin, 0, sizeof(int) * 8, st);
+  }
+  if (!cl.counters && (e = cudaMalloc(&cl.counters, sizeof(int) * 8)) != cudaSuccess) return e;
+  cudaMemsetAsync(cl.counters, 0, sizeof(int) * 8, st);
+  cudaMemsetAsync(cl.count, 0, sizeof(int) * ((size_t)cl.ncells + 1), st);
+  cudaMemsetAsync(cl.fill, 0, sizeof(int) * ((size_t)cl.ncells + 1), st);
+  const int T = 256;
+  if (n > 0)
+    k_cl_assign<<<nb(n, T), T, 0, st>>>(*pos, n, cl.rep, cl.nrep, cl.cell, cl.count, cl.counters,
+                                        d_status);
+  if ((e = scan_exclusive(cl.count, cl.start, cl.ncells + 1, sc, st)) != cudaSuccess) return e;
+  if (n > 0) {
+    k_cl_scatter<<<nb(n, T), T, 0, st>>>(cl.cell, n, cl.start, cl.fill, cl.unsorted);
+    k_cl_rank<<<nb(n, T), T, 0, st>>>(cl.unsorted, cl.cell, cl.orig, n, cl.start, cl.perm);
+    // permute the state into cell order
+    k_gather<md_double4><<<nb(n, T), T, 0, st>>>(*pos, cl.pos_tmp, cl.perm, n);
+    std::swap(*pos, cl.pos_tmp);
+    for (int k = 0; k < 5; k++)
+      if (v3[k] && *v3[k]) {
+        k_gather3<<<nb(n, T), T, 0, st>>>(*v3[k], cl.v3_tmp[k], cl.perm, n);
+        std::swap(*v3[k], cl.v3_tmp[k]);
+      }
+    k_gather<int><<<nb(n, T), T, 0, st>>>(cl.orig, cl.itmp, cl.perm, n);
+    std::swap(cl.orig, cl.itmp);
+    k_cl_posf<<<nb(n, T), T, 0, st>>>(*pos, cl.pos_build, posf, n);
+  }
+  // segments: greedy cut of the columns (fill is free again and holds the flags)
+  const int zmax = std::max(1, std::min(cl.Z, kClusterMaxZ));
+  k_seg_flags<<<nb(cl.ncols, 128), 128, 0, st>>>(cl.rep, cl.nrep, cl.ncols, cl.ncells, cl.count,
+                                                 cl.fill, cl.block,
+                                                 std::min(cl.stage_cap, kClusterMaxStaged), zmax);
+  if ((e = scan_exclusive(cl.fill, cl.segidx, cl.ncells + 1, sc, st)) != cudaSuccess) return e;
+  k_seg_emit<<<nb(cl.ncells, 256), 256, 0, st>>>(cl.rep, cl.nrep, cl.ncells, cl.fill, cl.segidx,
+                                                 cl.seg);
+  k_cl_segments<<<nb(cl.ncells, 128), 128, 0, st>>>(cl.seg, cl.segidx + cl.ncells, cl.rep,
+                                                    cl.start, cl.counters);
+  int hc[8];
+  int status = 0, nseg = 0;
+  cudaMemcpyAsync(hc, cl.counters, sizeof(hc), cudaMemcpyDeviceToHost, st);
+  cudaMemcpyAsync(&status, d_status, sizeof(int), cudaMemcpyDeviceToHost, st);
+  cudaMemcpyAsync(&nseg, cl.segidx + cl.ncells, sizeof(int), cudaMemcpyDeviceToHost, st);
+  if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
+  if (status & ST_NONFINITE) {
+    err = "non-finite position at list build";
+    return -1;
+  }
+  cl.nseg = nseg;
+  cl.max_staged = hc[0];
+  cl.maxcell = hc[4];
+  if (cl.max_staged > kClusterMaxStaged) {
+    err = "segment neighbourhood of " + std::to_string(cl.max_staged) +
+          " atoms exceeds the shared-memory stage (use fewer cells per segment)";
+    return -1;
+  }
+  static bool attrs = false;
+  if (!attrs) {
+    allow_smem(k_cl_rows<0>);
+    allow_smem(k_cl_rows<1>);
+    allow_smem(k_lj_cl<false, false, false>);
+    allow_smem(k_lj_cl<false, true, false>);
+    allow_smem(k_lj_cl<true, false, false>);
+    allow_smem(k_lj_cl<true, true, false>);
+    allow_smem(k_lj_cl<false, false, true>);
+    allow_smem(k_lj_cl<false, true, true>);
+    attrs = true;
+  }
+  const float margin = (float)(1e-6 * (reps.empty() ? 0.0 : reps.back().L + rv) + 1e-6);
+  const float rv_keep = rv + margin;
+  cl.rv = rv;
+  cl.rv2 = rv_keep * rv_keep;
+  cl.ld = (std::max(n, 1) + 31) / 32 * 32;
+  const size_t smem = stage_bytes(cl.max_staged);
+  if (cl.nseg > 0)
+    k_cl_rows<0><<<cl.nseg, 256, smem, st>>>(cl.seg, cl.rep, cl.start, cl.pos_build, cl.rv2,
+                                             nullptr, cl.len, cl.ld, 0, cl.counters);
+  cudaMemcpyAsync(hc, cl.counters, sizeof(hc), cudaMemcpyDeviceToHost, st);
+  if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
+  cl.maxlen = hc[1];
+  {
+    unsigned long long ent;
+    memcpy(&ent, hc + 2, sizeof(ent));
+    cl.entries = (long long)ent;
+  }
+  cl.cap = std::min(65535, (int)(std::max(cl.maxlen, 1) * cl.headroom) + 8);
+  const long long need = (long long)cl.cap * cl.ld;
+  if (need > cl.rows_elems || !cl.rows) {
+    if ((e = realloc_dev(cl.rows, (size_t)need)) != cudaSuccess) return e;
+    cl.rows_elems = need;
+  }
+  cl.rmap_ok = encode_tiled_2d(&cl.rmap, CU_TENSOR_MAP_DATA_TYPE_UINT16, cl.rows,
+                               (uint64_t)cl.ld, (uint64_t)cl.cap, (uint64_t)cl.ld * 2,
+                               (uint32_t)(cl.block + 8), (uint32_t)kClusterTileSlots);
+  if (!cl.rmap_ok) {
+    err = "TMA descriptor of the cluster rows could not be encoded";
+    return -1;
+  }
+  if (cl.nseg > 0)
+    k_cl_rows<1><<<cl.nseg, 256, smem, st>>>(cl.seg, cl.rep, cl.start, cl.pos_build, cl.rv2,
+                                             cl.rows, cl.len, cl.ld, cl.cap, cl.counters);
+  cl.trip_dist = 0.5 * ((double)rv - rcut) - (double)margin;
+  cudaMemsetAsync(cl.skin, 0, sizeof(int) * 4, st);  // trip flags and overflow
+  cl.built = true;
+  return (int)cudaGetLastError();
+}
+
+void launch_lj_cluster(const ClusterForceArgs& f, bool energy, cudaStream_t st) {
+  const ClusterList& cl = *f.cl;
+  if (cl.nseg == 0) return;
+  const size_t smem = 2 * kClusterTileSlots * (size_t)(cl.block + 8) * sizeof(uint16_t) +
+                      stage_bytes(cl.max_staged);
+  ClStep a;
+  a.seg = cl.seg;
+  a.reps = cl.rep;
+  a.start = cl.start;
+  a.posf = f.posf;
+  a.pos = f.pos;
+  a.f3 = f.f3;
+  a.rows = cl.rows;
+  a.len = cl.len;
+  a.ld = cl.ld;
+  a.cap = cl.cap;
+  a.rv2 = cl.rv2;
+  a.pos_build = cl.pos_build;
+  a.skin = cl.skin;
+  a.flag_read = f.step % 3;
+  a.flag_set = (f.step + 1) % 3;
+  a.flag_clear = (f.step + 2) % 3;
+  a.rcutsq = f.rcutsq;
+  a.sp = f.sp;
+  a.epart = f.epart;
+  a.status = f.status;
+  if (f.gear) a.g = *f.gear;
+  else memset(&a.g, 0, sizeof(a.g));
+#define MDGB_CL_LAUNCH(E, A, G) \
+  k_lj_cl<E, A, G><<<cl.nseg, cl.block, smem, st>>>(cl.rmap, a)
+  if (energy) {
+    if (f.all_ng) MDGB_CL_LAUNCH(true, true, false); else MDGB_CL_LAUNCH(true, false, false);
+  } else if (f.gear) {
+    if (f.all_ng) MDGB_CL_LAUNCH(false, true, true); else MDGB_CL_LAUNCH(false, false, true);
+  } else {
+    if (f.all_ng) MDGB_CL_LAUNCH(false, true, false); else MDGB_CL_LAUNCH(false, false, false);
+  }
+#undef MDGB_CL_LAUNCH
+}
+
+int cluster_reference_rows(const ClusterList& cl, const md_double4* pos, int nlistsize,
+                           int* d_out, signed char* d_img, int* d_nlargest, cudaStream_t st) {
+  if (cl.nseg == 0) return 0;
+  k_cl_ref_rows<<<cl.nseg, 128, 0, st>>>(cl.seg, cl.rep, cl.start, cl.orig, pos, nlistsize,
+                                         d_out, d_img, d_nlargest);
+  return (int)cudaGetLastError();
+}
+
+void launch_unpermute(const double* in, double* out, const int* orig, int n, int width,
+                      cudaStream_t st) {
+  if (n > 0) k_unpermute<<<nb(n, 256), 256, 0, st>>>(in, out, orig, n, width);
+}
+
+void launch_permute_in(const double* in, double* out, const int* orig, int n, int width,
+                       cudaStream_t st) {
+  if (n > 0) k_permute_in<<<nb(n, 256), 256, 0, st>>>(in, out, orig, n, width);
+}
+
+void cluster_free(ClusterList& cl) {
+  std::vector<void*> ptrs = {cl.rep,  cl.seg,      cl.count,     cl.start,   cl.fill, cl.segidx,
+                             cl.cell, cl.unsorted, cl.perm,      cl.orig,    cl.itmp,
+                             cl.rows, cl.len,      cl.pos_build, cl.pos_tmp, cl.skin,
+                             cl.counters};
+  for (int k = 0; k < 5; k++) ptrs.push_back(cl.v3_tmp[k]);
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  cl = ClusterList();
+}
+
+}  // namespace mdgb

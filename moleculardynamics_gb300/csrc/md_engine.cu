@@ -20,6 +20,7 @@
 #include <vector>
 
 #include "../../include/mdgb.h"
+#include "md_cluster.h"
 #include "md_forces.h"
 #include "md_integrate.h"
 #include "md_neighbor.cuh"
@@ -63,7 +64,7 @@ int next_build(float maxnlmove, double vmax, double dt, int t) {
   return nb > 2147483647LL ? 2147483647 : (int)nb;
 }
 
-constexpr int kKernels = 6;  // timing ids of md_kernel_time
+constexpr int kKernels = 7;  // timing ids of md_kernel_time
 
 __global__ void k_begin(md_double4* pos, double* vel, int n, double half_box, int clamp,
                         double vxcm) {
@@ -98,6 +99,13 @@ struct md_ctx {
          *f3_tmp = nullptr;
   float4* posf = nullptr;
   NeighborList lj, mb;
+  // precision form, periodic, LJ only: the cluster kernel; the state is then
+  // stored in cell order and cl.orig maps it to the caller's numbering
+  bool cluster = false;
+  ClusterList cl;
+  double* io = nullptr;  // 4 doubles per atom: permuted transfers
+  md_double4* pos_alt = nullptr;  // next positions of the fused force + Gear kernel
+  float4* posf_alt = nullptr;
   // bond-order scratch
   uint32_t* mb_sl = nullptr;
   int* mb_slen = nullptr;
@@ -123,10 +131,11 @@ struct md_ctx {
   bool timing = false;
   std::vector<cudaEvent_t> ev_pool;
   std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> pending;
-  double kt_ms[kKernels] = {0, 0, 0, 0, 0, 0};
-  long long kt_n[kKernels] = {0, 0, 0, 0, 0, 0};
+  double kt_ms[kKernels] = {0, 0, 0, 0, 0, 0, 0};
+  long long kt_n[kKernels] = {0, 0, 0, 0, 0, 0, 0};
 
   bool mixed() const { return cfg.precision == MD_PREC_MIXED; }
+  bool permuted() const { return cluster && cl.built; }
   bool walls() const { return !cfg.periodic; }
 };
 
@@ -270,10 +279,29 @@ MbArgs mb_args(md_ctx* c, double* f3, int ljexist) {
 
 // Host.cpp:132-135 / :157-161: LJ over all atoms (overwrites), bond order
 // over the first n_mb atoms (accumulates when LJ is on).
+ClusterForceArgs cl_args(md_ctx* c, double* f3, double* epart) {
+  ClusterForceArgs a;
+  a.cl = &c->cl;
+  a.posf = c->posf;
+  a.pos = c->pos;
+  a.f3 = f3;
+  a.step = c->t;
+  a.rcutsq = (double)c->lj_rcutsq;
+  a.sp = c->sp;
+  a.all_ng = c->all_ng;
+  a.epart = epart;
+  a.status = c->status;
+  a.gear = nullptr;
+  return a;
+}
+
 md_status forces(md_ctx* c, double* f3) {
   if (c->cfg.use_lj) {
     Timed tm(c, 0);
-    launch_lj(lj_args(c, f3, nullptr), c->mixed(), false, c->st);
+    if (c->cluster)
+      launch_lj_cluster(cl_args(c, f3, nullptr), false, c->st);
+    else
+      launch_lj(lj_args(c, f3, nullptr), c->mixed(), false, c->st);
     c->stats.launches++;
   }
   if (c->cfg.use_mb && c->cfg.n_mb > 0) {
@@ -296,11 +324,14 @@ GearArgs gear_args(md_ctx* c, int parity) {
   g.k = c->gear;
   g.sp = c->sp;
   g.posf = c->mixed() ? c->posf : nullptr;
-  const bool skin = c->cfg.use_lj && c->lj.compact && c->lj.pos_build;
-  g.pos_build = skin ? c->lj.pos_build : nullptr;
-  g.trip2 = skin ? (float)(c->lj.trip_dist * c->lj.trip_dist) : 0.f;
-  if (skin && c->lj.trip_dist <= 0) g.trip2 = -1.f;  // skin too thin: always walk full rows
-  g.trip = skin ? c->lj.skin + (parity & 1) : nullptr;
+  const float4* pb = c->cluster ? c->cl.pos_build : (c->lj.compact ? c->lj.pos_build : nullptr);
+  const double trip = c->cluster ? c->cl.trip_dist : c->lj.trip_dist;
+  int* skinf = c->cluster ? c->cl.skin : c->lj.skin;
+  const bool skin = c->cfg.use_lj && pb;
+  g.pos_build = skin ? pb : nullptr;
+  g.trip2 = skin ? (float)(trip * trip) : 0.f;
+  if (skin && trip <= 0) g.trip2 = -1.f;  // skin too thin: always walk full rows
+  g.trip = skin ? skinf + (c->cluster ? parity % 3 : parity & 1) : nullptr;
   g.status = c->status;
   g.exact = !c->mixed();
   for (int k = 0; k < 3; k++) g.inv_mass[k] = 1.0 / (double)c->sp.mass[k];
@@ -343,6 +374,39 @@ md_status rebuild(md_ctx* c, int t) {
   const bool both = c->cfg.periodic != 0;
   const double dt = (double)c->cfg.dt;
   bool did_lj = false;
+  if (c->cluster && c->cfg.use_lj && (c->lj_next == t || both)) {
+    if (c->cl.skin) {
+      int sk[5];
+      CK(cudaMemcpy(sk, c->cl.skin, sizeof(sk), cudaMemcpyDeviceToHost), "skin");
+      c->stats.list_trips += sk[4];
+      if (sk[3]) c->cl.headroom *= 1.5f;  // a refreshed row did not fit: more room
+      CK(cudaMemsetAsync(c->cl.skin + 4, 0, sizeof(int), c->st), "skin");
+    }
+    CK(cudaMemsetAsync(c->status, 0, sizeof(int), c->st), "status");
+    std::vector<ClusterReplica> reps(1);
+    reps[0].n = c->n;
+    reps[0].L = c->cfg.box;
+    double** v3[5] = {&c->vel, &c->acc, &c->b, &c->c, &c->f3};
+    std::string e;
+    int r = cluster_build(c->cl, reps, c->cfg.lj_rs, sqrt((double)c->lj_rcutsq), &c->pos, v3,
+                          c->posf, c->sc, c->status, c->st, e);
+    c->stats.launches += 17;
+    if (r != 0) {
+      if (r == -1) return fail(c, e.find("non-finite") != std::string::npos ? MD_NONFINITE : MD_BAD_CONFIG, e);
+      return cuda_fail(c, (cudaError_t)r, "LJ cluster build");
+    }
+    c->lj_next = next_build(c->lj_maxnlmove, vmax, dt, t);
+    c->stats.list_builds++;
+    c->stats.lj_max_row = c->cl.maxlen;
+    c->stats.lj_nlargest = 0;
+    c->stats.lj_cells = c->cl.h_rep[0].G;
+    c->stats.lj_list_entries = c->cl.entries;
+    c->stats.lj_tma = 0;
+    c->stats.lj_cluster = 1;
+    c->stats.cluster_segments = c->cl.nseg;
+    c->stats.cluster_max_staged = c->cl.max_staged;
+    return MD_OK;
+  }
   if (c->cfg.use_lj && (c->lj_next == t || both)) {
     if (c->lj.skin) {
       int sk[4];
@@ -416,10 +480,13 @@ md_status make_record(md_ctx* c, int t, double* rec16) {
   c->stats.launches += 5;
   CK(cudaMemsetAsync(elj, 0, sizeof(double) * 8, c->st), "record");
   if (c->cfg.use_lj) {
-    int B = lj_blocks(c->n);
+    int B = c->cluster ? cluster_blocks(c->cl) : lj_blocks(c->n);
     md_status s = ensure_epart(c, 3LL * B);
     if (s != MD_OK) return s;
-    launch_lj(lj_args(c, c->f3_tmp, c->epart), c->mixed(), true, c->st);
+    if (c->cluster)
+      launch_lj_cluster(cl_args(c, c->f3_tmp, c->epart), true, c->st);
+    else
+      launch_lj(lj_args(c, c->f3_tmp, c->epart), c->mixed(), true, c->st);
     launch_sum_partials(c->epart, B, 3, elj, c->st);
     c->stats.launches += 2;
   }
@@ -487,10 +554,38 @@ md_status step_once(md_ctx* c, bool last) {
     c->stats.launches++;
   }
   c->predicted = false;
-  forces(c, c->f3);
-  if (c->walls()) CK(cudaMemsetAsync(c->wall_flag, 0, sizeof(int), c->st), "wall flag");
   const bool output = c->cfg.output_timesteps > 0 && c->printout == t;
   const bool fuse = c->mixed() && !c->walls() && !last && !output && !due(c, t + 1);
+  if (c->cluster && fuse) {
+    // forces of step t, correct of step t and predict of step t + 1 in one
+    // kernel; the next positions go to the other buffer
+    GearArgs g = gear_args(c, t + 1);
+    ClusterGearArgs cg;
+    cg.pos_next = c->pos_alt;
+    cg.posf_next = c->posf_alt;
+    cg.vel = c->vel;
+    cg.acc = c->acc;
+    cg.b = c->b;
+    cg.c = c->c;
+    cg.k = c->gear;
+    for (int k = 0; k < 3; k++) cg.inv_mass[k] = g.inv_mass[k];
+    cg.trip2 = g.trip2;
+    ClusterForceArgs a = cl_args(c, nullptr, nullptr);
+    a.gear = &cg;
+    {
+      Timed tm(c, 6);
+      launch_lj_cluster(a, false, c->st);
+    }
+    std::swap(c->pos, c->pos_alt);
+    std::swap(c->posf, c->posf_alt);
+    c->predicted = true;
+    c->stats.launches++;
+    c->t++;
+    c->stats.steps++;
+    return MD_OK;
+  }
+  forces(c, c->f3);
+  if (c->walls()) CK(cudaMemsetAsync(c->wall_flag, 0, sizeof(int), c->st), "wall flag");
   {
     Timed tm(c, 3);
     if (fuse) {
@@ -564,11 +659,21 @@ md_status md_create(const md_config* cfg, md_ctx** out) {
     // the bond-order third-body pass needs distinct stencil cells
     if (cfg->use_mb && floor(cfg->box / (double)cfg->mb_rs) < 3) return MD_BAD_CONFIG;
   }
+  const bool cluster_ok = cfg->precision == MD_PREC_MIXED && cfg->periodic && cfg->use_lj &&
+                          !(cfg->use_mb && cfg->n_mb > 0);
+  if (cfg->lj_kernel < MD_LJ_AUTO || cfg->lj_kernel > MD_LJ_CLUSTER) return MD_BAD_CONFIG;
+  if (cfg->lj_kernel == MD_LJ_CLUSTER && !cluster_ok) return MD_BAD_CONFIG;
+  if (cfg->cluster_cells < 0 || cfg->cluster_cells > kClusterMaxZ) return MD_BAD_CONFIG;
+  if (cfg->cluster_threads < 0 || cfg->cluster_threads > 224 || cfg->cluster_threads % 32)
+    return MD_BAD_CONFIG;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= cfg->device || cfg->device < 0)
     return MD_NO_DEVICE;
   md_ctx* c = new md_ctx();
   c->cfg = *cfg;
+  c->cluster = cluster_ok && cfg->lj_kernel != MD_LJ_ROWS;
+  if (cfg->cluster_cells > 0) c->cl.Z = cfg->cluster_cells;
+  if (cfg->cluster_threads > 0) c->cl.block = cfg->cluster_threads;
   c->n = (int)n;
   c->sp = species_table(cfg->species);
   c->gear = gear_coef((double)cfg->dt);
@@ -591,6 +696,13 @@ md_status md_create(const md_config* cfg, md_ctx** out) {
   for (double** p : vecs)
     if ((e = cudaMalloc(p, sizeof(double) * 3 * N)) != cudaSuccess) return bail(e, "state");
   if ((e = cudaMalloc(&c->posf, sizeof(float4) * N)) != cudaSuccess) return bail(e, "posf");
+  if (c->cluster) {
+    if ((e = cudaMalloc(&c->io, sizeof(double) * 4 * N)) != cudaSuccess) return bail(e, "io");
+    if ((e = cudaMalloc(&c->pos_alt, sizeof(md_double4) * N)) != cudaSuccess)
+      return bail(e, "pos");
+    if ((e = cudaMalloc(&c->posf_alt, sizeof(float4) * N)) != cudaSuccess)
+      return bail(e, "posf");
+  }
   if ((e = cudaMalloc(&c->status, sizeof(int) * 4)) != cudaSuccess) return bail(e, "flags");
   c->wall_flag = c->status + 1;
   c->missing = c->status + 2;
@@ -611,7 +723,8 @@ void md_destroy(md_ctx* c) {
   if (c->st) cudaStreamSynchronize(c->st);
   list_free(c->lj);
   list_free(c->mb);
-  void* ptrs[] = {c->pos, c->vel, c->acc, c->b, c->c, c->f3, c->f3_tmp, c->posf, c->mb_sl,
+  cluster_free(c->cl);
+  void* ptrs[] = {c->io, c->pos_alt, c->posf_alt, c->pos, c->vel, c->acc, c->b, c->c, c->f3, c->f3_tmp, c->posf, c->mb_sl,
                   c->mb_slen, c->xsi, c->xsj, c->va, c->status, c->epart, c->dsc, c->rec,
                   c->sc.dpart, c->sc.umax, c->sc.counts, c->sc.block_sums};
   for (void* p : ptrs)
@@ -629,21 +742,47 @@ md_status md_upload(md_ctx* c, const double* pos4, const double* vel3) {
   return md_upload_state(c, pos4, vel3, nullptr, nullptr, nullptr);
 }
 
+// host -> device array of `width` doubles per atom, in the caller's numbering
+md_status put_array(md_ctx* c, double* dst, const double* src, int width) {
+  const size_t B = sizeof(double) * (size_t)width * (size_t)c->n;
+  if (!c->permuted()) {
+    CK(cudaMemcpyAsync(dst, src, B, cudaMemcpyHostToDevice, c->st), "upload");
+    return MD_OK;
+  }
+  CK(cudaMemcpyAsync(c->io, src, B, cudaMemcpyHostToDevice, c->st), "upload");
+  launch_permute_in(c->io, dst, c->cl.orig, c->n, width, c->st);
+  // io is reused by the next transfer: complete this one first
+  CK(cudaStreamSynchronize(c->st), "upload");
+  return MD_OK;
+}
+
+md_status get_array(md_ctx* c, double* dst, const double* src, int width) {
+  const size_t B = sizeof(double) * (size_t)width * (size_t)c->n;
+  if (!c->permuted()) {
+    CK(cudaMemcpyAsync(dst, src, B, cudaMemcpyDeviceToHost, c->st), "download");
+    return MD_OK;
+  }
+  launch_unpermute(src, c->io, c->cl.orig, c->n, width, c->st);
+  CK(cudaMemcpyAsync(dst, c->io, B, cudaMemcpyDeviceToHost, c->st), "download");
+  CK(cudaStreamSynchronize(c->st), "download");
+  return MD_OK;
+}
+
 md_status md_upload_state(md_ctx* c, const double* pos4, const double* vel3, const double* a3,
                           const double* b3, const double* c3) {
   if (!c) return MD_BAD_ARGUMENT;
   const size_t N = (size_t)c->n;
+  md_status s = MD_OK;
   if (pos4) {
     int all = 1;
     for (size_t i = 0; i < N && all; i++) all = (int)pos4[4 * i + 3] == SP_NG;
     c->all_ng = all;
-    CK(cudaMemcpyAsync(c->pos, pos4, sizeof(double) * 4 * N, cudaMemcpyHostToDevice, c->st), "upload");
+    if ((s = put_array(c, (double*)c->pos, pos4, 4)) != MD_OK) return s;
   }
-  if (vel3)
-    CK(cudaMemcpyAsync(c->vel, vel3, sizeof(double) * 3 * N, cudaMemcpyHostToDevice, c->st), "upload");
-  if (a3) CK(cudaMemcpyAsync(c->acc, a3, sizeof(double) * 3 * N, cudaMemcpyHostToDevice, c->st), "upload");
-  if (b3) CK(cudaMemcpyAsync(c->b, b3, sizeof(double) * 3 * N, cudaMemcpyHostToDevice, c->st), "upload");
-  if (c3) CK(cudaMemcpyAsync(c->c, c3, sizeof(double) * 3 * N, cudaMemcpyHostToDevice, c->st), "upload");
+  if (vel3 && (s = put_array(c, c->vel, vel3, 3)) != MD_OK) return s;
+  if (a3 && (s = put_array(c, c->acc, a3, 3)) != MD_OK) return s;
+  if (b3 && (s = put_array(c, c->b, b3, 3)) != MD_OK) return s;
+  if (c3 && (s = put_array(c, c->c, c3, 3)) != MD_OK) return s;
   if (c->mixed() && pos4) launch_posf(c->pos, c->posf, c->n, c->st);
   CK(cudaStreamSynchronize(c->st), "upload");
   return MD_OK;
@@ -651,22 +790,20 @@ md_status md_upload_state(md_ctx* c, const double* pos4, const double* vel3, con
 
 md_status md_download(md_ctx* c, double* pos4, double* vel3) {
   if (!c) return MD_BAD_ARGUMENT;
-  const size_t N = (size_t)c->n;
-  if (pos4)
-    CK(cudaMemcpyAsync(pos4, c->pos, sizeof(double) * 4 * N, cudaMemcpyDeviceToHost, c->st), "download");
-  if (vel3)
-    CK(cudaMemcpyAsync(vel3, c->vel, sizeof(double) * 3 * N, cudaMemcpyDeviceToHost, c->st), "download");
+  md_status s = MD_OK;
+  if (pos4 && (s = get_array(c, pos4, (const double*)c->pos, 4)) != MD_OK) return s;
+  if (vel3 && (s = get_array(c, vel3, c->vel, 3)) != MD_OK) return s;
   CK(cudaStreamSynchronize(c->st), "download");
   return MD_OK;
 }
 
 md_status md_download_state(md_ctx* c, double* a3, double* b3, double* c3, double* f3) {
   if (!c) return MD_BAD_ARGUMENT;
-  const size_t B = sizeof(double) * 3 * (size_t)c->n;
-  if (a3) CK(cudaMemcpyAsync(a3, c->acc, B, cudaMemcpyDeviceToHost, c->st), "download");
-  if (b3) CK(cudaMemcpyAsync(b3, c->b, B, cudaMemcpyDeviceToHost, c->st), "download");
-  if (c3) CK(cudaMemcpyAsync(c3, c->c, B, cudaMemcpyDeviceToHost, c->st), "download");
-  if (f3) CK(cudaMemcpyAsync(f3, c->f3, B, cudaMemcpyDeviceToHost, c->st), "download");
+  md_status s = MD_OK;
+  if (a3 && (s = get_array(c, a3, c->acc, 3)) != MD_OK) return s;
+  if (b3 && (s = get_array(c, b3, c->b, 3)) != MD_OK) return s;
+  if (c3 && (s = get_array(c, c3, c->c, 3)) != MD_OK) return s;
+  if (f3 && (s = get_array(c, f3, c->f3, 3)) != MD_OK) return s;
   CK(cudaStreamSynchronize(c->st), "download");
   return MD_OK;
 }
@@ -761,8 +898,10 @@ md_status md_compute_forces(md_ctx* c, double* f3, double* energy5) {
   // forces of the same evaluation as Host.cpp:132-135 (f3_tmp holds LJ then
   // bond order written by the energy kernels without accumulation; redo it)
   forces(c, c->f3_tmp);
-  if (f3)
-    CK(cudaMemcpyAsync(f3, c->f3_tmp, sizeof(double) * 3 * (size_t)c->n, cudaMemcpyDeviceToHost, c->st), "forces");
+  if (f3) {
+    md_status gs = get_array(c, f3, c->f3_tmp, 3);
+    if (gs != MD_OK) return gs;
+  }
   CK(cudaStreamSynchronize(c->st), "forces");
   if (energy5) {
     energy5[0] = e[8];
@@ -777,6 +916,39 @@ md_status md_compute_forces(md_ctx* c, double* f3, double* energy5) {
 md_status md_neighbor_list(md_ctx* c, int which, int* rows, signed char* images,
                            long long capacity, int* nlistsize, int* nlargest) {
   if (!c || (which != 0 && which != 1)) return MD_BAD_ARGUMENT;
+  if (which == 0 && c->cluster) {
+    if (!c->cl.built) return fail(c, MD_BAD_ARGUMENT, "list not built (call md_begin)");
+    long long nls = 27LL * c->cl.maxcell;
+    if (nls > c->n - 1) nls = c->n - 1;
+    if (nls < 0) nls = 0;
+    int* d_rows = nullptr;
+    signed char* d_img = nullptr;
+    int* d_nl = c->sc.counts;
+    CK(cudaMemsetAsync(d_nl, 0, sizeof(int), c->st), "list rows");
+    const long long need = nls * c->n;
+    if (rows && capacity < need) return fail(c, MD_LIST_OVERFLOW, "rows buffer too small");
+    if (rows && need > 0) {
+      CK(cudaMalloc(&d_rows, sizeof(int) * (size_t)need), "list rows");
+      if (images && cudaMalloc(&d_img, (size_t)need) != cudaSuccess) {
+        cudaFree(d_rows);
+        return fail(c, MD_OUT_OF_MEMORY, "list images");
+      }
+    }
+    cluster_reference_rows(c->cl, c->pos, (int)nls, d_rows, d_img, d_nl, c->st);
+    int h_nl = 0;
+    cudaError_t e = cudaMemcpyAsync(&h_nl, d_nl, sizeof(int), cudaMemcpyDeviceToHost, c->st);
+    if (e == cudaSuccess && d_rows)
+      e = cudaMemcpyAsync(rows, d_rows, sizeof(int) * (size_t)need, cudaMemcpyDeviceToHost, c->st);
+    if (e == cudaSuccess && d_img)
+      e = cudaMemcpyAsync(images, d_img, (size_t)need, cudaMemcpyDeviceToHost, c->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
+    if (d_rows) cudaFree(d_rows);
+    if (d_img) cudaFree(d_img);
+    if (e != cudaSuccess) return cuda_fail(c, e, "list rows");
+    if (nlistsize) *nlistsize = (int)nls;
+    if (nlargest) *nlargest = h_nl;
+    return MD_OK;
+  }
   NeighborList& nl = which == 0 ? c->lj : c->mb;
   if (!nl.cell3) return fail(c, MD_BAD_ARGUMENT, "list not built (call md_begin)");
   if (nlistsize) *nlistsize = nl.nlistsize;
@@ -806,15 +978,83 @@ md_status md_neighbor_list(md_ctx* c, int which, int* rows, signed char* images,
 md_status md_get_stats(const md_ctx* c, md_stats* out) {
   if (!c || !out) return MD_BAD_ARGUMENT;
   *out = c->stats;
-  if (c->lj.skin) {
+  int* skin = c->cluster ? c->cl.skin : c->lj.skin;
+  if (skin) {
     // skin refreshes since the last list build are still on the device
-    int sk[4];
+    int sk[5] = {0, 0, 0, 0, 0};
+    const size_t words = c->cluster ? 5 : 4;  // the row-list flags hold 4 ints
     if (cudaStreamSynchronize(c->st) != cudaSuccess ||
-        cudaMemcpy(sk, c->lj.skin, sizeof(sk), cudaMemcpyDeviceToHost) != cudaSuccess)
+        cudaMemcpy(sk, skin, sizeof(int) * words, cudaMemcpyDeviceToHost) != cudaSuccess)
       return MD_CUDA_ERROR;
-    out->list_trips += sk[3];
+    out->list_trips += c->cluster ? sk[4] : sk[3];
   }
   return MD_OK;
+}
+
+md_status md_autotune(md_ctx* c, int evals, md_tune_result* out) {
+  if (!c || evals < 1) return MD_BAD_ARGUMENT;
+  if (out) memset(out, 0, sizeof(*out));
+  if (!c->cluster) return MD_OK;  // only the cluster kernel has tiles to pick
+  if (!c->begun) return fail(c, MD_BAD_ARGUMENT, "md_begin has not been called");
+  const bool fixed_threads = c->cfg.cluster_threads > 0;
+  std::vector<int> threads = fixed_threads ? std::vector<int>{c->cl.block}
+                                           : std::vector<int>{64, 96, 128, 160, 192};
+  const std::vector<int> caps = {1152, 1536, kClusterMaxStaged};
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0), "autotune");
+  CK(cudaEventCreate(&e1), "autotune");
+  double best = 1e300;
+  int best_t = c->cl.block, best_c = c->cl.stage_cap, tried = 0;
+  std::vector<ClusterReplica> reps(1);
+  reps[0].n = c->n;
+  reps[0].L = c->cfg.box;
+  double** v3[5] = {&c->vel, &c->acc, &c->b, &c->c, &c->f3};
+  auto build = [&](int t, int cap) -> md_status {
+    c->cl.block = t;
+    c->cl.stage_cap = cap;
+    std::string e;
+    int r = cluster_build(c->cl, reps, c->cfg.lj_rs, sqrt((double)c->lj_rcutsq), &c->pos, v3,
+                          c->posf, c->sc, c->status, c->st, e);
+    if (r == -1) return fail(c, MD_BAD_CONFIG, e);
+    if (r != 0) return cuda_fail(c, (cudaError_t)r, "autotune build");
+    return MD_OK;
+  };
+  md_status s = MD_OK;
+  for (int t : threads)
+    for (int cap : caps) {
+      if ((s = build(t, cap)) != MD_OK) break;
+      launch_lj_cluster(cl_args(c, c->f3_tmp, nullptr), false, c->st);  // warm
+      cudaEventRecord(e0, c->st);
+      for (int k = 0; k < evals; k++)
+        launch_lj_cluster(cl_args(c, c->f3_tmp, nullptr), false, c->st);
+      cudaEventRecord(e1, c->st);
+      cudaError_t ce = cudaEventSynchronize(e1);
+      float ms = 0;
+      if (ce == cudaSuccess) ce = cudaEventElapsedTime(&ms, e0, e1);
+      if (ce != cudaSuccess) {
+        s = cuda_fail(c, ce, "autotune");
+        break;
+      }
+      tried++;
+      if (ms < best) {
+        best = ms;
+        best_t = t;
+        best_c = cap;
+      }
+    }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (s != MD_OK) return s;
+  if ((s = build(best_t, best_c)) != MD_OK) return s;
+  c->stats.cluster_segments = c->cl.nseg;
+  c->stats.cluster_max_staged = c->cl.max_staged;
+  if (out) {
+    out->threads = best_t;
+    out->stage_cap = best_c;
+    out->candidates = tried;
+    out->best_ms = best / evals;
+  }
+  return check_status(c);
 }
 
 md_status md_set_timing(md_ctx* c, int on) {

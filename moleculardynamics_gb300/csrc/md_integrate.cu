@@ -8,6 +8,7 @@
 // them in a fixed order.
 #include <cmath>
 
+#include "md_gear.cuh"
 #include "md_integrate.h"
 #include "md_potential.cuh"
 
@@ -65,25 +66,37 @@ __global__ void __launch_bounds__(256) k_gear(GearArgs a) {
   if (MODE != G_PREDICT) {
     const double mass = mass_of(type, a.sp);
     const double im = type == SP_N ? a.inv_mass[0] : (type == SP_O ? a.inv_mass[1] : a.inv_mass[2]);
+    if (EXACT) {
 #pragma unroll
-    for (int d = 0; d < 3; d++) {
-      const double f = a.f3[3 * i + d];
-      if (EXACT) {
-        const double ai = xdiv(f, mass);
+      for (int d = 0; d < 3; d++) {
+        const double ai = xdiv(a.f3[3 * i + d], mass);
         const double corr = xsub(ai, ac[d]);
         rr[d] = xadd(rr[d], xmul(k.cr, corr));
         v[d] = xadd(v[d], xmul(k.cv, corr));
         ac[d] = ai;
         b[d] = xadd(b[d], xmul(k.cb, corr));
         c[d] = xadd(c[d], xmul(k.cc, corr));
-      } else {
-        const double ai = f * im;
-        const double corr = ai - ac[d];
-        rr[d] = fma(k.cr, corr, rr[d]);
-        v[d] = fma(k.cv, corr, v[d]);
-        ac[d] = ai;
-        b[d] = fma(k.cb, corr, b[d]);
-        c[d] = fma(k.cc, corr, c[d]);
+      }
+    } else {
+      GearAtom s;
+      double f[3];
+#pragma unroll
+      for (int d = 0; d < 3; d++) {
+        s.r[d] = rr[d];
+        s.v[d] = v[d];
+        s.a[d] = ac[d];
+        s.b[d] = b[d];
+        s.c[d] = c[d];
+        f[d] = a.f3[3 * i + d];
+      }
+      gear_correct_fma(s, f, im, k);
+#pragma unroll
+      for (int d = 0; d < 3; d++) {
+        rr[d] = s.r[d];
+        v[d] = s.v[d];
+        ac[d] = s.a[d];
+        b[d] = s.b[d];
+        c[d] = s.c[d];
       }
     }
     if (MODE == G_CORRECT && a.walls) {
@@ -101,20 +114,33 @@ __global__ void __launch_bounds__(256) k_gear(GearArgs a) {
       atomicOr(a.status, ST_NONFINITE);
   }
   if (MODE != G_CORRECT) {
+    if (EXACT) {
 #pragma unroll
-    for (int d = 0; d < 3; d++) {
-      if (EXACT) {
+      for (int d = 0; d < 3; d++) {
         rr[d] = xadd(xadd(xadd(xadd(rr[d], xmul(k.c1, v[d])), xmul(k.c2, ac[d])),
                           xmul(k.c3, b[d])),
                      xmul(k.c4, c[d]));
         v[d] = xadd(xadd(xadd(v[d], xmul(k.c1, ac[d])), xmul(k.c2, b[d])), xmul(k.c3, c[d]));
         ac[d] = xadd(xadd(ac[d], xmul(k.c1, b[d])), xmul(k.c2, c[d]));
         b[d] = xadd(b[d], xmul(k.c1, c[d]));
-      } else {
-        rr[d] = fma(k.c4, c[d], fma(k.c3, b[d], fma(k.c2, ac[d], fma(k.c1, v[d], rr[d]))));
-        v[d] = fma(k.c3, c[d], fma(k.c2, b[d], fma(k.c1, ac[d], v[d])));
-        ac[d] = fma(k.c2, c[d], fma(k.c1, b[d], ac[d]));
-        b[d] = fma(k.c1, c[d], b[d]);
+      }
+    } else {
+      GearAtom s;
+#pragma unroll
+      for (int d = 0; d < 3; d++) {
+        s.r[d] = rr[d];
+        s.v[d] = v[d];
+        s.a[d] = ac[d];
+        s.b[d] = b[d];
+        s.c[d] = c[d];
+      }
+      gear_predict_fma(s, k);
+#pragma unroll
+      for (int d = 0; d < 3; d++) {
+        rr[d] = s.r[d];
+        v[d] = s.v[d];
+        ac[d] = s.a[d];
+        b[d] = s.b[d];
       }
     }
   }

@@ -81,6 +81,11 @@ int list_reference_rows(const NeighborList& nl, const md_double4* pos, int* d_ou
                         signed char* d_img, cudaStream_t st);
 void list_free(NeighborList& nl);
 Grid make_grid_reference(double box_list, float rs);
+// 2-D tiled TMA descriptor (no swizzle, zero fill out of range); 1 on success
+int encode_tiled_2d(CUtensorMap* map, CUtensorMapDataType type, void* base, uint64_t dim0,
+                    uint64_t dim1, uint64_t stride_bytes, uint32_t box0, uint32_t box1);
+// exclusive prefix sum of n ints (n <= 2^24)
+cudaError_t scan_exclusive(const int* in, int* out, int n, Scratch& sc, cudaStream_t st);
 Grid make_grid_periodic(double L, float rs);
 
 // Walk context handed to kernels that iterate full candidate rows.

@@ -199,6 +199,19 @@ extern "C" md_status md_read_config(const char* path, md_config* cfg, char* stri
     set_err("bad value for ReferenceEnergy");
     return MD_BAD_CONFIG;
   }
+  if (get_str(p, "LJKernel", sv)) {
+    std::string u = upper(sv);
+    if (u.rfind("AUTO", 0) == 0)
+      c.lj_kernel = MD_LJ_AUTO;
+    else if (u.rfind("ROWS", 0) == 0)
+      c.lj_kernel = MD_LJ_ROWS;
+    else if (u.rfind("CLUSTER", 0) == 0)
+      c.lj_kernel = MD_LJ_CLUSTER;
+    else {
+      set_err("bad value for LJKernel (AUTO, ROWS or CLUSTER)");
+      return MD_BAD_CONFIG;
+    }
+  }
   *cfg = c;
   if (strings) {
     put(strings, in);

@@ -260,6 +260,20 @@ static EncodeTiledFn encode_fn() {
   return fn;
 }
 
+int encode_tiled_2d(CUtensorMap* map, CUtensorMapDataType type, void* base, uint64_t dim0,
+                    uint64_t dim1, uint64_t stride_bytes, uint32_t box0, uint32_t box1) {
+  EncodeTiledFn fn = encode_fn();
+  if (!fn || stride_bytes % 16 != 0) return 0;
+  cuuint64_t dims[2] = {(cuuint64_t)dim0, (cuuint64_t)dim1};
+  cuuint64_t strides[1] = {(cuuint64_t)stride_bytes};
+  cuuint32_t box[2] = {box0, box1};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = fn(map, type, 2, base, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                  CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? 1 : 0;
+}
+
 // TMA descriptor of a compact list: a 2-D uint32 tensor of n atoms (x) by
 // cap slots (y), row stride ld * 4 bytes; tiles of kListTileAtoms x
 // kListTileSlots.  Out-of-range atoms and slots read as zero.
@@ -317,7 +331,7 @@ RowWalker make_walker(const NeighborList& nl) {
   return w;
 }
 
-static cudaError_t scan_exclusive(const int* in, int* out, int n, Scratch& sc, cudaStream_t st) {
+cudaError_t scan_exclusive(const int* in, int* out, int n, Scratch& sc, cudaStream_t st) {
   int tiles = blocks(n, kScanTile);
   if (tiles > kScanTile) return cudaErrorInvalidValue;
   if (sc.block_sums_cap < 2 * tiles + 2) {

@@ -24,8 +24,10 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(PKG, "libmdgb.so")
 
 PREC_FP64, PREC_MIXED = 0, 1
+LJ_AUTO, LJ_ROWS, LJ_CLUSTER = 0, 1, 2
 SPECIES_NEON, SPECIES_ARGON = 0, 1
-KERNEL_LJ, KERNEL_MB, KERNEL_PREDICT, KERNEL_CORRECT, KERNEL_LIST, KERNEL_STEP = range(6)
+(KERNEL_LJ, KERNEL_MB, KERNEL_PREDICT, KERNEL_CORRECT, KERNEL_LIST, KERNEL_STEP,
+ KERNEL_FUSED) = range(7)
 
 
 class EngineError(RuntimeError):
@@ -40,7 +42,8 @@ class MdConfig(C.Structure):
                 ("mb_rcut", C.c_float), ("use_lj", C.c_int), ("use_mb", C.c_int),
                 ("output_timesteps", C.c_int), ("energy_loss", C.c_float), ("periodic", C.c_int),
                 ("box", C.c_double), ("precision", C.c_int), ("species", C.c_int),
-                ("device", C.c_int), ("reference_energy", C.c_int)]
+                ("device", C.c_int), ("reference_energy", C.c_int), ("lj_kernel", C.c_int),
+                ("cluster_cells", C.c_int), ("cluster_threads", C.c_int)]
 
 
 THERMO_FIELDS = ["time", "temperature", "e", "ek", "eu", "com_x", "com_y", "com_z",
@@ -58,7 +61,13 @@ class MdStats(C.Structure):
                 ("missing_xi", C.c_longlong), ("launches", C.c_longlong),
                 ("lj_max_row", C.c_int), ("lj_nlargest", C.c_int), ("mb_nlargest", C.c_int),
                 ("lj_cells", C.c_int), ("mb_cells", C.c_int), ("lj_list_entries", C.c_longlong),
-                ("lj_tma", C.c_int)]
+                ("lj_tma", C.c_int), ("lj_cluster", C.c_int), ("cluster_segments", C.c_int),
+                ("cluster_max_staged", C.c_int)]
+
+
+class MdTuneResult(C.Structure):
+    _fields_ = [("threads", C.c_int), ("stage_cap", C.c_int), ("candidates", C.c_int),
+                ("best_ms", C.c_double)]
 
 
 class ListSettings(C.Structure):
@@ -81,7 +90,7 @@ EXPORTS = ["md_create", "md_destroy", "md_status_string", "md_last_error", "md_u
            "mdgb_build_neighbor_list", "mdgb_free", "mdgb_perform_calculations",
            "mdgb_calculate_potential", "mdgb_set_species", "mdgb_last_status", "md_read_config",
            "md_write_results", "md_host_alloc", "md_host_free",
-           "mdgb_many_body_forces_static"]
+           "mdgb_many_body_forces_static", "md_autotune"]
 
 
 def load(path: str | None = None) -> C.CDLL:
@@ -117,6 +126,7 @@ def load(path: str | None = None) -> C.CDLL:
     L.md_set_timing.argtypes = [C.c_void_p, C.c_int]
     L.md_kernel_time.argtypes = [C.c_void_p, C.c_int, P(C.c_double), P(C.c_longlong)]
     L.md_synchronize.argtypes = [C.c_void_p]
+    L.md_autotune.argtypes = [C.c_void_p, C.c_int, P(MdTuneResult)]
     L.md_host_alloc.restype = C.c_void_p
     L.md_host_alloc.argtypes = [C.c_size_t]
     L.md_host_free.argtypes = [C.c_void_p]
@@ -150,10 +160,11 @@ def load(path: str | None = None) -> C.CDLL:
 def make_config(n_lj=0, n_mb=0, dt=2.0, timesteps=0, lj_rs=9.534, lj_rcut=8.5125, mb_rs=3.5,
                 mb_rcut=3.0, use_lj=1, use_mb=0, output_timesteps=0, energy_loss=1.0,
                 periodic=0, box=0.0, precision=PREC_FP64, species=SPECIES_ARGON, device=0,
-                reference_energy=0) -> MdConfig:
+                reference_energy=0, lj_kernel=0, cluster_cells=0,
+                cluster_threads=0) -> MdConfig:
     return MdConfig(n_lj, n_mb, dt, timesteps, lj_rs, lj_rcut, mb_rs, mb_rcut, use_lj, use_mb,
                     output_timesteps, energy_loss, periodic, box, precision, species, device,
-                    reference_energy)
+                    reference_energy, lj_kernel, cluster_cells, cluster_threads)
 
 
 class Engine:
@@ -258,6 +269,11 @@ class Engine:
         s = MdStats()
         self._ck(self.lib.md_get_stats(self.h, C.byref(s)), "md_get_stats")
         return {k: getattr(s, k) for k, _ in MdStats._fields_}
+
+    def autotune(self, evals: int = 3) -> dict:
+        r = MdTuneResult()
+        self._ck(self.lib.md_autotune(self.h, evals, C.byref(r)), "md_autotune")
+        return {k: getattr(r, k) for k, _ in MdTuneResult._fields_}
 
     def set_timing(self, on: bool):
         self._ck(self.lib.md_set_timing(self.h, int(on)), "md_set_timing")

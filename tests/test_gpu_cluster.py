@@ -1,0 +1,181 @@
+"""The cluster kernel of the precision form (periodic, LJ only) through the C ABI.
+
+Bars: candidate rows and images bit-exact against the oracle (the state is
+stored in cell order on the device; rows come back in the caller's
+numbering); forces within 1e-4 relative RMS of the FP64 path at the same
+positions; forces bit-identical across segment lengths and block sizes (the
+per-atom pair order and arithmetic do not depend on them); downloads return
+the caller's numbering.
+"""
+import numpy as np
+import pytest
+
+from conftest import rel_rms
+from systems import argon_fcc
+
+pytestmark = pytest.mark.gpu
+
+RS, RC = 9.534, 8.5125
+
+
+def _engine(eng, n, L, **kw):
+    kw.setdefault("precision", eng.PREC_MIXED)
+    cfg = eng.make_config(n_lj=n, lj_rs=RS, lj_rcut=RC, periodic=1, box=L, **kw)
+    return eng.Engine(cfg)
+
+
+@pytest.mark.parametrize("ncell,natoms", [(4, None), (6, None), (8, None), (20, 32000)])
+def test_cluster_rows_bit_exact(eng, oracle, ncell, natoms):
+    pos, vel, L = argon_fcc(ncell, natoms=natoms, noise=0.2)
+    n = len(pos)
+    with _engine(eng, n, L, lj_kernel=eng.LJ_CLUSTER) as e:
+        e.upload(pos, vel)
+        e.begin(0.0)
+        rows, nls, nlargest, img = e.neighbor_list(0, images=True)
+        gpos, gvel = e.download()
+        st = e.stats()
+    assert st["lj_cluster"] == 1
+    p = pos.copy()
+    nl = oracle.build_list(p, RS, L, periodic=True)
+    assert (nls, nlargest) == (nl.nlistsize, nl.nlargest)
+    assert np.array_equal(rows, nl.rows)
+    assert np.array_equal(img, nl.code)
+    oracle.free_list(nl)
+    assert np.array_equal(gpos, p)      # wrapped positions, caller's numbering
+    assert np.array_equal(gvel, vel)
+
+
+@pytest.mark.parametrize("ncell", [4, 8, 16])
+def test_cluster_forces_vs_fp64(eng, ncell):
+    pos, vel, L = argon_fcc(ncell, noise=0.1)
+    n = len(pos)
+    out = {}
+    for kind in ("fp64", "cluster"):
+        kw = dict(precision=eng.PREC_FP64) if kind == "fp64" else dict(lj_kernel=eng.LJ_CLUSTER)
+        with _engine(eng, n, L, **kw) as e:
+            e.upload(pos, vel)
+            e.begin(0.0)
+            out[kind] = e.compute_forces()
+    err = rel_rms(out["cluster"][0], out["fp64"][0])
+    assert err < 1e-4, err
+    for k in range(3):   # E, E_shifted, W
+        assert abs(out["cluster"][1][k] - out["fp64"][1][k]) < 1e-5 * abs(out["fp64"][1][k])
+
+
+def test_cluster_matches_rows_kernel(eng):
+    """Cluster and row-list kernels evaluate the same pairs in FP32."""
+    pos, vel, L = argon_fcc(10, noise=0.1)
+    n = len(pos)
+    out = {}
+    for k in (eng.LJ_ROWS, eng.LJ_CLUSTER):
+        with _engine(eng, n, L, lj_kernel=k) as e:
+            e.upload(pos, vel)
+            e.begin(0.0)
+            out[k] = e.compute_forces()[0]
+    assert rel_rms(out[eng.LJ_CLUSTER], out[eng.LJ_ROWS]) < 1e-6
+
+
+def test_cluster_independent_of_tiling(eng):
+    pos, vel, L = argon_fcc(12, noise=0.1)
+    n = len(pos)
+    ref = None
+    for cells, threads in [(0, 0), (1, 32), (3, 224), (64, 64)]:
+        with _engine(eng, n, L, lj_kernel=eng.LJ_CLUSTER, cluster_cells=cells,
+                     cluster_threads=threads) as e:
+            e.upload(pos, vel)
+            e.begin(0.0)
+            e.step(20)
+            p, v = e.download()
+            f, en = e.compute_forces()
+        if ref is None:
+            ref = (p, v, f)
+        else:
+            assert np.array_equal(p, ref[0]) and np.array_equal(v, ref[1])
+            assert np.array_equal(f, ref[2])
+
+
+def test_cluster_trips_and_refresh(eng):
+    """Skin trips refresh the 16-bit rows from shared memory; after 150 steps
+    the forces still agree with the FP64 path at the same positions."""
+    pos, vel, L = argon_fcc(10, temperature=300.0, seed=6, noise=0.1)
+    n = len(pos)
+    rs = 8.7
+    cfg = eng.make_config(n_lj=n, lj_rs=rs, lj_rcut=RC, periodic=1, box=L,
+                          precision=eng.PREC_MIXED, lj_kernel=eng.LJ_CLUSTER)
+    with eng.Engine(cfg) as e:
+        e.upload(pos, vel)
+        e.begin(0.0)
+        e.step(150)
+        st = e.stats()
+        p, v = e.download()
+        fm, _ = e.compute_forces()
+    cfg = eng.make_config(n_lj=n, lj_rs=rs, lj_rcut=RC, periodic=1, box=L)
+    with eng.Engine(cfg) as e:
+        e.upload(p, v)
+        e.begin(0.0)
+        f64, _ = e.compute_forces()
+    assert st["list_trips"] > 0
+    assert rel_rms(fm, f64) < 1e-4
+
+
+def test_cluster_mixed_species(eng):
+    """N and O atoms among the argon: the type-selecting pair path."""
+    pos, vel, L = argon_fcc(8, noise=0.1)
+    pos[::7, 3] = 0
+    pos[3::11, 3] = 1
+    n = len(pos)
+    out = {}
+    for kind in ("fp64", "cluster"):
+        kw = dict(precision=eng.PREC_FP64) if kind == "fp64" else dict(lj_kernel=eng.LJ_CLUSTER)
+        with _engine(eng, n, L, species=0, **kw) as e:
+            e.upload(pos, vel)
+            e.begin(0.0)
+            out[kind] = e.compute_forces()[0]
+    assert rel_rms(out["cluster"], out["fp64"]) < 1e-4
+
+
+def test_cluster_state_round_trip(eng):
+    """Upload after a permuting build maps through the caller's numbering."""
+    pos, vel, L = argon_fcc(8, noise=0.1)
+    n = len(pos)
+    rng = np.random.default_rng(5)
+    a3, b3, c3 = (rng.standard_normal((n, 3)) for _ in range(3))
+    with _engine(eng, n, L, lj_kernel=eng.LJ_CLUSTER) as e:
+        e.upload(pos, vel)
+        e.begin(0.0)
+        p0, _ = e.download()
+        e.upload_state(p0, vel, a3, b3, c3)
+        p1, v1 = e.download()
+        st = e.download_state()
+    assert np.array_equal(p1, p0) and np.array_equal(v1, vel)
+    assert np.array_equal(st["acc"], a3) and np.array_equal(st["b"], b3)
+    assert np.array_equal(st["c"], c3)
+
+
+def test_cluster_energy_conservation(eng):
+    pos, vel, L = argon_fcc(8, seed=9)
+    n = len(pos)
+    with _engine(eng, n, L, lj_kernel=eng.LJ_CLUSTER, output_timesteps=100) as e:
+        e.upload(pos, vel)
+        e.begin(0.0)
+        e.step(1000)
+        rec = e.records()
+    etot = rec[:, 3] + rec[:, 12]          # ek + shifted LJ energy
+    eps = 9.960172e-5
+    drift = abs(etot[-1] - etot[0]) / n / eps
+    assert drift < 1e-4, drift
+
+
+def test_autotune_keeps_forces(eng):
+    """The autotuner only changes tiling: forces stay bit-identical."""
+    pos, vel, L = argon_fcc(12, noise=0.1)
+    n = len(pos)
+    with _engine(eng, n, L, lj_kernel=eng.LJ_CLUSTER) as e:
+        e.upload(pos, vel)
+        e.begin(0.0)
+        f0, _ = e.compute_forces()
+        r = e.autotune(2)
+        f1, _ = e.compute_forces()
+        e.step(10)
+    assert r["candidates"] >= 1 and r["threads"] in (64, 96, 128, 160, 192)
+    assert np.array_equal(f0, f1)
