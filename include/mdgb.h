@@ -176,6 +176,28 @@ typedef struct md_tune_result {
   double best_ms;          /* force evaluation time of the choice */
 } md_tune_result;
 md_status md_autotune(md_ctx* ctx, int evals, md_tune_result* out);
+/* CUDA graphs for the cluster path (default on): windows of fused steps
+ * with nothing else due are replayed as one captured graph. */
+md_status md_set_graphs(md_ctx* ctx, int on);
+
+/* ---- batched form: many independent periodic replicas in one context ----
+ * Replica k has natoms[k] atoms in a cubic periodic box of edge boxes[k];
+ * its atoms are the k-th consecutive range of the arrays given to
+ * md_upload / md_download (real4 / real3, in replica order).  cfg gives the
+ * shared settings (dt, list radii, species); it must select the precision
+ * form (MD_PREC_MIXED), LJ only, and output_timesteps <= 0 (records come
+ * from md_batch_records).  Every step of all replicas is one launch of the
+ * persistent cluster kernel (forces + Gear), replayed from CUDA graphs
+ * between list builds; md_step, md_autotune, md_get_stats and the timing
+ * calls work on the batch as on any context.  No counterpart in the
+ * reference, which runs one system per process (cpu/cpumd/Host.cpp). */
+md_status md_batch_create(const md_config* cfg, int nrep, const int* natoms,
+                          const double* boxes, md_ctx** out);
+int md_batch_size(const md_ctx* ctx);
+/* One record per replica of the current state (md_thermo layout; eu = the
+ * replica's LJ energy over the force's pairs, e_mb = 0). */
+md_status md_batch_records(md_ctx* ctx, md_thermo* out, int max_records);
+
 /* Wait for all work of the context; returns the first deferred error. */
 md_status md_synchronize(md_ctx* ctx);
 /* Page-locked host memory for fast md_upload/md_download (NULL on failure). */

@@ -283,8 +283,8 @@ struct SegShared {
 };
 
 __device__ __forceinline__ void load_segment(SegShared& sh, const ClusterSegment* seg,
-                                             const ClusterReplica* reps) {
-  const int* src = (const int*)&seg[blockIdx.x];
+                                             const ClusterReplica* reps, int sidx) {
+  const int* src = (const int*)&seg[sidx];
   int* dst = (int*)&sh.S;
   for (int k = threadIdx.x; k < (int)(sizeof(ClusterSegment) / 4); k += blockDim.x)
     dst[k] = src[k];
@@ -324,13 +324,15 @@ __device__ __forceinline__ void stage(const SegShared& sh, const float4* __restr
 }
 
 // The same staging by bulk copies: thread 0 issues one cp.async.bulk per
-// piece, all completing on `bar` (phase 0); after the wait the image pieces
+// piece, all completing on `bar` (phase `parity`); after the wait the image pieces
 // are shifted in place.  Returns false (uniformly) if the bounded wait ran
 // out; the caller then leaves after the copies land or time out.
 __device__ __forceinline__ bool stage_bulk(const SegShared& sh, const float4* __restrict__ src,
-                                           float4* st, uint64_t* bar, int* status) {
+                                           float4* st, uint64_t* bar, uint32_t parity,
+                                           int* status) {
   const ClusterSegment& S = sh.S;
   if (threadIdx.x == 0) {
+    fence_proxy_async();  // earlier generic accesses to the stage come first
     mbar_expect_tx(bar, (uint32_t)S.staged * (uint32_t)sizeof(float4));
     for (int k = 0; k < S.npieces; k++) {
       const ClusterPiece& pc = S.piece[k];
@@ -338,9 +340,9 @@ __device__ __forceinline__ bool stage_bulk(const SegShared& sh, const float4* __
         bulk_load(st + pc.dst, src + pc.src, (uint32_t)pc.count * (uint32_t)sizeof(float4), bar);
     }
   }
-  const bool got = mbar_wait(bar, 0u, status);
+  const bool got = mbar_wait(bar, parity, status);
   if (!__syncthreads_and(got)) {
-    if (threadIdx.x == 0) mbar_wait(bar, 0u, status);
+    if (threadIdx.x == 0) mbar_wait(bar, parity, status);
     return false;
   }
   const float Lf = sh.r.Lf, Llo = sh.r.Llo;
@@ -438,7 +440,7 @@ __global__ void __launch_bounds__(256)
               int* __restrict__ counters) {
   extern __shared__ float4 st[];
   __shared__ SegShared sh;
-  load_segment(sh, seg, reps);
+  load_segment(sh, seg, reps, blockIdx.x);
   __syncthreads();
   stage(sh, pb, st);
   fill_offsets(sh, start);
@@ -502,6 +504,26 @@ __device__ __forceinline__ void block_sums(double (&v)[NV], double* out) {
   }
 }
 
+// block sum of NV doubles into out[NV * slot + k]
+template <int NV>
+__device__ __forceinline__ void block_sums_at(double (&v)[NV], double* out, int slot) {
+  __shared__ double sm[NV][32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int k = 0; k < NV; k++) {
+    double x = v[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    if (lane == 0) sm[k][warp] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x < NV) {
+    double s = 0;
+    for (int w = 0; w < nw; w++) s += sm[threadIdx.x][w];
+    out[NV * slot + threadIdx.x] = s;
+  }
+}
+
 // Pair (p, q) within 1e-5 of the cutoff: decided in FP64 as the FP64 path
 // decides it (same image, same roundings).
 __device__ __noinline__ bool band_inside(const SegShared& sh, const md_double4* pos, int p,
@@ -526,6 +548,7 @@ __device__ __noinline__ bool band_inside(const SegShared& sh, const md_double4* 
 
 // Arguments of the segment force kernel (device copy of ClusterForceArgs).
 struct ClStep {
+  int nseg;
   const ClusterSegment* seg;
   const ClusterReplica* reps;
   const int* start;
@@ -546,13 +569,14 @@ struct ClStep {
   ClusterGearArgs g;
 };
 
-// FP32 LJ force of one segment.  ev: E, E_shifted, W (as md_forces.cu).
+// FP32 LJ force, persistent: each block walks segments blockIdx.x,
+// blockIdx.x + gridDim.x, ...  ev: E, E_shifted, W per segment (as md_forces.cu).
 // GEAR: the Gear correct of this step and predict of the next follow for each
 // atom in the same thread (cpu/common/Device.cpp:17-85 in FP64 with FMAs).
 // Dynamic shared memory: two row tiles [16][blockDim + 8] of uint16 (TMA
 // destinations), then the staged positions.
 template <bool ENERGY, bool ALL_NG, bool GEAR>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(224, 3)
     k_lj_cl(const __grid_constant__ CUtensorMap rmap, const ClStep a) {
   extern __shared__ __align__(128) unsigned char dyn[];
   const int tid = threadIdx.x;
@@ -570,10 +594,16 @@ __global__ void __launch_bounds__(256)
     mbar_init(&bar[2], 1);
     fence_mbar_init();
   }
-  load_segment(sh, a.seg, a.reps);
   __syncthreads();
   const bool tripped = s_trip != 0;
-  if (!stage_bulk(sh, a.posf, st, &bar[2], a.status)) return;
+  uint32_t phase = 0u;       // bit b: parity to wait for on bar[b] (b = 2: staging)
+  uint32_t inflight = 0u;    // bit b: a copy into buffer b is in flight (issuing thread)
+  bool trip_next = false;
+  for (int sidx = blockIdx.x; sidx < a.nseg; sidx += gridDim.x) {
+  load_segment(sh, a.seg, a.reps, sidx);
+  __syncthreads();
+  if (!stage_bulk(sh, a.posf, st, &bar[2], (phase >> 2) & 1u, a.status)) return;
+  phase ^= 4u;
   if (tripped) fill_offsets(sh, a.start);
   __syncthreads();
   const bool minimg = sh.r.G == 1;
@@ -585,10 +615,7 @@ __global__ void __launch_bounds__(256)
   const float s2_o = a.sp.sig[1] * a.sp.sig[1], c_o = 24.0f * a.sp.eps[1];
   const uint32_t tile_elems = kClusterTileSlots * BX;
   const uint32_t tile_bytes = tile_elems * sizeof(uint16_t);
-  uint32_t phase = 0u;       // bit b: parity to wait for on bar[b]
-  uint32_t inflight = 0u;    // bit b: a copy into buffer b is in flight (issuing thread)
   double ev[3] = {0.0, 0.0, 0.0};
-  bool trip_next = false;
   const int p0 = sh.S.p0, p1 = sh.S.p1;
   for (int base = p0; base < p1; base += blockDim.x) {
     const int p = base + tid;
@@ -785,12 +812,14 @@ __global__ void __launch_bounds__(256)
       }
     }
   }
+  if (ENERGY) block_sums_at<3>(ev, a.epart, sidx);
+  __syncthreads();  // the next segment overwrites sh and the stage
+  }
   if (GEAR && trip_next) a.skin[a.flag_set] = 1;
   if (blockIdx.x == 0 && tid == 0) {
     if (tripped) atomicAdd(&a.skin[4], 1);
     a.skin[a.flag_clear] = 0;  // flag of step t + 2 starts clear
   }
-  if (ENERGY) block_sums<3>(ev, a.epart);
 }
 
 // reference-layout rows, original numbering (single replica)
@@ -800,7 +829,7 @@ __global__ void __launch_bounds__(256)
                   const md_double4* __restrict__ pos, int nls, int* __restrict__ out,
                   signed char* __restrict__ img, int* __restrict__ nlargest) {
   __shared__ SegShared sh;
-  load_segment(sh, seg, reps);
+  load_segment(sh, seg, reps, blockIdx.x);
   __syncthreads();
   fill_offsets(sh, start);
   __syncthreads();
@@ -1060,6 +1089,7 @@ void launch_lj_cluster(const ClusterForceArgs& f, bool energy, cudaStream_t st) 
   const size_t smem = 2 * kClusterTileSlots * (size_t)(cl.block + 8) * sizeof(uint16_t) +
                       stage_bytes(cl.max_staged);
   ClStep a;
+  a.nseg = cl.nseg;
   a.seg = cl.seg;
   a.reps = cl.rep;
   a.start = cl.start;
@@ -1082,8 +1112,26 @@ void launch_lj_cluster(const ClusterForceArgs& f, bool energy, cudaStream_t st) 
   a.status = f.status;
   if (f.gear) a.g = *f.gear;
   else memset(&a.g, 0, sizeof(a.g));
-#define MDGB_CL_LAUNCH(E, A, G) \
-  k_lj_cl<E, A, G><<<cl.nseg, cl.block, smem, st>>>(cl.rmap, a)
+  // persistent grid: as many blocks as fit on the GPU at once, at most one
+  // per segment
+  auto grid_for = [&](const void* kern) {
+    static int sms = 0;
+    if (!sms) {
+      int dev = 0;
+      cudaGetDevice(&dev);
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+      if (sms <= 0) sms = 1;
+    }
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, cl.block, smem) !=
+            cudaSuccess ||
+        per_sm < 1)
+      per_sm = 1;
+    return std::min(cl.nseg, sms * per_sm);
+  };
+#define MDGB_CL_LAUNCH(E, A, G)                                                            \
+  k_lj_cl<E, A, G><<<grid_for((const void*)k_lj_cl<E, A, G>), cl.block, smem, st>>>(cl.rmap, \
+                                                                                      a)
   if (energy) {
     if (f.all_ng) MDGB_CL_LAUNCH(true, true, false); else MDGB_CL_LAUNCH(true, false, false);
   } else if (f.gear) {
@@ -1100,6 +1148,38 @@ int cluster_reference_rows(const ClusterList& cl, const md_double4* pos, int nli
   k_cl_ref_rows<<<cl.nseg, 128, 0, st>>>(cl.seg, cl.rep, cl.start, cl.orig, pos, nlistsize,
                                          d_out, d_img, d_nlargest);
   return (int)cudaGetLastError();
+}
+
+// per-replica sums of the per-segment LJ energies (segments of a replica
+// are the contiguous range starting at the segment of its first cell)
+__global__ void k_rep_energy(const ClusterReplica* __restrict__ reps, int nrep, int ncells,
+                             const int* __restrict__ segidx, const double* __restrict__ epart,
+                             double* __restrict__ out3) {
+  const int k = blockIdx.x;
+  const int s0 = segidx[reps[k].cell0];
+  const int s1 = segidx[k + 1 < nrep ? reps[k + 1].cell0 : ncells];
+  __shared__ double sm[3][32];
+  double v[3] = {0.0, 0.0, 0.0};
+  for (int s = s0 + threadIdx.x; s < s1; s += blockDim.x)
+    for (int d = 0; d < 3; d++) v[d] += epart[3 * (size_t)s + d];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int d = 0; d < 3; d++) {
+    double x = v[d];
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    if (lane == 0) sm[d][warp] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x < 3) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += sm[threadIdx.x][w];
+    out3[3 * k + threadIdx.x] = t;
+  }
+}
+
+void launch_rep_energy(const ClusterList& cl, const double* epart, double* out3,
+                       cudaStream_t st) {
+  if (cl.nrep > 0)
+    k_rep_energy<<<cl.nrep, 128, 0, st>>>(cl.rep, cl.nrep, cl.ncells, cl.segidx, epart, out3);
 }
 
 void launch_unpermute(const double* in, double* out, const int* orig, int n, int width,

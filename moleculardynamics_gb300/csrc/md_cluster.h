@@ -136,6 +136,11 @@ int cluster_blocks(const ClusterList& cl);
 int cluster_reference_rows(const ClusterList& cl, const md_double4* pos, int nlistsize,
                            int* d_out, signed char* d_img, int* d_nlargest, cudaStream_t st);
 
+// out3[3k..3k+2] = sum of epart over the segments of replica k (the
+// per-segment energies of an energy launch of launch_lj_cluster)
+void launch_rep_energy(const ClusterList& cl, const double* epart, double* out3,
+                       cudaStream_t st);
+
 // out[orig[p]] = in[p] for arrays of `width` doubles per atom
 void launch_unpermute(const double* in, double* out, const int* orig, int n, int width,
                       cudaStream_t st);

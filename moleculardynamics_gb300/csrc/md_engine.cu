@@ -106,6 +106,17 @@ struct md_ctx {
   double* io = nullptr;  // 4 doubles per atom: permuted transfers
   md_double4* pos_alt = nullptr;  // next positions of the fused force + Gear kernel
   float4* posf_alt = nullptr;
+  // independent periodic replicas (batched form): atoms of replica k are
+  // [sum of n before k, + n), each in its own box
+  bool batch = false;
+  std::vector<ClusterReplica> reps_in;
+  int* rep_ranges = nullptr;    // device: (first atom, atoms) per replica
+  double* rep_buf = nullptr;    // device: 3 energies + 16 record doubles per replica
+  // CUDA graph of a window of fused steps (replayed while nothing else is due)
+  bool graphs = false;
+  cudaGraphExec_t gexec = nullptr;
+  std::vector<unsigned char> gsig;
+  long long graph_windows = 0;
   // bond-order scratch
   uint32_t* mb_sl = nullptr;
   int* mb_slen = nullptr;
@@ -131,6 +142,7 @@ struct md_ctx {
   bool timing = false;
   std::vector<cudaEvent_t> ev_pool;
   std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> pending;
+  std::vector<int> pending_weight;  // launches each pending interval stands for
   double kt_ms[kKernels] = {0, 0, 0, 0, 0, 0, 0};
   long long kt_n[kKernels] = {0, 0, 0, 0, 0, 0, 0};
 
@@ -171,8 +183,9 @@ cudaEvent_t take_event(md_ctx* c) {
 struct Timed {
   md_ctx* c;
   int id;
+  int weight;
   cudaEvent_t a = nullptr, b = nullptr;
-  Timed(md_ctx* c_, int id_) : c(c_), id(id_) {
+  Timed(md_ctx* c_, int id_, int weight_ = 1) : c(c_), id(id_), weight(weight_) {
     if (c->timing) {
       a = take_event(c);
       b = take_event(c);
@@ -183,21 +196,24 @@ struct Timed {
     if (c->timing) {
       cudaEventRecord(b, c->st);
       c->pending.push_back({id, {a, b}});
+      c->pending_weight.push_back(weight);
     }
   }
 };
 
 void resolve_timing(md_ctx* c) {
-  for (auto& p : c->pending) {
+  for (size_t k = 0; k < c->pending.size(); k++) {
+    auto& p = c->pending[k];
     float ms = 0;
     if (cudaEventElapsedTime(&ms, p.second.first, p.second.second) == cudaSuccess) {
       c->kt_ms[p.first] += ms;
-      c->kt_n[p.first]++;
+      c->kt_n[p.first] += c->pending_weight[k];
     }
     c->ev_pool.push_back(p.second.first);
     c->ev_pool.push_back(p.second.second);
   }
   c->pending.clear();
+  c->pending_weight.clear();
 }
 
 md_status ensure_epart(md_ctx* c, long long need) {
@@ -279,6 +295,16 @@ MbArgs mb_args(md_ctx* c, double* f3, int ljexist) {
 
 // Host.cpp:132-135 / :157-161: LJ over all atoms (overwrites), bond order
 // over the first n_mb atoms (accumulates when LJ is on).
+// replicas of the cluster structure: the batch's, or the one periodic box
+std::vector<ClusterReplica> cluster_reps(const md_ctx* c) {
+  if (c->batch) return c->reps_in;
+  std::vector<ClusterReplica> reps(1);
+  memset(reps.data(), 0, sizeof(ClusterReplica));
+  reps[0].n = c->n;
+  reps[0].L = c->cfg.box;
+  return reps;
+}
+
 ClusterForceArgs cl_args(md_ctx* c, double* f3, double* epart) {
   ClusterForceArgs a;
   a.cl = &c->cl;
@@ -383,9 +409,7 @@ md_status rebuild(md_ctx* c, int t) {
       CK(cudaMemsetAsync(c->cl.skin + 4, 0, sizeof(int), c->st), "skin");
     }
     CK(cudaMemsetAsync(c->status, 0, sizeof(int), c->st), "status");
-    std::vector<ClusterReplica> reps(1);
-    reps[0].n = c->n;
-    reps[0].L = c->cfg.box;
+    std::vector<ClusterReplica> reps = cluster_reps(c);
     double** v3[5] = {&c->vel, &c->acc, &c->b, &c->c, &c->f3};
     std::string e;
     int r = cluster_build(c->cl, reps, c->cfg.lj_rs, sqrt((double)c->lj_rcutsq), &c->pos, v3,
@@ -537,6 +561,120 @@ bool due(const md_ctx* c, int t) {
   return (c->cfg.use_lj && c->lj_next == t) || (c->cfg.use_mb && c->mb_next == t);
 }
 
+// Forces of step t, correct of step t and predict of step t + 1 in one
+// kernel (cluster path); the next positions go to the other buffer.
+void launch_fused(md_ctx* c) {
+  GearArgs g = gear_args(c, c->t + 1);
+  ClusterGearArgs cg;
+  cg.pos_next = c->pos_alt;
+  cg.posf_next = c->posf_alt;
+  cg.vel = c->vel;
+  cg.acc = c->acc;
+  cg.b = c->b;
+  cg.c = c->c;
+  cg.k = c->gear;
+  for (int k = 0; k < 3; k++) cg.inv_mass[k] = g.inv_mass[k];
+  cg.trip2 = g.trip2;
+  ClusterForceArgs a = cl_args(c, nullptr, nullptr);
+  a.gear = &cg;
+  launch_lj_cluster(a, false, c->st);
+}
+
+void advance_fused(md_ctx* c) {
+  std::swap(c->pos, c->pos_alt);
+  std::swap(c->posf, c->posf_alt);
+  c->predicted = true;
+  c->stats.launches++;
+  c->t++;
+  c->stats.steps++;
+}
+
+// A window of kGraphSteps fused steps replayed as one CUDA graph.  The
+// window starts at step t with the prediction in place and needs no list
+// build, record or call boundary inside.  The graph is captured again only
+// when anything it bakes in changed (buffers after a list build, tiles, the
+// step's phase in the 3-step rotation of the skin flags).
+constexpr int kGraphSteps = 6;  // even (buffers return to place) and a multiple of 3
+
+bool window_ok(const md_ctx* c, int s, int nsteps) {
+  if (!c->cluster || !c->graphs || !c->predicted) return false;
+  if (s + kGraphSteps > nsteps - 1) return false;  // the call's last step is not fused
+  const int t = c->t;
+  for (int u = 0; u < kGraphSteps; u++) {
+    if (c->cfg.output_timesteps > 0 && c->printout == t + u) return false;
+    if (due(c, t + u + 1)) return false;
+  }
+  return true;
+}
+
+md_status run_window(md_ctx* c) {
+  struct Sig {
+    int t6, nseg, max_staged, block, all_ng, cap, ld;
+    float trip2;
+    const void* ptr[14];
+    unsigned char rmap[sizeof(CUtensorMap)];
+  } sig;
+  memset(&sig, 0, sizeof(sig));
+  sig.t6 = c->t % kGraphSteps;
+  sig.nseg = c->cl.nseg;
+  sig.max_staged = c->cl.max_staged;
+  sig.block = c->cl.block;
+  sig.all_ng = c->all_ng;
+  sig.cap = c->cl.cap;
+  sig.ld = c->cl.ld;
+  sig.trip2 = gear_args(c, c->t + 1).trip2;
+  const void* ptrs[14] = {c->pos, c->pos_alt, c->posf, c->posf_alt, c->vel, c->acc, c->b, c->c,
+                          c->cl.seg, c->cl.rows, c->cl.len, c->cl.pos_build, c->cl.skin,
+                          c->cl.rep};
+  memcpy(sig.ptr, ptrs, sizeof(ptrs));
+  memcpy(sig.rmap, &c->cl.rmap, sizeof(CUtensorMap));
+  const unsigned char* sb = (const unsigned char*)&sig;
+  const bool same = c->gexec && c->gsig.size() == sizeof(sig) &&
+                    memcmp(c->gsig.data(), sb, sizeof(sig)) == 0;
+  if (!same) {
+    // capture the window's launches (the host state is restored afterwards)
+    const int t0 = c->t;
+    const md_stats st0 = c->stats;
+    cudaGraph_t g = nullptr;
+    CK(cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal), "graph capture");
+    for (int u = 0; u < kGraphSteps; u++) {
+      launch_fused(c);
+      advance_fused(c);
+    }
+    cudaError_t e = cudaStreamEndCapture(c->st, &g);
+    c->t = t0;
+    c->stats = st0;  // kGraphSteps swaps: buffers are back in place
+    if (e != cudaSuccess) return cuda_fail(c, e, "graph capture");
+    bool updated = false;
+    if (c->gexec) {
+      cudaGraphExecUpdateResultInfo info;
+      updated = cudaGraphExecUpdate(c->gexec, g, &info) == cudaSuccess;
+      if (!updated) {
+        cudaGetLastError();
+        cudaGraphExecDestroy(c->gexec);
+        c->gexec = nullptr;
+      }
+    }
+    if (!updated) {
+      e = cudaGraphInstantiate(&c->gexec, g, 0);
+      if (e != cudaSuccess) {
+        cudaGraphDestroy(g);
+        c->gexec = nullptr;
+        return cuda_fail(c, e, "graph instantiate");
+      }
+    }
+    cudaGraphDestroy(g);
+    c->gsig.assign(sb, sb + sizeof(sig));
+  }
+  {
+    Timed tm(c, 6, kGraphSteps);
+    CK(cudaGraphLaunch(c->gexec, c->st), "graph launch");
+  }
+  for (int u = 0; u < kGraphSteps; u++) advance_fused(c);
+  c->graph_windows++;
+  return MD_OK;
+}
+
 // One iteration of cpu/cpumd/Host.cpp:141-195.  In the precision form with a
 // periodic box, correct(t) and predict(t+1) run as one kernel unless step
 // t+1 rebuilds a list, step t records output, or this is the last step of
@@ -557,31 +695,11 @@ md_status step_once(md_ctx* c, bool last) {
   const bool output = c->cfg.output_timesteps > 0 && c->printout == t;
   const bool fuse = c->mixed() && !c->walls() && !last && !output && !due(c, t + 1);
   if (c->cluster && fuse) {
-    // forces of step t, correct of step t and predict of step t + 1 in one
-    // kernel; the next positions go to the other buffer
-    GearArgs g = gear_args(c, t + 1);
-    ClusterGearArgs cg;
-    cg.pos_next = c->pos_alt;
-    cg.posf_next = c->posf_alt;
-    cg.vel = c->vel;
-    cg.acc = c->acc;
-    cg.b = c->b;
-    cg.c = c->c;
-    cg.k = c->gear;
-    for (int k = 0; k < 3; k++) cg.inv_mass[k] = g.inv_mass[k];
-    cg.trip2 = g.trip2;
-    ClusterForceArgs a = cl_args(c, nullptr, nullptr);
-    a.gear = &cg;
     {
       Timed tm(c, 6);
-      launch_lj_cluster(a, false, c->st);
+      launch_fused(c);
     }
-    std::swap(c->pos, c->pos_alt);
-    std::swap(c->posf, c->posf_alt);
-    c->predicted = true;
-    c->stats.launches++;
-    c->t++;
-    c->stats.steps++;
+    advance_fused(c);
     return MD_OK;
   }
   forces(c, c->f3);
@@ -672,6 +790,7 @@ md_status md_create(const md_config* cfg, md_ctx** out) {
   md_ctx* c = new md_ctx();
   c->cfg = *cfg;
   c->cluster = cluster_ok && cfg->lj_kernel != MD_LJ_ROWS;
+  c->graphs = c->cluster;
   if (cfg->cluster_cells > 0) c->cl.Z = cfg->cluster_cells;
   if (cfg->cluster_threads > 0) c->cl.block = cfg->cluster_threads;
   c->n = (int)n;
@@ -724,7 +843,8 @@ void md_destroy(md_ctx* c) {
   list_free(c->lj);
   list_free(c->mb);
   cluster_free(c->cl);
-  void* ptrs[] = {c->io, c->pos_alt, c->posf_alt, c->pos, c->vel, c->acc, c->b, c->c, c->f3, c->f3_tmp, c->posf, c->mb_sl,
+  if (c->gexec) cudaGraphExecDestroy(c->gexec);
+  void* ptrs[] = {c->rep_ranges, c->rep_buf, c->io, c->pos_alt, c->posf_alt, c->pos, c->vel, c->acc, c->b, c->c, c->f3, c->f3_tmp, c->posf, c->mb_sl,
                   c->mb_slen, c->xsi, c->xsj, c->va, c->status, c->epart, c->dsc, c->rec,
                   c->sc.dpart, c->sc.umax, c->sc.counts, c->sc.block_sums};
   for (void* p : ptrs)
@@ -842,8 +962,15 @@ md_status md_step(md_ctx* c, int nsteps) {
   if (!c->begun) return fail(c, MD_BAD_ARGUMENT, "md_begin has not been called");
   {
     Timed whole(c, 5);
-    for (int s = 0; s < nsteps; s++) {
-      md_status r = step_once(c, s == nsteps - 1);
+    for (int s = 0; s < nsteps;) {
+      md_status r;
+      if (window_ok(c, s, nsteps)) {
+        r = run_window(c);
+        s += kGraphSteps;
+      } else {
+        r = step_once(c, s == nsteps - 1);
+        s++;
+      }
       if (r != MD_OK) return r;
     }
   }
@@ -918,6 +1045,7 @@ md_status md_neighbor_list(md_ctx* c, int which, int* rows, signed char* images,
   if (!c || (which != 0 && which != 1)) return MD_BAD_ARGUMENT;
   if (which == 0 && c->cluster) {
     if (!c->cl.built) return fail(c, MD_BAD_ARGUMENT, "list not built (call md_begin)");
+    if (c->batch) return fail(c, MD_BAD_ARGUMENT, "reference rows of a batch: not available");
     long long nls = 27LL * c->cl.maxcell;
     if (nls > c->n - 1) nls = c->n - 1;
     if (nls < 0) nls = 0;
@@ -1005,9 +1133,7 @@ md_status md_autotune(md_ctx* c, int evals, md_tune_result* out) {
   CK(cudaEventCreate(&e1), "autotune");
   double best = 1e300;
   int best_t = c->cl.block, best_c = c->cl.stage_cap, tried = 0;
-  std::vector<ClusterReplica> reps(1);
-  reps[0].n = c->n;
-  reps[0].L = c->cfg.box;
+  std::vector<ClusterReplica> reps = cluster_reps(c);
   double** v3[5] = {&c->vel, &c->acc, &c->b, &c->c, &c->f3};
   auto build = [&](int t, int cap) -> md_status {
     c->cl.block = t;
@@ -1054,6 +1180,86 @@ md_status md_autotune(md_ctx* c, int evals, md_tune_result* out) {
     out->candidates = tried;
     out->best_ms = best / evals;
   }
+  return check_status(c);
+}
+
+md_status md_set_graphs(md_ctx* c, int on) {
+  if (!c) return MD_BAD_ARGUMENT;
+  c->graphs = on && c->cluster;
+  return MD_OK;
+}
+
+md_status md_batch_create(const md_config* cfg, int nrep, const int* natoms, const double* boxes,
+                          md_ctx** out) {
+  if (!cfg || !out || !natoms || !boxes || nrep < 1) return MD_BAD_ARGUMENT;
+  *out = nullptr;
+  if (cfg->precision != MD_PREC_MIXED || !cfg->use_lj || (cfg->use_mb && cfg->n_mb > 0) ||
+      cfg->output_timesteps > 0)
+    return MD_BAD_CONFIG;
+  long long total = 0;
+  double bmin = 1e300;
+  for (int k = 0; k < nrep; k++) {
+    if (natoms[k] < 1 || !(boxes[k] > 2.0 * (double)cfg->lj_rs)) return MD_BAD_CONFIG;
+    total += natoms[k];
+    bmin = fmin(bmin, boxes[k]);
+  }
+  if (total > kMaxAtoms) return MD_BAD_CONFIG;
+  md_config c1 = *cfg;
+  c1.n_lj = (int)total;
+  c1.n_mb = 0;
+  c1.use_mb = 0;
+  c1.periodic = 1;
+  c1.box = bmin;
+  c1.lj_kernel = MD_LJ_CLUSTER;
+  md_ctx* c = nullptr;
+  md_status s = md_create(&c1, &c);
+  if (s != MD_OK) return s;
+  c->batch = true;
+  c->reps_in.assign(nrep, ClusterReplica{});
+  std::vector<int> ranges(2 * (size_t)nrep);
+  int a0 = 0;
+  for (int k = 0; k < nrep; k++) {
+    memset(&c->reps_in[k], 0, sizeof(ClusterReplica));
+    c->reps_in[k].n = natoms[k];
+    c->reps_in[k].L = boxes[k];
+    ranges[2 * k] = a0;
+    ranges[2 * k + 1] = natoms[k];
+    a0 += natoms[k];
+  }
+  cudaError_t e;
+  if ((e = cudaMalloc(&c->rep_ranges, sizeof(int) * ranges.size())) != cudaSuccess ||
+      (e = cudaMalloc(&c->rep_buf, sizeof(double) * 19 * (size_t)nrep)) != cudaSuccess ||
+      (e = cudaMemcpy(c->rep_ranges, ranges.data(), sizeof(int) * ranges.size(),
+                      cudaMemcpyHostToDevice)) != cudaSuccess) {
+    md_destroy(c);
+    return e == cudaErrorMemoryAllocation ? MD_OUT_OF_MEMORY : MD_CUDA_ERROR;
+  }
+  *out = c;
+  return MD_OK;
+}
+
+int md_batch_size(const md_ctx* c) { return c && c->batch ? (int)c->reps_in.size() : 0; }
+
+md_status md_batch_records(md_ctx* c, md_thermo* out, int max_records) {
+  if (!c || !out) return MD_BAD_ARGUMENT;
+  if (!c->batch) return fail(c, MD_BAD_ARGUMENT, "not a batch context");
+  if (!c->begun) return fail(c, MD_BAD_ARGUMENT, "md_begin has not been called");
+  const int nrep = (int)c->reps_in.size();
+  const int B = cluster_blocks(c->cl);
+  md_status s = ensure_epart(c, 3LL * (B > 0 ? B : 1));
+  if (s != MD_OK) return s;
+  double* e3 = c->rep_buf;
+  double* rec = c->rep_buf + 3 * (size_t)nrep;
+  launch_lj_cluster(cl_args(c, c->f3_tmp, c->epart), true, c->st);
+  launch_rep_energy(c->cl, c->epart, e3, c->st);
+  launch_rep_records(c->pos, c->vel, c->rep_ranges, nrep, c->sp, e3,
+                     (double)c->t * (double)c->cfg.dt, (double)c->t, rec, c->st);
+  c->stats.launches += 3;
+  const int n = nrep < max_records ? nrep : max_records;
+  if (n > 0)
+    CK(cudaMemcpyAsync(out, rec, sizeof(md_thermo) * (size_t)n, cudaMemcpyDeviceToHost, c->st),
+       "batch records");
+  CK(cudaStreamSynchronize(c->st), "batch records");
   return check_status(c);
 }
 

@@ -233,6 +233,27 @@ __device__ __forceinline__ void block_store(double (&v)[NV], double* out) {
   }
 }
 
+// block sum of NV doubles into the shared array out[NV] (all threads see it
+// after a barrier)
+template <int NV>
+__device__ __forceinline__ void block_sum_shared(double (&v)[NV], double* out) {
+  __shared__ double sm[NV][kRedThreads / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int k = 0; k < NV; k++) {
+    double x = v[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    if (lane == 0) sm[k][warp] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x < NV) {
+    double s = 0;
+    for (int w = 0; w < nw; w++) s += sm[threadIdx.x][w];
+    out[threadIdx.x] = s;
+  }
+}
+
 // common/DebugCalculations.cpp:81-110
 __global__ void k_thermo1(const md_double4* __restrict__ pos, const double* __restrict__ vel,
                           int n, Species sp, double* part) {
@@ -396,6 +417,63 @@ __global__ void k_record(const double* __restrict__ th8, const double* __restric
   rec[15] = step;
 }
 
+// One record per replica: PerformCalculations (common/DebugCalculations.cpp:
+// 46-124) over the replica's atoms [r0, r0 + rn), with its LJ energies e3.
+__global__ void __launch_bounds__(kRedThreads)
+    k_rep_record(const md_double4* __restrict__ pos, const double* __restrict__ vel,
+                 const int* __restrict__ ranges, Species sp, const double* __restrict__ e3,
+                 double time, double step, double* __restrict__ rec) {
+  const int k = blockIdx.x;
+  const int r0 = ranges[2 * k], rn = ranges[2 * k + 1];
+  __shared__ double s8[8];
+  double v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  for (int i = r0 + threadIdx.x; i < r0 + rn; i += blockDim.x) {
+    const md_double4 p = pos[i];
+    const double m = mass_of((int)p.w, sp);
+    const double vx = vel[3 * i], vy = vel[3 * i + 1], vz = vel[3 * i + 2];
+    v[0] += m * norm2_exact(vx, vy, vz);
+    v[1] += m * vx;
+    v[2] += m * vy;
+    v[3] += m * vz;
+    v[4] += m;
+    v[5] += m * p.x;
+    v[6] += m * p.y;
+    v[7] += m * p.z;
+  }
+  block_sum_shared<8>(v, s8);
+  __syncthreads();
+  const double tot = s8[4];
+  const double cx = s8[1] / tot, cy = s8[2] / tot, cz = s8[3] / tot;
+  double w[1] = {0};
+  for (int i = r0 + threadIdx.x; i < r0 + rn; i += blockDim.x) {
+    const double m = mass_of((int)pos[i].w, sp);
+    const double dx = vel[3 * i] - cx, dy = vel[3 * i + 1] - cy, dz = vel[3 * i + 2] - cz;
+    w[0] += m * norm2_exact(dx, dy, dz);
+  }
+  __shared__ double t1[1];
+  block_sum_shared<1>(w, t1);
+  __syncthreads();
+  if (threadIdx.x) return;
+  double* o = rec + 16 * (size_t)k;
+  const double ek = s8[0] / 2, eu = e3[3 * k];
+  o[0] = time;
+  o[1] = t1[0] / (3.0f * ((double)rn) * MD_KB);
+  o[2] = ek + eu;
+  o[3] = ek;
+  o[4] = eu;
+  o[5] = s8[5] / tot;
+  o[6] = s8[6] / tot;
+  o[7] = s8[7] / tot;
+  o[8] = s8[1];
+  o[9] = s8[2];
+  o[10] = s8[3];
+  o[11] = e3[3 * k];
+  o[12] = e3[3 * k + 1];
+  o[13] = 0.0;
+  o[14] = e3[3 * k + 2];
+  o[15] = step;
+}
+
 inline int nblk(long long n, int t) { return (int)((n + t - 1) / t); }
 
 }  // namespace
@@ -447,6 +525,12 @@ void launch_thermo(const md_double4* pos, const double* vel, int n, Species sp, 
   k_thermo2<<<B, kRedThreads, 0, st>>>(pos, vel, n, sp, s8, part);
   k_sum_partials<<<1, kRedThreads, 0, st>>>(part, B, 1, t1);
   k_thermo_final<<<1, 32, 0, st>>>(s8, t1, n, out);
+}
+void launch_rep_records(const md_double4* pos, const double* vel, const int* ranges, int nrep,
+                        Species sp, const double* e3, double time, double step, double* rec,
+                        cudaStream_t st) {
+  if (nrep > 0)
+    k_rep_record<<<nrep, kRedThreads, 0, st>>>(pos, vel, ranges, sp, e3, time, step, rec);
 }
 void launch_sum_partials(const double* part, int nblocks, int nv, double* out,
                          cudaStream_t st) {

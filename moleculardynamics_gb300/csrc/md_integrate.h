@@ -52,6 +52,12 @@ void launch_thermo(const md_double4* pos, const double* vel, int n, Species sp, 
 // Deterministic sum of nv-vectors over nblocks partials: out[k] = sum_b part[nv*b + k].
 void launch_sum_partials(const double* part, int nblocks, int nv, double* out,
                          cudaStream_t st);
+// Per-replica records (16 doubles each, md_thermo layout): thermo of atoms
+// [ranges[2k], ranges[2k] + ranges[2k+1]) and LJ energies e3[3k..3k+2]
+// (E, E_shifted, W).
+void launch_rep_records(const md_double4* pos, const double* vel, const int* ranges, int nrep,
+                        Species sp, const double* e3, double time, double step, double* rec,
+                        cudaStream_t st);
 // calculatePotentional (common/DebugCalculations.cpp:129-270) into out[0..1].
 // part: >= 2 * n doubles.
 void launch_ref_potential(const md_double4* pos, int n, Species sp, double* part, double* out,

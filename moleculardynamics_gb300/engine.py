@@ -90,7 +90,8 @@ EXPORTS = ["md_create", "md_destroy", "md_status_string", "md_last_error", "md_u
            "mdgb_build_neighbor_list", "mdgb_free", "mdgb_perform_calculations",
            "mdgb_calculate_potential", "mdgb_set_species", "mdgb_last_status", "md_read_config",
            "md_write_results", "md_host_alloc", "md_host_free",
-           "mdgb_many_body_forces_static", "md_autotune"]
+           "mdgb_many_body_forces_static", "md_autotune", "md_set_graphs", "md_batch_create",
+           "md_batch_size", "md_batch_records"]
 
 
 def load(path: str | None = None) -> C.CDLL:
@@ -127,6 +128,10 @@ def load(path: str | None = None) -> C.CDLL:
     L.md_kernel_time.argtypes = [C.c_void_p, C.c_int, P(C.c_double), P(C.c_longlong)]
     L.md_synchronize.argtypes = [C.c_void_p]
     L.md_autotune.argtypes = [C.c_void_p, C.c_int, P(MdTuneResult)]
+    L.md_set_graphs.argtypes = [C.c_void_p, C.c_int]
+    L.md_batch_create.argtypes = [P(MdConfig), C.c_int, _ip, _dp, P(C.c_void_p)]
+    L.md_batch_size.argtypes = [C.c_void_p]
+    L.md_batch_records.argtypes = [C.c_void_p, C.c_void_p, C.c_int]
     L.md_host_alloc.restype = C.c_void_p
     L.md_host_alloc.argtypes = [C.c_size_t]
     L.md_host_free.argtypes = [C.c_void_p]
@@ -286,6 +291,38 @@ class Engine:
 
     def synchronize(self):
         self._ck(self.lib.md_synchronize(self.h), "md_synchronize")
+
+    def set_graphs(self, on: bool):
+        self._ck(self.lib.md_set_graphs(self.h, int(on)), "md_set_graphs")
+
+
+class Batch(Engine):
+    """Many independent periodic replicas in one md_ctx (md_batch_create):
+    replica k holds natoms[k] atoms in a box of edge boxes[k]; arrays given to
+    upload/download hold the replicas one after another."""
+
+    def __init__(self, cfg: MdConfig, natoms, boxes):
+        self.lib = load()
+        na = np.ascontiguousarray(natoms, np.int32)
+        bx = np.ascontiguousarray(boxes, np.float64)
+        self.natoms = na
+        self.boxes = bx
+        cfg.n_lj = int(na.sum())
+        cfg.n_mb = 0
+        self.cfg = cfg
+        self.n = int(na.sum())
+        h = C.c_void_p()
+        s = self.lib.md_batch_create(C.byref(cfg), len(na), na, bx, C.byref(h))
+        if s != 0:
+            raise EngineError(s, "md_batch_create: " + self.lib.md_status_string(s).decode())
+        self.h = h
+
+    def replica_records(self) -> np.ndarray:
+        """(nrep, 16) records of the current state, md_thermo layout."""
+        k = len(self.natoms)
+        out = (MdThermo * k)()
+        self._ck(self.lib.md_batch_records(self.h, out, k), "md_batch_records")
+        return np.array([[getattr(r, f) for f in THERMO_FIELDS] for r in out]).reshape(k, 16)
 
 
 class Shim:

@@ -95,3 +95,29 @@ def write_input(path: str, pos4: np.ndarray, vel3: np.ndarray) -> None:
 def read_input(path: str, n: int):
     vals = np.loadtxt(path).reshape(-1)[: 7 * n].reshape(n, 7)
     return np.ascontiguousarray(vals[:, :4]), np.ascontiguousarray(vals[:, 4:])
+
+
+def make_batch(nrep: int = 256, nmin: int = 256, nmax: int = 32000, tmin: float = 60.0,
+               tmax: float = 150.0, seed: int = 4096, rho_star: float = 0.8442):
+    """An ensemble of independent argon replicas of uneven sizes.
+
+    Replica sizes are drawn log-uniform on [nmin, nmax]; replica k is the
+    first N_k sites of a ceil((N_k / 4)^(1/3))^3 FCC lattice at density
+    rho_star (so its box is that lattice's edge), with Maxwell-Boltzmann
+    velocities at a temperature drawn uniform on [tmin, tmax].
+    Returns (pos4, vel3, natoms, boxes, temperatures), the atoms of the
+    replicas one after another."""
+    rng = np.random.default_rng(seed)
+    sizes = np.rint(np.exp(rng.uniform(np.log(nmin), np.log(nmax), nrep))).astype(np.int64)
+    temps = rng.uniform(tmin, tmax, nrep)
+    seeds = rng.integers(0, 2**31 - 1, nrep)
+    a = fcc_constant(rho_star)
+    pos, vel, boxes = [], [], []
+    for n_k, t_k, s_k in zip(sizes, temps, seeds):
+        ncell = int(np.ceil((n_k / 4.0) ** (1.0 / 3.0) - 1e-9))
+        p, v, L = make_system("fcc", ncell, float(t_k), seed=int(s_k), a=a, natoms=int(n_k))
+        pos.append(p)
+        vel.append(v)
+        boxes.append(L)
+    return (np.ascontiguousarray(np.concatenate(pos)), np.ascontiguousarray(np.concatenate(vel)),
+            sizes.astype(np.int32), np.asarray(boxes, np.float64), temps)
