@@ -230,6 +230,91 @@ def run_reference_arm(args, rank, world):
     return 0
 
 
+def batched_form(eng, device, steps: int, loop_steps: int, seed: int = 4096) -> dict:
+    """The batched form on the 256-replica ensemble (sizes log-uniform on
+    [256, 32000], T uniform on [60, 150] K): all replicas in one context, one
+    persistent launch per MD step replayed from CUDA graphs.  Compared with
+    looping the plain FP64 path, and the single-system precision path,
+    replica by replica over the same replicas."""
+    from moleculardynamics_gb300 import lattice as lat
+    pos, vel, natoms, boxes, temps = lat.make_batch(256, 256, 32000, 60.0, 150.0, seed=seed)
+    n = int(natoms.sum())
+    cfg = eng.make_config(dt=2.0, lj_rs=2.8 * SIGMA, lj_rcut=2.5 * SIGMA, periodic=1,
+                          precision=eng.PREC_MIXED, species=eng.SPECIES_ARGON, device=device)
+    b = eng.Batch(cfg, natoms, boxes)
+    b.upload(pos, vel)
+    b.begin(0.0)
+    tune = b.autotune(2)
+    b.step(100)
+    b.synchronize()
+    r0 = b.replica_records()
+    s0 = b.stats()
+    b.set_timing(True)
+    b.step(steps)
+    b.synchronize()
+    ms, _ = b.kernel_time(eng.KERNEL_STEP)
+    fu_ms, fu_n = b.kernel_time(eng.KERNEL_FUSED)
+    s1 = b.stats()
+    b.set_timing(False)
+    r1 = b.replica_records()
+    value = n * steps / (ms / 1e3)
+    e0 = r0[:, 3] + r0[:, 12]
+    e1 = r1[:, 3] + r1[:, 12]
+    drift = np.abs(e1 - e0) / natoms / EPS / steps * 1000.0
+    # force error against the FP64 path, replica by replica (a sample)
+    bp, bv = b.download()
+    fb, _ = b.compute_forces()
+    b.close()
+    off = np.concatenate([[0], np.cumsum(natoms)])
+    rms = []
+    for k in np.linspace(0, len(natoms) - 1, 8).astype(int):
+        p, v = bp[off[k]:off[k + 1]], bv[off[k]:off[k + 1]]
+        e = engine_for(eng, len(p), float(boxes[k]), eng.PREC_FP64, device, output=0)
+        e.upload(np.ascontiguousarray(p), np.ascontiguousarray(v))
+        e.begin(0.0)
+        fa, _ = e.compute_forces()
+        e.close()
+        fk = fb[off[k]:off[k + 1]]
+        rms.append(float(np.sqrt(((fk - fa) ** 2).sum(1).mean()) / np.sqrt((fa ** 2).sum(1).mean())))
+
+    def loop(precision):
+        tot_ms = 0.0
+        for k in range(len(natoms)):
+            e = engine_for(eng, int(natoms[k]), float(boxes[k]), precision, device, output=0)
+            e.upload(np.ascontiguousarray(pos[off[k]:off[k + 1]]),
+                     np.ascontiguousarray(vel[off[k]:off[k + 1]]))
+            e.begin(0.0)
+            e.step(2)
+            e.synchronize()
+            e.set_timing(True)
+            e.step(loop_steps)
+            e.synchronize()
+            tot_ms += e.kernel_time(eng.KERNEL_STEP)[0]
+            e.close()
+        return n * loop_steps / (tot_ms / 1e3)
+
+    v64 = loop(eng.PREC_FP64)
+    v32 = loop(eng.PREC_MIXED)
+    return {
+        "metric": "atom-steps/s of the whole ensemble on 1 GB300", "value": value,
+        "unit": "atom-steps/s", "md_steps": steps,
+        "config": {"replicas": len(natoms), "atoms": n, "sizes": [int(natoms.min()), int(natoms.max())],
+                   "temperatures_K": [float(temps.min()), float(temps.max())],
+                   "dt_fs": 2.0, "form": "precision pairs, FP64 Gear, one persistent launch "
+                                         "per step, CUDA-graph windows of 6 steps",
+                   "autotune": tune},
+        "fused_kernel_ms": fu_ms / max(fu_n, 1),
+        "list_builds": s1["list_builds"] - s0["list_builds"],
+        "plain_fp64_loop": {"value": v64, "md_steps_per_replica": loop_steps},
+        "precision_single_loop": {"value": v32, "md_steps_per_replica": loop_steps},
+        "speedup_vs_plain_fp64_loop": value / v64,
+        "speedup_vs_precision_loop": value / v32,
+        "accuracy": {"force_rms_rel_vs_fp64_max": max(rms),
+                     "energy_drift_eps_per_atom_per_1000_steps_max": float(drift.max()),
+                     "energy_drift_eps_per_atom_per_1000_steps_mean": float(drift.mean())},
+    }
+
+
 def run_gb300(args, rank, world):
     from moleculardynamics_gb300 import build as b
     from moleculardynamics_gb300 import engine as eng
@@ -398,6 +483,9 @@ def run_gb300(args, rank, world):
                               "lj_force_ms": lj64_ms / max(lj64_n, 1)}
         line["speedup_vs_plain_fp64"] = value / world / v64
         line["accuracy"]["force_rms_rel_vs_fp64"] = rms
+    if rank == 0 and not args.no_forms:
+        line["forms"] = {"batched": batched_form(eng, device, args.batch_steps,
+                                                  args.batch_loop_steps)}
     if rank == 0 and world == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1
         csteps = args.cpu_md_steps
@@ -428,6 +516,9 @@ def main():
     ap.add_argument("--ref-md-steps", type=int, default=2)
     ap.add_argument("--lj-kernel", default="auto", choices=["auto", "rows", "cluster"])
     ap.add_argument("--no-tune", action="store_true", help="skip the cluster autotuner")
+    ap.add_argument("--no-forms", action="store_true", help="skip the batched/surrogate forms")
+    ap.add_argument("--batch-steps", type=int, default=1000)
+    ap.add_argument("--batch-loop-steps", type=int, default=10)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world, _ = dist_env()

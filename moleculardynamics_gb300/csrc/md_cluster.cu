@@ -549,6 +549,7 @@ __device__ __noinline__ bool band_inside(const SegShared& sh, const md_double4* 
 // Arguments of the segment force kernel (device copy of ClusterForceArgs).
 struct ClStep {
   int nseg;
+  int* sched;  // [0] next segment to hand out, [1] blocks finished
   const ClusterSegment* seg;
   const ClusterReplica* reps;
   const int* start;
@@ -569,8 +570,8 @@ struct ClStep {
   ClusterGearArgs g;
 };
 
-// FP32 LJ force, persistent: each block walks segments blockIdx.x,
-// blockIdx.x + gridDim.x, ...  ev: E, E_shifted, W per segment (as md_forces.cu).
+// FP32 LJ force, persistent: each block takes segments from a shared
+// counter until none is left.  ev: E, E_shifted, W per segment (as md_forces.cu).
 // GEAR: the Gear correct of this step and predict of the next follow for each
 // atom in the same thread (cpu/common/Device.cpp:17-85 in FP64 with FMAs).
 // Dynamic shared memory: two row tiles [16][blockDim + 8] of uint16 (TMA
@@ -599,10 +600,21 @@ __global__ void __launch_bounds__(224, 3)
   uint32_t phase = 0u;       // bit b: parity to wait for on bar[b] (b = 2: staging)
   uint32_t inflight = 0u;    // bit b: a copy into buffer b is in flight (issuing thread)
   bool trip_next = false;
-  for (int sidx = blockIdx.x; sidx < a.nseg; sidx += gridDim.x) {
+  bool aborted = false;
+  __shared__ int s_seg;
+  for (;;) {
+  // segments are handed out dynamically; the last block to leave resets
+  // the counters for the next launch
+  if (tid == 0) s_seg = atomicAdd(&a.sched[0], 1);
+  __syncthreads();
+  const int sidx = s_seg;
+  if (sidx >= a.nseg) break;
   load_segment(sh, a.seg, a.reps, sidx);
   __syncthreads();
-  if (!stage_bulk(sh, a.posf, st, &bar[2], (phase >> 2) & 1u, a.status)) return;
+  if (!stage_bulk(sh, a.posf, st, &bar[2], (phase >> 2) & 1u, a.status)) {
+    aborted = true;
+    break;
+  }
   phase ^= 4u;
   if (tripped) fill_offsets(sh, a.start);
   __syncthreads();
@@ -729,7 +741,8 @@ __global__ void __launch_bounds__(224, 3)
         if (tid == 0)
           for (int b = 0; b < 2; b++)
             if ((inflight >> b) & 1u) mbar_wait(&bar[b], (phase >> b) & 1u, a.status);
-        return;
+        aborted = true;
+        break;
       }
     } else if (live) {
       // skin exceeded: the full candidate row from shared memory, and a
@@ -812,8 +825,16 @@ __global__ void __launch_bounds__(224, 3)
       }
     }
   }
+  if (aborted) break;
   if (ENERGY) block_sums_at<3>(ev, a.epart, sidx);
   __syncthreads();  // the next segment overwrites sh and the stage
+  }
+  if (tid == 0) {
+    __threadfence();
+    if (atomicAdd(&a.sched[1], 1) == (int)gridDim.x - 1) {
+      a.sched[0] = 0;
+      a.sched[1] = 0;
+    }
   }
   if (GEAR && trip_next) a.skin[a.flag_set] = 1;
   if (blockIdx.x == 0 && tid == 0) {
@@ -981,6 +1002,10 @@ int cluster_build(ClusterList& cl, const std::vector<ClusterReplica>& reps_in, f
     cudaMemsetAsync(cl.skin, 0, sizeof(int) * 8, st);
   }
   if (!cl.counters && (e = cudaMalloc(&cl.counters, sizeof(int) * 8)) != cudaSuccess) return e;
+  if (!cl.sched) {
+    if ((e = cudaMalloc(&cl.sched, sizeof(int) * 2)) != cudaSuccess) return e;
+    cudaMemsetAsync(cl.sched, 0, sizeof(int) * 2, st);
+  }
   cudaMemsetAsync(cl.counters, 0, sizeof(int) * 8, st);
   cudaMemsetAsync(cl.count, 0, sizeof(int) * ((size_t)cl.ncells + 1), st);
   cudaMemsetAsync(cl.fill, 0, sizeof(int) * ((size_t)cl.ncells + 1), st);
@@ -1090,6 +1115,7 @@ void launch_lj_cluster(const ClusterForceArgs& f, bool energy, cudaStream_t st) 
                       stage_bytes(cl.max_staged);
   ClStep a;
   a.nseg = cl.nseg;
+  a.sched = cl.sched;
   a.seg = cl.seg;
   a.reps = cl.rep;
   a.start = cl.start;
@@ -1196,7 +1222,7 @@ void cluster_free(ClusterList& cl) {
   std::vector<void*> ptrs = {cl.rep,  cl.seg,      cl.count,     cl.start,   cl.fill, cl.segidx,
                              cl.cell, cl.unsorted, cl.perm,      cl.orig,    cl.itmp,
                              cl.rows, cl.len,      cl.pos_build, cl.pos_tmp, cl.skin,
-                             cl.counters};
+                             cl.counters, cl.sched};
   for (int k = 0; k < 5; k++) ptrs.push_back(cl.v3_tmp[k]);
   for (void* p : ptrs)
     if (p) cudaFree(p);

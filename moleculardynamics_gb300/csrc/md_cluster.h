@@ -87,6 +87,7 @@ struct ClusterList {
   CUtensorMap rmap;                               // TMA map of rows: {ld atoms, cap slots}
   int rmap_ok = 0;
   int* counters = nullptr;                        // device: max staged, max len, entries, max cell
+  int* sched = nullptr;                           // device: persistent kernel's work counters
   bool built = false;
 };
 
