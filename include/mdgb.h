@@ -198,6 +198,12 @@ int md_batch_size(const md_ctx* ctx);
  * replica's LJ energy over the force's pairs, e_mb = 0). */
 md_status md_batch_records(md_ctx* ctx, md_thermo* out, int max_records);
 
+/* Tensor-core self-test (no counterpart in the reference): c[128 x ncols] =
+ * a[128 x kdim] * b[ncols x kdim]^T on tcgen05 with BF16 operands rounded to
+ * nearest from the FP32 inputs and FP32 accumulation; row-major host arrays;
+ * ncols in {32, 64, 128}, kdim a multiple of 16 up to 128. */
+md_status mdgb_tc_selftest(const float* a, const float* b, float* c, int ncols, int kdim);
+
 /* Wait for all work of the context; returns the first deferred error. */
 md_status md_synchronize(md_ctx* ctx);
 /* Page-locked host memory for fast md_upload/md_download (NULL on failure). */

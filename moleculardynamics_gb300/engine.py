@@ -78,6 +78,7 @@ class ListSettings(C.Structure):
 
 _dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
 _ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+_fp = np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")
 _lib = None
 
 # every exported symbol of include/mdgb.h
@@ -91,7 +92,7 @@ EXPORTS = ["md_create", "md_destroy", "md_status_string", "md_last_error", "md_u
            "mdgb_calculate_potential", "mdgb_set_species", "mdgb_last_status", "md_read_config",
            "md_write_results", "md_host_alloc", "md_host_free",
            "mdgb_many_body_forces_static", "md_autotune", "md_set_graphs", "md_batch_create",
-           "md_batch_size", "md_batch_records"]
+           "md_batch_size", "md_batch_records", "mdgb_tc_selftest"]
 
 
 def load(path: str | None = None) -> C.CDLL:
@@ -129,6 +130,7 @@ def load(path: str | None = None) -> C.CDLL:
     L.md_synchronize.argtypes = [C.c_void_p]
     L.md_autotune.argtypes = [C.c_void_p, C.c_int, P(MdTuneResult)]
     L.md_set_graphs.argtypes = [C.c_void_p, C.c_int]
+    L.mdgb_tc_selftest.argtypes = [_fp, _fp, _fp, C.c_int, C.c_int]
     L.md_batch_create.argtypes = [P(MdConfig), C.c_int, _ip, _dp, P(C.c_void_p)]
     L.md_batch_size.argtypes = [C.c_void_p]
     L.md_batch_records.argtypes = [C.c_void_p, C.c_void_p, C.c_int]
@@ -391,6 +393,19 @@ class Shim:
         self.lib.mdgb_calculate_potential(pos4, C.byref(a), C.byref(b), len(pos4))
         self._ck("mdgb_calculate_potential")
         return a.value, b.value
+
+
+def tc_selftest(A: np.ndarray, B: np.ndarray) -> np.ndarray:
+    """C = A B^T on the tensor cores (tcgen05, BF16 operands, FP32 accumulate);
+    A is 128 x K, B is N x K."""
+    L = load()
+    A = np.ascontiguousarray(A, np.float32)
+    B = np.ascontiguousarray(B, np.float32)
+    Cm = np.zeros((128, B.shape[0]), np.float32)
+    s = L.mdgb_tc_selftest(A, B, Cm, B.shape[0], A.shape[1])
+    if s != 0:
+        raise EngineError(s, "mdgb_tc_selftest")
+    return Cm
 
 
 def pinned(shape, dtype=np.float64):
