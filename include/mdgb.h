@@ -198,6 +198,69 @@ int md_batch_size(const md_ctx* ctx);
  * replica's LJ energy over the force's pairs, e_mb = 0). */
 md_status md_batch_records(md_ctx* ctx, md_thermo* out, int max_records);
 
+/* ---- learned surrogate of the bond-order term (no counterpart in the
+ * reference) ----
+ * Per-atom descriptors: 16 radial and 16 angular Behler symmetry functions
+ * (FP32) of the neighbours within `cutoff` (at most the bond-order RCUT).
+ * Network: 32-64-64-1 MLP (tanh) giving a per-atom energy; BF16 weights on
+ * the tensor cores (tcgen05) with FP32 accumulation; forces from its
+ * analytic gradient.  Trained with Adam on per-atom energies of the exact
+ * method: E_i = sum_j 1/2 (Vr - b Va + Vdw) over i's bond-order pairs.
+ * Attached to a context, it replaces the exact bond-order forces while its
+ * force error, measured against the exact kernel every check_every steps
+ * (relative RMS over the bond-order atoms), stays within threshold; the
+ * exact kernel computes the forces otherwise. */
+typedef struct md_surrogate md_surrogate;
+typedef struct md_surrogate_stats {
+  long long surrogate_steps;   /* steps whose bond-order forces came from the network */
+  long long exact_steps;       /* steps that used the exact kernel */
+  long long checks;            /* exact-kernel checks of the network */
+  long long rejected_checks;   /* checks whose error exceeded the threshold */
+  double last_error;           /* relative RMS force error at the last check */
+} md_surrogate_stats;
+md_status md_surrogate_create(int device, unsigned long long seed, float cutoff,
+                              md_surrogate** out);
+void md_surrogate_destroy(md_surrogate* s);
+int md_surrogate_param_count(void);
+/* appends bond-order atoms offset, offset + stride, ... of ctx's current
+ * state (descriptors + exact per-atom energies) to the training set, and the
+ * whole state (positions, neighbours, exact forces and energies) to the
+ * force-matching configurations */
+md_status md_surrogate_collect(md_surrogate* s, md_ctx* ctx, int stride, int offset, int* added);
+md_status md_surrogate_samples(const md_surrogate* s, int* count);
+/* Adam steps on random batches of the training set; *loss = mean squared
+ * error of the normalised per-atom energy over the last steps */
+md_status md_surrogate_train(md_surrogate* s, int steps, int batch, float lr, double* loss);
+/* force matching over the collected configurations (one per Adam step):
+ * loss = w_energy * mean((t - t*)^2) + w_force * mean(|F - F*|^2) / var(F*),
+ * t the normalised per-atom energy, F the bond-order forces; the losses of
+ * the last pass over the configurations come back in loss_energy/loss_force */
+md_status md_surrogate_train_forces(md_surrogate* s, int steps, float lr, float w_energy,
+                                    float w_force, double* loss_energy, double* loss_force);
+/* s = NULL detaches */
+md_status md_surrogate_attach(md_ctx* ctx, md_surrogate* s, double threshold, int check_every);
+md_status md_surrogate_report(const md_ctx* ctx, md_surrogate_stats* out);
+/* network bond-order forces (n_mb x real3) and energy at ctx's state */
+md_status md_surrogate_forces(md_surrogate* s, md_ctx* ctx, double* force3, double* energy);
+/* descriptors (n_mb x 32): raw, or normalised as the network sees them */
+md_status md_surrogate_descriptors(md_surrogate* s, md_ctx* ctx, float* g, int normalised);
+/* FP32 parameters: W1 [64][32], b1 [64], W2 [64][64], b2 [64], w3 [64], b3 */
+md_status md_surrogate_params(md_surrogate* s, float* params, int set);
+/* input normalisation (x = (g - mean) * istd) and target scaling
+ * (E = mu + sigma * t), mu_sigma = {mu, sigma} */
+md_status md_surrogate_normalisation(md_surrogate* s, float* mean32, float* istd32,
+                                     double* mu_sigma, int set);
+/* loss = mean over rows of (net(x) - t)^2 and its gradient (FP32, same
+ * layout as the parameters), from the training kernels */
+md_status md_surrogate_loss_grad(md_surrogate* s, const float* x, const float* t, int n,
+                                 float* grad, double* loss);
+/* parameter gradient of sum_i v_i . dt/dx(x_i) (the force-matching term of
+ * the training kernels) for normalised inputs x and directions v (n x 32) */
+md_status md_surrogate_force_grad(md_surrogate* s, const float* x, const float* v, int n,
+                                  float* grad);
+/* network output t (n) and dt/dx (n x 32) for normalised inputs x (n x 32) */
+md_status md_surrogate_net(md_surrogate* s, const float* x, int n, float* t, float* dtdx);
+
 /* Tensor-core self-test (no counterpart in the reference): c[128 x ncols] =
  * a[128 x kdim] * b[ncols x kdim]^T on tcgen05 with BF16 operands rounded to
  * nearest from the FP32 inputs and FP32 accumulation; row-major host arrays;

@@ -24,6 +24,7 @@
 #include "md_forces.h"
 #include "md_integrate.h"
 #include "md_neighbor.cuh"
+#include "md_surrogate.h"
 
 using namespace mdgb;
 
@@ -115,6 +116,15 @@ struct md_ctx {
   // CUDA graph of a window of fused steps (replayed while nothing else is due)
   bool graphs = false;
   cudaGraphExec_t gexec = nullptr;
+  // learned surrogate of the bond-order term (not owned): used while its
+  // force error, measured by the exact kernel every sur_every steps, stays
+  // within sur_threshold; otherwise the exact kernel computes the forces
+  md_surrogate* sur = nullptr;
+  double sur_threshold = 0.0, sur_err = -1.0;
+  int sur_every = 10, sur_last_check = -1;
+  bool sur_use = false;
+  long long sur_steps = 0, sur_exact_steps = 0, sur_checks = 0, sur_rejects = 0;
+  double *sur_fx = nullptr, *sur_fs = nullptr;  // check buffers (3 doubles per many-body atom)
   std::vector<unsigned char> gsig;
   long long graph_windows = 0;
   // bond-order scratch
@@ -129,7 +139,8 @@ struct md_ctx {
   Scratch sc;
   double* epart = nullptr;
   long long epart_cap = 0;
-  double* dsc = nullptr;  // device scalars: th8[0..7] elj[8..10] emb[11..13] ref[14..15]
+  double* dsc = nullptr;  // device scalars: th8[0..7] elj[8..10] emb[11..13] ref[14..15],
+                          // record scratch [16..31], surrogate energy [32]
   double* rec = nullptr;
   int rec_cap = 0, nrec = 0;
   // schedule
@@ -321,7 +332,43 @@ ClusterForceArgs cl_args(md_ctx* c, double* f3, double* epart) {
   return a;
 }
 
-md_status forces(md_ctx* c, double* f3) {
+// bond-order forces of the step: exact, or the surrogate's (checked against
+// the exact kernel every sur_every steps)
+md_status mb_forces_step(md_ctx* c, double* f3) {
+  const int nmb = c->cfg.n_mb;
+  const int acc = c->cfg.use_lj;
+  if (c->t - c->sur_last_check >= c->sur_every || c->sur_last_check < 0 || c->t < c->sur_last_check) {
+    MbArgs a = mb_args(c, c->sur_fx, 0);
+    launch_mb(a, c->mixed(), false, c->st);
+    int r = sur_forces(*c->sur, c->pos, nmb, make_walker(c->mb), c->sur_fs, 0, nullptr, c->status,
+                       c->st);
+    if (r) return r == -1 ? fail(c, MD_BAD_ARGUMENT, "surrogate not trained")
+                          : cuda_fail(c, (cudaError_t)r, "surrogate forces");
+    double err = 0;
+    r = sur_rel_err(c->sur_fs, c->sur_fx, nmb, c->sur->scratch, &err, c->st);
+    if (r) return cuda_fail(c, (cudaError_t)r, "surrogate check");
+    c->sur_err = err;
+    c->sur_use = err <= c->sur_threshold;
+    c->sur_last_check = c->t;
+    c->sur_checks++;
+    if (!c->sur_use) c->sur_rejects++;
+    c->stats.launches += 12;
+  }
+  if (c->sur_use) {
+    int r = sur_forces(*c->sur, c->pos, nmb, make_walker(c->mb), f3, acc, nullptr, c->status,
+                       c->st);
+    if (r) return cuda_fail(c, (cudaError_t)r, "surrogate forces");
+    c->sur_steps++;
+    c->stats.launches += 7;
+  } else {
+    launch_mb(mb_args(c, f3, acc), c->mixed(), false, c->st);
+    c->sur_exact_steps++;
+    c->stats.launches += 3;
+  }
+  return MD_OK;
+}
+
+md_status forces(md_ctx* c, double* f3, bool step = false) {
   if (c->cfg.use_lj) {
     Timed tm(c, 0);
     if (c->cluster)
@@ -332,6 +379,7 @@ md_status forces(md_ctx* c, double* f3) {
   }
   if (c->cfg.use_mb && c->cfg.n_mb > 0) {
     Timed tm(c, 1);
+    if (step && c->sur) return mb_forces_step(c, f3);
     launch_mb(mb_args(c, f3, c->cfg.use_lj), c->mixed(), false, c->st);
     c->stats.launches += 3;
   }
@@ -702,7 +750,10 @@ md_status step_once(md_ctx* c, bool last) {
     advance_fused(c);
     return MD_OK;
   }
-  forces(c, c->f3);
+  {
+    md_status fs = forces(c, c->f3, true);
+    if (fs != MD_OK) return fs;
+  }
   if (c->walls()) CK(cudaMemsetAsync(c->wall_flag, 0, sizeof(int), c->st), "wall flag");
   {
     Timed tm(c, 3);
@@ -831,8 +882,8 @@ md_status md_create(const md_config* cfg, md_ctx** out) {
   if ((e = cudaMalloc(&c->sc.umax, sizeof(unsigned long long) * 4)) != cudaSuccess)
     return bail(e, "scratch");
   if ((e = cudaMalloc(&c->sc.counts, sizeof(int) * 8)) != cudaSuccess) return bail(e, "scratch");
-  if ((e = cudaMalloc(&c->dsc, sizeof(double) * 32)) != cudaSuccess) return bail(e, "scratch");
-  cudaMemsetAsync(c->dsc, 0, sizeof(double) * 32, c->st);
+  if ((e = cudaMalloc(&c->dsc, sizeof(double) * 40)) != cudaSuccess) return bail(e, "scratch");
+  cudaMemsetAsync(c->dsc, 0, sizeof(double) * 40, c->st);
   *out = c;
   return MD_OK;
 }
@@ -844,7 +895,7 @@ void md_destroy(md_ctx* c) {
   list_free(c->mb);
   cluster_free(c->cl);
   if (c->gexec) cudaGraphExecDestroy(c->gexec);
-  void* ptrs[] = {c->rep_ranges, c->rep_buf, c->io, c->pos_alt, c->posf_alt, c->pos, c->vel, c->acc, c->b, c->c, c->f3, c->f3_tmp, c->posf, c->mb_sl,
+  void* ptrs[] = {c->sur_fx, c->sur_fs, c->rep_ranges, c->rep_buf, c->io, c->pos_alt, c->posf_alt, c->pos, c->vel, c->acc, c->b, c->c, c->f3, c->f3_tmp, c->posf, c->mb_sl,
                   c->mb_slen, c->xsi, c->xsj, c->va, c->status, c->epart, c->dsc, c->rec,
                   c->sc.dpart, c->sc.umax, c->sc.counts, c->sc.block_sums};
   for (void* p : ptrs)
@@ -1261,6 +1312,205 @@ md_status md_batch_records(md_ctx* c, md_thermo* out, int max_records) {
        "batch records");
   CK(cudaStreamSynchronize(c->st), "batch records");
   return check_status(c);
+}
+
+md_status md_surrogate_create(int device, unsigned long long seed, float cutoff,
+                              md_surrogate** out) {
+  if (!out || !(cutoff > 0.5f)) return MD_BAD_ARGUMENT;
+  *out = nullptr;
+  if (cudaSetDevice(device) != cudaSuccess) return MD_NO_DEVICE;
+  md_surrogate* s = new md_surrogate();
+  s->device = device;
+  s->rc = cutoff;
+  if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      sur_init(*s, seed, s->stream) != 0) {
+    delete s;
+    return MD_CUDA_ERROR;
+  }
+  *out = s;
+  return MD_OK;
+}
+
+void md_surrogate_destroy(md_surrogate* s) {
+  if (!s) return;
+  if (s->stream) cudaStreamSynchronize(s->stream);
+  delete s;
+}
+
+int md_surrogate_param_count(void) { return sur_param_count(); }
+
+md_status md_surrogate_collect(md_surrogate* s, md_ctx* c, int stride, int offset, int* added) {
+  if (!s || !c || stride < 1 || offset < 0) return MD_BAD_ARGUMENT;
+  if (!c->begun) return fail(c, MD_BAD_ARGUMENT, "md_begin has not been called");
+  if (!c->cfg.use_mb || c->cfg.n_mb < 1 || !c->mb.cell3)
+    return fail(c, MD_BAD_ARGUMENT, "no bond-order atoms");
+  if (s->rc > c->cfg.mb_rcut + 1e-6f)
+    return fail(c, MD_BAD_ARGUMENT, "descriptor cutoff beyond the bond-order cutoff");
+  const int n = c->cfg.n_mb;
+  int r = sur_descriptors(*s, c->pos, n, make_walker(c->mb), false, c->status, c->st);
+  if (r) return cuda_fail(c, (cudaError_t)r, "surrogate descriptors");
+  const int B = mb_blocks(n);
+  md_status ms = ensure_epart(c, 3LL * B);
+  if (ms != MD_OK) return ms;
+  MbArgs a = mb_args(c, c->f3_tmp, 0);
+  a.epart1 = c->epart;
+  a.epart2 = c->epart + 2LL * B;
+  a.eatom = s->eatom;
+  launch_mb(a, c->mixed(), true, c->st);
+  r = sur_collect(*s, n, s->eatom, stride, offset, c->st, added);
+  if (r) return cuda_fail(c, (cudaError_t)r, "surrogate samples");
+  // the whole configuration, for force matching (f3_tmp holds the exact
+  // bond-order forces: the energy launch overwrites it)
+  r = sur_add_config(*s, c->pos, n, c->mb.grid.box, c->f3_tmp, s->eatom, c->st);
+  if (r) return cuda_fail(c, (cudaError_t)r, "surrogate configuration");
+  return check_status(c);
+}
+
+md_status md_surrogate_train_forces(md_surrogate* s, int steps, float lr, float w_energy,
+                                    float w_force, double* loss_energy, double* loss_force) {
+  if (!s || steps < 0 || !(lr > 0.f) || w_energy < 0.f || w_force < 0.f) return MD_BAD_ARGUMENT;
+  if (s->cfgs.empty()) return MD_BAD_ARGUMENT;
+  s->w_energy = w_energy;
+  s->w_force = w_force;
+  int r = sur_train_fm(*s, steps, lr, loss_energy, loss_force, s->stream);
+  if (r == -1) return MD_BAD_ARGUMENT;
+  if (r) return MD_CUDA_ERROR;
+  int st = 0;
+  cudaMemcpy(&st, s->status_d, sizeof(int), cudaMemcpyDeviceToHost);
+  return st & ST_TMA_TIMEOUT ? MD_TIMEOUT : MD_OK;
+}
+
+md_status md_surrogate_force_grad(md_surrogate* s, const float* x, const float* v, int n,
+                                  float* grad) {
+  if (!s || !x || !v || !grad || n < 1) return MD_BAD_ARGUMENT;
+  return sur_force_grad(*s, x, v, n, grad, s->stream) ? MD_CUDA_ERROR : MD_OK;
+}
+
+md_status md_surrogate_train(md_surrogate* s, int steps, int batch, float lr, double* loss) {
+  if (!s || steps < 0 || batch < 1 || !(lr > 0.f)) return MD_BAD_ARGUMENT;
+  if (s->ns < 1) return MD_BAD_ARGUMENT;
+  int r = sur_train(*s, steps, batch, lr, loss, s->stream);
+  if (r == -1) return MD_BAD_ARGUMENT;
+  if (r) return MD_CUDA_ERROR;
+  int st = 0;
+  cudaMemcpy(&st, s->status_d, sizeof(int), cudaMemcpyDeviceToHost);
+  return st & ST_TMA_TIMEOUT ? MD_TIMEOUT : MD_OK;
+}
+
+md_status md_surrogate_samples(const md_surrogate* s, int* count) {
+  if (!s || !count) return MD_BAD_ARGUMENT;
+  *count = s->ns;
+  return MD_OK;
+}
+
+md_status md_surrogate_attach(md_ctx* c, md_surrogate* s, double threshold, int check_every) {
+  if (!c || check_every < 1) return MD_BAD_ARGUMENT;
+  if (s && (!c->cfg.use_mb || c->cfg.n_mb < 1))
+    return fail(c, MD_BAD_ARGUMENT, "no bond-order atoms");
+  if (s && !s->normalised) return fail(c, MD_BAD_ARGUMENT, "surrogate not trained");
+  if (s && s->rc > c->cfg.mb_rcut + 1e-6f)
+    return fail(c, MD_BAD_ARGUMENT, "descriptor cutoff beyond the bond-order cutoff");
+  if (s && !c->sur_fx) {
+    const size_t B = sizeof(double) * 3 * (size_t)c->cfg.n_mb;
+    CK(cudaMalloc(&c->sur_fx, B), "surrogate check buffers");
+    CK(cudaMalloc(&c->sur_fs, B), "surrogate check buffers");
+  }
+  c->sur = s;
+  c->sur_threshold = threshold;
+  c->sur_every = check_every;
+  c->sur_last_check = -1;
+  c->sur_use = false;
+  c->sur_err = -1.0;
+  c->sur_steps = c->sur_exact_steps = c->sur_checks = c->sur_rejects = 0;
+  return MD_OK;
+}
+
+md_status md_surrogate_report(const md_ctx* c, md_surrogate_stats* out) {
+  if (!c || !out) return MD_BAD_ARGUMENT;
+  out->surrogate_steps = c->sur_steps;
+  out->exact_steps = c->sur_exact_steps;
+  out->checks = c->sur_checks;
+  out->rejected_checks = c->sur_rejects;
+  out->last_error = c->sur_err;
+  return MD_OK;
+}
+
+md_status md_surrogate_forces(md_surrogate* s, md_ctx* c, double* f3, double* energy) {
+  if (!s || !c) return MD_BAD_ARGUMENT;
+  if (!c->begun) return fail(c, MD_BAD_ARGUMENT, "md_begin has not been called");
+  if (!c->cfg.use_mb || c->cfg.n_mb < 1) return fail(c, MD_BAD_ARGUMENT, "no bond-order atoms");
+  if (!s->normalised) return fail(c, MD_BAD_ARGUMENT, "surrogate not trained");
+  const int n = c->cfg.n_mb;
+  double* e_dev = c->dsc + 32;
+  int r = sur_forces(*s, c->pos, n, make_walker(c->mb), c->f3_tmp, 0, e_dev, c->status, c->st);
+  if (r) return cuda_fail(c, (cudaError_t)r, "surrogate forces");
+  if (f3)
+    CK(cudaMemcpyAsync(f3, c->f3_tmp, sizeof(double) * 3 * (size_t)n, cudaMemcpyDeviceToHost,
+                       c->st),
+       "surrogate forces");
+  double e = 0;
+  CK(cudaMemcpyAsync(&e, e_dev, sizeof(double), cudaMemcpyDeviceToHost, c->st), "surrogate");
+  CK(cudaStreamSynchronize(c->st), "surrogate");
+  if (energy) *energy = e;
+  return check_status(c);
+}
+
+md_status md_surrogate_descriptors(md_surrogate* s, md_ctx* c, float* g, int normalised) {
+  if (!s || !c || !g) return MD_BAD_ARGUMENT;
+  if (!c->begun) return fail(c, MD_BAD_ARGUMENT, "md_begin has not been called");
+  if (!c->cfg.use_mb || c->cfg.n_mb < 1) return fail(c, MD_BAD_ARGUMENT, "no bond-order atoms");
+  if (normalised && !s->normalised) return fail(c, MD_BAD_ARGUMENT, "surrogate not trained");
+  const int n = c->cfg.n_mb;
+  int r = sur_descriptors(*s, c->pos, n, make_walker(c->mb), normalised != 0, c->status, c->st);
+  if (r) return cuda_fail(c, (cudaError_t)r, "surrogate descriptors");
+  CK(cudaMemcpyAsync(g, s->X, sizeof(float) * kSurDesc * (size_t)n, cudaMemcpyDeviceToHost,
+                     c->st),
+     "descriptors");
+  CK(cudaStreamSynchronize(c->st), "descriptors");
+  return check_status(c);
+}
+
+md_status md_surrogate_params(md_surrogate* s, float* params, int set) {
+  if (!s || !params) return MD_BAD_ARGUMENT;
+  int r = set ? sur_set_params(*s, params, s->stream) : sur_get_params(*s, params, s->stream);
+  return r ? MD_CUDA_ERROR : MD_OK;
+}
+
+md_status md_surrogate_normalisation(md_surrogate* s, float* mean32, float* istd32,
+                                     double* mu_sigma, int set) {
+  if (!s) return MD_BAD_ARGUMENT;
+  const size_t B = sizeof(float) * kSurDesc;
+  if (set) {
+    if (!mean32 || !istd32 || !mu_sigma || !(mu_sigma[1] > 0)) return MD_BAD_ARGUMENT;
+    if (cudaMemcpy(s->mean_d, mean32, B, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(s->istd_d, istd32, B, cudaMemcpyHostToDevice) != cudaSuccess)
+      return MD_CUDA_ERROR;
+    s->mu = mu_sigma[0];
+    s->sigma = mu_sigma[1];
+    s->normalised = true;
+    return MD_OK;
+  }
+  if (!s->normalised) return MD_BAD_ARGUMENT;
+  if (mean32 && cudaMemcpy(mean32, s->mean_d, B, cudaMemcpyDeviceToHost) != cudaSuccess)
+    return MD_CUDA_ERROR;
+  if (istd32 && cudaMemcpy(istd32, s->istd_d, B, cudaMemcpyDeviceToHost) != cudaSuccess)
+    return MD_CUDA_ERROR;
+  if (mu_sigma) {
+    mu_sigma[0] = s->mu;
+    mu_sigma[1] = s->sigma;
+  }
+  return MD_OK;
+}
+
+md_status md_surrogate_loss_grad(md_surrogate* s, const float* x, const float* t, int n,
+                                 float* grad, double* loss) {
+  if (!s || !x || !t || !grad || !loss || n < 1) return MD_BAD_ARGUMENT;
+  return sur_loss_grad(*s, x, t, n, grad, loss, s->stream) ? MD_CUDA_ERROR : MD_OK;
+}
+
+md_status md_surrogate_net(md_surrogate* s, const float* x, int n, float* t, float* dtdx) {
+  if (!s || !x || !t || !dtdx || n < 1) return MD_BAD_ARGUMENT;
+  return sur_net_eval(*s, x, n, t, dtdx, s->stream) ? MD_CUDA_ERROR : MD_OK;
 }
 
 md_status md_set_timing(md_ctx* c, int on) {

@@ -515,7 +515,8 @@ __global__ void __launch_bounds__(128)
     k_mb_pass1(const md_double4* __restrict__ pos, const float4* __restrict__ posf,
                double* __restrict__ f3, int n, const uint32_t* __restrict__ sl,
                const int* __restrict__ slen, Grid g, int ljexist, T* __restrict__ xsi_s,
-               T* __restrict__ xsj_s, T* __restrict__ va_s, double* __restrict__ epart) {
+               T* __restrict__ xsj_s, T* __restrict__ va_s, double* __restrict__ epart,
+               double* __restrict__ eatom) {
   const int warps = blockDim.x >> 5;
   const int i = blockIdx.x * warps + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
@@ -631,6 +632,12 @@ __global__ void __launch_bounds__(128)
       if (ENERGY) ev[0] += (double)(0.5f * ((vr - bo * va) + vdw));
     }
     double sx = warp_sum((double)fx), sy = warp_sum((double)fy), sz = warp_sum((double)fz);
+    if (ENERGY && eatom) {
+      // per-atom share: sum over j of 1/2 (Vr - b Va + Vdw) (the i-sum of
+      // common/DebugCalculations.cpp:129-270 restricted to the force's pairs)
+      const double ei = warp_sum(ev[0]);
+      if (lane == 0) eatom[i] = ei;
+    }
     if (lane == 0) {
       if (ljexist) {
         f3[3 * i] += sx;
@@ -834,13 +841,13 @@ static void launch_mb_t(const MbArgs& a, bool energy, cudaStream_t st) {
   T* va = (T*)a.va;
   if (energy) {
     k_mb_pass1<T, true><<<B, 128, 0, st>>>(a.pos, a.posf, a.f3, a.n, a.sl, a.slen, a.grid,
-                                           a.ljexist, xsi, xsj, va, a.epart1);
+                                           a.ljexist, xsi, xsj, va, a.epart1, a.eatom);
     k_mb_pass2<T, true><<<B, 128, 0, st>>>(a.pos, a.posf, a.f3, a.n, a.sl, a.slen, a.grid,
                                            a.cell3, a.ref_rows, a.ref_nls, a.ref_nlargest, a.rcutsq, xsi, xsj, va,
                                            a.missing, a.epart2);
   } else {
     k_mb_pass1<T, false><<<B, 128, 0, st>>>(a.pos, a.posf, a.f3, a.n, a.sl, a.slen, a.grid,
-                                            a.ljexist, xsi, xsj, va, nullptr);
+                                            a.ljexist, xsi, xsj, va, nullptr, nullptr);
     k_mb_pass2<T, false><<<B, 128, 0, st>>>(a.pos, a.posf, a.f3, a.n, a.sl, a.slen, a.grid,
                                             a.cell3, a.ref_rows, a.ref_nls, a.ref_nlargest, a.rcutsq, xsi, xsj,
                                             va, a.missing, nullptr);

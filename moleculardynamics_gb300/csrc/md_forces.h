@@ -49,6 +49,7 @@ struct MbArgs {
   int* missing;
   double* epart1;       // 2 doubles per pass-1 block
   double* epart2;       // 1 double per pass-2 block
+  double* eatom = nullptr;  // energy launches: per-atom energy (sum over j of half the pair)
 };
 
 void launch_lj(const ForceArgs& a, bool fp32, bool energy, cudaStream_t st);

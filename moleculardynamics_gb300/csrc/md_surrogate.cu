@@ -3,16 +3,18 @@
 // functions (16 radial, 16 angular, FP32), a 32-64-64-1 MLP with BF16
 // weights on the tensor cores (tcgen05, FP32 accumulation in tensor memory),
 // forces from the network's analytic gradient, Adam training on per-atom
-// energies of the exact method.  This file starts with the tensor-core GEMM
-// building block and its self-test.
+// energies of the exact method, and the tensor-core self-test.
 #include <cuda_bf16.h>
 
 #include <cmath>
 #include <cstring>
 #include <vector>
 
+#include <algorithm>
+
 #include "../../include/mdgb.h"
-#include "md_internal.h"
+#include "md_neighbor.cuh"
+#include "md_surrogate.h"
 #include "md_tc.cuh"
 
 namespace mdgb {
@@ -69,9 +71,1396 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   if (warp == 0) tc_dealloc(taddr, ncols);
 }
 
+// ---------------------------------------------------------------- surrogate
+constexpr int kDesc = kSurDesc, kHid = 64, kRad = 16, kAng = 16;
+constexpr int kSgMax = 64;  // neighbours within the descriptor cutoff
+constexpr int oW1 = 0, oB1 = oW1 + kHid * kDesc, oW2 = oB1 + kHid, oB2 = oW2 + kHid * kHid,
+              oW3 = oB2 + kHid, oB3 = oW3 + kHid, kParams = oB3 + 1;  // 6337
+
+DescParams default_desc(float rc) {
+  DescParams P;
+  P.rc = rc;
+  const float d = (rc - 0.8f) / (kRad - 1);
+  P.eta_r = 0.5f / (d * d);
+  for (int k = 0; k < kRad; k++) P.rs[k] = 0.8f + d * k;
+  const int zetas[4] = {1, 2, 4, 16};
+  const float etas[2] = {0.02f, 0.25f};
+  for (int f = 0; f < kAng; f++) {
+    P.zeta[f] = zetas[f % 4];
+    P.lam[f] = (f / 4) % 2 ? -1.f : 1.f;
+    P.eta_a[f] = etas[f / 8];
+    P.pref[f] = powf(2.f, 1.f - (float)P.zeta[f]);
+  }
+  return P;
+}
+
+__device__ __forceinline__ void fcut(float r, float rc, float& fc, float& dfc) {
+  const float a = 3.14159265358979f / rc;
+  float s, c;
+  __sincosf(a * r, &s, &c);
+  fc = 0.5f * (c + 1.f);
+  dfc = -0.5f * a * s;
+}
+
+__device__ __forceinline__ float ipow(float b, int z) {
+  float r = 1.f;
+  for (int k = 0; k < z; k++) r *= b;
+  return r;
+}
+
+// neighbours of i within rc (from the bond-order candidate rows), as
+// packed entries with their periodic image
+__global__ void k_sg_short(const md_double4* __restrict__ pos, RowWalker w, float rc,
+                           uint32_t* __restrict__ sl, int* __restrict__ slen,
+                           int* __restrict__ status) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= w.n) return;
+  const md_double4 pi = pos[i];
+  const double rc2 = (double)rc * rc;
+  int cnt = 0;
+  walk_row(w, pos, i, [&](int m, int ix, int iy, int iz) {
+    const md_double4 pm = pos[m];
+    const double dx = pm.x + ix * w.g.box - pi.x, dy = pm.y + iy * w.g.box - pi.y,
+                 dz = pm.z + iz * w.g.box - pi.z;
+    if (dx * dx + dy * dy + dz * dz < rc2) {
+      if (cnt < kSgMax) sl[(size_t)i * kSgMax + cnt] = pack_entry(m, ix, iy, iz);
+      cnt++;
+    }
+  });
+  if (cnt > kSgMax) {
+    atomicOr(status, ST_CELL_OVERFLOW);
+    cnt = kSgMax;
+  }
+  slen[i] = cnt;
+}
+
+// offsets d_j = r_j - r_i (FP32) of i's neighbours
+__device__ __forceinline__ int load_nbrs(int i, const md_double4* pos, const uint32_t* sl,
+                                         const int* slen, double box, float3* d, float* r,
+                                         int* idx) {
+  const md_double4 pi = pos[i];
+  const int S = slen[i];
+  for (int s = 0; s < S; s++) {
+    const uint32_t e = sl[(size_t)i * kSgMax + s];
+    const int j = entry_index(e);
+    const md_double4 pj = pos[j];
+    const double dx = pj.x + entry_img(e, 0) * box - pi.x;
+    const double dy = pj.y + entry_img(e, 1) * box - pi.y;
+    const double dz = pj.z + entry_img(e, 2) * box - pi.z;
+    d[s] = make_float3((float)dx, (float)dy, (float)dz);
+    r[s] = sqrtf(d[s].x * d[s].x + d[s].y * d[s].y + d[s].z * d[s].z);
+    idx[s] = j;
+  }
+  return S;
+}
+
+// descriptors of atom i; out: normalised (G - mean) * istd, or raw G
+__global__ void __launch_bounds__(128)
+    k_sg_desc(const md_double4* __restrict__ pos, int n, const uint32_t* __restrict__ sl,
+              const int* __restrict__ slen, double box, DescParams P,
+              const float* __restrict__ mean, const float* __restrict__ istd,
+              float* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float3 d[kSgMax];
+  float r[kSgMax];
+  int idx[kSgMax];
+  const int S = load_nbrs(i, pos, sl, slen, box, d, r, idx);
+  float G[kDesc];
+  for (int f = 0; f < kDesc; f++) G[f] = 0.f;
+  float fc[kSgMax];
+  for (int s = 0; s < S; s++) {
+    float dfc;
+    fcut(r[s], P.rc, fc[s], dfc);
+    for (int k = 0; k < kRad; k++) {
+      const float t = r[s] - P.rs[k];
+      G[k] += __expf(-P.eta_r * t * t) * fc[s];
+    }
+  }
+  for (int a = 0; a < S; a++)
+    for (int b = a + 1; b < S; b++) {
+      const float c = (d[a].x * d[b].x + d[a].y * d[b].y + d[a].z * d[b].z) / (r[a] * r[b]);
+      const float q = r[a] * r[a] + r[b] * r[b];
+      const float ff = fc[a] * fc[b];
+      for (int f = 0; f < kAng; f++) {
+        const float base = fmaxf(1.f + P.lam[f] * c, 0.f);
+        G[kRad + f] += P.pref[f] * ipow(base, P.zeta[f]) * __expf(-P.eta_a[f] * q) * ff;
+      }
+    }
+  for (int f = 0; f < kDesc; f++)
+    out[(size_t)i * kDesc + f] = mean ? (G[f] - mean[f]) * istd[f] : G[f];
+}
+
+// forces from g_if = dE_i/dG_if (atomics into F32, n x 3 floats, zeroed)
+__global__ void __launch_bounds__(128)
+    k_sg_force(const md_double4* __restrict__ pos, int n, const uint32_t* __restrict__ sl,
+               const int* __restrict__ slen, double box, DescParams P,
+               const float* __restrict__ gcoef, float* __restrict__ F32) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float3 d[kSgMax];
+  float r[kSgMax];
+  int idx[kSgMax];
+  const int S = load_nbrs(i, pos, sl, slen, box, d, r, idx);
+  float g[kDesc];
+  for (int f = 0; f < kDesc; f++) g[f] = gcoef[(size_t)i * kDesc + f];
+  float fc[kSgMax], dfc[kSgMax];
+  float fix = 0.f, fiy = 0.f, fiz = 0.f;
+  for (int s = 0; s < S; s++) {
+    fcut(r[s], P.rc, fc[s], dfc[s]);
+    float sum = 0.f;  // sum_k g_k dphi_k/dr
+    for (int k = 0; k < kRad; k++) {
+      const float t = r[s] - P.rs[k];
+      const float e = __expf(-P.eta_r * t * t);
+      sum += g[k] * e * (-2.f * P.eta_r * t * fc[s] + dfc[s]);
+    }
+    const float ir = 1.f / r[s];
+    const float gx = sum * d[s].x * ir, gy = sum * d[s].y * ir, gz = sum * d[s].z * ir;
+    // dG/dr_j = +grad, dG/dr_i = -grad; F = -dE/dr
+    atomicAdd(&F32[3 * idx[s]], -gx);
+    atomicAdd(&F32[3 * idx[s] + 1], -gy);
+    atomicAdd(&F32[3 * idx[s] + 2], -gz);
+    fix += gx;
+    fiy += gy;
+    fiz += gz;
+  }
+  for (int a = 0; a < S; a++) {
+    float ajx = 0.f, ajy = 0.f, ajz = 0.f;
+    for (int b = a + 1; b < S; b++) {
+      const float rab = r[a] * r[b];
+      const float c = (d[a].x * d[b].x + d[a].y * d[b].y + d[a].z * d[b].z) / rab;
+      const float q = r[a] * r[a] + r[b] * r[b];
+      float A = 0.f, Ba = 0.f, Bb = 0.f;
+      for (int f = 0; f < kAng; f++) {
+        const float base = 1.f + P.lam[f] * c;
+        if (base <= 0.f) continue;
+        const float pz1 = ipow(base, P.zeta[f] - 1);
+        const float pz = pz1 * base;
+        const float ex = __expf(-P.eta_a[f] * q);
+        const float gf = g[kRad + f] * P.pref[f];
+        // T = pz ex fc_a fc_b
+        A += gf * (float)P.zeta[f] * P.lam[f] * pz1 * ex * fc[a] * fc[b];
+        Ba += gf * pz * ex * fc[b] * (-2.f * P.eta_a[f] * r[a] * fc[a] + dfc[a]);
+        Bb += gf * pz * ex * fc[a] * (-2.f * P.eta_a[f] * r[b] * fc[b] + dfc[b]);
+      }
+      const float ia = 1.f / r[a], ib = 1.f / r[b];
+      // dc/dd_a = d_b / (ra rb) - c d_a / ra^2
+      const float gax = A * (d[b].x / rab - c * d[a].x * ia * ia) + Ba * d[a].x * ia;
+      const float gay = A * (d[b].y / rab - c * d[a].y * ia * ia) + Ba * d[a].y * ia;
+      const float gaz = A * (d[b].z / rab - c * d[a].z * ia * ia) + Ba * d[a].z * ia;
+      const float gbx = A * (d[a].x / rab - c * d[b].x * ib * ib) + Bb * d[b].x * ib;
+      const float gby = A * (d[a].y / rab - c * d[b].y * ib * ib) + Bb * d[b].y * ib;
+      const float gbz = A * (d[a].z / rab - c * d[b].z * ib * ib) + Bb * d[b].z * ib;
+      ajx += gax;
+      ajy += gay;
+      ajz += gaz;
+      atomicAdd(&F32[3 * idx[b]], -gbx);
+      atomicAdd(&F32[3 * idx[b] + 1], -gby);
+      atomicAdd(&F32[3 * idx[b] + 2], -gbz);
+      fix += gax + gbx;
+      fiy += gay + gby;
+      fiz += gaz + gbz;
+    }
+    atomicAdd(&F32[3 * idx[a]], -ajx);
+    atomicAdd(&F32[3 * idx[a] + 1], -ajy);
+    atomicAdd(&F32[3 * idx[a] + 2], -ajz);
+  }
+  atomicAdd(&F32[3 * i], fix);
+  atomicAdd(&F32[3 * i + 1], fiy);
+  atomicAdd(&F32[3 * i + 2], fiz);
+}
+
+__global__ void k_sg_store(const float* __restrict__ F32, double* __restrict__ f3, int n,
+                           int accumulate) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= 3 * n) return;
+  f3[k] = accumulate ? f3[k] + (double)F32[k] : (double)F32[k];
+}
+
+// ---- the network: 32 -> 64 (tanh) -> 64 (tanh) -> 1, BF16 weights ----
+// Device weight copies for the tensor cores, K-major B operands:
+// W1 [64 out][32 in], W1T [32 in][64 out], W2 [64 out][64 in], W2T [64 in][64 out].
+struct NetDev {
+  const __nv_bfloat16 *W1, *W1T, *W2, *W2T;
+  const float* P;  // FP32 master parameters (biases and w3 used from here)
+};
+
+// shared-memory plan of the network kernels (bytes)
+constexpr int kSmA = 0;                  // 128 x 64 BF16 operand (16 KB)
+constexpr int kSmB = kSmA + 16384;       // 128 x 64 BF16 operand (16 KB)
+constexpr int kSmW1 = kSmB + 16384;      // 64 x 32 (4 KB)
+constexpr int kSmW1T = kSmW1 + 4096;     // 32 x 64 (4 KB)
+constexpr int kSmW2 = kSmW1T + 4096;     // 64 x 64 (8 KB)
+constexpr int kSmW2T = kSmW2 + 8192;     // 64 x 64 (8 KB)
+constexpr int kSmAT = kSmW2T + 8192;     // training: 128 x 128 BF16 (32 KB)
+constexpr int kSmBT = kSmAT + 32768;     // training: 64 x 128 BF16 (16 KB)
+constexpr int kSmTrain = kSmBT + 16384;  // 104 KB
+constexpr int kSmALo = kSmAT;            // inference: low BF16 parts of A / B operands
+constexpr int kSmBLo = kSmALo + 16384;
+constexpr int kSmInfer = kSmBLo + 16384; // 88 KB
+
+__device__ __forceinline__ void put_bf16(unsigned char* base, int r, int k, int K, float v) {
+  *(__nv_bfloat16*)(base + tc_offset(r, k, K)) = __float2bfloat16_rn(v);
+}
+
+// weights (row-major BF16 R x K in global) into the K-major tile layout
+__device__ __forceinline__ void load_tile(unsigned char* dst, const __nv_bfloat16* src, int R,
+                                          int K) {
+  for (int e = threadIdx.x; e < R * K; e += blockDim.x)
+    *(__nv_bfloat16*)(dst + tc_offset(e / K, e % K, K)) = src[e];
+}
+
+// a value as the sum of two BF16 numbers (hi = round(v), lo = round(v - hi)):
+// products of hi and lo parts with BF16 weights keep the network input and
+// hidden activations to about 16 significant bits, so the energy is a smooth
+// function of the positions and the forces are its gradient
+__device__ __forceinline__ void put_split(unsigned char* hi, unsigned char* lo, int r, int k,
+                                          int K, float v) {
+  const __nv_bfloat16 h = __float2bfloat16_rn(v);
+  *(__nv_bfloat16*)(hi + tc_offset(r, k, K)) = h;
+  *(__nv_bfloat16*)(lo + tc_offset(r, k, K)) = __float2bfloat16_rn(v - __bfloat162float(h));
+}
+
+// operands written by threads -> visible to the tensor core; then one thread
+// issues the product (A + Alo when given) and all wait for its completion
+__device__ __forceinline__ bool tc_run(uint32_t d, const unsigned char* A, const unsigned char* B,
+                                       int N, int K, uint64_t* bar, uint32_t& phase,
+                                       int* status, const unsigned char* Alo = nullptr) {
+  fence_proxy_async();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (threadIdx.x == 0) {
+    if (Alo) {
+      tc_gemm_issue(d, A, B, N, K, nullptr);
+      tc_gemm_issue(d, Alo, B, N, K, bar, true);
+    } else {
+      tc_gemm_issue(d, A, B, N, K, bar);
+    }
+  }
+  const bool ok = mbar_wait(bar, phase, status);
+  phase ^= 1u;
+  tc_fence_after();
+  return __syncthreads_and(ok);
+}
+
+__device__ __forceinline__ float tanh_fast(float x) {
+  // tanh(x) = 1 - 2 / (exp(2x) + 1)
+  return 1.f - 2.f / (__expf(2.f * x) + 1.f);
+}
+
+// Inference on 128 atoms per CTA: t_i = net(x_i) and dt/dx_i (4 tensor-core
+// products: two forward, two for the input gradient; every A operand as a
+// pair of BF16 parts).
+__global__ void __launch_bounds__(128, 1)
+    k_net_infer(const float* __restrict__ X, int n, NetDev w, float* __restrict__ t_out,
+                float* __restrict__ dtdx, int* status) {
+  extern __shared__ __align__(1024) unsigned char sm[];
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ uint32_t s_taddr;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const int row = 32 * warp + (tid & 31);
+  const int i = blockIdx.x * 128 + row;
+  const bool live = i < n;
+  unsigned char* A = sm + kSmA;
+  unsigned char* B = sm + kSmB;
+  unsigned char* Al = sm + kSmALo;
+  unsigned char* Bl = sm + kSmBLo;
+  load_tile(sm + kSmW1, w.W1, kHid, kDesc);
+  load_tile(sm + kSmW1T, w.W1T, kDesc, kHid);
+  load_tile(sm + kSmW2, w.W2, kHid, kHid);
+  load_tile(sm + kSmW2T, w.W2T, kHid, kHid);
+  for (int f = 0; f < kDesc; f++)
+    put_split(A, Al, row, f, kDesc, live ? X[(size_t)i * kDesc + f] : 0.f);
+  if (warp == 0) tc_alloc(&s_taddr, 128);
+  if (tid == 0) {
+    mbar_init(&bar, 1);
+    fence_mbar_init();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tm = s_taddr + ((uint32_t)(32 * warp) << 16);
+  uint32_t phase = 0;
+  bool ok = tc_run(s_taddr, A, sm + kSmW1, kHid, kDesc, &bar, phase, status, Al);
+  float h1[kHid];
+  if (ok) {
+    for (int c0 = 0; c0 < kHid; c0 += 16) {
+      float v[16];
+      tc_ld16(tm + c0, v);
+#pragma unroll
+      for (int k = 0; k < 16; k++) {
+        h1[c0 + k] = tanh_fast(v[k] + w.P[oB1 + c0 + k]);
+        put_split(B, Bl, row, c0 + k, kHid, h1[c0 + k]);
+      }
+    }
+    ok = tc_run(s_taddr + 64, B, sm + kSmW2, kHid, kHid, &bar, phase, status, Bl);
+  }
+  if (ok) {
+    float t = w.P[oB3];
+    for (int c0 = 0; c0 < kHid; c0 += 16) {
+      float v[16];
+      tc_ld16(tm + 64 + c0, v);
+#pragma unroll
+      for (int k = 0; k < 16; k++) {
+        const float h2 = tanh_fast(v[k] + w.P[oB2 + c0 + k]);
+        const float w3 = w.P[oW3 + c0 + k];
+        t = fmaf(w3, h2, t);
+        put_split(A, Al, row, c0 + k, kHid, w3 * (1.f - h2 * h2));  // delta2
+      }
+    }
+    if (live) t_out[i] = t;
+    ok = tc_run(s_taddr, A, sm + kSmW2T, kHid, kHid, &bar, phase, status, Al);
+  }
+  if (ok) {
+    for (int c0 = 0; c0 < kHid; c0 += 16) {
+      float v[16];
+      tc_ld16(tm + c0, v);
+#pragma unroll
+      for (int k = 0; k < 16; k++)
+        put_split(B, Bl, row, c0 + k, kHid, v[k] * (1.f - h1[c0 + k] * h1[c0 + k]));  // delta1
+    }
+    ok = tc_run(s_taddr + 64, B, sm + kSmW1T, kDesc, kHid, &bar, phase, status, Bl);
+  }
+  if (ok) {  // every lane reads (tcgen05.ld is warp-collective); live rows store
+    for (int c0 = 0; c0 < kDesc; c0 += 16) {
+      float v[16];
+      tc_ld16(tm + 64 + c0, v);
+      if (live) {
+#pragma unroll
+        for (int k = 0; k < 16; k++) dtdx[(size_t)i * kDesc + c0 + k] = v[k];
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) tc_dealloc(s_taddr, 128);
+}
+
+// 64-bit mix of (seed, k) for batch sampling
+__device__ __forceinline__ unsigned long long mix2(unsigned long long a, unsigned long long b) {
+  unsigned long long z = a * 0x9E3779B97F4A7C15ULL + b + 0x632BE59BD9B4E019ULL;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+  return z ^ (z >> 31);
+}
+
+__device__ __forceinline__ float col_sum(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// One training pass over 128 samples per CTA: forward, squared loss on the
+// normalised per-atom energy, backward; gradients are accumulated into grad
+// (FP32, same layout as the parameters) and loss into loss[0].
+// Samples: rows sel(k) of X/T, sel = explicit list, or hashed from seed.
+__global__ void __launch_bounds__(128, 1)
+    k_net_train(const float* __restrict__ X, const float* __restrict__ T, int nsamples,
+                const int* __restrict__ rows, int nrows, unsigned long long seed, NetDev w,
+                float inv_batch, float* __restrict__ grad, double* __restrict__ loss,
+                int* status) {
+  extern __shared__ __align__(1024) unsigned char sm[];
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ uint32_t s_taddr;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int row = 32 * warp + lane;
+  const int k = blockIdx.x * 128 + row;
+  const bool live = k < nrows;
+  int src = 0;
+  if (live) src = rows ? rows[k] : (int)(mix2(seed, (unsigned long long)k) % (unsigned long long)nsamples);
+  unsigned char* A = sm + kSmA;
+  unsigned char* B = sm + kSmB;
+  unsigned char* AT = sm + kSmAT;
+  unsigned char* BT = sm + kSmBT;
+  load_tile(sm + kSmW1, w.W1, kHid, kDesc);
+  load_tile(sm + kSmW2, w.W2, kHid, kHid);
+  load_tile(sm + kSmW2T, w.W2T, kHid, kHid);
+  for (int e = tid; e < 32768 / 16; e += blockDim.x) ((uint4*)AT)[e] = make_uint4(0, 0, 0, 0);
+  float x[kDesc];
+  for (int f = 0; f < kDesc; f++) {
+    x[f] = live ? X[(size_t)src * kDesc + f] : 0.f;
+    put_bf16(A, row, f, kDesc, x[f]);
+  }
+  if (warp == 0) tc_alloc(&s_taddr, 256);
+  if (tid == 0) {
+    mbar_init(&bar, 1);
+    fence_mbar_init();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tm = s_taddr + ((uint32_t)(32 * warp) << 16);
+  uint32_t phase = 0;
+  float h1[kHid];
+  bool ok = tc_run(s_taddr, A, sm + kSmW1, kHid, kDesc, &bar, phase, status);
+  if (ok) {
+    for (int c0 = 0; c0 < kHid; c0 += 16) {
+      float v[16];
+      tc_ld16(tm + c0, v);
+#pragma unroll
+      for (int q = 0; q < 16; q++) {
+        const int c = c0 + q;
+        h1[c] = tanh_fast(v[q] + w.P[oB1 + c]);
+        put_bf16(B, row, c, kHid, h1[c]);
+        put_bf16(BT, c, row, 128, h1[c]);  // H1^T: B operand of the W2 gradient
+      }
+    }
+    ok = tc_run(s_taddr + 64, B, sm + kSmW2, kHid, kHid, &bar, phase, status);
+  }
+  float d3 = 0.f;
+  if (ok) {
+    float h2[kHid];
+    float t = w.P[oB3];
+    for (int c0 = 0; c0 < kHid; c0 += 16) {
+      float v[16];
+      tc_ld16(tm + 64 + c0, v);
+#pragma unroll
+      for (int q = 0; q < 16; q++) {
+        h2[c0 + q] = tanh_fast(v[q] + w.P[oB2 + c0 + q]);
+        t = fmaf(w.P[oW3 + c0 + q], h2[c0 + q], t);
+      }
+    }
+    const float res = live ? t - T[src] : 0.f;
+    d3 = 2.f * res * inv_batch;
+    const double l = (double)res * res * inv_batch;
+    const double lw = (double)col_sum((float)l);
+    if (lane == 0) atomicAdd(loss, lw);
+    const float gb3 = col_sum(d3);
+    if (lane == 0) atomicAdd(&grad[oB3], gb3);
+    for (int c = 0; c < kHid; c++) {
+      const float gw3 = col_sum(d3 * h2[c]);
+      const float d2 = d3 * w.P[oW3 + c] * (1.f - h2[c] * h2[c]);
+      const float gb2 = col_sum(d2);
+      if (lane == 0) {
+        atomicAdd(&grad[oW3 + c], gw3);
+        atomicAdd(&grad[oB2 + c], gb2);
+      }
+      put_bf16(A, row, c, kHid, d2);   // delta2 for dH1 = delta2 W2
+      put_bf16(AT, c, row, 128, d2);   // delta2^T for the W2 gradient
+    }
+    // W2 gradient (rows out, cols in) and dH1, one commit for both
+    fence_proxy_async();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (tid == 0) {
+      const uint32_t a0 = smem_addr(AT), b0 = smem_addr(BT);
+      const uint32_t idesc = tc_idesc_bf16(128, kHid);
+      for (int j = 0; j < 128 / 16; j++)
+        tc_mma(s_taddr + 128, tc_desc(a0 + j * 256u, 128u, 128u * 16u),
+               tc_desc(b0 + j * 256u, 128u, 128u * 16u), idesc, j > 0);
+      const uint32_t a1 = smem_addr(A), b1 = smem_addr(sm + kSmW2T);
+      for (int j = 0; j < kHid / 16; j++)
+        tc_mma(s_taddr, tc_desc(a1 + j * 256u, 128u, kHid * 16u),
+               tc_desc(b1 + j * 256u, 128u, kHid * 16u), idesc, j > 0);
+      tc_commit(&bar);
+    }
+    const bool got = mbar_wait(&bar, phase, status);
+    phase ^= 1u;
+    tc_fence_after();
+    ok = __syncthreads_and(got);
+  }
+  if (ok) {
+    if (warp < 2) {  // rows 0..63 of the W2 gradient
+      for (int c0 = 0; c0 < kHid; c0 += 16) {
+        float v[16];
+        tc_ld16(tm + 128 + c0, v);
+#pragma unroll
+        for (int q = 0; q < 16; q++) atomicAdd(&grad[oW2 + row * kHid + c0 + q], v[q]);
+      }
+    }
+    for (int c0 = 0; c0 < kHid; c0 += 16) {
+      float v[16];
+      tc_ld16(tm + c0, v);
+#pragma unroll
+      for (int q = 0; q < 16; q++) {
+        const int c = c0 + q;
+        const float d1 = v[q] * (1.f - h1[c] * h1[c]);
+        const float gb1 = col_sum(d1);
+        if (lane == 0) atomicAdd(&grad[oB1 + c], gb1);
+        put_bf16(AT, c, row, 128, d1);  // delta1^T
+      }
+    }
+    for (int f = 0; f < kDesc; f++) put_bf16(BT, f, row, 128, x[f]);  // X^T
+    ok = tc_run(s_taddr + 192, AT, BT, kDesc, 128, &bar, phase, status);
+  }
+  if (ok && warp < 2) {  // rows 0..63 of the W1 gradient
+    for (int c0 = 0; c0 < kDesc; c0 += 16) {
+      float v[16];
+      tc_ld16(tm + 192 + c0, v);
+#pragma unroll
+      for (int q = 0; q < 16; q++) atomicAdd(&grad[oW1 + row * kDesc + c0 + q], v[q]);
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) tc_dealloc(s_taddr, 256);
+}
+
+// q_if = sum_j (e_j - e_i) . dG_if/dd_j for the force residual e (n x 3),
+// written as v_if = scale * istd_f * q_if (the loss' sensitivity to dt/dx)
+__global__ void __launch_bounds__(128)
+    k_sg_ctrans(const md_double4* __restrict__ pos, int n, const uint32_t* __restrict__ sl,
+                const int* __restrict__ slen, double box, DescParams P,
+                const float* __restrict__ e3, float scale, const float* __restrict__ istd,
+                float* __restrict__ V) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float3 d[kSgMax];
+  float r[kSgMax];
+  int idx[kSgMax];
+  const int S = load_nbrs(i, pos, sl, slen, box, d, r, idx);
+  float q[kDesc];
+  for (int f = 0; f < kDesc; f++) q[f] = 0.f;
+  const float eix = e3[3 * i], eiy = e3[3 * i + 1], eiz = e3[3 * i + 2];
+  float fc[kSgMax], dfc[kSgMax];
+  float3 de[kSgMax];
+  for (int s = 0; s < S; s++) {
+    fcut(r[s], P.rc, fc[s], dfc[s]);
+    de[s] = make_float3(e3[3 * idx[s]] - eix, e3[3 * idx[s] + 1] - eiy, e3[3 * idx[s] + 2] - eiz);
+    const float ir = 1.f / r[s];
+    const float ud = (d[s].x * de[s].x + d[s].y * de[s].y + d[s].z * de[s].z) * ir;  // u . de
+    for (int k = 0; k < kRad; k++) {
+      const float t = r[s] - P.rs[k];
+      const float ex = __expf(-P.eta_r * t * t);
+      q[k] += ex * (-2.f * P.eta_r * t * fc[s] + dfc[s]) * ud;
+    }
+  }
+  for (int a = 0; a < S; a++)
+    for (int b = a + 1; b < S; b++) {
+      const float rab = r[a] * r[b];
+      const float c = (d[a].x * d[b].x + d[a].y * d[b].y + d[a].z * d[b].z) / rab;
+      const float q2 = r[a] * r[a] + r[b] * r[b];
+      const float ia = 1.f / r[a], ib = 1.f / r[b];
+      // (dc/dd_a) . de_a + (dc/dd_b) . de_b, and the radial projections
+      const float dca = (d[b].x * de[a].x + d[b].y * de[a].y + d[b].z * de[a].z) / rab -
+                        c * (d[a].x * de[a].x + d[a].y * de[a].y + d[a].z * de[a].z) * ia * ia;
+      const float dcb = (d[a].x * de[b].x + d[a].y * de[b].y + d[a].z * de[b].z) / rab -
+                        c * (d[b].x * de[b].x + d[b].y * de[b].y + d[b].z * de[b].z) * ib * ib;
+      const float ua = (d[a].x * de[a].x + d[a].y * de[a].y + d[a].z * de[a].z) * ia;
+      const float ub = (d[b].x * de[b].x + d[b].y * de[b].y + d[b].z * de[b].z) * ib;
+      for (int f = 0; f < kAng; f++) {
+        const float base = 1.f + P.lam[f] * c;
+        if (base <= 0.f) continue;
+        const float pz1 = ipow(base, P.zeta[f] - 1);
+        const float pz = pz1 * base;
+        const float ex = __expf(-P.eta_a[f] * q2);
+        const float A = P.pref[f] * (float)P.zeta[f] * P.lam[f] * pz1 * ex * fc[a] * fc[b];
+        const float Ba = P.pref[f] * pz * ex * fc[b] * (-2.f * P.eta_a[f] * r[a] * fc[a] + dfc[a]);
+        const float Bb = P.pref[f] * pz * ex * fc[a] * (-2.f * P.eta_a[f] * r[b] * fc[b] + dfc[b]);
+        q[kRad + f] += A * (dca + dcb) + Ba * ua + Bb * ub;
+      }
+    }
+  for (int f = 0; f < kDesc; f++) V[(size_t)i * kDesc + f] = scale * istd[f] * q[f];
+}
+
+// e = F_pred - F_exact (FP32) and sum e^2 into acc[0]
+__global__ void k_fm_resid(const float* __restrict__ F32, const double* __restrict__ fx, int n3,
+                           float* __restrict__ e3, double* __restrict__ acc) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  double s = 0.0;
+  if (k < n3) {
+    const float e = F32[k] - (float)fx[k];
+    e3[k] = e;
+    s = (double)e * e;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) atomicAdd(acc, s);
+}
+
+// shared-memory plan of the force-term training kernel (bytes)
+constexpr int kFA = 0, kFA2 = 16384, kFB = 32768, kFB2 = 49152;
+constexpr int kFW1 = 65536, kFW2 = kFW1 + 4096, kFW2T = kFW2 + 8192;
+constexpr int kFAT = kFW2T + 8192, kFAT2 = kFAT + 32768;
+constexpr int kFBT = kFAT2 + 32768, kFBT2 = kFBT + 16384;
+constexpr int kSmForce = kFBT2 + 16384;  // 180 KB
+
+// Parameter gradient of sum_i v_i . dt/dx(x_i) (the force-matching term),
+// accumulated into grad: the network's tangent along v (forward) and the
+// adjoint of that tangent, eight tensor-core products per 128 rows.
+__global__ void __launch_bounds__(128, 1)
+    k_net_train_force(const float* __restrict__ X, const float* __restrict__ V, int n, NetDev w,
+                      float* __restrict__ grad, int* status) {
+  extern __shared__ __align__(1024) unsigned char sm[];
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ uint32_t s_taddr;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int row = 32 * warp + lane;
+  const int i = blockIdx.x * 128 + row;
+  const bool live = i < n;
+  unsigned char *A = sm + kFA, *A2 = sm + kFA2, *B = sm + kFB, *B2 = sm + kFB2;
+  unsigned char *AT = sm + kFAT, *AT2 = sm + kFAT2, *BT = sm + kFBT, *BT2 = sm + kFBT2;
+  load_tile(sm + kFW1, w.W1, kHid, kDesc);
+  load_tile(sm + kFW2, w.W2, kHid, kHid);
+  load_tile(sm + kFW2T, w.W2T, kHid, kHid);
+  for (int e = tid; e < 2 * 32768 / 16; e += blockDim.x) ((uint4*)AT)[e] = make_uint4(0, 0, 0, 0);
+  for (int f = 0; f < kDesc; f++) {
+    put_bf16(A, row, f, kDesc, live ? X[(size_t)i * kDesc + f] : 0.f);
+    put_bf16(A2, row, f, kDesc, live ? V[(size_t)i * kDesc + f] : 0.f);
+  }
+  if (warp == 0) tc_alloc(&s_taddr, 512);
+  if (tid == 0) {
+    mbar_init(&bar, 1);
+    fence_mbar_init();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t T0 = s_taddr;
+  const uint32_t tm = s_taddr + ((uint32_t)(32 * warp) << 16);
+  uint32_t phase = 0;
+  auto sync_issue = [&](auto&& issue) {
+    fence_proxy_async();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (tid == 0) {
+      issue();
+      tc_commit(&bar);
+    }
+    const bool got = mbar_wait(&bar, phase, status);
+    phase ^= 1u;
+    tc_fence_after();
+    return __syncthreads_and(got);
+  };
+  // z1 = x W1^T and its tangent zd1 = v W1^T
+  bool ok = sync_issue([&] {
+    tc_gemm_issue(T0, A, sm + kFW1, kHid, kDesc, nullptr);
+    tc_gemm_issue(T0 + 64, A2, sm + kFW1, kHid, kDesc, nullptr);
+  });
+  float h1[kHid], zd1[kHid];
+  if (ok) {
+    for (int c0 = 0; c0 < kHid; c0 += 16) {
+      float z[16], zd[16];
+      tc_ld16(tm + c0, z);
+      tc_ld16(tm + 64 + c0, zd);
+#pragma unroll
+      for (int q = 0; q < 16; q++) {
+        const int c = c0 + q;
+        h1[c] = tanh_fast(z[q] + w.P[oB1 + c]);
+        zd1[c] = zd[q];
+        const float hd = (1.f - h1[c] * h1[c]) * zd[q];
+        put_bf16(B, row, c, kHid, h1[c]);
+        put_bf16(B2, row, c, kHid, hd);
+        put_bf16(BT, c, row, 128, h1[c]);
+        put_bf16(BT2, c, row, 128, hd);
+      }
+    }
+    ok = sync_issue([&] {
+      tc_gemm_issue(T0 + 128, B, sm + kFW2, kHid, kHid, nullptr);
+      tc_gemm_issue(T0 + 192, B2, sm + kFW2, kHid, kHid, nullptr);
+    });
+  }
+  if (ok) {
+    for (int c0 = 0; c0 < kHid; c0 += 16) {
+      float z[16], zd[16];
+      tc_ld16(tm + 128 + c0, z);
+      tc_ld16(tm + 192 + c0, zd);
+#pragma unroll
+      for (int q = 0; q < 16; q++) {
+        const int c = c0 + q;
+        const float h2 = tanh_fast(z[q] + w.P[oB2 + c]);
+        const float s2 = 1.f - h2 * h2;
+        const float w3 = w.P[oW3 + c];
+        const float hd2 = s2 * zd[q];
+        const float a_zd2 = live ? w3 * s2 : 0.f;
+        const float a_z2 = w3 * (-2.f * h2 * zd[q]) * s2;
+        const float gw3 = col_sum(hd2), gb2 = col_sum(a_z2);
+        if (lane == 0) {
+          atomicAdd(&grad[oW3 + c], gw3);
+          atomicAdd(&grad[oB2 + c], gb2);
+        }
+        put_bf16(A, row, c, kHid, a_z2);
+        put_bf16(A2, row, c, kHid, a_zd2);
+        put_bf16(AT, c, row, 128, a_z2);
+        put_bf16(AT2, c, row, 128, a_zd2);
+      }
+    }
+    // W2 gradient a_z2^T h1 + a_zd2^T hd1; a_h1 = a_z2 W2; a_hd1 = a_zd2 W2
+    ok = sync_issue([&] {
+      tc_gemm_issue(T0 + 256, AT, BT, kHid, 128, nullptr);
+      tc_gemm_issue(T0 + 256, AT2, BT2, kHid, 128, nullptr, true);
+      tc_gemm_issue(T0, A, sm + kFW2T, kHid, kHid, nullptr);
+      tc_gemm_issue(T0 + 64, A2, sm + kFW2T, kHid, kHid, nullptr);
+    });
+  }
+  if (ok) {
+    if (warp < 2) {
+      for (int c0 = 0; c0 < kHid; c0 += 16) {
+        float g[16];
+        tc_ld16(tm + 256 + c0, g);
+#pragma unroll
+        for (int q = 0; q < 16; q++) atomicAdd(&grad[oW2 + row * kHid + c0 + q], g[q]);
+      }
+    }
+    for (int c0 = 0; c0 < kHid; c0 += 16) {
+      float ah[16], ahd[16];
+      tc_ld16(tm + c0, ah);
+      tc_ld16(tm + 64 + c0, ahd);
+#pragma unroll
+      for (int q = 0; q < 16; q++) {
+        const int c = c0 + q;
+        const float s1 = 1.f - h1[c] * h1[c];
+        const float a_zd1 = ahd[q] * s1;
+        const float a_z1 = (ah[q] + ahd[q] * (-2.f * h1[c] * zd1[c])) * s1;
+        const float gb1 = col_sum(a_z1);
+        if (lane == 0) atomicAdd(&grad[oB1 + c], gb1);
+        put_bf16(AT, c, row, 128, a_z1);
+        put_bf16(AT2, c, row, 128, a_zd1);
+      }
+    }
+    for (int f = 0; f < kDesc; f++) {
+      put_bf16(BT, f, row, 128, live ? X[(size_t)i * kDesc + f] : 0.f);
+      put_bf16(BT2, f, row, 128, live ? V[(size_t)i * kDesc + f] : 0.f);
+    }
+    // W1 gradient a_z1^T x + a_zd1^T v
+    ok = sync_issue([&] {
+      tc_gemm_issue(T0 + 320, AT, BT, kDesc, 128, nullptr);
+      tc_gemm_issue(T0 + 320, AT2, BT2, kDesc, 128, nullptr, true);
+    });
+  }
+  if (ok && warp < 2) {
+    for (int c0 = 0; c0 < kDesc; c0 += 16) {
+      float g[16];
+      tc_ld16(tm + 320 + c0, g);
+#pragma unroll
+      for (int q = 0; q < 16; q++) atomicAdd(&grad[oW1 + row * kDesc + c0 + q], g[q]);
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) tc_dealloc(s_taddr, 512);
+}
+
+// Adam (Kingma & Ba): m = b1 m + (1-b1) g; v = b2 v + (1-b2) g^2;
+// p -= lr mhat / (sqrt(vhat) + eps); then the BF16 operand copies
+__global__ void k_adam(float* __restrict__ P, float* __restrict__ M, float* __restrict__ V,
+                       const float* __restrict__ G, int step, float lr, float b1, float b2,
+                       float eps) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= kParams) return;
+  const float g = G[k];
+  const float m = b1 * M[k] + (1.f - b1) * g;
+  const float v = b2 * V[k] + (1.f - b2) * g * g;
+  M[k] = m;
+  V[k] = v;
+  const float mh = m / (1.f - powf(b1, (float)step));
+  const float vh = v / (1.f - powf(b2, (float)step));
+  P[k] -= lr * mh / (sqrtf(vh) + eps);
+}
+
+__global__ void k_net_cast(const float* __restrict__ P, __nv_bfloat16* W1, __nv_bfloat16* W1T,
+                           __nv_bfloat16* W2, __nv_bfloat16* W2T) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < kHid * kDesc) {
+    const int o = k / kDesc, in = k % kDesc;
+    const __nv_bfloat16 b = __float2bfloat16_rn(P[oW1 + k]);
+    W1[k] = b;
+    W1T[in * kHid + o] = b;
+  }
+  if (k < kHid * kHid) {
+    const int o = k / kHid, in = k % kHid;
+    const __nv_bfloat16 b = __float2bfloat16_rn(P[oW2 + k]);
+    W2[k] = b;
+    W2T[in * kHid + o] = b;
+  }
+}
+
+// energy E_i = mu + sigma t_i; gcoef = sigma * dt/dx * istd; block sums of E
+__global__ void k_sg_scale(const float* __restrict__ t, const float* __restrict__ dtdx, int n,
+                           double mu, double sigma, const float* __restrict__ istd,
+                           float* __restrict__ gcoef, double* __restrict__ eatom) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  if (eatom) eatom[i] = mu + sigma * (double)t[i];
+  for (int f = 0; f < kDesc; f++)
+    gcoef[(size_t)i * kDesc + f] = (float)sigma * dtdx[(size_t)i * kDesc + f] * istd[f];
+}
+
+__global__ void k_sum_d(const double* __restrict__ v, int n, double* __restrict__ out) {
+  __shared__ double sm[256];
+  double s = 0.0;
+  for (int k = threadIdx.x; k < n; k += blockDim.x) s += v[k];
+  sm[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) sm[threadIdx.x] += sm[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[0] = sm[0];
+}
+
+// sum |a - b|^2 and |b|^2 over 3n values (relative RMS of a against b)
+__global__ void k_err2(const double* __restrict__ a, const double* __restrict__ b, int n3,
+                       double* __restrict__ out) {
+  __shared__ double s1[256], s2[256];
+  double x = 0.0, y = 0.0;
+  for (int k = threadIdx.x; k < n3; k += blockDim.x) {
+    const double d = a[k] - b[k];
+    x += d * d;
+    y += b[k] * b[k];
+  }
+  s1[threadIdx.x] = x;
+  s2[threadIdx.x] = y;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) {
+      s1[threadIdx.x] += s1[threadIdx.x + w];
+      s2[threadIdx.x] += s2[threadIdx.x + w];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    out[0] = s1[0];
+    out[1] = s2[0];
+  }
+}
+
+// ------------------------------------------------------------ host side
+
+template <typename T>
+cudaError_t sur_grow(T*& p, long long& have, long long need) {
+  if (need <= have && p) return cudaSuccess;
+  if (p) cudaFree(p);
+  p = nullptr;
+  cudaError_t e = cudaMalloc(&p, sizeof(T) * (size_t)(need > 0 ? need : 1));
+  have = e == cudaSuccess ? need : 0;
+  return e;
+}
+
+NetDev net_of(const Surrogate& s) {
+  NetDev w;
+  w.W1 = s.W1;
+  w.W1T = s.W1T;
+  w.W2 = s.W2;
+  w.W2T = s.W2T;
+  w.P = s.P_d;
+  return w;
+}
+
+__global__ void k_normalise(const float* __restrict__ G, const double* __restrict__ E, int n,
+                            const float* __restrict__ mean, const float* __restrict__ istd,
+                            double mu, double sigma, float* __restrict__ X,
+                            float* __restrict__ T) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  for (int f = 0; f < kDesc; f++)
+    X[(size_t)k * kDesc + f] = (G[(size_t)k * kDesc + f] - mean[f]) * istd[f];
+  T[k] = (float)((E[k] - mu) / sigma);
+}
+
+__global__ void k_collect(const float* __restrict__ Graw, const double* __restrict__ eatom,
+                          int n, int stride, int offset, float* __restrict__ SG,
+                          double* __restrict__ SE, int base) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = offset + q * stride;
+  if (i >= n) return;
+  for (int f = 0; f < kDesc; f++) SG[(size_t)(base + q) * kDesc + f] = Graw[(size_t)i * kDesc + f];
+  SE[base + q] = eatom[i];
+}
+
+inline int sblocks(long long n, int t) { return (int)((n + t - 1) / t); }
+
+bool attrs_set = false;
+void set_attrs() {
+  if (attrs_set) return;
+  cudaFuncSetAttribute(k_net_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmInfer);
+  cudaFuncSetAttribute(k_net_train, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmTrain);
+  cudaFuncSetAttribute(k_net_train_force, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmForce);
+  attrs_set = true;
+}
+
 }  // namespace
 
+int sur_init(Surrogate& s, unsigned long long seed, cudaStream_t st) {
+  cudaError_t e;
+  s.P = default_desc(s.rc);
+  long long h = 0;
+  for (float** p : {&s.P_d, &s.M_d, &s.V_d, &s.G_d}) {
+    h = 0;
+    if ((e = sur_grow(*p, h, kParams)) != cudaSuccess) return e;
+  }
+  for (__nv_bfloat16** p : {&s.W1, &s.W1T, &s.W2, &s.W2T}) {
+    h = 0;
+    if ((e = sur_grow(*p, h, kHid * kHid)) != cudaSuccess) return e;
+  }
+  for (float** p : {&s.mean_d, &s.istd_d}) {
+    h = 0;
+    if ((e = sur_grow(*p, h, kDesc)) != cudaSuccess) return e;
+  }
+  h = 0;
+  if ((e = sur_grow(s.loss_d, h, 4)) != cudaSuccess) return e;
+  h = 0;
+  if ((e = sur_grow(s.scratch, h, 8)) != cudaSuccess) return e;
+  h = 0;
+  if ((e = sur_grow(s.status_d, h, 1)) != cudaSuccess) return e;
+  cudaMemsetAsync(s.status_d, 0, sizeof(int), st);
+  s.seed = seed;
+  // Xavier-uniform weights from a 64-bit LCG, zero biases
+  std::vector<float> P(kParams, 0.f);
+  unsigned long long x = seed * 6364136223846793005ULL + 1442695040888963407ULL;
+  auto uni = [&]() {
+    x = x * 6364136223846793005ULL + 1442695040888963407ULL;
+    return (float)((x >> 11) * (1.0 / 9007199254740992.0)) * 2.f - 1.f;
+  };
+  const float a1 = sqrtf(6.f / (kDesc + kHid)), a2 = sqrtf(6.f / (kHid + kHid)),
+              a3 = sqrtf(6.f / (kHid + 1));
+  for (int k = 0; k < kHid * kDesc; k++) P[oW1 + k] = a1 * uni();
+  for (int k = 0; k < kHid * kHid; k++) P[oW2 + k] = a2 * uni();
+  for (int k = 0; k < kHid; k++) P[oW3 + k] = a3 * uni();
+  return sur_set_params(s, P.data(), st);
+}
+
+int sur_set_params(Surrogate& s, const float* P, cudaStream_t st) {
+  cudaError_t e;
+  if ((e = cudaMemcpyAsync(s.P_d, P, sizeof(float) * kParams, cudaMemcpyHostToDevice, st)) !=
+      cudaSuccess)
+    return e;
+  cudaMemsetAsync(s.M_d, 0, sizeof(float) * kParams, st);
+  cudaMemsetAsync(s.V_d, 0, sizeof(float) * kParams, st);
+  s.adam_step = 0;
+  k_net_cast<<<sblocks(kHid * kHid, 256), 256, 0, st>>>(s.P_d, s.W1, s.W1T, s.W2, s.W2T);
+  return cudaStreamSynchronize(st);
+}
+
+int sur_get_params(const Surrogate& s, float* P, cudaStream_t st) {
+  cudaError_t e = cudaMemcpyAsync(P, s.P_d, sizeof(float) * kParams, cudaMemcpyDeviceToHost, st);
+  if (e != cudaSuccess) return e;
+  return cudaStreamSynchronize(st);
+}
+
+int sur_param_count() { return kParams; }
+
+// neighbours, then descriptors (normalised when `normalised`) for atoms [0, n)
+int sur_descriptors(Surrogate& s, const md_double4* pos, int n, const RowWalker& w,
+                    bool normalised, int* d_status, cudaStream_t st) {
+  cudaError_t e;
+  if ((e = sur_grow(s.sl, s.n_sl, (long long)n * kSgMax)) != cudaSuccess) return e;
+  long long h = s.n_alloc;
+  if (n > s.n_alloc) {
+    for (float** p : {&s.X, &s.dtdx, &s.gcoef}) {
+      h = 0;
+      if ((e = sur_grow(*p, h, (long long)n * kDesc)) != cudaSuccess) return e;
+    }
+    h = 0;
+    if ((e = sur_grow(s.t, h, n)) != cudaSuccess) return e;
+    h = 0;
+    if ((e = sur_grow(s.F32, h, 3LL * n)) != cudaSuccess) return e;
+    h = 0;
+    if ((e = sur_grow(s.eatom, h, n)) != cudaSuccess) return e;
+    h = 0;
+    if ((e = sur_grow(s.slen, h, n)) != cudaSuccess) return e;
+    s.n_alloc = n;
+  }
+  if (n == 0) return 0;
+  k_sg_short<<<sblocks(n, 128), 128, 0, st>>>(pos, w, s.rc, s.sl, s.slen, d_status);
+  k_sg_desc<<<sblocks(n, 128), 128, 0, st>>>(pos, n, s.sl, s.slen, w.g.box, s.P,
+                                             normalised ? s.mean_d : nullptr,
+                                             normalised ? s.istd_d : nullptr, s.X);
+  return (int)cudaGetLastError();
+}
+
+int sur_collect(Surrogate& s, int n, const double* eatom, int stride, int offset,
+                cudaStream_t st, int* added) {
+  cudaError_t e;
+  const int cnt = offset < n ? (n - offset + stride - 1) / stride : 0;
+  if (s.ns + cnt > s.ns_cap) {
+    const long long cap = std::max<long long>(2LL * (s.ns + cnt), 4096);
+    float* nG = nullptr;
+    double* nE = nullptr;
+    if ((e = cudaMalloc(&nG, sizeof(float) * kDesc * cap)) != cudaSuccess) return e;
+    if ((e = cudaMalloc(&nE, sizeof(double) * cap)) != cudaSuccess) {
+      cudaFree(nG);
+      return e;
+    }
+    if (s.ns > 0) {
+      cudaMemcpyAsync(nG, s.SG, sizeof(float) * kDesc * s.ns, cudaMemcpyDeviceToDevice, st);
+      cudaMemcpyAsync(nE, s.SE, sizeof(double) * s.ns, cudaMemcpyDeviceToDevice, st);
+    }
+    if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
+    if (s.SG) cudaFree(s.SG);
+    if (s.SE) cudaFree(s.SE);
+    s.SG = nG;
+    s.SE = nE;
+    s.ns_cap = (int)cap;
+  }
+  if (cnt > 0)
+    k_collect<<<sblocks(cnt, 256), 256, 0, st>>>(s.X, eatom, n, stride, offset, s.SG, s.SE, s.ns);
+  s.ns += cnt;
+  if (added) *added = cnt;
+  return (int)cudaGetLastError();
+}
+
+// fixes the input/target normalisation from the samples (first training)
+namespace {
+int sur_normalise(Surrogate& s, cudaStream_t st) {
+  std::vector<float> G((size_t)s.ns * kDesc);
+  std::vector<double> E(s.ns);
+  cudaError_t e;
+  if ((e = cudaMemcpyAsync(G.data(), s.SG, sizeof(float) * G.size(), cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+      (e = cudaMemcpyAsync(E.data(), s.SE, sizeof(double) * E.size(), cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+      (e = cudaStreamSynchronize(st)) != cudaSuccess)
+    return e;
+  float mean[kDesc], istd[kDesc];
+  for (int f = 0; f < kDesc; f++) {
+    double m = 0, v = 0;
+    for (int k = 0; k < s.ns; k++) m += G[(size_t)k * kDesc + f];
+    m /= s.ns;
+    for (int k = 0; k < s.ns; k++) {
+      const double d = G[(size_t)k * kDesc + f] - m;
+      v += d * d;
+    }
+    v /= s.ns;
+    mean[f] = (float)m;
+    istd[f] = (float)(1.0 / sqrt(v + 1e-12));
+  }
+  double mu = 0, var = 0;
+  for (double x : E) mu += x;
+  mu /= s.ns;
+  for (double x : E) var += (x - mu) * (x - mu);
+  var /= s.ns;
+  s.mu = mu;
+  s.sigma = sqrt(var) > 0 ? sqrt(var) : 1.0;
+  cudaMemcpyAsync(s.mean_d, mean, sizeof(mean), cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(s.istd_d, istd, sizeof(istd), cudaMemcpyHostToDevice, st);
+  s.normalised = true;
+  return cudaStreamSynchronize(st);
+}
+}  // namespace
+
+int sur_train(Surrogate& s, int steps, int batch, float lr, double* loss_out, cudaStream_t st) {
+  if (s.ns < 1) return -1;
+  cudaError_t e;
+  set_attrs();
+  if (!s.normalised) {
+    int r = sur_normalise(s, st);
+    if (r) return r;
+  }
+  long long h = s.nsx;
+  if ((e = sur_grow(s.SX, h, (long long)s.ns * kDesc)) != cudaSuccess) return e;
+  h = s.nsx;
+  if ((e = sur_grow(s.ST, h, s.ns)) != cudaSuccess) return e;
+  s.nsx = s.ns;
+  k_normalise<<<sblocks(s.ns, 256), 256, 0, st>>>(s.SG, s.SE, s.ns, s.mean_d, s.istd_d, s.mu,
+                                                  s.sigma, s.SX, s.ST);
+  const int tiles = (batch + 127) / 128;
+  const float inv = 1.f / (float)(tiles * 128);
+  double acc = 0;
+  int nacc = 0;
+  for (int it = 0; it < steps; it++) {
+    cudaMemsetAsync(s.G_d, 0, sizeof(float) * kParams, st);
+    cudaMemsetAsync(s.loss_d, 0, sizeof(double), st);
+    k_net_train<<<tiles, 128, kSmTrain, st>>>(s.SX, s.ST, s.ns, nullptr, tiles * 128,
+                                              s.seed + 0x9E37ULL * (unsigned long long)(s.adam_step + 1),
+                                              net_of(s), inv, s.G_d, s.loss_d, s.status_d);
+    s.adam_step++;
+    k_adam<<<sblocks(kParams, 256), 256, 0, st>>>(s.P_d, s.M_d, s.V_d, s.G_d, s.adam_step, lr,
+                                                 0.9f, 0.999f, 1e-8f);
+    k_net_cast<<<sblocks(kHid * kHid, 256), 256, 0, st>>>(s.P_d, s.W1, s.W1T, s.W2, s.W2T);
+    if (it >= steps - 16) {  // mean loss of the last steps
+      double l = 0;
+      cudaMemcpyAsync(&l, s.loss_d, sizeof(double), cudaMemcpyDeviceToHost, st);
+      if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
+      acc += l;
+      nacc++;
+    }
+  }
+  if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
+  if (loss_out) *loss_out = nacc ? acc / nacc : 0.0;
+  return (int)cudaGetLastError();
+}
+
+int sur_loss_grad(Surrogate& s, const float* X, const float* T, int n, float* grad,
+                  double* loss, cudaStream_t st) {
+  cudaError_t e;
+  set_attrs();
+  long long h = s.nxg;
+  if ((e = sur_grow(s.Xg, h, (long long)n * kDesc)) != cudaSuccess) return e;
+  h = s.nxg;
+  if ((e = sur_grow(s.Tg, h, n)) != cudaSuccess) return e;
+  h = s.nxg;
+  if ((e = sur_grow(s.rows_d, h, n)) != cudaSuccess) return e;
+  s.nxg = n;
+  std::vector<int> rows(n);
+  for (int k = 0; k < n; k++) rows[k] = k;
+  cudaMemcpyAsync(s.Xg, X, sizeof(float) * kDesc * n, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(s.Tg, T, sizeof(float) * n, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(s.rows_d, rows.data(), sizeof(int) * n, cudaMemcpyHostToDevice, st);
+  cudaMemsetAsync(s.G_d, 0, sizeof(float) * kParams, st);
+  cudaMemsetAsync(s.loss_d, 0, sizeof(double), st);
+  k_net_train<<<(n + 127) / 128, 128, kSmTrain, st>>>(s.Xg, s.Tg, n, s.rows_d, n, 0ULL,
+                                                      net_of(s), 1.f / (float)n, s.G_d,
+                                                      s.loss_d, s.status_d);
+  cudaMemcpyAsync(grad, s.G_d, sizeof(float) * kParams, cudaMemcpyDeviceToHost, st);
+  cudaMemcpyAsync(loss, s.loss_d, sizeof(double), cudaMemcpyDeviceToHost, st);
+  if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
+  return (int)cudaGetLastError();
+}
+
+// network outputs for given normalised inputs: t (n) and dt/dx (n x 32)
+int sur_net_eval(Surrogate& s, const float* X, int n, float* t, float* dtdx, cudaStream_t st) {
+  cudaError_t e;
+  set_attrs();
+  long long h = s.nxg;
+  if ((e = sur_grow(s.Xg, h, (long long)n * kDesc)) != cudaSuccess) return e;
+  h = s.nxg;
+  if ((e = sur_grow(s.Tg, h, (long long)n * (kDesc + 1))) != cudaSuccess) return e;
+  s.nxg = n;
+  cudaMemcpyAsync(s.Xg, X, sizeof(float) * kDesc * n, cudaMemcpyHostToDevice, st);
+  k_net_infer<<<(n + 127) / 128, 128, kSmInfer, st>>>(s.Xg, n, net_of(s), s.Tg, s.Tg + n,
+                                                     s.status_d);
+  cudaMemcpyAsync(t, s.Tg, sizeof(float) * n, cudaMemcpyDeviceToHost, st);
+  cudaMemcpyAsync(dtdx, s.Tg + n, sizeof(float) * kDesc * n, cudaMemcpyDeviceToHost, st);
+  if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
+  return (int)cudaGetLastError();
+}
+
+// bond-order forces (into f3, added when accumulate) and per-atom energies
+// of atoms [0, n) from the network; energy_dev (optional) gets their sum
+int sur_forces(Surrogate& s, const md_double4* pos, int n, const RowWalker& w, double* f3,
+               int accumulate, double* energy_dev, int* d_status, cudaStream_t st) {
+  if (!s.normalised) return -1;
+  set_attrs();
+  int r = sur_descriptors(s, pos, n, w, true, d_status, st);
+  if (r) return r;
+  if (n == 0) return 0;
+  k_net_infer<<<(n + 127) / 128, 128, kSmInfer, st>>>(s.X, n, net_of(s), s.t, s.dtdx, s.status_d);
+  k_sg_scale<<<sblocks(n, 256), 256, 0, st>>>(s.t, s.dtdx, n, s.mu, s.sigma, s.istd_d, s.gcoef,
+                                              s.eatom);
+  cudaMemsetAsync(s.F32, 0, sizeof(float) * 3 * (size_t)n, st);
+  k_sg_force<<<sblocks(n, 128), 128, 0, st>>>(pos, n, s.sl, s.slen, w.g.box, s.P, s.gcoef, s.F32);
+  k_sg_store<<<sblocks(3LL * n, 256), 256, 0, st>>>(s.F32, f3, n, accumulate);
+  if (energy_dev) k_sum_d<<<1, 256, 0, st>>>(s.eatom, n, energy_dev);
+  return (int)cudaGetLastError();
+}
+
+int sur_add_config(Surrogate& s, const md_double4* pos, int n, double box, const double* fx,
+                   const double* eatom, cudaStream_t st) {
+  SurConfig c;
+  c.n = n;
+  c.box = box;
+  cudaError_t e;
+  if ((e = cudaMalloc(&c.pos, sizeof(md_double4) * n)) != cudaSuccess ||
+      (e = cudaMalloc(&c.sl, sizeof(uint32_t) * (size_t)n * kSgMax)) != cudaSuccess ||
+      (e = cudaMalloc(&c.slen, sizeof(int) * n)) != cudaSuccess ||
+      (e = cudaMalloc(&c.fx, sizeof(double) * 3 * n)) != cudaSuccess ||
+      (e = cudaMalloc(&c.eatom, sizeof(double) * n)) != cudaSuccess ||
+      (e = cudaMalloc(&c.G, sizeof(float) * kDesc * n)) != cudaSuccess) {
+    for (void* p : {(void*)c.pos, (void*)c.sl, (void*)c.slen, (void*)c.fx, (void*)c.eatom,
+                    (void*)c.G})
+      if (p) cudaFree(p);
+    return e;
+  }
+  cudaMemcpyAsync(c.pos, pos, sizeof(md_double4) * n, cudaMemcpyDeviceToDevice, st);
+  cudaMemcpyAsync(c.sl, s.sl, sizeof(uint32_t) * (size_t)n * kSgMax, cudaMemcpyDeviceToDevice, st);
+  cudaMemcpyAsync(c.slen, s.slen, sizeof(int) * n, cudaMemcpyDeviceToDevice, st);
+  cudaMemcpyAsync(c.fx, fx, sizeof(double) * 3 * n, cudaMemcpyDeviceToDevice, st);
+  cudaMemcpyAsync(c.eatom, eatom, sizeof(double) * n, cudaMemcpyDeviceToDevice, st);
+  cudaMemcpyAsync(c.G, s.X, sizeof(float) * kDesc * n, cudaMemcpyDeviceToDevice, st);
+  if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
+  s.cfgs.push_back(c);
+  return 0;
+}
+
+namespace {
+// normalisation from the stored configurations (first training)
+int sur_normalise_cfgs(Surrogate& s, cudaStream_t st) {
+  double sum[kDesc] = {0}, sq[kDesc] = {0}, esum = 0, esq = 0, fsq = 0;
+  long long cnt = 0;
+  for (const SurConfig& c : s.cfgs) {
+    std::vector<float> G((size_t)c.n * kDesc);
+    std::vector<double> E(c.n), F(3 * (size_t)c.n);
+    cudaMemcpyAsync(G.data(), c.G, sizeof(float) * G.size(), cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(E.data(), c.eatom, sizeof(double) * E.size(), cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(F.data(), c.fx, sizeof(double) * F.size(), cudaMemcpyDeviceToHost, st);
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return e;
+    for (int k = 0; k < c.n; k++) {
+      for (int f = 0; f < kDesc; f++) {
+        const double g = G[(size_t)k * kDesc + f];
+        sum[f] += g;
+        sq[f] += g * g;
+      }
+      esum += E[k];
+      esq += E[k] * E[k];
+    }
+    for (double f : F) fsq += f * f;
+    cnt += c.n;
+  }
+  float mean[kDesc], istd[kDesc];
+  for (int f = 0; f < kDesc; f++) {
+    const double m = sum[f] / cnt, v = sq[f] / cnt - m * m;
+    mean[f] = (float)m;
+    istd[f] = (float)(1.0 / sqrt(fmax(v, 0.0) + 1e-12));
+  }
+  s.mu = esum / cnt;
+  const double ev = esq / cnt - s.mu * s.mu;
+  s.sigma = ev > 0 ? sqrt(ev) : 1.0;
+  s.force_var = fsq / (3.0 * cnt) > 0 ? fsq / (3.0 * cnt) : 1.0;
+  cudaMemcpyAsync(s.mean_d, mean, sizeof(mean), cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(s.istd_d, istd, sizeof(istd), cudaMemcpyHostToDevice, st);
+  s.normalised = true;
+  return cudaStreamSynchronize(st);
+}
+}  // namespace
+
+int sur_train_fm(Surrogate& s, int steps, float lr, double* loss_e, double* loss_f,
+                 cudaStream_t st) {
+  if (s.cfgs.empty()) return -1;
+  cudaError_t e;
+  set_attrs();
+  if (!s.normalised) {
+    int r = sur_normalise_cfgs(s, st);
+    if (r) return r;
+  }
+  int nmax = 0;
+  for (SurConfig& c : s.cfgs) {
+    nmax = std::max(nmax, c.n);
+    if (!c.X) {
+      if ((e = cudaMalloc(&c.X, sizeof(float) * kDesc * c.n)) != cudaSuccess) return e;
+      if ((e = cudaMalloc(&c.T, sizeof(float) * c.n)) != cudaSuccess) return e;
+      k_normalise<<<sblocks(c.n, 256), 256, 0, st>>>(c.G, c.eatom, c.n, s.mean_d, s.istd_d,
+                                                     s.mu, s.sigma, c.X, c.T);
+    }
+  }
+  // scratch of the largest configuration
+  if (nmax > s.n_alloc) {
+    long long h;
+    for (float** p : {&s.dtdx, &s.gcoef}) {
+      h = 0;
+      if ((e = sur_grow(*p, h, (long long)nmax * kDesc)) != cudaSuccess) return e;
+    }
+    h = 0;
+    if ((e = sur_grow(s.t, h, nmax)) != cudaSuccess) return e;
+    h = 0;
+    if ((e = sur_grow(s.F32, h, 3LL * nmax)) != cudaSuccess) return e;
+    h = 0;
+    if ((e = sur_grow(s.eatom, h, nmax)) != cudaSuccess) return e;
+    h = 0;
+    if ((e = sur_grow(s.X, h, (long long)nmax * kDesc)) != cudaSuccess) return e;
+    h = 0;
+    if ((e = sur_grow(s.slen, h, nmax)) != cudaSuccess) return e;
+    s.n_alloc = nmax;
+  }
+  if (nmax > s.n_fm) {
+    long long h = 0;
+    if ((e = sur_grow(s.V, h, (long long)nmax * kDesc)) != cudaSuccess) return e;
+    h = 0;
+    if ((e = sur_grow(s.E3, h, 3LL * nmax)) != cudaSuccess) return e;
+    s.n_fm = nmax;
+  }
+  if (nmax > s.n_iota) {
+    std::vector<int> io(nmax);
+    for (int k = 0; k < nmax; k++) io[k] = k;
+    long long h = 0;
+    if ((e = sur_grow(s.iota_d, h, nmax)) != cudaSuccess) return e;
+    cudaMemcpyAsync(s.iota_d, io.data(), sizeof(int) * nmax, cudaMemcpyHostToDevice, st);
+    if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
+    s.n_iota = nmax;
+  }
+  const NetDev w = net_of(s);
+  double acc_e = 0, acc_f = 0;
+  int nacc = 0;
+  const int ncfg = (int)s.cfgs.size();
+  for (int it = 0; it < steps; it++) {
+    const SurConfig& c = s.cfgs[(it * 7919 + (int)(s.seed % 101)) % ncfg];
+    const int n = c.n;
+    const int tiles = (n + 127) / 128;
+    // forces of the current network on this configuration
+    k_net_infer<<<tiles, 128, kSmInfer, st>>>(c.X, n, w, s.t, s.dtdx, s.status_d);
+    k_sg_scale<<<sblocks(n, 256), 256, 0, st>>>(s.t, s.dtdx, n, s.mu, s.sigma, s.istd_d,
+                                                s.gcoef, s.eatom);
+    cudaMemsetAsync(s.F32, 0, sizeof(float) * 3 * (size_t)n, st);
+    k_sg_force<<<sblocks(n, 128), 128, 0, st>>>(c.pos, n, c.sl, c.slen, c.box, s.P, s.gcoef,
+                                                s.F32);
+    cudaMemsetAsync(s.scratch, 0, sizeof(double) * 2, st);
+    k_fm_resid<<<sblocks(3LL * n, 256), 256, 0, st>>>(s.F32, c.fx, 3 * n, s.E3, s.scratch);
+    // dL_F/d(dt/dx) = -2 kappa sigma istd q with kappa = w_force / (3 n var_F)
+    const float kappa = (float)(s.w_force / (3.0 * n * s.force_var));
+    k_sg_ctrans<<<sblocks(n, 128), 128, 0, st>>>(c.pos, n, c.sl, c.slen, c.box, s.P, s.E3,
+                                                 (float)(-2.0 * kappa * s.sigma), s.istd_d, s.V);
+    cudaMemsetAsync(s.G_d, 0, sizeof(float) * kParams, st);
+    cudaMemsetAsync(s.loss_d, 0, sizeof(double), st);
+    if (s.w_energy > 0.f)
+      k_net_train<<<tiles, 128, kSmTrain, st>>>(c.X, c.T, n, s.iota_d, n, 0ULL, w,
+                                                s.w_energy / (float)n, s.G_d, s.loss_d,
+                                                s.status_d);
+    if (s.w_force > 0.f)
+      k_net_train_force<<<tiles, 128, kSmForce, st>>>(c.X, s.V, n, w, s.G_d, s.status_d);
+    s.adam_step++;
+    k_adam<<<sblocks(kParams, 256), 256, 0, st>>>(s.P_d, s.M_d, s.V_d, s.G_d, s.adam_step, lr,
+                                                 0.9f, 0.999f, 1e-8f);
+    k_net_cast<<<sblocks(kHid * kHid, 256), 256, 0, st>>>(s.P_d, s.W1, s.W1T, s.W2, s.W2T);
+    if (it >= steps - std::min(steps, 2 * ncfg)) {  // losses over the last pass
+      double le = 0, lf[2];
+      cudaMemcpyAsync(&le, s.loss_d, sizeof(double), cudaMemcpyDeviceToHost, st);
+      cudaMemcpyAsync(lf, s.scratch, sizeof(double) * 2, cudaMemcpyDeviceToHost, st);
+      if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
+      acc_e += s.w_energy > 0.f ? le / s.w_energy : 0.0;
+      acc_f += lf[0] / (3.0 * n * s.force_var);
+      nacc++;
+    }
+  }
+  if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
+  s.last_loss_e = nacc ? acc_e / nacc : 0.0;
+  s.last_loss_f = nacc ? acc_f / nacc : 0.0;
+  if (loss_e) *loss_e = s.last_loss_e;
+  if (loss_f) *loss_f = s.last_loss_f;
+  return (int)cudaGetLastError();
+}
+
+int sur_force_grad(Surrogate& s, const float* X, const float* V, int n, float* grad,
+                   cudaStream_t st) {
+  cudaError_t e;
+  set_attrs();
+  float *dX = nullptr, *dV = nullptr;
+  if ((e = cudaMalloc(&dX, sizeof(float) * kDesc * n)) != cudaSuccess) return e;
+  if ((e = cudaMalloc(&dV, sizeof(float) * kDesc * n)) != cudaSuccess) {
+    cudaFree(dX);
+    return e;
+  }
+  cudaMemcpyAsync(dX, X, sizeof(float) * kDesc * n, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(dV, V, sizeof(float) * kDesc * n, cudaMemcpyHostToDevice, st);
+  cudaMemsetAsync(s.G_d, 0, sizeof(float) * kParams, st);
+  k_net_train_force<<<(n + 127) / 128, 128, kSmForce, st>>>(dX, dV, n, net_of(s), s.G_d,
+                                                           s.status_d);
+  cudaMemcpyAsync(grad, s.G_d, sizeof(float) * kParams, cudaMemcpyDeviceToHost, st);
+  e = cudaStreamSynchronize(st);
+  cudaFree(dX);
+  cudaFree(dV);
+  if (e != cudaSuccess) return e;
+  return (int)cudaGetLastError();
+}
+
+int sur_rel_err(const double* a, const double* b, int n, double* scratch, double* err,
+                cudaStream_t st) {
+  k_err2<<<1, 256, 0, st>>>(a, b, 3 * n, scratch);
+  double h[2];
+  cudaError_t e = cudaMemcpyAsync(h, scratch, sizeof(h), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return e;
+  *err = h[1] > 0 ? sqrt(h[0] / h[1]) : 0.0;
+  return 0;
+}
+
 }  // namespace mdgb
+
+md_surrogate::~md_surrogate() {
+  void* ptrs[] = {P_d, M_d,   V_d, G_d,   W1,    W1T,     W2,     W2T,    mean_d, istd_d,
+                  sl,  slen,  X,   t,     dtdx,  gcoef,   F32,    eatom,  SG,     SE,
+                  SX,  ST,    loss_d, scratch, rows_d, Xg, Tg, status_d};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  for (void* p : {(void*)iota_d, (void*)V, (void*)E3})
+    if (p) cudaFree(p);
+  for (mdgb::SurConfig& c : cfgs)
+    for (void* p : {(void*)c.pos, (void*)c.sl, (void*)c.slen, (void*)c.fx, (void*)c.eatom,
+                    (void*)c.G, (void*)c.X, (void*)c.T})
+      if (p) cudaFree(p);
+  if (stream) cudaStreamDestroy(stream);
+}
 
 using namespace mdgb;
 

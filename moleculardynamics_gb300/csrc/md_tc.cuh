@@ -94,19 +94,21 @@ __device__ __forceinline__ void tc_ld16(uint32_t taddr, float (&v)[16]) {
   for (int k = 0; k < 16; k++) v[k] = __uint_as_float(r[k]);
 }
 
-// D[128 x N] = A[128 x K] * B[N x K]^T with A and B in shared memory
-// (layout above); issued by the calling thread, completion on bar
+// D[128 x N] (+)= A[128 x K] * B[N x K]^T with A and B in shared memory
+// (layout above); issued by the calling thread; with bar, completion of all
+// earlier products of this thread is signalled there
 __device__ __forceinline__ void tc_gemm_issue(uint32_t d_tmem, const void* A, const void* B,
-                                              int N, int K, uint64_t* bar) {
+                                              int N, int K, uint64_t* bar,
+                                              bool accumulate = false) {
   const uint32_t a0 = smem_addr(A), b0 = smem_addr(B);
   const uint32_t sbo = (uint32_t)K * 16u;
   const uint32_t idesc = tc_idesc_bf16(128, N);
   for (int j = 0; j < K / 16; j++) {
     // K = 16 per instruction: two core matrices along K
     tc_mma(d_tmem, tc_desc(a0 + j * 256u, 128u, sbo), tc_desc(b0 + j * 256u, 128u, sbo), idesc,
-           j > 0);
+           accumulate || j > 0);
   }
-  tc_commit(bar);
+  if (bar) tc_commit(bar);
 }
 
 }  // namespace mdgb

@@ -70,6 +70,12 @@ class MdTuneResult(C.Structure):
                 ("best_ms", C.c_double)]
 
 
+class MdSurrogateStats(C.Structure):
+    _fields_ = [("surrogate_steps", C.c_longlong), ("exact_steps", C.c_longlong),
+                ("checks", C.c_longlong), ("rejected_checks", C.c_longlong),
+                ("last_error", C.c_double)]
+
+
 class ListSettings(C.Structure):
     _fields_ = [("maxnlmove", C.c_float), ("maxnlmovesq", C.c_float), ("rcut", C.c_float),
                 ("rs", C.c_float), ("rcutsq", C.c_float), ("nlistsize", C.c_int),
@@ -92,7 +98,12 @@ EXPORTS = ["md_create", "md_destroy", "md_status_string", "md_last_error", "md_u
            "mdgb_calculate_potential", "mdgb_set_species", "mdgb_last_status", "md_read_config",
            "md_write_results", "md_host_alloc", "md_host_free",
            "mdgb_many_body_forces_static", "md_autotune", "md_set_graphs", "md_batch_create",
-           "md_batch_size", "md_batch_records", "mdgb_tc_selftest"]
+           "md_batch_size", "md_batch_records", "mdgb_tc_selftest", "md_surrogate_create",
+           "md_surrogate_destroy", "md_surrogate_param_count", "md_surrogate_collect",
+           "md_surrogate_samples", "md_surrogate_train", "md_surrogate_attach",
+           "md_surrogate_report", "md_surrogate_forces", "md_surrogate_descriptors",
+           "md_surrogate_params", "md_surrogate_normalisation", "md_surrogate_loss_grad",
+           "md_surrogate_net", "md_surrogate_train_forces", "md_surrogate_force_grad"]
 
 
 def load(path: str | None = None) -> C.CDLL:
@@ -131,6 +142,24 @@ def load(path: str | None = None) -> C.CDLL:
     L.md_autotune.argtypes = [C.c_void_p, C.c_int, P(MdTuneResult)]
     L.md_set_graphs.argtypes = [C.c_void_p, C.c_int]
     L.mdgb_tc_selftest.argtypes = [_fp, _fp, _fp, C.c_int, C.c_int]
+    L.md_surrogate_create.argtypes = [C.c_int, C.c_ulonglong, C.c_float, P(C.c_void_p)]
+    L.md_surrogate_destroy.argtypes = [C.c_void_p]
+    L.md_surrogate_param_count.restype = C.c_int
+    L.md_surrogate_collect.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, P(C.c_int)]
+    L.md_surrogate_samples.argtypes = [C.c_void_p, P(C.c_int)]
+    L.md_surrogate_train.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_float, P(C.c_double)]
+    L.md_surrogate_attach.argtypes = [C.c_void_p, C.c_void_p, C.c_double, C.c_int]
+    L.md_surrogate_report.argtypes = [C.c_void_p, P(MdSurrogateStats)]
+    L.md_surrogate_forces.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, P(C.c_double)]
+    L.md_surrogate_descriptors.argtypes = [C.c_void_p, C.c_void_p, _fp, C.c_int]
+    L.md_surrogate_params.argtypes = [C.c_void_p, _fp, C.c_int]
+    L.md_surrogate_normalisation.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                             C.c_int]
+    L.md_surrogate_loss_grad.argtypes = [C.c_void_p, _fp, _fp, C.c_int, _fp, P(C.c_double)]
+    L.md_surrogate_net.argtypes = [C.c_void_p, _fp, C.c_int, _fp, _fp]
+    L.md_surrogate_train_forces.argtypes = [C.c_void_p, C.c_int, C.c_float, C.c_float,
+                                            C.c_float, P(C.c_double), P(C.c_double)]
+    L.md_surrogate_force_grad.argtypes = [C.c_void_p, _fp, _fp, C.c_int, _fp]
     L.md_batch_create.argtypes = [P(MdConfig), C.c_int, _ip, _dp, P(C.c_void_p)]
     L.md_batch_size.argtypes = [C.c_void_p]
     L.md_batch_records.argtypes = [C.c_void_p, C.c_void_p, C.c_int]
@@ -296,6 +325,141 @@ class Engine:
 
     def set_graphs(self, on: bool):
         self._ck(self.lib.md_set_graphs(self.h, int(on)), "md_set_graphs")
+
+
+class Surrogate:
+    """Learned surrogate of the bond-order term (md_surrogate_*)."""
+
+    def __init__(self, seed: int = 1, cutoff: float = 3.0, device: int = 0):
+        self.lib = load()
+        h = C.c_void_p()
+        s = self.lib.md_surrogate_create(device, seed, cutoff, C.byref(h))
+        if s != 0:
+            raise EngineError(s, "md_surrogate_create")
+        self.h = h
+        self.nparams = self.lib.md_surrogate_param_count()
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.md_surrogate_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _ck(self, s, what):
+        if s != 0:
+            raise EngineError(s, what)
+
+    def collect(self, e: "Engine", stride: int = 1, offset: int = 0) -> int:
+        n = C.c_int()
+        s = self.lib.md_surrogate_collect(self.h, e.h, stride, offset, C.byref(n))
+        if s != 0:
+            raise EngineError(s, "md_surrogate_collect: " + self.lib.md_last_error(e.h).decode())
+        return n.value
+
+    def samples(self) -> int:
+        n = C.c_int()
+        self._ck(self.lib.md_surrogate_samples(self.h, C.byref(n)), "md_surrogate_samples")
+        return n.value
+
+    def train(self, steps: int, batch: int = 1024, lr: float = 1e-3) -> float:
+        loss = C.c_double()
+        self._ck(self.lib.md_surrogate_train(self.h, steps, batch, lr, C.byref(loss)),
+                 "md_surrogate_train")
+        return loss.value
+
+    def train_forces(self, steps: int, lr: float = 1e-3, w_energy: float = 1.0,
+                     w_force: float = 1.0):
+        le, lf = C.c_double(), C.c_double()
+        self._ck(self.lib.md_surrogate_train_forces(self.h, steps, lr, w_energy, w_force,
+                                                    C.byref(le), C.byref(lf)),
+                 "md_surrogate_train_forces")
+        return le.value, lf.value
+
+    def force_grad(self, x, v):
+        x = np.ascontiguousarray(x, np.float32)
+        v = np.ascontiguousarray(v, np.float32)
+        g = np.zeros(self.nparams, np.float32)
+        self._ck(self.lib.md_surrogate_force_grad(self.h, x, v, len(x), g),
+                 "md_surrogate_force_grad")
+        return g
+
+    def attach(self, e: "Engine", threshold: float, check_every: int = 10):
+        s = self.lib.md_surrogate_attach(e.h, self.h, threshold, check_every)
+        if s != 0:
+            raise EngineError(s, "md_surrogate_attach: " + self.lib.md_last_error(e.h).decode())
+
+    @staticmethod
+    def detach(e: "Engine"):
+        e._ck(e.lib.md_surrogate_attach(e.h, None, 0.0, 1), "md_surrogate_attach")
+
+    @staticmethod
+    def report(e: "Engine") -> dict:
+        r = MdSurrogateStats()
+        e._ck(e.lib.md_surrogate_report(e.h, C.byref(r)), "md_surrogate_report")
+        return {k: getattr(r, k) for k, _ in MdSurrogateStats._fields_}
+
+    def forces(self, e: "Engine"):
+        f = np.zeros((e.cfg.n_mb, 3))
+        en = C.c_double()
+        s = self.lib.md_surrogate_forces(self.h, e.h, f.ctypes.data, C.byref(en))
+        if s != 0:
+            raise EngineError(s, "md_surrogate_forces: " + self.lib.md_last_error(e.h).decode())
+        return f, en.value
+
+    def descriptors(self, e: "Engine", normalised: bool = False) -> np.ndarray:
+        g = np.zeros((e.cfg.n_mb, 32), np.float32)
+        s = self.lib.md_surrogate_descriptors(self.h, e.h, g, int(normalised))
+        if s != 0:
+            raise EngineError(s, "md_surrogate_descriptors: " +
+                              self.lib.md_last_error(e.h).decode())
+        return g
+
+    def params(self, new=None) -> np.ndarray:
+        if new is not None:
+            p = np.ascontiguousarray(new, np.float32)
+            self._ck(self.lib.md_surrogate_params(self.h, p, 1), "md_surrogate_params")
+            return p
+        p = np.zeros(self.nparams, np.float32)
+        self._ck(self.lib.md_surrogate_params(self.h, p, 0), "md_surrogate_params")
+        return p
+
+    def normalisation(self, mean=None, istd=None, mu=0.0, sigma=1.0):
+        if mean is not None:
+            m = np.ascontiguousarray(mean, np.float32)
+            i = np.ascontiguousarray(istd, np.float32)
+            ms = np.array([mu, sigma], np.float64)
+            self._ck(self.lib.md_surrogate_normalisation(self.h, m.ctypes.data, i.ctypes.data,
+                                                         ms.ctypes.data, 1),
+                     "md_surrogate_normalisation")
+            return
+        m = np.zeros(32, np.float32)
+        i = np.zeros(32, np.float32)
+        ms = np.zeros(2)
+        self._ck(self.lib.md_surrogate_normalisation(self.h, m.ctypes.data, i.ctypes.data,
+                                                     ms.ctypes.data, 0),
+                 "md_surrogate_normalisation")
+        return m, i, ms[0], ms[1]
+
+    def loss_grad(self, x, t):
+        x = np.ascontiguousarray(x, np.float32)
+        t = np.ascontiguousarray(t, np.float32)
+        g = np.zeros(self.nparams, np.float32)
+        loss = C.c_double()
+        self._ck(self.lib.md_surrogate_loss_grad(self.h, x, t, len(t), g, C.byref(loss)),
+                 "md_surrogate_loss_grad")
+        return loss.value, g
+
+    def net(self, x):
+        x = np.ascontiguousarray(x, np.float32)
+        t = np.zeros(len(x), np.float32)
+        d = np.zeros((len(x), 32), np.float32)
+        self._ck(self.lib.md_surrogate_net(self.h, x, len(x), t, d), "md_surrogate_net")
+        return t, d
 
 
 class Batch(Engine):
