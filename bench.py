@@ -315,6 +315,97 @@ def batched_form(eng, device, steps: int, loop_steps: int, seed: int = 4096) -> 
     }
 
 
+def surrogate_form(eng, device, train_steps: int, run_steps: int, seed: int = 5) -> dict:
+    """The learned bond-order surrogate on the 32,768-atom nitrogen diamond
+    (16^3 cells, nearest neighbour 1.5 A, 0.02 A noise).  Training data:
+    trajectories of the exact FP64 method at 300, 700, 1100 and 1500 K on
+    4,096-atom boxes of the same lattice, 50 snapshots = 204,800 atomic
+    environments; the network is trained by force matching with the
+    tensor-core kernels.  Then NVE runs of the 32,768-atom system with the
+    surrogate (exact-kernel checks every 10 steps) and with the exact method
+    alone are timed from the same state."""
+    from moleculardynamics_gb300 import lattice as lat
+    a = 4 * 1.5 / np.sqrt(3.0)
+
+    def system(T, sd, ncell=16):
+        return lat.make_system("diamond", ncell, T, seed=sd, a=a, noise=0.02,
+                               species=lat.SPECIES_N, mass_table="neon")
+
+    def engine(pos, vel, L):
+        cfg = eng.make_config(n_mb=len(pos), use_lj=0, use_mb=1, mb_rs=3.5, mb_rcut=3.0, dt=0.5,
+                              periodic=1, box=L, species=eng.SPECIES_NEON, device=device)
+        e = eng.Engine(cfg)
+        e.upload(pos, vel)
+        e.begin(0.0)
+        return e
+
+    s = eng.Surrogate(seed=seed, cutoff=3.0, device=device)
+    t0 = time.perf_counter()
+    nsnap = 0
+    for k, T in enumerate((300.0, 700.0, 1100.0, 1500.0)):
+        pos, vel, L = system(T, seed + k, ncell=8)
+        e = engine(pos, vel, L)
+        for q in range(13 if k < 2 else 12):
+            e.step(8)
+            s.collect(e)
+            nsnap += 1
+        e.close()
+    t_collect = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    loss_e, loss_f = s.train_forces(train_steps, lr=2e-3, w_energy=0.1, w_force=1.0)
+    t_train = time.perf_counter() - t0
+    pos, vel, L = system(900.0, seed + 10)
+    n = len(pos)
+
+    def run(threshold):
+        e = engine(pos, vel, L)
+        if threshold is not None:
+            s.attach(e, threshold, 10)
+        e.step(5)
+        e.synchronize()
+        th0 = e.thermo_now()
+        es0 = s.forces(e)[1] if threshold is not None else e.compute_forces()[1][3]
+        e.set_timing(True)
+        e.step(run_steps)
+        e.synchronize()
+        ms, _ = e.kernel_time(eng.KERNEL_STEP)
+        e.set_timing(False)
+        th1 = e.thermo_now()
+        fx, en = e.compute_forces()
+        fs, es1 = s.forces(e)
+        rep = eng.Surrogate.report(e) if threshold is not None else None
+        e.close()
+        if threshold is None:
+            es1 = en[3]
+        rms = float(np.sqrt(((fs - fx) ** 2).sum(1).mean() / (fx ** 2).sum(1).mean()))
+        drift = ((th1["ek"] + es1) - (th0["ek"] + es0)) / n / run_steps * 1000.0
+        return {"ms_per_step": ms / run_steps, "value": n * run_steps / (ms / 1e3),
+                "force_rms_rel_vs_exact": rms, "energy_drift_per_atom_per_1000_steps": drift,
+                "surrogate": rep}
+
+    exact = run(None)
+    strict = run(1e-4)
+    loose = run(1.0)
+    s.close()
+    return {
+        "metric": "atom-steps/s of the bond-order system on 1 GB300", "unit": "atom-steps/s",
+        "config": {"atoms": n, "lattice": "N diamond 16^3 cells, 1.5 A bonds, 0.02 A noise",
+                   "training": f"{nsnap} snapshots of 4,096-atom boxes along exact trajectories "
+                               f"at 300, 700, 1100, 1500 K (every 8 steps) = {nsnap * 4096} atomic "
+                               f"environments; force matching, {train_steps} Adam steps",
+                   "network": "32-64-64-1 tanh, BF16 weights on tcgen05, FP32 accumulation",
+                   "run": f"{run_steps} NVE steps at 900 K (dt 0.5 fs), FP64 Gear",
+                   "threshold_policy": "exact-kernel check every 10 steps"},
+        "train": {"loss_energy": loss_e, "loss_force": loss_f, "collect_s": t_collect,
+                  "train_s": t_train},
+        "exact": exact,
+        "surrogate_threshold_1e-4": strict,
+        "surrogate_accepting": loose,
+        "speedup_accepting_vs_exact": exact["ms_per_step"] / loose["ms_per_step"],
+        "speedup_threshold_1e-4_vs_exact": exact["ms_per_step"] / strict["ms_per_step"],
+    }
+
+
 def run_gb300(args, rank, world):
     from moleculardynamics_gb300 import build as b
     from moleculardynamics_gb300 import engine as eng
@@ -485,7 +576,9 @@ def run_gb300(args, rank, world):
         line["accuracy"]["force_rms_rel_vs_fp64"] = rms
     if rank == 0 and not args.no_forms:
         line["forms"] = {"batched": batched_form(eng, device, args.batch_steps,
-                                                  args.batch_loop_steps)}
+                                                  args.batch_loop_steps),
+                         "surrogate": surrogate_form(eng, device, args.sur_train_steps,
+                                                     args.sur_run_steps)}
     if rank == 0 and world == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1
         csteps = args.cpu_md_steps
@@ -519,6 +612,8 @@ def main():
     ap.add_argument("--no-forms", action="store_true", help="skip the batched/surrogate forms")
     ap.add_argument("--batch-steps", type=int, default=1000)
     ap.add_argument("--batch-loop-steps", type=int, default=10)
+    ap.add_argument("--sur-train-steps", type=int, default=20000)
+    ap.add_argument("--sur-run-steps", type=int, default=200)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world, _ = dist_env()

@@ -34,14 +34,16 @@ def test_struct_layouts_match_the_header(eng, tmp_path):
     import ctypes as C
     src = tmp_path / "sz.c"
     src.write_text('#include "mdgb.h"\n#include <stdio.h>\n#include <stddef.h>\n'
-                   'int main(void){printf("%zu %zu %zu %zu\\n", sizeof(md_config),'
-                   ' sizeof(md_thermo), sizeof(md_stats), sizeof(mdgb_list_settings));return 0;}\n')
+                   'int main(void){printf("%zu %zu %zu %zu %zu %zu\\n", sizeof(md_config),'
+                   ' sizeof(md_thermo), sizeof(md_stats), sizeof(mdgb_list_settings),'
+                   ' sizeof(md_tune_result), sizeof(md_surrogate_stats));return 0;}\n')
     exe = tmp_path / "sz"
     subprocess.run(["gcc", "-I", INCLUDE, str(src), "-o", str(exe)], check=True)
     sizes = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True,
                                             check=True).stdout.split()]
     assert sizes == [C.sizeof(eng.MdConfig), C.sizeof(eng.MdThermo), C.sizeof(eng.MdStats),
-                     C.sizeof(eng.ListSettings)]
+                     C.sizeof(eng.ListSettings), C.sizeof(eng.MdTuneResult),
+                     C.sizeof(eng.MdSurrogateStats)]
     assert C.sizeof(eng.MdThermo) == 16 * 8
 
 
