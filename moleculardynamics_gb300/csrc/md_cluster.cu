@@ -431,7 +431,8 @@ __device__ __forceinline__ float min_img(float d, float Lf, float invL) {
   return d - Lf * rintf(d * invL);
 }
 
-// 4. compact rows from the build-time positions (MODE 0: count, 1: write)
+// 4. compact rows from the build-time positions (MODE 0: count, 1: write,
+// 2: both, rows longer than cap truncated and reported through the counters)
 template <int MODE>
 __global__ void __launch_bounds__(256)
     k_cl_rows(const ClusterSegment* __restrict__ seg, const ClusterReplica* __restrict__ reps,
@@ -462,17 +463,17 @@ __global__ void __launch_bounds__(256)
         dz = min_img(dz, Lf, invL);
       }
       if (dx * dx + dy * dy + dz * dz < rv2) {
-        if (MODE == 1 && kept < cap) rows[(size_t)kept * ld + p] = (uint16_t)q;
+        if (MODE != 0 && kept < cap) rows[(size_t)kept * ld + p] = (uint16_t)q;
         kept++;
       }
     });
-    if (MODE == 0) {
+    if (MODE != 1) {
       len[p] = (uint16_t)min(kept, 65535);
       mx = max(mx, kept);
       tot += (unsigned long long)kept;
     }
   }
-  if (MODE == 0) {
+  if (MODE != 1) {
     atomicMax(&counters[1], mx);
     atomicAdd((unsigned long long*)(counters + 2), tot);
   }
@@ -709,18 +710,33 @@ __global__ void __launch_bounds__(224, 3)
           if (wrem > 0) {
             const int rem = L - t * kClusterTileSlots;
             const uint16_t* tl = tiles + b * tile_elems + col;
-            float cx = 0.f, cy = 0.f, cz = 0.f;
+            // even and odd slots in two sums: two independent FMA chains
+            float ax = 0.f, ay = 0.f, az = 0.f, bx = 0.f, by = 0.f, bz = 0.f;
+            if (wrem >= kClusterTileSlots) {
 #pragma unroll
-            for (int kk = 0; kk < kClusterTileSlots; kk++) {
-              if (kk < wrem) {
-                const bool valid = kk < rem;
-                const int q = valid ? (int)tl[kk * BX] : self;
-                pair(q, valid, cx, cy, cz);
+              for (int kk = 0; kk < kClusterTileSlots; kk += 2) {
+                const bool v0 = kk < rem, v1 = kk + 1 < rem;
+                const int q0 = v0 ? (int)tl[kk * BX] : self;
+                const int q1 = v1 ? (int)tl[(kk + 1) * BX] : self;
+                pair(q0, v0, ax, ay, az);
+                pair(q1, v1, bx, by, bz);
+              }
+            } else {
+#pragma unroll
+              for (int kk = 0; kk < kClusterTileSlots; kk++) {
+                if (kk < wrem) {
+                  const bool valid = kk < rem;
+                  const int q = valid ? (int)tl[kk * BX] : self;
+                  if (kk & 1)
+                    pair(q, valid, bx, by, bz);
+                  else
+                    pair(q, valid, ax, ay, az);
+                }
               }
             }
-            kahan_add(hx, lx, cx);
-            kahan_add(hy, ly, cy);
-            kahan_add(hz, lz, cz);
+            kahan_add(hx, lx, ax + bx);
+            kahan_add(hy, ly, ay + by);
+            kahan_add(hz, lz, az + bz);
           }
         }
         // everyone is done with buffer b (and every wait succeeded)
@@ -1061,6 +1077,7 @@ int cluster_build(ClusterList& cl, const std::vector<ClusterReplica>& reps_in, f
   if (!attrs) {
     allow_smem(k_cl_rows<0>);
     allow_smem(k_cl_rows<1>);
+    allow_smem(k_cl_rows<2>);
     allow_smem(k_lj_cl<false, false, false>);
     allow_smem(k_lj_cl<false, true, false>);
     allow_smem(k_lj_cl<true, false, false>);
@@ -1075,9 +1092,17 @@ int cluster_build(ClusterList& cl, const std::vector<ClusterReplica>& reps_in, f
   cl.rv2 = rv_keep * rv_keep;
   cl.ld = (std::max(n, 1) + 31) / 32 * 32;
   const size_t smem = stage_bytes(cl.max_staged);
-  if (cl.nseg > 0)
-    k_cl_rows<0><<<cl.nseg, 256, smem, st>>>(cl.seg, cl.rep, cl.start, cl.pos_build, cl.rv2,
-                                             nullptr, cl.len, cl.ld, 0, cl.counters);
+  // one pass into the rows of the previous capacity when there are some;
+  // a second (writing) pass only when a row outgrew them
+  const bool have_rows = cl.rows && cl.cap > 0 && (long long)cl.cap * cl.ld <= cl.rows_elems;
+  if (cl.nseg > 0) {
+    if (have_rows)
+      k_cl_rows<2><<<cl.nseg, 256, smem, st>>>(cl.seg, cl.rep, cl.start, cl.pos_build, cl.rv2,
+                                               cl.rows, cl.len, cl.ld, cl.cap, cl.counters);
+    else
+      k_cl_rows<0><<<cl.nseg, 256, smem, st>>>(cl.seg, cl.rep, cl.start, cl.pos_build, cl.rv2,
+                                               nullptr, cl.len, cl.ld, 0, cl.counters);
+  }
   cudaMemcpyAsync(hc, cl.counters, sizeof(hc), cudaMemcpyDeviceToHost, st);
   if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
   cl.maxlen = hc[1];
@@ -1086,11 +1111,15 @@ int cluster_build(ClusterList& cl, const std::vector<ClusterReplica>& reps_in, f
     memcpy(&ent, hc + 2, sizeof(ent));
     cl.entries = (long long)ent;
   }
-  cl.cap = std::min(65535, (int)(std::max(cl.maxlen, 1) * cl.headroom) + 8);
-  const long long need = (long long)cl.cap * cl.ld;
-  if (need > cl.rows_elems || !cl.rows) {
-    if ((e = realloc_dev(cl.rows, (size_t)need)) != cudaSuccess) return e;
-    cl.rows_elems = need;
+  const int want = std::min(65535, (int)(std::max(cl.maxlen, 1) * cl.headroom) + 8);
+  const bool fits = have_rows && want <= cl.cap;
+  if (!fits) {
+    cl.cap = want;
+    const long long need = (long long)cl.cap * cl.ld;
+    if (need > cl.rows_elems || !cl.rows) {
+      if ((e = realloc_dev(cl.rows, (size_t)need)) != cudaSuccess) return e;
+      cl.rows_elems = need;
+    }
   }
   cl.rmap_ok = encode_tiled_2d(&cl.rmap, CU_TENSOR_MAP_DATA_TYPE_UINT16, cl.rows,
                                (uint64_t)cl.ld, (uint64_t)cl.cap, (uint64_t)cl.ld * 2,
@@ -1099,7 +1128,7 @@ int cluster_build(ClusterList& cl, const std::vector<ClusterReplica>& reps_in, f
     err = "TMA descriptor of the cluster rows could not be encoded";
     return -1;
   }
-  if (cl.nseg > 0)
+  if (!fits && cl.nseg > 0)
     k_cl_rows<1><<<cl.nseg, 256, smem, st>>>(cl.seg, cl.rep, cl.start, cl.pos_build, cl.rv2,
                                              cl.rows, cl.len, cl.ld, cl.cap, cl.counters);
   cl.trip_dist = 0.5 * ((double)rv - rcut) - (double)margin;
