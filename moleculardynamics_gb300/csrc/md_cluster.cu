@@ -93,7 +93,10 @@ __global__ void k_cl_assign(md_double4* __restrict__ pos, int n, const ClusterRe
   const int id = r.G == 1 ? r.cell0 : cid(r, c[0], c[1], c[2]);
   cell[i] = id;
   const int old = atomicAdd(&count[id], 1);
-  atomicMax(&counters[4], old + 1);
+  // largest cell population: one atomic per warp
+  const unsigned m = __activemask();
+  const unsigned big = __reduce_max_sync(m, (unsigned)(old + 1));
+  if ((int)(threadIdx.x & 31) == __ffs(m) - 1) atomicMax(&counters[4], (int)big);
 }
 
 __global__ void k_cl_scatter(const int* __restrict__ cell, int n, const int* __restrict__ start,
@@ -474,8 +477,16 @@ __global__ void __launch_bounds__(256)
     }
   }
   if (MODE != 1) {
-    atomicMax(&counters[1], mx);
-    atomicAdd((unsigned long long*)(counters + 2), tot);
+    // one atomic per warp (all threads of the block reach this point)
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+      tot += __shfl_xor_sync(0xffffffffu, tot, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+      atomicMax(&counters[1], mx);
+      atomicAdd((unsigned long long*)(counters + 2), tot);
+    }
   }
 }
 

@@ -78,7 +78,9 @@ __global__ void k_cell_assign(md_double4* __restrict__ pos, int n, Grid g, int* 
   }
   atom_slot[i] = (int)h;
   int old = atomicAdd(&count[h], 1);
-  atomicMax(&counters[0], old + 1);
+  const unsigned m = __activemask();
+  const unsigned big = __reduce_max_sync(m, (unsigned)(old + 1));
+  if ((int)(threadIdx.x & 31) == __ffs(m) - 1) atomicMax(&counters[0], (int)big);
 }
 
 // exclusive scan, 4 items per thread, 1024 threads per block
@@ -198,9 +200,16 @@ __global__ void k_rows(RowWalker w, const md_double4* __restrict__ pos,
   });
   if (MODE == 0) {
     len[i] = kept;
-    atomicMax(&counters[1], full);
-    atomicMax(&counters[2], kept);
-    atomicAdd((unsigned long long*)(counters + 4), (unsigned long long)kept);
+    // one atomic per warp for each counter
+    const unsigned m = __activemask();
+    const unsigned fmax_w = __reduce_max_sync(m, (unsigned)full);
+    const unsigned kmax_w = __reduce_max_sync(m, (unsigned)kept);
+    const unsigned ksum_w = __reduce_add_sync(m, (unsigned)kept);
+    if ((int)(threadIdx.x & 31) == __ffs(m) - 1) {
+      atomicMax(&counters[1], (int)fmax_w);
+      atomicMax(&counters[2], (int)kmax_w);
+      atomicAdd((unsigned long long*)(counters + 4), (unsigned long long)ksum_w);
+    }
   }
 }
 
