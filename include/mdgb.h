@@ -73,6 +73,8 @@ typedef struct md_config {
   int lj_kernel;           /* MD_LJ_AUTO, MD_LJ_ROWS or MD_LJ_CLUSTER (precision form) */
   int cluster_cells;       /* cells per segment of the cluster kernel (0: default) */
   int cluster_threads;     /* threads per segment block (0: default; multiple of 32, <= 224) */
+  int cluster_row_loads;   /* rows of the cluster kernel: 0 default / autotuned, 1 TMA tiles in
+                              shared memory, 2 per-lane register prefetch */
 } md_config;
 
 /* LJ kernel of the precision form.  ROWS: compact rows of packed atom
@@ -165,13 +167,14 @@ md_status md_get_stats(const md_ctx* ctx, md_stats* out);
 md_status md_set_timing(md_ctx* ctx, int on);
 md_status md_kernel_time(const md_ctx* ctx, int kernel, double* total_ms, long long* launches);
 /* Autotuner of the cluster kernel (precision form, periodic): times `evals`
- * force evaluations on the current state for each candidate block size and
- * staged-atom cap per segment, keeps the fastest and rebuilds the list with
- * it.  Forces do not depend on the choice (same pairs, same order).  No-op
+ * force evaluations on the current state for each candidate block size,
+ * staged-atom cap per segment and row-load scheme, keeps the fastest and
+ * rebuilds the list with it.  Forces do not depend on the choice (same pairs, same order).  No-op
  * for the other kernels.  Call after md_begin. */
 typedef struct md_tune_result {
   int threads;             /* threads per segment block */
   int stage_cap;           /* staged atoms per segment (cap of the column cut) */
+  int row_loads;           /* 1 TMA tiles, 2 register prefetch */
   int candidates;          /* configurations timed */
   double best_ms;          /* force evaluation time of the choice */
 } md_tune_result;

@@ -588,14 +588,17 @@ struct ClStep {
 // atom in the same thread (cpu/common/Device.cpp:17-85 in FP64 with FMAs).
 // Dynamic shared memory: two row tiles [16][blockDim + 8] of uint16 (TMA
 // destinations), then the staged positions.
-template <bool ENERGY, bool ALL_NG, bool GEAR>
+// TMA_ROWS: row tiles by TMA into shared memory (block-synchronised); else
+// each lane prefetches its next 16 row entries into registers (no barriers)
+template <bool ENERGY, bool ALL_NG, bool GEAR, bool TMA_ROWS>
 __global__ void __launch_bounds__(224, 3)
     k_lj_cl(const __grid_constant__ CUtensorMap rmap, const ClStep a) {
   extern __shared__ __align__(128) unsigned char dyn[];
   const int tid = threadIdx.x;
   const int BX = blockDim.x + 8;
   uint16_t* tiles = (uint16_t*)dyn;
-  float4* st = (float4*)(dyn + 2 * kClusterTileSlots * BX * sizeof(uint16_t));
+  float4* st =
+      (float4*)(dyn + (TMA_ROWS ? 2 * kClusterTileSlots * BX * sizeof(uint16_t) : 0));
   __shared__ SegShared sh;
   __shared__ __align__(8) uint64_t bar[3];  // two row tiles, staging
   __shared__ int s_max[8];
@@ -689,7 +692,63 @@ __global__ void __launch_bounds__(224, 3)
         ev[2] += 0.5 * (double)(r2 * fij);
       }
     };
-    if (!tripped) {
+    // 16 row slots: even and odd slots in two sums (two independent FMA
+    // chains), folded into the compensated sum; wrem is warp-uniform
+    auto chunk16 = [&](auto&& get, int rem, int wrem) {
+      float ax = 0.f, ay = 0.f, az = 0.f, bx = 0.f, by = 0.f, bz = 0.f;
+      if (wrem >= kClusterTileSlots) {
+#pragma unroll
+        for (int kk = 0; kk < kClusterTileSlots; kk += 2) {
+          const bool v0 = kk < rem, v1 = kk + 1 < rem;
+          const int q0 = v0 ? get(kk) : self;
+          const int q1 = v1 ? get(kk + 1) : self;
+          pair(q0, v0, ax, ay, az);
+          pair(q1, v1, bx, by, bz);
+        }
+      } else {
+#pragma unroll
+        for (int kk = 0; kk < kClusterTileSlots; kk++) {
+          if (kk < wrem) {
+            const bool valid = kk < rem;
+            const int q = valid ? get(kk) : self;
+            if (kk & 1)
+              pair(q, valid, bx, by, bz);
+            else
+              pair(q, valid, ax, ay, az);
+          }
+        }
+      }
+      kahan_add(hx, lx, ax + bx);
+      kahan_add(hy, ly, ay + by);
+      kahan_add(hz, lz, az + bz);
+    };
+    if (!tripped && !TMA_ROWS) {
+      const int L = live ? (int)a.len[p] : 0;
+      int wmax = L;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) wmax = max(wmax, __shfl_xor_sync(0xffffffffu, wmax, o));
+      const uint16_t* rp = a.rows + (live ? p : 0);
+      // two entries per register; slots below the warp's longest row only
+      auto fetch = [&](int t0, uint32_t (&dst)[kClusterTileSlots / 2]) {
+#pragma unroll
+        for (int k = 0; k < kClusterTileSlots / 2; k++) {
+          const int s0 = t0 + 2 * k, s1 = s0 + 1;
+          const uint32_t lo = s0 < wmax ? (uint32_t)__ldg(rp + (size_t)s0 * a.ld) : 0u;
+          const uint32_t hi = s1 < wmax ? (uint32_t)__ldg(rp + (size_t)s1 * a.ld) : 0u;
+          dst[k] = lo | (hi << 16);
+        }
+      };
+      uint32_t nx[kClusterTileSlots / 2];
+      fetch(0, nx);
+      for (int t0 = 0; t0 < wmax; t0 += kClusterTileSlots) {
+        uint32_t cu[kClusterTileSlots / 2];
+#pragma unroll
+        for (int k = 0; k < kClusterTileSlots / 2; k++) cu[k] = nx[k];
+        fetch(t0 + kClusterTileSlots, nx);  // next chunk in flight while this one computes
+        chunk16([&](int kk) { return (int)((cu[kk >> 1] >> ((kk & 1) * 16)) & 0xFFFFu); },
+                L - t0, wmax - t0);
+      }
+    } else if (!tripped) {
       const int L = live ? (int)a.len[p] : 0;
       int wmax = L;
 #pragma unroll
@@ -719,35 +778,8 @@ __global__ void __launch_bounds__(224, 3)
           phase ^= 1u << b;
           inflight &= ~(1u << b);
           if (wrem > 0) {
-            const int rem = L - t * kClusterTileSlots;
             const uint16_t* tl = tiles + b * tile_elems + col;
-            // even and odd slots in two sums: two independent FMA chains
-            float ax = 0.f, ay = 0.f, az = 0.f, bx = 0.f, by = 0.f, bz = 0.f;
-            if (wrem >= kClusterTileSlots) {
-#pragma unroll
-              for (int kk = 0; kk < kClusterTileSlots; kk += 2) {
-                const bool v0 = kk < rem, v1 = kk + 1 < rem;
-                const int q0 = v0 ? (int)tl[kk * BX] : self;
-                const int q1 = v1 ? (int)tl[(kk + 1) * BX] : self;
-                pair(q0, v0, ax, ay, az);
-                pair(q1, v1, bx, by, bz);
-              }
-            } else {
-#pragma unroll
-              for (int kk = 0; kk < kClusterTileSlots; kk++) {
-                if (kk < wrem) {
-                  const bool valid = kk < rem;
-                  const int q = valid ? (int)tl[kk * BX] : self;
-                  if (kk & 1)
-                    pair(q, valid, bx, by, bz);
-                  else
-                    pair(q, valid, ax, ay, az);
-                }
-              }
-            }
-            kahan_add(hx, lx, ax + bx);
-            kahan_add(hy, ly, ay + by);
-            kahan_add(hz, lz, az + bz);
+            chunk16([&](int kk) { return (int)tl[kk * BX]; }, L - t * kClusterTileSlots, wrem);
           }
         }
         // everyone is done with buffer b (and every wait succeeded)
@@ -1089,12 +1121,18 @@ int cluster_build(ClusterList& cl, const std::vector<ClusterReplica>& reps_in, f
     allow_smem(k_cl_rows<0>);
     allow_smem(k_cl_rows<1>);
     allow_smem(k_cl_rows<2>);
-    allow_smem(k_lj_cl<false, false, false>);
-    allow_smem(k_lj_cl<false, true, false>);
-    allow_smem(k_lj_cl<true, false, false>);
-    allow_smem(k_lj_cl<true, true, false>);
-    allow_smem(k_lj_cl<false, false, true>);
-    allow_smem(k_lj_cl<false, true, true>);
+    allow_smem(k_lj_cl<false, false, false, true>);
+    allow_smem(k_lj_cl<false, true, false, true>);
+    allow_smem(k_lj_cl<true, false, false, true>);
+    allow_smem(k_lj_cl<true, true, false, true>);
+    allow_smem(k_lj_cl<false, false, true, true>);
+    allow_smem(k_lj_cl<false, true, true, true>);
+    allow_smem(k_lj_cl<false, false, false, false>);
+    allow_smem(k_lj_cl<false, true, false, false>);
+    allow_smem(k_lj_cl<true, false, false, false>);
+    allow_smem(k_lj_cl<true, true, false, false>);
+    allow_smem(k_lj_cl<false, false, true, false>);
+    allow_smem(k_lj_cl<false, true, true, false>);
     attrs = true;
   }
   const float margin = (float)(1e-6 * (reps.empty() ? 0.0 : reps.back().L + rv) + 1e-6);
@@ -1151,8 +1189,9 @@ int cluster_build(ClusterList& cl, const std::vector<ClusterReplica>& reps_in, f
 void launch_lj_cluster(const ClusterForceArgs& f, bool energy, cudaStream_t st) {
   const ClusterList& cl = *f.cl;
   if (cl.nseg == 0) return;
-  const size_t smem = 2 * kClusterTileSlots * (size_t)(cl.block + 8) * sizeof(uint16_t) +
-                      stage_bytes(cl.max_staged);
+  const size_t smem =
+      (cl.tma_rows ? 2 * kClusterTileSlots * (size_t)(cl.block + 8) * sizeof(uint16_t) : 0) +
+      stage_bytes(cl.max_staged);
   ClStep a;
   a.nseg = cl.nseg;
   a.sched = cl.sched;
@@ -1195,17 +1234,23 @@ void launch_lj_cluster(const ClusterForceArgs& f, bool energy, cudaStream_t st) 
       per_sm = 1;
     return std::min(cl.nseg, sms * per_sm);
   };
-#define MDGB_CL_LAUNCH(E, A, G)                                                            \
-  k_lj_cl<E, A, G><<<grid_for((const void*)k_lj_cl<E, A, G>), cl.block, smem, st>>>(cl.rmap, \
-                                                                                      a)
+#define MDGB_CL_LAUNCH2(E, A, G, T)                                                         \
+  k_lj_cl<E, A, G, T><<<grid_for((const void*)k_lj_cl<E, A, G, T>), cl.block, smem, st>>>( \
+      cl.rmap, a)
+#define MDGB_CL_LAUNCH(E, A, G)          \
+  if (cl.tma_rows)                       \
+    MDGB_CL_LAUNCH2(E, A, G, true);      \
+  else                                   \
+    MDGB_CL_LAUNCH2(E, A, G, false)
   if (energy) {
-    if (f.all_ng) MDGB_CL_LAUNCH(true, true, false); else MDGB_CL_LAUNCH(true, false, false);
+    if (f.all_ng) { MDGB_CL_LAUNCH(true, true, false); } else { MDGB_CL_LAUNCH(true, false, false); }
   } else if (f.gear) {
-    if (f.all_ng) MDGB_CL_LAUNCH(false, true, true); else MDGB_CL_LAUNCH(false, false, true);
+    if (f.all_ng) { MDGB_CL_LAUNCH(false, true, true); } else { MDGB_CL_LAUNCH(false, false, true); }
   } else {
-    if (f.all_ng) MDGB_CL_LAUNCH(false, true, false); else MDGB_CL_LAUNCH(false, false, false);
+    if (f.all_ng) { MDGB_CL_LAUNCH(false, true, false); } else { MDGB_CL_LAUNCH(false, false, false); }
   }
 #undef MDGB_CL_LAUNCH
+#undef MDGB_CL_LAUNCH2
 }
 
 int cluster_reference_rows(const ClusterList& cl, const md_double4* pos, int nlistsize,

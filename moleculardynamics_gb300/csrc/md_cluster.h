@@ -84,6 +84,7 @@ struct ClusterList {
   int Z = kClusterMaxZ;                           // cells per segment (upper bound)
   int block = 128;                                // threads per segment block (<= 224)
   int stage_cap = kClusterMaxStaged;              // staged atoms per segment (soft cap)
+  bool tma_rows = true;                           // row tiles by TMA (else register prefetch)
   CUtensorMap rmap;                               // TMA map of rows: {ld atoms, cap slots}
   int rmap_ok = 0;
   int* counters = nullptr;                        // device: max staged, max len, entries, max cell

@@ -835,6 +835,7 @@ md_status md_create(const md_config* cfg, md_ctx** out) {
   if (cfg->cluster_cells < 0 || cfg->cluster_cells > kClusterMaxZ) return MD_BAD_CONFIG;
   if (cfg->cluster_threads < 0 || cfg->cluster_threads > 224 || cfg->cluster_threads % 32)
     return MD_BAD_CONFIG;
+  if (cfg->cluster_row_loads < 0 || cfg->cluster_row_loads > 2) return MD_BAD_CONFIG;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= cfg->device || cfg->device < 0)
     return MD_NO_DEVICE;
@@ -844,6 +845,7 @@ md_status md_create(const md_config* cfg, md_ctx** out) {
   c->graphs = c->cluster;
   if (cfg->cluster_cells > 0) c->cl.Z = cfg->cluster_cells;
   if (cfg->cluster_threads > 0) c->cl.block = cfg->cluster_threads;
+  if (cfg->cluster_row_loads > 0) c->cl.tma_rows = cfg->cluster_row_loads == 1;
   c->n = (int)n;
   c->sp = species_table(cfg->species);
   c->gear = gear_coef((double)cfg->dt);
@@ -1179,16 +1181,20 @@ md_status md_autotune(md_ctx* c, int evals, md_tune_result* out) {
   std::vector<int> threads = fixed_threads ? std::vector<int>{c->cl.block}
                                            : std::vector<int>{64, 96, 128, 160, 192};
   const std::vector<int> caps = {1152, 1536, kClusterMaxStaged};
+  const std::vector<int> loads = c->cfg.cluster_row_loads > 0
+                                     ? std::vector<int>{c->cfg.cluster_row_loads}
+                                     : std::vector<int>{1, 2};
   cudaEvent_t e0, e1;
   CK(cudaEventCreate(&e0), "autotune");
   CK(cudaEventCreate(&e1), "autotune");
   double best = 1e300;
-  int best_t = c->cl.block, best_c = c->cl.stage_cap, tried = 0;
+  int best_t = c->cl.block, best_c = c->cl.stage_cap, best_l = c->cl.tma_rows ? 1 : 2, tried = 0;
   std::vector<ClusterReplica> reps = cluster_reps(c);
   double** v3[5] = {&c->vel, &c->acc, &c->b, &c->c, &c->f3};
-  auto build = [&](int t, int cap) -> md_status {
+  auto build = [&](int t, int cap, int ld) -> md_status {
     c->cl.block = t;
     c->cl.stage_cap = cap;
+    c->cl.tma_rows = ld == 1;
     std::string e;
     int r = cluster_build(c->cl, reps, c->cfg.lj_rs, sqrt((double)c->lj_rcutsq), &c->pos, v3,
                           c->posf, c->sc, c->status, c->st, e);
@@ -1197,9 +1203,13 @@ md_status md_autotune(md_ctx* c, int evals, md_tune_result* out) {
     return MD_OK;
   };
   md_status s = MD_OK;
-  for (int t : threads)
-    for (int cap : caps) {
-      if ((s = build(t, cap)) != MD_OK) break;
+  std::vector<int3> cand;
+  for (int ld : loads)
+    for (int t : threads)
+      for (int cap : caps) cand.push_back(make_int3(ld, t, cap));
+  for (const int3& k3 : cand) {
+      const int ld = k3.x, t = k3.y, cap = k3.z;
+      if ((s = build(t, cap, ld)) != MD_OK) break;
       launch_lj_cluster(cl_args(c, c->f3_tmp, nullptr), false, c->st);  // warm
       cudaEventRecord(e0, c->st);
       for (int k = 0; k < evals; k++)
@@ -1217,17 +1227,19 @@ md_status md_autotune(md_ctx* c, int evals, md_tune_result* out) {
         best = ms;
         best_t = t;
         best_c = cap;
+        best_l = ld;
       }
     }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (s != MD_OK) return s;
-  if ((s = build(best_t, best_c)) != MD_OK) return s;
+  if ((s = build(best_t, best_c, best_l)) != MD_OK) return s;
   c->stats.cluster_segments = c->cl.nseg;
   c->stats.cluster_max_staged = c->cl.max_staged;
   if (out) {
     out->threads = best_t;
     out->stage_cap = best_c;
+    out->row_loads = best_l;
     out->candidates = tried;
     out->best_ms = best / evals;
   }
