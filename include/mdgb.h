@@ -73,8 +73,9 @@ typedef struct md_config {
   int lj_kernel;           /* MD_LJ_AUTO, MD_LJ_ROWS or MD_LJ_CLUSTER (precision form) */
   int cluster_cells;       /* cells per segment of the cluster kernel (0: default) */
   int cluster_threads;     /* threads per segment block (0: default; multiple of 32, <= 224) */
-  int cluster_row_loads;   /* rows of the cluster kernel: 0 default / autotuned, 1 TMA tiles in
-                              shared memory, 2 per-lane register prefetch */
+  int cluster_row_loads;   /* rows of the cluster kernel: 0 default / autotuned, 1 TMA tiles of
+                              the block in shared memory, 2 per-lane register prefetch, 3 TMA
+                              tiles of each warp */
 } md_config;
 
 /* LJ kernel of the precision form.  ROWS: compact rows of packed atom
@@ -174,7 +175,7 @@ md_status md_kernel_time(const md_ctx* ctx, int kernel, double* total_ms, long l
 typedef struct md_tune_result {
   int threads;             /* threads per segment block */
   int stage_cap;           /* staged atoms per segment (cap of the column cut) */
-  int row_loads;           /* 1 TMA tiles, 2 register prefetch */
+  int row_loads;           /* 1 block TMA tiles, 2 register prefetch, 3 warp TMA tiles */
   int candidates;          /* configurations timed */
   double best_ms;          /* force evaluation time of the choice */
 } md_tune_result;

@@ -588,17 +588,25 @@ struct ClStep {
 // atom in the same thread (cpu/common/Device.cpp:17-85 in FP64 with FMAs).
 // Dynamic shared memory: two row tiles [16][blockDim + 8] of uint16 (TMA
 // destinations), then the staged positions.
-// TMA_ROWS: row tiles by TMA into shared memory (block-synchronised); else
-// each lane prefetches its next 16 row entries into registers (no barriers)
-template <bool ENERGY, bool ALL_NG, bool GEAR, bool TMA_ROWS>
+// Row loads: ROWS 0, tiles of the whole block by TMA into shared memory
+// (block-synchronised); 1, each lane prefetches its next 16 entries into
+// registers; 2, tiles of each warp by TMA (warp-synchronised, each warp
+// walks only its own longest row)
+constexpr int kWarpTileAtoms = 40;  // 32 atoms + up to 8 for the 16-byte start
+constexpr int kWarpTileBytes = kWarpTileAtoms * kClusterTileSlots * 2;
+
+template <bool ENERGY, bool ALL_NG, bool GEAR, int ROWS>
 __global__ void __launch_bounds__(224, 3)
     k_lj_cl(const __grid_constant__ CUtensorMap rmap, const ClStep a) {
   extern __shared__ __align__(128) unsigned char dyn[];
   const int tid = threadIdx.x;
   const int BX = blockDim.x + 8;
   uint16_t* tiles = (uint16_t*)dyn;
-  float4* st =
-      (float4*)(dyn + (TMA_ROWS ? 2 * kClusterTileSlots * BX * sizeof(uint16_t) : 0));
+  const int tile_region =
+      ROWS == 0 ? 2 * kClusterTileSlots * BX * (int)sizeof(uint16_t)
+                : (ROWS == 2 ? (int)(blockDim.x >> 5) * 2 * kWarpTileBytes : 0);
+  float4* st = (float4*)(dyn + tile_region);
+  __shared__ __align__(8) uint64_t wbar[7][2];  // ROWS 2: two tile barriers per warp
   __shared__ SegShared sh;
   __shared__ __align__(8) uint64_t bar[3];  // two row tiles, staging
   __shared__ int s_max[8];
@@ -608,6 +616,11 @@ __global__ void __launch_bounds__(224, 3)
     mbar_init(&bar[0], 1);
     mbar_init(&bar[1], 1);
     mbar_init(&bar[2], 1);
+    if (ROWS == 2)
+      for (int w = 0; w < (int)(blockDim.x >> 5); w++) {
+        mbar_init(&wbar[w][0], 1);
+        mbar_init(&wbar[w][1], 1);
+      }
     fence_mbar_init();
   }
   __syncthreads();
@@ -722,7 +735,59 @@ __global__ void __launch_bounds__(224, 3)
       kahan_add(hy, ly, ay + by);
       kahan_add(hz, lz, az + bz);
     };
-    if (!tripped && !TMA_ROWS) {
+    if (!tripped && ROWS == 2) {
+      const int warp = tid >> 5, lane = tid & 31;
+      const int L = live ? (int)a.len[p] : 0;
+      int wmax = L;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) wmax = max(wmax, __shfl_xor_sync(0xffffffffu, wmax, o));
+      const int Tw = (wmax + kClusterTileSlots - 1) / kClusterTileSlots;
+      const int wb = base + 32 * warp;
+      const int x0 = wb & ~7;  // 16-byte aligned start of the warp's tile
+      const int col = lane + (wb - x0);
+      uint16_t* wt = (uint16_t*)(dyn + (size_t)warp * 2 * kWarpTileBytes);
+      uint64_t* wb2 = wbar[warp];
+      if (lane == 0) {
+        for (int t = 0; t < 2 && t < Tw; t++) {
+          fence_proxy_async();
+          mbar_expect_tx(&wb2[t], kWarpTileBytes);
+          tma_load_2d(wt + t * (kWarpTileBytes / 2), &rmap, x0, t * kClusterTileSlots, &wb2[t]);
+          inflight |= 1u << t;
+        }
+      }
+      __syncwarp();
+      bool wfailed = false;
+      for (int t = 0; t < Tw; t++) {
+        const int b = t & 1;
+        const bool got = __all_sync(0xffffffffu, mbar_wait(&wb2[b], (phase >> b) & 1u, a.status));
+        if (!got) {
+          wfailed = true;
+          break;
+        }
+        phase ^= 1u << b;
+        inflight &= ~(1u << b);
+        const uint16_t* tl = wt + b * (kWarpTileBytes / 2) + col;
+        chunk16([&](int kk) { return (int)tl[kk * kWarpTileAtoms]; }, L - t * kClusterTileSlots,
+                wmax - t * kClusterTileSlots);
+        __syncwarp();  // the warp is done with buffer b
+        if (lane == 0 && t + 2 < Tw) {
+          fence_proxy_async();
+          mbar_expect_tx(&wb2[b], kWarpTileBytes);
+          tma_load_2d(wt + b * (kWarpTileBytes / 2), &rmap, x0, (t + 2) * kClusterTileSlots,
+                      &wb2[b]);
+          inflight |= 1u << b;
+        }
+      }
+      if (!__syncthreads_and(!wfailed)) {
+        // a bounded wait ran out somewhere: copies still in flight land (or
+        // time out) before the block leaves
+        if (lane == 0)
+          for (int b = 0; b < 2; b++)
+            if ((inflight >> b) & 1u) mbar_wait(&wb2[b], (phase >> b) & 1u, a.status);
+        aborted = true;
+        break;
+      }
+    } else if (!tripped && ROWS == 1) {
       const int L = live ? (int)a.len[p] : 0;
       int wmax = L;
 #pragma unroll
@@ -1121,18 +1186,24 @@ int cluster_build(ClusterList& cl, const std::vector<ClusterReplica>& reps_in, f
     allow_smem(k_cl_rows<0>);
     allow_smem(k_cl_rows<1>);
     allow_smem(k_cl_rows<2>);
-    allow_smem(k_lj_cl<false, false, false, true>);
-    allow_smem(k_lj_cl<false, true, false, true>);
-    allow_smem(k_lj_cl<true, false, false, true>);
-    allow_smem(k_lj_cl<true, true, false, true>);
-    allow_smem(k_lj_cl<false, false, true, true>);
-    allow_smem(k_lj_cl<false, true, true, true>);
-    allow_smem(k_lj_cl<false, false, false, false>);
-    allow_smem(k_lj_cl<false, true, false, false>);
-    allow_smem(k_lj_cl<true, false, false, false>);
-    allow_smem(k_lj_cl<true, true, false, false>);
-    allow_smem(k_lj_cl<false, false, true, false>);
-    allow_smem(k_lj_cl<false, true, true, false>);
+    allow_smem(k_lj_cl<false, false, false, 0>);
+    allow_smem(k_lj_cl<false, true, false, 0>);
+    allow_smem(k_lj_cl<true, false, false, 0>);
+    allow_smem(k_lj_cl<true, true, false, 0>);
+    allow_smem(k_lj_cl<false, false, true, 0>);
+    allow_smem(k_lj_cl<false, true, true, 0>);
+    allow_smem(k_lj_cl<false, false, false, 1>);
+    allow_smem(k_lj_cl<false, true, false, 1>);
+    allow_smem(k_lj_cl<true, false, false, 1>);
+    allow_smem(k_lj_cl<true, true, false, 1>);
+    allow_smem(k_lj_cl<false, false, true, 1>);
+    allow_smem(k_lj_cl<false, true, true, 1>);
+    allow_smem(k_lj_cl<false, false, false, 2>);
+    allow_smem(k_lj_cl<false, true, false, 2>);
+    allow_smem(k_lj_cl<true, false, false, 2>);
+    allow_smem(k_lj_cl<true, true, false, 2>);
+    allow_smem(k_lj_cl<false, false, true, 2>);
+    allow_smem(k_lj_cl<false, true, true, 2>);
     attrs = true;
   }
   const float margin = (float)(1e-6 * (reps.empty() ? 0.0 : reps.back().L + rv) + 1e-6);
@@ -1172,7 +1243,10 @@ int cluster_build(ClusterList& cl, const std::vector<ClusterReplica>& reps_in, f
   }
   cl.rmap_ok = encode_tiled_2d(&cl.rmap, CU_TENSOR_MAP_DATA_TYPE_UINT16, cl.rows,
                                (uint64_t)cl.ld, (uint64_t)cl.cap, (uint64_t)cl.ld * 2,
-                               (uint32_t)(cl.block + 8), (uint32_t)kClusterTileSlots);
+                               (uint32_t)(cl.block + 8), (uint32_t)kClusterTileSlots) &&
+               encode_tiled_2d(&cl.rmap_w, CU_TENSOR_MAP_DATA_TYPE_UINT16, cl.rows,
+                               (uint64_t)cl.ld, (uint64_t)cl.cap, (uint64_t)cl.ld * 2,
+                               (uint32_t)kWarpTileAtoms, (uint32_t)kClusterTileSlots);
   if (!cl.rmap_ok) {
     err = "TMA descriptor of the cluster rows could not be encoded";
     return -1;
@@ -1189,9 +1263,10 @@ int cluster_build(ClusterList& cl, const std::vector<ClusterReplica>& reps_in, f
 void launch_lj_cluster(const ClusterForceArgs& f, bool energy, cudaStream_t st) {
   const ClusterList& cl = *f.cl;
   if (cl.nseg == 0) return;
-  const size_t smem =
-      (cl.tma_rows ? 2 * kClusterTileSlots * (size_t)(cl.block + 8) * sizeof(uint16_t) : 0) +
-      stage_bytes(cl.max_staged);
+  const size_t tiles =
+      cl.row_loads == 1 ? 2 * kClusterTileSlots * (size_t)(cl.block + 8) * sizeof(uint16_t)
+                        : (cl.row_loads == 3 ? (size_t)(cl.block / 32) * 2 * kWarpTileBytes : 0);
+  const size_t smem = tiles + stage_bytes(cl.max_staged);
   ClStep a;
   a.nseg = cl.nseg;
   a.sched = cl.sched;
@@ -1234,14 +1309,16 @@ void launch_lj_cluster(const ClusterForceArgs& f, bool energy, cudaStream_t st) 
       per_sm = 1;
     return std::min(cl.nseg, sms * per_sm);
   };
-#define MDGB_CL_LAUNCH2(E, A, G, T)                                                         \
+#define MDGB_CL_LAUNCH2(E, A, G, T, M)                                                      \
   k_lj_cl<E, A, G, T><<<grid_for((const void*)k_lj_cl<E, A, G, T>), cl.block, smem, st>>>( \
-      cl.rmap, a)
-#define MDGB_CL_LAUNCH(E, A, G)          \
-  if (cl.tma_rows)                       \
-    MDGB_CL_LAUNCH2(E, A, G, true);      \
-  else                                   \
-    MDGB_CL_LAUNCH2(E, A, G, false)
+      M, a)
+#define MDGB_CL_LAUNCH(E, A, G)                  \
+  if (cl.row_loads == 1)                         \
+    MDGB_CL_LAUNCH2(E, A, G, 0, cl.rmap);        \
+  else if (cl.row_loads == 3)                    \
+    MDGB_CL_LAUNCH2(E, A, G, 2, cl.rmap_w);      \
+  else                                           \
+    MDGB_CL_LAUNCH2(E, A, G, 1, cl.rmap)
   if (energy) {
     if (f.all_ng) { MDGB_CL_LAUNCH(true, true, false); } else { MDGB_CL_LAUNCH(true, false, false); }
   } else if (f.gear) {

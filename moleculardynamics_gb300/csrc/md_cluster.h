@@ -84,8 +84,10 @@ struct ClusterList {
   int Z = kClusterMaxZ;                           // cells per segment (upper bound)
   int block = 128;                                // threads per segment block (<= 224)
   int stage_cap = kClusterMaxStaged;              // staged atoms per segment (soft cap)
-  bool tma_rows = true;                           // row tiles by TMA (else register prefetch)
+  int row_loads = 1;                              // 1 block TMA tiles, 2 register prefetch,
+                                                  // 3 per-warp TMA tiles
   CUtensorMap rmap;                               // TMA map of rows: {ld atoms, cap slots}
+  CUtensorMap rmap_w;                             // the same with per-warp boxes
   int rmap_ok = 0;
   int* counters = nullptr;                        // device: max staged, max len, entries, max cell
   int* sched = nullptr;                           // device: persistent kernel's work counters

@@ -835,7 +835,7 @@ md_status md_create(const md_config* cfg, md_ctx** out) {
   if (cfg->cluster_cells < 0 || cfg->cluster_cells > kClusterMaxZ) return MD_BAD_CONFIG;
   if (cfg->cluster_threads < 0 || cfg->cluster_threads > 224 || cfg->cluster_threads % 32)
     return MD_BAD_CONFIG;
-  if (cfg->cluster_row_loads < 0 || cfg->cluster_row_loads > 2) return MD_BAD_CONFIG;
+  if (cfg->cluster_row_loads < 0 || cfg->cluster_row_loads > 3) return MD_BAD_CONFIG;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= cfg->device || cfg->device < 0)
     return MD_NO_DEVICE;
@@ -845,7 +845,7 @@ md_status md_create(const md_config* cfg, md_ctx** out) {
   c->graphs = c->cluster;
   if (cfg->cluster_cells > 0) c->cl.Z = cfg->cluster_cells;
   if (cfg->cluster_threads > 0) c->cl.block = cfg->cluster_threads;
-  if (cfg->cluster_row_loads > 0) c->cl.tma_rows = cfg->cluster_row_loads == 1;
+  if (cfg->cluster_row_loads > 0) c->cl.row_loads = cfg->cluster_row_loads;
   c->n = (int)n;
   c->sp = species_table(cfg->species);
   c->gear = gear_coef((double)cfg->dt);
@@ -1183,18 +1183,18 @@ md_status md_autotune(md_ctx* c, int evals, md_tune_result* out) {
   const std::vector<int> caps = {1152, 1536, kClusterMaxStaged};
   const std::vector<int> loads = c->cfg.cluster_row_loads > 0
                                      ? std::vector<int>{c->cfg.cluster_row_loads}
-                                     : std::vector<int>{1, 2};
+                                     : std::vector<int>{1, 2, 3};
   cudaEvent_t e0, e1;
   CK(cudaEventCreate(&e0), "autotune");
   CK(cudaEventCreate(&e1), "autotune");
   double best = 1e300;
-  int best_t = c->cl.block, best_c = c->cl.stage_cap, best_l = c->cl.tma_rows ? 1 : 2, tried = 0;
+  int best_t = c->cl.block, best_c = c->cl.stage_cap, best_l = c->cl.row_loads, tried = 0;
   std::vector<ClusterReplica> reps = cluster_reps(c);
   double** v3[5] = {&c->vel, &c->acc, &c->b, &c->c, &c->f3};
   auto build = [&](int t, int cap, int ld) -> md_status {
     c->cl.block = t;
     c->cl.stage_cap = cap;
-    c->cl.tma_rows = ld == 1;
+    c->cl.row_loads = ld;
     std::string e;
     int r = cluster_build(c->cl, reps, c->cfg.lj_rs, sqrt((double)c->lj_rcutsq), &c->pos, v3,
                           c->posf, c->sc, c->status, c->st, e);

@@ -205,6 +205,7 @@ __global__ void __launch_bounds__(128)
   float g[kDesc];
   for (int f = 0; f < kDesc; f++) g[f] = gcoef[(size_t)i * kDesc + f];
   float fc[kSgMax], dfc[kSgMax];
+  float3 fn[kSgMax];  // force on each neighbour from atom i's energy, added once at the end
   float fix = 0.f, fiy = 0.f, fiz = 0.f;
   for (int s = 0; s < S; s++) {
     fcut(r[s], P.rc, fc[s], dfc[s]);
@@ -217,9 +218,7 @@ __global__ void __launch_bounds__(128)
     const float ir = 1.f / r[s];
     const float gx = sum * d[s].x * ir, gy = sum * d[s].y * ir, gz = sum * d[s].z * ir;
     // dG/dr_j = +grad, dG/dr_i = -grad; F = -dE/dr
-    atomicAdd(&F32[3 * idx[s]], -gx);
-    atomicAdd(&F32[3 * idx[s] + 1], -gy);
-    atomicAdd(&F32[3 * idx[s] + 2], -gz);
+    fn[s] = make_float3(-gx, -gy, -gz);
     fix += gx;
     fiy += gy;
     fiz += gz;
@@ -254,16 +253,21 @@ __global__ void __launch_bounds__(128)
       ajx += gax;
       ajy += gay;
       ajz += gaz;
-      atomicAdd(&F32[3 * idx[b]], -gbx);
-      atomicAdd(&F32[3 * idx[b] + 1], -gby);
-      atomicAdd(&F32[3 * idx[b] + 2], -gbz);
+      fn[b].x -= gbx;
+      fn[b].y -= gby;
+      fn[b].z -= gbz;
       fix += gax + gbx;
       fiy += gay + gby;
       fiz += gaz + gbz;
     }
-    atomicAdd(&F32[3 * idx[a]], -ajx);
-    atomicAdd(&F32[3 * idx[a] + 1], -ajy);
-    atomicAdd(&F32[3 * idx[a] + 2], -ajz);
+    fn[a].x -= ajx;
+    fn[a].y -= ajy;
+    fn[a].z -= ajz;
+  }
+  for (int s = 0; s < S; s++) {
+    atomicAdd(&F32[3 * idx[s]], fn[s].x);
+    atomicAdd(&F32[3 * idx[s] + 1], fn[s].y);
+    atomicAdd(&F32[3 * idx[s] + 2], fn[s].z);
   }
   atomicAdd(&F32[3 * i], fix);
   atomicAdd(&F32[3 * i + 1], fiy);
