@@ -83,6 +83,7 @@ DescParams default_desc(float rc) {
   const float d = (rc - 0.8f) / (kRad - 1);
   P.eta_r = 0.5f / (d * d);
   for (int k = 0; k < kRad; k++) P.rs[k] = 0.8f + d * k;
+  // the kernels rely on this layout (ang_pair): f = 8 e + 4 l + z
   const int zetas[4] = {1, 2, 4, 16};
   const float etas[2] = {0.02f, 0.25f};
   for (int f = 0; f < kAng; f++) {
@@ -102,36 +103,97 @@ __device__ __forceinline__ void fcut(float r, float rc, float& fc, float& dfc) {
   dfc = -0.5f * a * s;
 }
 
-__device__ __forceinline__ float ipow(float b, int z) {
-  float r = 1.f;
-  for (int k = 0; k < z; k++) r *= b;
-  return r;
+// Angular factors of one neighbour pair for the 16 functions f = 8 e + 4 l + z
+// of default_desc's table (eta index e, lambda index l for +1 / -1, zeta index
+// z for 1, 2, 4, 16): powers of both bases by squaring and one exponential
+// per eta, instead of 16 of each.
+struct AngPair {
+  float b[2];        // 1 + lambda cos
+  float pz[2][4];    // b ^ zeta
+  float pz1[2][4];   // b ^ (zeta - 1)
+  float ex[2];       // exp(-eta q)
+};
+
+__device__ __forceinline__ void ang_pair(float c, float q, const DescParams& P, AngPair& A) {
+#pragma unroll
+  for (int l = 0; l < 2; l++) {
+    const float b = l ? 1.f - c : 1.f + c;
+    const float p2 = b * b, p4 = p2 * p2, p8 = p4 * p4;
+    A.b[l] = b;
+    A.pz[l][0] = b;
+    A.pz[l][1] = p2;
+    A.pz[l][2] = p4;
+    A.pz[l][3] = p8 * p8;
+    A.pz1[l][0] = 1.f;
+    A.pz1[l][1] = b;
+    A.pz1[l][2] = p2 * b;
+    A.pz1[l][3] = p8 * p4 * p2 * b;
+  }
+  A.ex[0] = __expf(-P.eta_a[0] * q);
+  A.ex[1] = __expf(-P.eta_a[8] * q);
 }
 
-// neighbours of i within rc (from the bond-order candidate rows), as
-// packed entries with their periodic image
-__global__ void k_sg_short(const md_double4* __restrict__ pos, RowWalker w, float rc,
-                           uint32_t* __restrict__ sl, int* __restrict__ slen,
-                           int* __restrict__ status) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= w.n) return;
-  const md_double4 pi = pos[i];
-  const double rc2 = (double)rc * rc;
+// neighbours of i within rc (from the bond-order candidate rows: the 27
+// build-time cells around i, as walk_row visits them), as packed entries
+// with their periodic image; one warp per atom, lanes over a cell's atoms,
+// kept entries compacted in candidate order with a ballot
+// (distances in FP32 from an FP32 copy of the positions: a neighbour at the
+// cutoff enters the descriptors with weight fc(rc) = 0 either way)
+__global__ void __launch_bounds__(128)
+    k_sg_short(const float4* __restrict__ pos, RowWalker w, float rc,
+               uint32_t* __restrict__ sl, int* __restrict__ slen, int* __restrict__ status) {
+  const int lane = threadIdx.x & 31;
+  const int i = blockIdx.x * 4 + (threadIdx.x >> 5);
+  if (i >= w.n) return;  // whole warp
+  const float4 pi = pos[i];
+  const float rc2 = rc * rc;
+  const float boxf = (float)w.g.box;
+  const int cx = w.cell3[3 * i], cy = w.cell3[3 * i + 1], cz = w.cell3[3 * i + 2];
+  const int cells = w.g.cells;
   int cnt = 0;
-  walk_row(w, pos, i, [&](int m, int ix, int iy, int iz) {
-    const md_double4 pm = pos[m];
-    const double dx = pm.x + ix * w.g.box - pi.x, dy = pm.y + iy * w.g.box - pi.y,
-                 dz = pm.z + iz * w.g.box - pi.z;
-    if (dx * dx + dy * dy + dz * dz < rc2) {
-      if (cnt < kSgMax) sl[(size_t)i * kSgMax + cnt] = pack_entry(m, ix, iy, iz);
-      cnt++;
-    }
-  });
-  if (cnt > kSgMax) {
-    atomicOr(status, ST_CELL_OVERFLOW);
-    cnt = kSgMax;
+  for (int dx = -1; dx < 2; dx++)
+    for (int dy = -1; dy < 2; dy++)
+      for (int dz = -1; dz < 2; dz++) {
+        int nc[3] = {cx + dx, cy + dy, cz + dz};
+        int im[3] = {0, 0, 0};
+        bool out = false;
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+          if (!w.g.periodic) {
+            if (nc[d] >= cells || nc[d] < 0) out = true;
+          } else {
+            if (nc[d] < 0) { nc[d] += cells; im[d] = -1; }
+            if (nc[d] >= cells) { nc[d] -= cells; im[d] = 1; }
+          }
+        }
+        if (out) continue;
+        const int slot = table_find(w.keys, w.cap, cell_key(nc[0], nc[1], nc[2]));
+        if (slot < 0) continue;
+        const int a = w.start[slot], b = a + w.count[slot];
+        for (int q0 = a; q0 < b; q0 += 32) {
+          const int q = q0 + lane;
+          bool keep = false;
+          int m = 0;
+          if (q < b) {
+            m = w.sorted[q];
+            if (m != i) {
+              const float4 pm = pos[m];
+              const float ddx = fmaf((float)im[0], boxf, pm.x) - pi.x;
+              const float ddy = fmaf((float)im[1], boxf, pm.y) - pi.y;
+              const float ddz = fmaf((float)im[2], boxf, pm.z) - pi.z;
+              keep = ddx * ddx + ddy * ddy + ddz * ddz < rc2;
+            }
+          }
+          const unsigned mask = __ballot_sync(0xffffffffu, keep);
+          const int at = cnt + __popc(mask & ((1u << lane) - 1u));
+          if (keep && at < kSgMax) sl[(size_t)i * kSgMax + at] = pack_entry(m, im[0], im[1], im[2]);
+          cnt += __popc(mask);
+        }
+      }
+  if (lane == 0) {
+    if (cnt > kSgMax) atomicOr(status, ST_CELL_OVERFLOW);
+    slen[i] = cnt < kSgMax ? cnt : kSgMax;
   }
-  slen[i] = cnt;
 }
 
 // offsets d_j = r_j - r_i (FP32) of i's neighbours
@@ -154,124 +216,210 @@ __device__ __forceinline__ int load_nbrs(int i, const md_double4* pos, const uin
   return S;
 }
 
-// descriptors of atom i; out: normalised (G - mean) * istd, or raw G
+// ---- warp-per-atom descriptor and force kernels (4 atoms per block) ----
+struct NbrSm {
+  float dx[kSgMax], dy[kSgMax], dz[kSgMax], r[kSgMax], fc[kSgMax], dfc[kSgMax];
+  int idx[kSgMax];
+};
+
+// neighbours of atom i into the warp's shared arrays; returns their count
+__device__ __forceinline__ int warp_load_nbrs(int i, const md_double4* pos, const uint32_t* sl,
+                                              const int* slen, double box, float rc,
+                                              NbrSm& N) {
+  const int lane = threadIdx.x & 31;
+  const md_double4 pi = pos[i];
+  const int S = slen[i];
+  for (int s = lane; s < S; s += 32) {
+    const uint32_t e = sl[(size_t)i * kSgMax + s];
+    const int j = entry_index(e);
+    const md_double4 pj = pos[j];
+    const float dx = (float)(pj.x + entry_img(e, 0) * box - pi.x);
+    const float dy = (float)(pj.y + entry_img(e, 1) * box - pi.y);
+    const float dz = (float)(pj.z + entry_img(e, 2) * box - pi.z);
+    const float r = sqrtf(dx * dx + dy * dy + dz * dz);
+    float fc, dfc;
+    fcut(r, rc, fc, dfc);
+    N.dx[s] = dx;
+    N.dy[s] = dy;
+    N.dz[s] = dz;
+    N.r[s] = r;
+    N.fc[s] = fc;
+    N.dfc[s] = dfc;
+    N.idx[s] = j;
+  }
+  __syncwarp();
+  return S;
+}
+
+// k-th pair (a < b) of S neighbours in row-major order
+__device__ __forceinline__ void pair_of(int k, int S, int& a, int& b) {
+  const int m = 2 * S - 1;
+  int aa = (int)(0.5f * ((float)m - sqrtf((float)(m * m - 8 * k))));
+  aa = max(0, min(aa, S - 2));
+  auto off = [&](int x) { return x * (2 * S - x - 1) / 2; };
+  while (aa > 0 && off(aa) > k) aa--;
+  while (aa + 1 <= S - 2 && off(aa + 1) <= k) aa++;
+  a = aa;
+  b = k - off(aa) + aa + 1;
+}
+
+// sum over the warp of 32 per-lane vectors: lane f ends with component f
+__device__ __forceinline__ float warp_reduce_scatter32(float (&v)[32]) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int o = 16, h = 16; o > 0; o >>= 1, h >>= 1) {
+    const bool up = (lane & o) != 0;
+#pragma unroll
+    for (int k = 0; k < h; k++) {
+      const float send = up ? v[k] : v[k + h];
+      const float keep = up ? v[k + h] : v[k];
+      v[k] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+    }
+  }
+  return v[0];
+}
+
+// descriptors of atom i (one warp); out: normalised (G - mean) * istd, or raw G
 __global__ void __launch_bounds__(128)
     k_sg_desc(const md_double4* __restrict__ pos, int n, const uint32_t* __restrict__ sl,
               const int* __restrict__ slen, double box, DescParams P,
               const float* __restrict__ mean, const float* __restrict__ istd,
               float* __restrict__ out) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  float3 d[kSgMax];
-  float r[kSgMax];
-  int idx[kSgMax];
-  const int S = load_nbrs(i, pos, sl, slen, box, d, r, idx);
-  float G[kDesc];
-  for (int f = 0; f < kDesc; f++) G[f] = 0.f;
-  float fc[kSgMax];
-  for (int s = 0; s < S; s++) {
-    float dfc;
-    fcut(r[s], P.rc, fc[s], dfc);
+  __shared__ NbrSm nb[4];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int i = blockIdx.x * 4 + warp;
+  if (i >= n) return;  // whole warp
+  NbrSm& N = nb[warp];
+  const int S = warp_load_nbrs(i, pos, sl, slen, box, P.rc, N);
+  float v[32];
+#pragma unroll
+  for (int f = 0; f < 32; f++) v[f] = 0.f;
+  for (int s = lane; s < S; s += 32) {
+#pragma unroll
     for (int k = 0; k < kRad; k++) {
-      const float t = r[s] - P.rs[k];
-      G[k] += __expf(-P.eta_r * t * t) * fc[s];
+      const float t = N.r[s] - P.rs[k];
+      v[k] += __expf(-P.eta_r * t * t) * N.fc[s];
     }
   }
-  for (int a = 0; a < S; a++)
-    for (int b = a + 1; b < S; b++) {
-      const float c = (d[a].x * d[b].x + d[a].y * d[b].y + d[a].z * d[b].z) / (r[a] * r[b]);
-      const float q = r[a] * r[a] + r[b] * r[b];
-      const float ff = fc[a] * fc[b];
-      for (int f = 0; f < kAng; f++) {
-        const float base = fmaxf(1.f + P.lam[f] * c, 0.f);
-        G[kRad + f] += P.pref[f] * ipow(base, P.zeta[f]) * __expf(-P.eta_a[f] * q) * ff;
-      }
+  const int npair = S * (S - 1) / 2;
+  for (int k = lane; k < npair; k += 32) {
+    int a, b;
+    pair_of(k, S, a, b);
+    const float c = (N.dx[a] * N.dx[b] + N.dy[a] * N.dy[b] + N.dz[a] * N.dz[b]) / (N.r[a] * N.r[b]);
+    const float q = N.r[a] * N.r[a] + N.r[b] * N.r[b];
+    const float ff = N.fc[a] * N.fc[b];
+    AngPair T;
+    ang_pair(c, q, P, T);
+#pragma unroll
+    for (int f = 0; f < kAng; f++) {
+      const int e = f >> 3, l = (f >> 2) & 1, z = f & 3;
+      const float pz = T.b[l] > 0.f ? T.pz[l][z] : 0.f;
+      v[kRad + f] += P.pref[f] * pz * T.ex[e] * ff;
     }
-  for (int f = 0; f < kDesc; f++)
-    out[(size_t)i * kDesc + f] = mean ? (G[f] - mean[f]) * istd[f] : G[f];
+  }
+  const float G = warp_reduce_scatter32(v);
+  out[(size_t)i * kDesc + lane] = mean ? (G - mean[lane]) * istd[lane] : G;
 }
 
-// forces from g_if = dE_i/dG_if (atomics into F32, n x 3 floats, zeroed)
+// forces from g_if = dE_i/dG_if (one warp per atom i; neighbour forces
+// gathered in shared memory, then one global atomic per neighbour)
 __global__ void __launch_bounds__(128)
     k_sg_force(const md_double4* __restrict__ pos, int n, const uint32_t* __restrict__ sl,
                const int* __restrict__ slen, double box, DescParams P,
                const float* __restrict__ gcoef, float* __restrict__ F32) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  float3 d[kSgMax];
-  float r[kSgMax];
-  int idx[kSgMax];
-  const int S = load_nbrs(i, pos, sl, slen, box, d, r, idx);
-  float g[kDesc];
-  for (int f = 0; f < kDesc; f++) g[f] = gcoef[(size_t)i * kDesc + f];
-  float fc[kSgMax], dfc[kSgMax];
-  float3 fn[kSgMax];  // force on each neighbour from atom i's energy, added once at the end
+  __shared__ NbrSm nb[4];
+  __shared__ float fn[4][3][kSgMax];
+  __shared__ float gs[4][kDesc];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int i = blockIdx.x * 4 + warp;
+  if (i >= n) return;  // whole warp
+  NbrSm& N = nb[warp];
+  gs[warp][lane] = gcoef[(size_t)i * kDesc + lane];
+  for (int s = lane; s < kSgMax; s += 32) fn[warp][0][s] = fn[warp][1][s] = fn[warp][2][s] = 0.f;
+  const int S = warp_load_nbrs(i, pos, sl, slen, box, P.rc, N);  // ends with __syncwarp
+  const float* g = gs[warp];
   float fix = 0.f, fiy = 0.f, fiz = 0.f;
-  for (int s = 0; s < S; s++) {
-    fcut(r[s], P.rc, fc[s], dfc[s]);
+  for (int s = lane; s < S; s += 32) {
     float sum = 0.f;  // sum_k g_k dphi_k/dr
+#pragma unroll
     for (int k = 0; k < kRad; k++) {
-      const float t = r[s] - P.rs[k];
-      const float e = __expf(-P.eta_r * t * t);
-      sum += g[k] * e * (-2.f * P.eta_r * t * fc[s] + dfc[s]);
+      const float t = N.r[s] - P.rs[k];
+      sum += g[k] * __expf(-P.eta_r * t * t) * (-2.f * P.eta_r * t * N.fc[s] + N.dfc[s]);
     }
-    const float ir = 1.f / r[s];
-    const float gx = sum * d[s].x * ir, gy = sum * d[s].y * ir, gz = sum * d[s].z * ir;
+    const float ir = 1.f / N.r[s];
+    const float gx = sum * N.dx[s] * ir, gy = sum * N.dy[s] * ir, gz = sum * N.dz[s] * ir;
     // dG/dr_j = +grad, dG/dr_i = -grad; F = -dE/dr
-    fn[s] = make_float3(-gx, -gy, -gz);
+    fn[warp][0][s] -= gx;
+    fn[warp][1][s] -= gy;
+    fn[warp][2][s] -= gz;
     fix += gx;
     fiy += gy;
     fiz += gz;
   }
-  for (int a = 0; a < S; a++) {
-    float ajx = 0.f, ajy = 0.f, ajz = 0.f;
-    for (int b = a + 1; b < S; b++) {
-      const float rab = r[a] * r[b];
-      const float c = (d[a].x * d[b].x + d[a].y * d[b].y + d[a].z * d[b].z) / rab;
-      const float q = r[a] * r[a] + r[b] * r[b];
-      float A = 0.f, Ba = 0.f, Bb = 0.f;
-      for (int f = 0; f < kAng; f++) {
-        const float base = 1.f + P.lam[f] * c;
-        if (base <= 0.f) continue;
-        const float pz1 = ipow(base, P.zeta[f] - 1);
-        const float pz = pz1 * base;
-        const float ex = __expf(-P.eta_a[f] * q);
-        const float gf = g[kRad + f] * P.pref[f];
-        // T = pz ex fc_a fc_b
-        A += gf * (float)P.zeta[f] * P.lam[f] * pz1 * ex * fc[a] * fc[b];
-        Ba += gf * pz * ex * fc[b] * (-2.f * P.eta_a[f] * r[a] * fc[a] + dfc[a]);
-        Bb += gf * pz * ex * fc[a] * (-2.f * P.eta_a[f] * r[b] * fc[b] + dfc[b]);
-      }
-      const float ia = 1.f / r[a], ib = 1.f / r[b];
-      // dc/dd_a = d_b / (ra rb) - c d_a / ra^2
-      const float gax = A * (d[b].x / rab - c * d[a].x * ia * ia) + Ba * d[a].x * ia;
-      const float gay = A * (d[b].y / rab - c * d[a].y * ia * ia) + Ba * d[a].y * ia;
-      const float gaz = A * (d[b].z / rab - c * d[a].z * ia * ia) + Ba * d[a].z * ia;
-      const float gbx = A * (d[a].x / rab - c * d[b].x * ib * ib) + Bb * d[b].x * ib;
-      const float gby = A * (d[a].y / rab - c * d[b].y * ib * ib) + Bb * d[b].y * ib;
-      const float gbz = A * (d[a].z / rab - c * d[b].z * ib * ib) + Bb * d[b].z * ib;
-      ajx += gax;
-      ajy += gay;
-      ajz += gaz;
-      fn[b].x -= gbx;
-      fn[b].y -= gby;
-      fn[b].z -= gbz;
-      fix += gax + gbx;
-      fiy += gay + gby;
-      fiz += gaz + gbz;
+  __syncwarp();
+  const int npair = S * (S - 1) / 2;
+  for (int k = lane; k < npair; k += 32) {
+    int a, b;
+    pair_of(k, S, a, b);
+    const float ra = N.r[a], rb = N.r[b], rab = ra * rb;
+    const float c = (N.dx[a] * N.dx[b] + N.dy[a] * N.dy[b] + N.dz[a] * N.dz[b]) / rab;
+    const float q = ra * ra + rb * rb;
+    const float fca = N.fc[a], fcb = N.fc[b], dfa = N.dfc[a], dfb = N.dfc[b];
+    float A = 0.f, Ba = 0.f, Bb = 0.f;
+    AngPair T;
+    ang_pair(c, q, P, T);
+#pragma unroll
+    for (int f = 0; f < kAng; f++) {
+      const int e = f >> 3, l = (f >> 2) & 1, z = f & 3;
+      if (T.b[l] <= 0.f) continue;
+      const float pz1 = T.pz1[l][z], pz = T.pz[l][z], ex = T.ex[e];
+      const float gf = g[kRad + f] * P.pref[f];
+      A += gf * (float)P.zeta[f] * P.lam[f] * pz1 * ex * fca * fcb;
+      Ba += gf * pz * ex * fcb * (-2.f * P.eta_a[f] * ra * fca + dfa);
+      Bb += gf * pz * ex * fca * (-2.f * P.eta_a[f] * rb * fcb + dfb);
     }
-    fn[a].x -= ajx;
-    fn[a].y -= ajy;
-    fn[a].z -= ajz;
+    const float ia = 1.f / ra, ib = 1.f / rb;
+    // dc/dd_a = d_b / (ra rb) - c d_a / ra^2
+    const float gax = A * (N.dx[b] / rab - c * N.dx[a] * ia * ia) + Ba * N.dx[a] * ia;
+    const float gay = A * (N.dy[b] / rab - c * N.dy[a] * ia * ia) + Ba * N.dy[a] * ia;
+    const float gaz = A * (N.dz[b] / rab - c * N.dz[a] * ia * ia) + Ba * N.dz[a] * ia;
+    const float gbx = A * (N.dx[a] / rab - c * N.dx[b] * ib * ib) + Bb * N.dx[b] * ib;
+    const float gby = A * (N.dy[a] / rab - c * N.dy[b] * ib * ib) + Bb * N.dy[b] * ib;
+    const float gbz = A * (N.dz[a] / rab - c * N.dz[b] * ib * ib) + Bb * N.dz[b] * ib;
+    atomicAdd(&fn[warp][0][a], -gax);
+    atomicAdd(&fn[warp][1][a], -gay);
+    atomicAdd(&fn[warp][2][a], -gaz);
+    atomicAdd(&fn[warp][0][b], -gbx);
+    atomicAdd(&fn[warp][1][b], -gby);
+    atomicAdd(&fn[warp][2][b], -gbz);
+    fix += gax + gbx;
+    fiy += gay + gby;
+    fiz += gaz + gbz;
   }
-  for (int s = 0; s < S; s++) {
-    atomicAdd(&F32[3 * idx[s]], fn[s].x);
-    atomicAdd(&F32[3 * idx[s] + 1], fn[s].y);
-    atomicAdd(&F32[3 * idx[s] + 2], fn[s].z);
+  __syncwarp();
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    fix += __shfl_xor_sync(0xffffffffu, fix, o);
+    fiy += __shfl_xor_sync(0xffffffffu, fiy, o);
+    fiz += __shfl_xor_sync(0xffffffffu, fiz, o);
   }
-  atomicAdd(&F32[3 * i], fix);
-  atomicAdd(&F32[3 * i + 1], fiy);
-  atomicAdd(&F32[3 * i + 2], fiz);
+  for (int s = lane; s < S; s += 32) {
+    atomicAdd(&F32[3 * N.idx[s]], fn[warp][0][s]);
+    atomicAdd(&F32[3 * N.idx[s] + 1], fn[warp][1][s]);
+    atomicAdd(&F32[3 * N.idx[s] + 2], fn[warp][2][s]);
+  }
+  if (lane == 0) {
+    atomicAdd(&F32[3 * i], fix);
+    atomicAdd(&F32[3 * i + 1], fiy);
+    atomicAdd(&F32[3 * i + 2], fiz);
+  }
+}
+
+__global__ void k_sg_pos32(const md_double4* __restrict__ pos, int n, float4* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const md_double4 p = pos[i];
+  out[i] = make_float4((float)p.x, (float)p.y, (float)p.z, 0.f);
 }
 
 __global__ void k_sg_store(const float* __restrict__ F32, double* __restrict__ f3, int n,
@@ -644,12 +792,13 @@ __global__ void __launch_bounds__(128)
                         c * (d[b].x * de[b].x + d[b].y * de[b].y + d[b].z * de[b].z) * ib * ib;
       const float ua = (d[a].x * de[a].x + d[a].y * de[a].y + d[a].z * de[a].z) * ia;
       const float ub = (d[b].x * de[b].x + d[b].y * de[b].y + d[b].z * de[b].z) * ib;
+      AngPair T;
+      ang_pair(c, q2, P, T);
+#pragma unroll
       for (int f = 0; f < kAng; f++) {
-        const float base = 1.f + P.lam[f] * c;
-        if (base <= 0.f) continue;
-        const float pz1 = ipow(base, P.zeta[f] - 1);
-        const float pz = pz1 * base;
-        const float ex = __expf(-P.eta_a[f] * q2);
+        const int e = f >> 3, l = (f >> 2) & 1, z = f & 3;
+        if (T.b[l] <= 0.f) continue;
+        const float pz1 = T.pz1[l][z], pz = T.pz[l][z], ex = T.ex[e];
         const float A = P.pref[f] * (float)P.zeta[f] * P.lam[f] * pz1 * ex * fc[a] * fc[b];
         const float Ba = P.pref[f] * pz * ex * fc[b] * (-2.f * P.eta_a[f] * r[a] * fc[a] + dfc[a]);
         const float Bb = P.pref[f] * pz * ex * fc[a] * (-2.f * P.eta_a[f] * r[b] * fc[b] + dfc[b]);
@@ -896,12 +1045,13 @@ __global__ void k_sum_d(const double* __restrict__ v, int n, double* __restrict_
   if (threadIdx.x == 0) out[0] = sm[0];
 }
 
-// sum |a - b|^2 and |b|^2 over 3n values (relative RMS of a against b)
+// sum |a - b|^2 and |b|^2 over 3n values (relative RMS of a against b),
+// block partials added into out[0..1] (zeroed by the caller)
 __global__ void k_err2(const double* __restrict__ a, const double* __restrict__ b, int n3,
                        double* __restrict__ out) {
   __shared__ double s1[256], s2[256];
   double x = 0.0, y = 0.0;
-  for (int k = threadIdx.x; k < n3; k += blockDim.x) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n3; k += gridDim.x * blockDim.x) {
     const double d = a[k] - b[k];
     x += d * d;
     y += b[k] * b[k];
@@ -917,8 +1067,8 @@ __global__ void k_err2(const double* __restrict__ a, const double* __restrict__ 
     __syncthreads();
   }
   if (threadIdx.x == 0) {
-    out[0] = s1[0];
-    out[1] = s2[0];
+    atomicAdd(&out[0], s1[0]);
+    atomicAdd(&out[1], s2[0]);
   }
 }
 
@@ -1056,11 +1206,14 @@ int sur_descriptors(Surrogate& s, const md_double4* pos, int n, const RowWalker&
     if ((e = sur_grow(s.eatom, h, n)) != cudaSuccess) return e;
     h = 0;
     if ((e = sur_grow(s.slen, h, n)) != cudaSuccess) return e;
+    h = 0;
+    if ((e = sur_grow(s.pos32, h, n)) != cudaSuccess) return e;
     s.n_alloc = n;
   }
   if (n == 0) return 0;
-  k_sg_short<<<sblocks(n, 128), 128, 0, st>>>(pos, w, s.rc, s.sl, s.slen, d_status);
-  k_sg_desc<<<sblocks(n, 128), 128, 0, st>>>(pos, n, s.sl, s.slen, w.g.box, s.P,
+  k_sg_pos32<<<sblocks(n, 256), 256, 0, st>>>(pos, n, s.pos32);
+  k_sg_short<<<sblocks(n, 4), 128, 0, st>>>(s.pos32, w, s.rc, s.sl, s.slen, d_status);
+  k_sg_desc<<<sblocks(n, 4), 128, 0, st>>>(pos, n, s.sl, s.slen, w.g.box, s.P,
                                              normalised ? s.mean_d : nullptr,
                                              normalised ? s.istd_d : nullptr, s.X);
   return (int)cudaGetLastError();
@@ -1234,7 +1387,7 @@ int sur_forces(Surrogate& s, const md_double4* pos, int n, const RowWalker& w, d
   k_sg_scale<<<sblocks(n, 256), 256, 0, st>>>(s.t, s.dtdx, n, s.mu, s.sigma, s.istd_d, s.gcoef,
                                               s.eatom);
   cudaMemsetAsync(s.F32, 0, sizeof(float) * 3 * (size_t)n, st);
-  k_sg_force<<<sblocks(n, 128), 128, 0, st>>>(pos, n, s.sl, s.slen, w.g.box, s.P, s.gcoef, s.F32);
+  k_sg_force<<<sblocks(n, 4), 128, 0, st>>>(pos, n, s.sl, s.slen, w.g.box, s.P, s.gcoef, s.F32);
   k_sg_store<<<sblocks(3LL * n, 256), 256, 0, st>>>(s.F32, f3, n, accumulate);
   if (energy_dev) k_sum_d<<<1, 256, 0, st>>>(s.eatom, n, energy_dev);
   return (int)cudaGetLastError();
@@ -1346,6 +1499,11 @@ int sur_train_fm(Surrogate& s, int steps, float lr, double* loss_e, double* loss
     if ((e = sur_grow(s.X, h, (long long)nmax * kDesc)) != cudaSuccess) return e;
     h = 0;
     if ((e = sur_grow(s.slen, h, nmax)) != cudaSuccess) return e;
+    h = 0;
+    if ((e = sur_grow(s.pos32, h, nmax)) != cudaSuccess) return e;
+    h = 0;
+    if ((e = sur_grow(s.sl, h, (long long)nmax * kSgMax)) != cudaSuccess) return e;
+    s.n_sl = (long long)nmax * kSgMax;
     s.n_alloc = nmax;
   }
   if (nmax > s.n_fm) {
@@ -1377,7 +1535,7 @@ int sur_train_fm(Surrogate& s, int steps, float lr, double* loss_e, double* loss
     k_sg_scale<<<sblocks(n, 256), 256, 0, st>>>(s.t, s.dtdx, n, s.mu, s.sigma, s.istd_d,
                                                 s.gcoef, s.eatom);
     cudaMemsetAsync(s.F32, 0, sizeof(float) * 3 * (size_t)n, st);
-    k_sg_force<<<sblocks(n, 128), 128, 0, st>>>(c.pos, n, c.sl, c.slen, c.box, s.P, s.gcoef,
+    k_sg_force<<<sblocks(n, 4), 128, 0, st>>>(c.pos, n, c.sl, c.slen, c.box, s.P, s.gcoef,
                                                 s.F32);
     cudaMemsetAsync(s.scratch, 0, sizeof(double) * 2, st);
     k_fm_resid<<<sblocks(3LL * n, 256), 256, 0, st>>>(s.F32, c.fx, 3 * n, s.E3, s.scratch);
@@ -1440,7 +1598,8 @@ int sur_force_grad(Surrogate& s, const float* X, const float* V, int n, float* g
 
 int sur_rel_err(const double* a, const double* b, int n, double* scratch, double* err,
                 cudaStream_t st) {
-  k_err2<<<1, 256, 0, st>>>(a, b, 3 * n, scratch);
+  cudaMemsetAsync(scratch, 0, sizeof(double) * 2, st);
+  k_err2<<<std::min(256, sblocks(3LL * n, 256)), 256, 0, st>>>(a, b, 3 * n, scratch);
   double h[2];
   cudaError_t e = cudaMemcpyAsync(h, scratch, sizeof(h), cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
@@ -1457,7 +1616,7 @@ md_surrogate::~md_surrogate() {
                   SX,  ST,    loss_d, scratch, rows_d, Xg, Tg, status_d};
   for (void* p : ptrs)
     if (p) cudaFree(p);
-  for (void* p : {(void*)iota_d, (void*)V, (void*)E3})
+  for (void* p : {(void*)iota_d, (void*)V, (void*)E3, (void*)pos32})
     if (p) cudaFree(p);
   for (mdgb::SurConfig& c : cfgs)
     for (void* p : {(void*)c.pos, (void*)c.sl, (void*)c.slen, (void*)c.fx, (void*)c.eatom,

@@ -58,6 +58,7 @@ struct md_surrogate {
   uint32_t* sl = nullptr;
   int* slen = nullptr;
   float *X = nullptr, *t = nullptr, *dtdx = nullptr, *gcoef = nullptr, *F32 = nullptr;
+  float4* pos32 = nullptr;         // FP32 positions for the neighbour search
   double* eatom = nullptr;
   // training samples: raw descriptors and exact per-atom energies
   int ns = 0, ns_cap = 0;
