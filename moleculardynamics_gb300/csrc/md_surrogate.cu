@@ -1599,7 +1599,7 @@ int sur_force_grad(Surrogate& s, const float* X, const float* V, int n, float* g
 int sur_rel_err(const double* a, const double* b, int n, double* scratch, double* err,
                 cudaStream_t st) {
   cudaMemsetAsync(scratch, 0, sizeof(double) * 2, st);
-  k_err2<<<std::min(256, sblocks(3LL * n, 256)), 256, 0, st>>>(a, b, 3 * n, scratch);
+  k_err2<<<std::max(1, std::min(256, sblocks(3LL * n, 256))), 256, 0, st>>>(a, b, 3 * n, scratch);
   double h[2];
   cudaError_t e = cudaMemcpyAsync(h, scratch, sizeof(h), cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
