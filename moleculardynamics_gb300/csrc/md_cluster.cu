@@ -434,6 +434,24 @@ __device__ __forceinline__ float min_img(float d, float Lf, float invL) {
   return d - Lf * rintf(d * invL);
 }
 
+// Rows are padded with the segment's sentinel (staged entry `staged`, a
+// position far outside every cutoff) up to the longest row of the warp
+// rounded up to whole 16-slot tiles, so the force loop reads only real or
+// sentinel entries and needs no per-slot validity test.  Warp-collective.
+__device__ __forceinline__ void pad_rows(uint16_t* __restrict__ rows, int ld, int cap, int p,
+                                         bool live, int kept, int sentinel) {
+  int wm = live ? min(kept, cap) : 0;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) wm = max(wm, __shfl_xor_sync(0xffffffffu, wm, o));
+  const int padded = min((wm + kClusterTileSlots - 1) / kClusterTileSlots * kClusterTileSlots, cap);
+  if (live)
+    for (int k = min(kept, cap); k < padded; k++) rows[(size_t)k * ld + p] = (uint16_t)sentinel;
+}
+
+__device__ __forceinline__ void put_sentinel(float4* st, int staged) {
+  if (threadIdx.x == 0) st[staged] = make_float4(1e18f, 1e18f, 1e18f, __int_as_float(SP_NG));
+}
+
 // 4. compact rows from the build-time positions (MODE 0: count, 1: write,
 // 2: both, rows longer than cap truncated and reported through the counters)
 template <int MODE>
@@ -453,24 +471,29 @@ __global__ void __launch_bounds__(256)
   const float Lf = sh.r.Lf, invL = 1.0f / sh.r.Lf;
   int mx = 0;
   unsigned long long tot = 0;
-  for (int p = sh.S.p0 + threadIdx.x; p < sh.S.p1; p += blockDim.x) {
-    const int self = self_offset(sh, p);
-    const float4 pi = st[self];
+  for (int base = sh.S.p0; base < sh.S.p1; base += blockDim.x) {
+    const int p = base + threadIdx.x;
+    const bool live = p < sh.S.p1;
     int kept = 0;
-    walk_staged(sh, self, [&](int q) {
-      const float4 pj = st[q];
-      float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
-      if (minimg) {
-        dx = min_img(dx, Lf, invL);
-        dy = min_img(dy, Lf, invL);
-        dz = min_img(dz, Lf, invL);
-      }
-      if (dx * dx + dy * dy + dz * dz < rv2) {
-        if (MODE != 0 && kept < cap) rows[(size_t)kept * ld + p] = (uint16_t)q;
-        kept++;
-      }
-    });
-    if (MODE != 1) {
+    if (live) {
+      const int self = self_offset(sh, p);
+      const float4 pi = st[self];
+      walk_staged(sh, self, [&](int q) {
+        const float4 pj = st[q];
+        float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+        if (minimg) {
+          dx = min_img(dx, Lf, invL);
+          dy = min_img(dy, Lf, invL);
+          dz = min_img(dz, Lf, invL);
+        }
+        if (dx * dx + dy * dy + dz * dz < rv2) {
+          if (MODE != 0 && kept < cap) rows[(size_t)kept * ld + p] = (uint16_t)q;
+          kept++;
+        }
+      });
+    }
+    if (MODE != 0) pad_rows(rows, ld, cap, p, live, kept, sh.S.staged);
+    if (MODE != 1 && live) {
       len[p] = (uint16_t)min(kept, 65535);
       mx = max(mx, kept);
       tot += (unsigned long long)kept;
@@ -644,12 +667,18 @@ __global__ void __launch_bounds__(224, 3)
     break;
   }
   phase ^= 4u;
+  put_sentinel(st, sh.S.staged);
   if (tripped) fill_offsets(sh, a.start);
   __syncthreads();
   const bool minimg = sh.r.G == 1;
+  // without minimum images or energies the sentinel-padded rows need no
+  // per-slot validity test (the sentinel lies beyond every cutoff)
+  const bool fast = !ENERGY && !minimg;
   const float Lf = sh.r.Lf, invL = 1.0f / sh.r.Lf;
   const float rc2 = (float)a.rcutsq;
   const float rc_lo = rc2 * (1.0f - 1e-5f), rc_hi = rc2 * (1.0f + 1e-5f);
+  // |r2 - rc_mid| < rc_half covers (rc_lo, rc_hi) with a little to spare
+  const float rc_mid = 0.5f * (rc_lo + rc_hi), rc_half = 0.5f * (rc_hi - rc_lo) * 1.001f;
   const float s2_ng = a.sp.sig[2] * a.sp.sig[2], c_ng = 24.0f * a.sp.eps[2];
   const float s2_n = a.sp.sig[0] * a.sp.sig[0], c_n = 24.0f * a.sp.eps[0];
   const float s2_o = a.sp.sig[1] * a.sp.sig[1], c_o = 24.0f * a.sp.eps[1];
@@ -735,6 +764,73 @@ __global__ void __launch_bounds__(224, 3)
       kahan_add(hy, ly, ay + by);
       kahan_add(hz, lz, az + bz);
     };
+    // The padded-row form of a pair: no validity test, and the FP64 decision
+    // near the cutoff is deferred: `band` records that some pair of the
+    // chunk lies within 1e-5 of it.
+    auto pair_fast = [&](int q, float& cx, float& cy, float& cz, bool& band) {
+      const float4 pj = st[q];
+      const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+      const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+      float s2 = s2_ng, c24 = c_ng;
+      bool use = true;
+      if (!ALL_NG) {
+        const int tj = __float_as_int(pj.w);
+        use = tj == SP_NG || ti == SP_NG;
+        const int sel = lj_select(ti, tj);
+        s2 = sel == SP_N ? s2_n : (sel == SP_O ? s2_o : s2_ng);
+        c24 = sel == SP_N ? c_n : (sel == SP_O ? c_o : c_ng);
+      }
+      const float inv = rcp_approx(r2);
+      const float sr2 = s2 * inv;
+      const float sr6 = sr2 * sr2 * sr2;
+      float fij = c24 * inv * sr6 * fmaf(2.0f, sr6, -1.0f);
+      band |= use && fabsf(r2 - rc_mid) < rc_half;
+      fij = use && r2 <= rc_lo ? fij : 0.0f;
+      cx = fmaf(dx, fij, cx);
+      cy = fmaf(dy, fij, cy);
+      cz = fmaf(dz, fij, cz);
+    };
+    // 16 padded row slots; pairs in the band are added afterwards, each
+    // decided in FP64 (rare: about one atom in 600 has one)
+    auto chunk16_fast = [&](auto&& get) {
+      float ax = 0.f, ay = 0.f, az = 0.f, bx = 0.f, by = 0.f, bz = 0.f;
+      bool band = false;
+#pragma unroll
+      for (int kk = 0; kk < kClusterTileSlots; kk += 2) {
+        pair_fast(get(kk), ax, ay, az, band);
+        pair_fast(get(kk + 1), bx, by, bz, band);
+      }
+      if (band) {
+#pragma unroll 1
+        for (int kk = 0; kk < kClusterTileSlots; kk++) {
+          const int q = get(kk);
+          const float4 pj = st[q];
+          const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+          const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+          if (!(r2 > rc_lo && r2 < rc_hi)) continue;
+          float s2 = s2_ng, c24 = c_ng;
+          if (!ALL_NG) {
+            const int tj = __float_as_int(pj.w);
+            if (!(tj == SP_NG || ti == SP_NG)) continue;
+            const int sel = lj_select(ti, tj);
+            s2 = sel == SP_N ? s2_n : (sel == SP_O ? s2_o : s2_ng);
+            c24 = sel == SP_N ? c_n : (sel == SP_O ? c_o : c_ng);
+          }
+          if (!band_inside(sh, a.pos, p, q, a.rcutsq)) continue;
+          const float inv = rcp_approx(r2);
+          const float sr2 = s2 * inv;
+          const float sr6 = sr2 * sr2 * sr2;
+          const float fij = c24 * inv * sr6 * fmaf(2.0f, sr6, -1.0f);
+          ax = fmaf(dx, fij, ax);
+          ay = fmaf(dy, fij, ay);
+          az = fmaf(dz, fij, az);
+        }
+      }
+      kahan_add(hx, lx, ax + bx);
+      kahan_add(hy, ly, ay + by);
+      kahan_add(hz, lz, az + bz);
+    };
+    int kept_new = 0;  // fresh row length of a refresh step
     if (!tripped && ROWS == 2) {
       const int warp = tid >> 5, lane = tid & 31;
       const int L = live ? (int)a.len[p] : 0;
@@ -767,8 +863,11 @@ __global__ void __launch_bounds__(224, 3)
         phase ^= 1u << b;
         inflight &= ~(1u << b);
         const uint16_t* tl = wt + b * (kWarpTileBytes / 2) + col;
-        chunk16([&](int kk) { return (int)tl[kk * kWarpTileAtoms]; }, L - t * kClusterTileSlots,
-                wmax - t * kClusterTileSlots);
+        auto get = [&](int kk) { return (int)tl[kk * kWarpTileAtoms]; };
+        if (!fast)
+          chunk16(get, L - t * kClusterTileSlots, wmax - t * kClusterTileSlots);
+        else if (live)
+          chunk16_fast(get);
         __syncwarp();  // the warp is done with buffer b
         if (lane == 0 && t + 2 < Tw) {
           fence_proxy_async();
@@ -793,14 +892,19 @@ __global__ void __launch_bounds__(224, 3)
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) wmax = max(wmax, __shfl_xor_sync(0xffffffffu, wmax, o));
       const uint16_t* rp = a.rows + (live ? p : 0);
-      // two entries per register; slots below the warp's longest row only
+      // two entries per register; whole padded tiles below the warp's
+      // longest row only (t0 is a multiple of 16: the test is warp-uniform)
       auto fetch = [&](int t0, uint32_t (&dst)[kClusterTileSlots / 2]) {
+        if (t0 < wmax) {
 #pragma unroll
-        for (int k = 0; k < kClusterTileSlots / 2; k++) {
-          const int s0 = t0 + 2 * k, s1 = s0 + 1;
-          const uint32_t lo = s0 < wmax ? (uint32_t)__ldg(rp + (size_t)s0 * a.ld) : 0u;
-          const uint32_t hi = s1 < wmax ? (uint32_t)__ldg(rp + (size_t)s1 * a.ld) : 0u;
-          dst[k] = lo | (hi << 16);
+          for (int k = 0; k < kClusterTileSlots / 2; k++) {
+            const uint32_t lo = (uint32_t)__ldg(rp + (size_t)(t0 + 2 * k) * a.ld);
+            const uint32_t hi = (uint32_t)__ldg(rp + (size_t)(t0 + 2 * k + 1) * a.ld);
+            dst[k] = lo | (hi << 16);
+          }
+        } else {
+#pragma unroll
+          for (int k = 0; k < kClusterTileSlots / 2; k++) dst[k] = 0u;
         }
       };
       uint32_t nx[kClusterTileSlots / 2];
@@ -810,8 +914,11 @@ __global__ void __launch_bounds__(224, 3)
 #pragma unroll
         for (int k = 0; k < kClusterTileSlots / 2; k++) cu[k] = nx[k];
         fetch(t0 + kClusterTileSlots, nx);  // next chunk in flight while this one computes
-        chunk16([&](int kk) { return (int)((cu[kk >> 1] >> ((kk & 1) * 16)) & 0xFFFFu); },
-                L - t0, wmax - t0);
+        auto get = [&](int kk) { return (int)((cu[kk >> 1] >> ((kk & 1) * 16)) & 0xFFFFu); };
+        if (!fast)
+          chunk16(get, L - t0, wmax - t0);
+        else if (live)
+          chunk16_fast(get);
       }
     } else if (!tripped) {
       const int L = live ? (int)a.len[p] : 0;
@@ -844,7 +951,11 @@ __global__ void __launch_bounds__(224, 3)
           inflight &= ~(1u << b);
           if (wrem > 0) {
             const uint16_t* tl = tiles + b * tile_elems + col;
-            chunk16([&](int kk) { return (int)tl[kk * BX]; }, L - t * kClusterTileSlots, wrem);
+            auto get = [&](int kk) { return (int)tl[kk * BX]; };
+            if (!fast)
+              chunk16(get, L - t * kClusterTileSlots, wrem);
+            else if (live)
+              chunk16_fast(get);
           }
         }
         // everyone is done with buffer b (and every wait succeeded)
@@ -899,8 +1010,10 @@ __global__ void __launch_bounds__(224, 3)
       kahan_add(hz, lz, cz);
       if (kept > a.cap) atomicOr(&a.skin[3], 1);
       a.len[p] = (uint16_t)(kept < a.cap ? kept : a.cap);
+      kept_new = kept;
       a.pos_build[p] = a.posf[p];
     }
+    if (tripped) pad_rows(a.rows, a.ld, a.cap, p, live, kept_new, sh.S.staged);
     if (live) {
       const double f[3] = {(double)hx - (double)lx, (double)hy - (double)ly,
                            (double)hz - (double)lz};
@@ -1038,13 +1151,15 @@ cudaError_t realloc_dev(T*& p, size_t count) {
   return cudaMalloc(&p, sizeof(T) * (count > 0 ? count : 1));
 }
 
-size_t stage_bytes(int staged) { return sizeof(float4) * (size_t)std::max(staged, 1); }
+// staged positions plus the far sentinel that pads the rows (entry `staged`)
+size_t stage_bytes(int staged) { return sizeof(float4) * ((size_t)std::max(staged, 1) + 1); }
 
 template <typename K>
 void allow_smem(K kern) {
   cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       (int)(sizeof(float4) * kClusterMaxStaged +
-                             2 * kClusterTileSlots * 256 * sizeof(uint16_t)));
+                       (int)(sizeof(float4) * (kClusterMaxStaged + 1) +
+                             std::max(2 * kClusterTileSlots * 256 * sizeof(uint16_t),
+                                      (size_t)8 * 2 * kWarpTileBytes)));
 }
 
 }  // namespace
@@ -1231,7 +1346,10 @@ int cluster_build(ClusterList& cl, const std::vector<ClusterReplica>& reps_in, f
     memcpy(&ent, hc + 2, sizeof(ent));
     cl.entries = (long long)ent;
   }
-  const int want = std::min(65535, (int)(std::max(cl.maxlen, 1) * cl.headroom) + 8);
+  // whole 16-slot tiles: rows are padded to the warp's longest row rounded up
+  const int want =
+      std::min(65520, ((int)(std::max(cl.maxlen, 1) * cl.headroom) + 8 + kClusterTileSlots - 1) /
+                          kClusterTileSlots * kClusterTileSlots);
   const bool fits = have_rows && want <= cl.cap;
   if (!fits) {
     cl.cap = want;
