@@ -271,6 +271,13 @@ md_status md_surrogate_net(md_surrogate* s, const float* x, int n, float* t, flo
  * ncols in {32, 64, 128}, kdim a multiple of 16 up to 128. */
 md_status mdgb_tc_selftest(const float* a, const float* b, float* c, int ncols, int kdim);
 
+/* Self-test of the integer-operation conversions of the fused Gear update:
+ * wide[i] = widen(f[i]) (FP32 -> FP64, exact) and narrow[i] = narrow(d[i])
+ * (FP64 -> FP32, nearest-even), each beside the conversion instruction's
+ * result (wide_ref, narrow_ref), for count values on the device. */
+md_status mdgb_conv_selftest(const float* f, const double* d, int count, double* wide,
+                             double* wide_ref, float* narrow, float* narrow_ref);
+
 /* Wait for all work of the context; returns the first deferred error. */
 md_status md_synchronize(md_ctx* ctx);
 /* Page-locked host memory for fast md_upload/md_download (NULL on failure). */

@@ -18,6 +18,7 @@
 // flag is up, the block walks full candidate rows from shared memory and
 // refreshes the compact rows.
 #include <algorithm>
+#include <cfloat>
 #include <cmath>
 #include <cstring>
 
@@ -1015,15 +1016,17 @@ __global__ void __launch_bounds__(224, 3)
     }
     if (tripped) pad_rows(a.rows, a.ld, a.cap, p, live, kept_new, sh.S.staged);
     if (live) {
-      const double f[3] = {(double)hx - (double)lx, (double)hy - (double)ly,
-                           (double)hz - (double)lz};
+      // the compensated sums widened exactly (integer operations) and
+      // combined in FP64
+      const double f[3] = {widen_exact(hx) - widen_exact(lx), widen_exact(hy) - widen_exact(ly),
+                           widen_exact(hz) - widen_exact(lz)};
       if (!GEAR) {
         a.f3[3 * p] = f[0];
         a.f3[3 * p + 1] = f[1];
         a.f3[3 * p + 2] = f[2];
       } else {
         const md_double4 r = a.pos[p];
-        const int type = (int)r.w;
+        const int type = ti;  // the staged copy carries the species as an integer
         GearAtom s;
         s.r[0] = r.x;
         s.r[1] = r.y;
@@ -1038,7 +1041,6 @@ __global__ void __launch_bounds__(224, 3)
         const double im = type == SP_N ? a.g.inv_mass[0]
                                        : (type == SP_O ? a.g.inv_mass[1] : a.g.inv_mass[2]);
         gear_correct_fma(s, f, im, a.g.k);
-        if (!gear_finite(s)) atomicOr(a.status, ST_NONFINITE);
         gear_predict_fma(s, a.g.k);
 #pragma unroll
         for (int d = 0; d < 3; d++) {
@@ -1053,8 +1055,12 @@ __global__ void __launch_bounds__(224, 3)
         rn.z = s.r[2];
         rn.w = r.w;
         a.g.pos_next[p] = rn;
-        const float4 pf = make_float4((float)s.r[0], (float)s.r[1], (float)s.r[2],
+        const float4 pf = make_float4(narrow_rn(s.r[0]), narrow_rn(s.r[1]), narrow_rn(s.r[2]),
                                       __int_as_float(type));
+        // a non-finite force, velocity or derivative reaches the predicted
+        // position: one FP32 test covers the whole state
+        if (!(fabsf(pf.x) <= FLT_MAX && fabsf(pf.y) <= FLT_MAX && fabsf(pf.z) <= FLT_MAX))
+          atomicOr(a.status, ST_NONFINITE);
         a.g.posf_next[p] = pf;
         const float4 pb = a.pos_build[p];
         const float ddx = pf.x - pb.x, ddy = pf.y - pb.y, ddz = pf.z - pb.z;

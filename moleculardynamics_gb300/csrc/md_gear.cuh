@@ -38,6 +38,35 @@ __device__ __forceinline__ void gear_predict_fma(GearAtom& s, const GearCoef& k)
   }
 }
 
+// Exact FP32 -> FP64 widening by moving the IEEE-754 fields with integer
+// operations (sign; exponent rebiased 127 -> 1023; mantissa shifted left by
+// 29), keeping the FP64 pipe, which is narrow on this GPU, for the Gear
+// arithmetic.  Subnormal inputs become signed zero; infinities and NaNs keep
+// an all-ones exponent.
+__device__ __forceinline__ double widen_exact(float f) {
+  const uint32_t u = __float_as_uint(f);
+  const uint32_t e = (u >> 23) & 0xFFu;
+  const uint32_t ed = e == 0xFFu ? 0x7FFu : e + 896u;
+  const uint32_t hi = (u & 0x80000000u) | (e == 0u ? 0u : (ed << 20) | ((u >> 3) & 0xFFFFFu));
+  const uint32_t lo = e == 0u ? 0u : u << 29;
+  return __hiloint2double((int)hi, (int)lo);
+}
+
+// FP64 -> FP32 rounded to nearest, ties to even, by integer operations for
+// results in the normal FP32 range; zero, tiny, huge and non-finite values
+// take the conversion instruction.
+__device__ __forceinline__ float narrow_rn(double d) {
+  const uint64_t u = (uint64_t)__double_as_longlong(d);
+  const uint32_t hi = (uint32_t)(u >> 32);
+  const int e = (int)((hi >> 20) & 0x7FFu) - 896;  // FP32 biased exponent
+  if (e <= 0 || e >= 255) return __double2float_rn(d);
+  const uint32_t mf = (uint32_t)(u >> 29) & 0x7FFFFFu;  // top 23 mantissa bits
+  const uint32_t rest = (uint32_t)u & 0x1FFFFFFFu;      // the 29 dropped bits
+  const uint32_t up = rest > 0x10000000u || (rest == 0x10000000u && (mf & 1u));
+  // a carry out of the mantissa moves into the exponent, as rounding does
+  return __uint_as_float((hi & 0x80000000u) | (((uint32_t)e << 23) + mf + up));
+}
+
 __device__ __forceinline__ bool gear_finite(const GearAtom& s) {
   return isfinite(s.r[0]) && isfinite(s.r[1]) && isfinite(s.r[2]) && isfinite(s.v[0]) &&
          isfinite(s.v[1]) && isfinite(s.v[2]);

@@ -8,6 +8,7 @@
 // them in a fixed order.
 #include <cmath>
 
+#include "mdgb.h"
 #include "md_gear.cuh"
 #include "md_integrate.h"
 #include "md_potential.cuh"
@@ -552,3 +553,51 @@ void launch_record(const double* th8, const double* e_lj3, const double* e_mb3,
 }
 
 }  // namespace mdgb
+
+namespace {
+
+__global__ void k_conv_selftest(const float* f, const double* d, int n, double* w, double* wr,
+                                float* nr, float* nrr) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  w[i] = mdgb::widen_exact(f[i]);
+  wr[i] = (double)f[i];
+  nr[i] = mdgb::narrow_rn(d[i]);
+  nrr[i] = __double2float_rn(d[i]);
+}
+
+}  // namespace
+
+extern "C" md_status mdgb_conv_selftest(const float* f, const double* d, int count, double* wide,
+                                        double* wide_ref, float* narrow, float* narrow_ref) {
+  if (count <= 0 || !f || !d || !wide || !wide_ref || !narrow || !narrow_ref)
+    return MD_BAD_ARGUMENT;
+  const size_t n = (size_t)count;
+  float* df = nullptr;
+  double* dd = nullptr;
+  if (cudaMalloc(&df, n * sizeof(float) * 3) != cudaSuccess) return MD_CUDA_ERROR;
+  if (cudaMalloc(&dd, n * sizeof(double) * 3) != cudaSuccess) {
+    cudaFree(df);
+    return MD_CUDA_ERROR;
+  }
+  float* dn = df + n;
+  float* dnr = dn + n;
+  double* dw = dd + n;
+  double* dwr = dw + n;
+  md_status r = MD_OK;
+  if (cudaMemcpy(df, f, n * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(dd, d, n * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess)
+    r = MD_CUDA_ERROR;
+  if (r == MD_OK) {
+    k_conv_selftest<<<(count + 255) / 256, 256>>>(df, dd, count, dw, dwr, dn, dnr);
+    if (cudaDeviceSynchronize() != cudaSuccess ||
+        cudaMemcpy(wide, dw, n * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess ||
+        cudaMemcpy(wide_ref, dwr, n * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess ||
+        cudaMemcpy(narrow, dn, n * sizeof(float), cudaMemcpyDeviceToHost) != cudaSuccess ||
+        cudaMemcpy(narrow_ref, dnr, n * sizeof(float), cudaMemcpyDeviceToHost) != cudaSuccess)
+      r = MD_CUDA_ERROR;
+  }
+  cudaFree(df);
+  cudaFree(dd);
+  return r;
+}

@@ -99,7 +99,8 @@ EXPORTS = ["md_create", "md_destroy", "md_status_string", "md_last_error", "md_u
            "mdgb_calculate_potential", "mdgb_set_species", "mdgb_last_status", "md_read_config",
            "md_write_results", "md_host_alloc", "md_host_free",
            "mdgb_many_body_forces_static", "md_autotune", "md_set_graphs", "md_batch_create",
-           "md_batch_size", "md_batch_records", "mdgb_tc_selftest", "md_surrogate_create",
+           "md_batch_size", "md_batch_records", "mdgb_tc_selftest", "mdgb_conv_selftest",
+           "md_surrogate_create",
            "md_surrogate_destroy", "md_surrogate_param_count", "md_surrogate_collect",
            "md_surrogate_samples", "md_surrogate_train", "md_surrogate_attach",
            "md_surrogate_report", "md_surrogate_forces", "md_surrogate_descriptors",
@@ -143,6 +144,7 @@ def load(path: str | None = None) -> C.CDLL:
     L.md_autotune.argtypes = [C.c_void_p, C.c_int, P(MdTuneResult)]
     L.md_set_graphs.argtypes = [C.c_void_p, C.c_int]
     L.mdgb_tc_selftest.argtypes = [_fp, _fp, _fp, C.c_int, C.c_int]
+    L.mdgb_conv_selftest.argtypes = [_fp, _dp, C.c_int, _dp, _dp, _fp, _fp]
     L.md_surrogate_create.argtypes = [C.c_int, C.c_ulonglong, C.c_float, P(C.c_void_p)]
     L.md_surrogate_destroy.argtypes = [C.c_void_p]
     L.md_surrogate_param_count.restype = C.c_int
@@ -572,6 +574,24 @@ def tc_selftest(A: np.ndarray, B: np.ndarray) -> np.ndarray:
     if s != 0:
         raise EngineError(s, "mdgb_tc_selftest")
     return Cm
+
+
+def conv_selftest(f: np.ndarray, d: np.ndarray):
+    """The fused Gear update's integer-operation conversions on the device,
+    each beside the conversion instruction: (widen(f), (double)f,
+    narrow(d), __double2float_rn(d)); f and d of equal length."""
+    L = load()
+    f = np.ascontiguousarray(f, np.float32)
+    d = np.ascontiguousarray(d, np.float64)
+    n = len(f)
+    if len(d) != n:
+        raise ValueError("f and d differ in length")
+    w, wr = np.zeros(n), np.zeros(n)
+    nr, nrr = np.zeros(n, np.float32), np.zeros(n, np.float32)
+    s = L.mdgb_conv_selftest(f, d, n, w, wr, nr, nrr)
+    if s != 0:
+        raise EngineError(s, "mdgb_conv_selftest")
+    return w, wr, nr, nrr
 
 
 def pinned(shape, dtype=np.float64):
