@@ -148,10 +148,12 @@ def make_workload(name: str, seed: int = 2024):
     return pos, vel, L, prec
 
 
-def engine_for(eng, n, L, precision, device, output=MD_PER_BENCH_STEP, lj_kernel=0):
+def engine_for(eng, n, L, precision, device, output=MD_PER_BENCH_STEP, lj_kernel=0, threads=0,
+               row_loads=0):
     cfg = eng.make_config(n_lj=n, dt=2.0, lj_rs=2.8 * SIGMA, lj_rcut=2.5 * SIGMA, periodic=1,
                           box=L, precision=precision, species=eng.SPECIES_ARGON, device=device,
-                          output_timesteps=output, lj_kernel=lj_kernel)
+                          output_timesteps=output, lj_kernel=lj_kernel, cluster_threads=threads,
+                          cluster_row_loads=row_loads)
     return eng.Engine(cfg)
 
 
@@ -441,7 +443,8 @@ def run_gb300(args, rank, world):
     n = len(pos)
     precision = eng.PREC_MIXED if prec_name == "mixed" else eng.PREC_FP64
     lj_kernel = {"auto": eng.LJ_AUTO, "rows": eng.LJ_ROWS, "cluster": eng.LJ_CLUSTER}[args.lj_kernel]
-    e = engine_for(eng, n, L, precision, device, lj_kernel=lj_kernel)
+    e = engine_for(eng, n, L, precision, device, lj_kernel=lj_kernel, threads=args.threads,
+                   row_loads=args.row_loads)
     e.upload(pos, vel)
     e.begin(0.0)
     tune = e.autotune(3) if not args.no_tune else None
@@ -630,6 +633,11 @@ def main():
     ap.add_argument("--ref-md-steps", type=int, default=2)
     ap.add_argument("--lj-kernel", default="auto", choices=["auto", "rows", "cluster"])
     ap.add_argument("--no-tune", action="store_true", help="skip the cluster autotuner")
+    ap.add_argument("--threads", type=int, default=0,
+                    help="cluster segment threads (0: the autotuner chooses)")
+    ap.add_argument("--row-loads", type=int, default=0, choices=[0, 1, 2, 3],
+                    help="cluster row scheme: 1 block TMA tiles, 2 register prefetch, "
+                         "3 per-warp TMA tiles (0: the autotuner chooses)")
     ap.add_argument("--no-forms", action="store_true", help="skip the batched/surrogate forms")
     ap.add_argument("--batch-steps", type=int, default=1000)
     ap.add_argument("--batch-loop-steps", type=int, default=10)
