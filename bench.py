@@ -246,6 +246,7 @@ def batched_form(eng, device, steps: int, loop_steps: int, seed: int = 4096) -> 
     b = eng.Batch(cfg, natoms, boxes)
     b.upload(pos, vel)
     b.begin(0.0)
+    b.step(200)  # thermalise before tuning the tiles
     tune = b.autotune(2)
     b.step(100)
     b.synchronize()
@@ -447,10 +448,13 @@ def run_gb300(args, rank, world):
                    row_loads=args.row_loads)
     e.upload(pos, vel)
     e.begin(0.0)
-    tune = e.autotune(3) if not args.no_tune else None
+    # tiles are tuned on the thermalised state (on the initial lattice every
+    # row has the same length, which favours other tilings), then warmed again
     for _ in range(args.warmup):
         e.step(MD_PER_BENCH_STEP)
-    warm_steps = args.warmup * MD_PER_BENCH_STEP
+    tune = e.autotune(3) if not args.no_tune else None
+    e.step(MD_PER_BENCH_STEP)
+    warm_steps = (args.warmup + 1) * MD_PER_BENCH_STEP
     e.synchronize()
     e.set_timing(True)
     s0 = e.stats()
@@ -635,9 +639,10 @@ def main():
     ap.add_argument("--no-tune", action="store_true", help="skip the cluster autotuner")
     ap.add_argument("--threads", type=int, default=0,
                     help="cluster segment threads (0: the autotuner chooses)")
-    ap.add_argument("--row-loads", type=int, default=0, choices=[0, 1, 2, 3],
+    ap.add_argument("--row-loads", type=int, default=0, choices=[0, 1, 2, 3, 4],
                     help="cluster row scheme: 1 block TMA tiles, 2 register prefetch, "
-                         "3 per-warp TMA tiles (0: the autotuner chooses)")
+                         "3 per-warp TMA tiles, 4 block TMA tiles three deep "
+                         "(0: the autotuner chooses)")
     ap.add_argument("--no-forms", action="store_true", help="skip the batched/surrogate forms")
     ap.add_argument("--batch-steps", type=int, default=1000)
     ap.add_argument("--batch-loop-steps", type=int, default=10)

@@ -74,8 +74,8 @@ typedef struct md_config {
   int cluster_cells;       /* cells per segment of the cluster kernel (0: default) */
   int cluster_threads;     /* threads per segment block (0: default; multiple of 32, <= 224) */
   int cluster_row_loads;   /* rows of the cluster kernel: 0 default / autotuned, 1 TMA tiles of
-                              the block in shared memory, 2 per-lane register prefetch, 3 TMA
-                              tiles of each warp */
+                              the block in shared memory (two in flight), 2 per-lane register
+                              prefetch, 3 TMA tiles of each warp, 4 as 1 with three in flight */
 } md_config;
 
 /* LJ kernel of the precision form.  ROWS: compact rows of packed atom
@@ -168,16 +168,21 @@ md_status md_get_stats(const md_ctx* ctx, md_stats* out);
 md_status md_set_timing(md_ctx* ctx, int on);
 md_status md_kernel_time(const md_ctx* ctx, int kernel, double* total_ms, long long* launches);
 /* Autotuner of the cluster kernel (precision form, periodic): times `evals`
- * force evaluations on the current state for each candidate block size,
- * staged-atom cap per segment and row-load scheme, keeps the fastest and
- * rebuilds the list with it.  Forces do not depend on the choice (same pairs, same order).  No-op
- * for the other kernels.  Call after md_begin. */
+ * launches of the kernel the steps use (the fused force + Gear kernel in the
+ * precision form, on a scratch copy of the Gear state) on the current state
+ * for each candidate block size, staged-atom cap per segment and row-load
+ * scheme, keeps the fastest and rebuilds the list with it.  Forces do not
+ * depend on the choice (same pairs, same order).  No-op for the other
+ * kernels.  Call after md_begin, best on a thermalised state: on a perfect
+ * lattice every row has the same length, which favours other tilings. */
 typedef struct md_tune_result {
   int threads;             /* threads per segment block */
   int stage_cap;           /* staged atoms per segment (cap of the column cut) */
-  int row_loads;           /* 1 block TMA tiles, 2 register prefetch, 3 warp TMA tiles */
+  int row_loads;           /* 1 block TMA tiles, 2 register prefetch, 3 warp TMA tiles,
+                              4 block TMA tiles three deep */
   int candidates;          /* configurations timed */
-  double best_ms;          /* force evaluation time of the choice */
+  double best_ms;          /* launch time of the choice: the fused force + Gear kernel where
+                              steps fuse (precision form), else the force kernel */
 } md_tune_result;
 md_status md_autotune(md_ctx* ctx, int evals, md_tune_result* out);
 /* CUDA graphs for the cluster path (default on): windows of fused steps

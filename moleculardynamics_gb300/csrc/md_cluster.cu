@@ -604,6 +604,7 @@ struct ClStep {
   double* epart;
   int* status;
   ClusterGearArgs g;
+  int nbuf;  // row tiles in flight in the block-tile scheme (2 or 3)
 };
 
 // FP32 LJ force, persistent: each block takes segments from a shared
@@ -613,7 +614,7 @@ struct ClStep {
 // Dynamic shared memory: two row tiles [16][blockDim + 8] of uint16 (TMA
 // destinations), then the staged positions.
 // Row loads: ROWS 0, tiles of the whole block by TMA into shared memory
-// (block-synchronised); 1, each lane prefetches its next 16 entries into
+// (block-synchronised; two or three tiles in flight); 1, each lane prefetches its next 16 entries into
 // registers; 2, tiles of each warp by TMA (warp-synchronised, each warp
 // walks only its own longest row)
 constexpr int kWarpTileAtoms = 40;  // 32 atoms + up to 8 for the 16-byte start
@@ -626,20 +627,19 @@ __global__ void __launch_bounds__(224, 3)
   const int tid = threadIdx.x;
   const int BX = blockDim.x + 8;
   uint16_t* tiles = (uint16_t*)dyn;
+  const int nbuf = a.nbuf;  // block tiles in flight (ROWS 0): 2 or 3
   const int tile_region =
-      ROWS == 0 ? 2 * kClusterTileSlots * BX * (int)sizeof(uint16_t)
+      ROWS == 0 ? nbuf * kClusterTileSlots * BX * (int)sizeof(uint16_t)
                 : (ROWS == 2 ? (int)(blockDim.x >> 5) * 2 * kWarpTileBytes : 0);
   float4* st = (float4*)(dyn + tile_region);
   __shared__ __align__(8) uint64_t wbar[7][2];  // ROWS 2: two tile barriers per warp
   __shared__ SegShared sh;
-  __shared__ __align__(8) uint64_t bar[3];  // two row tiles, staging
+  __shared__ __align__(8) uint64_t bar[4];  // up to three row tiles, staging
   __shared__ int s_max[8];
   __shared__ int s_trip;
   if (tid == 0) {
     s_trip = (a.skin[a.flag_read] | a.skin[3]) != 0;
-    mbar_init(&bar[0], 1);
-    mbar_init(&bar[1], 1);
-    mbar_init(&bar[2], 1);
+    for (int k = 0; k < 4; k++) mbar_init(&bar[k], 1);
     if (ROWS == 2)
       for (int w = 0; w < (int)(blockDim.x >> 5); w++) {
         mbar_init(&wbar[w][0], 1);
@@ -649,7 +649,7 @@ __global__ void __launch_bounds__(224, 3)
   }
   __syncthreads();
   const bool tripped = s_trip != 0;
-  uint32_t phase = 0u;       // bit b: parity to wait for on bar[b] (b = 2: staging)
+  uint32_t phase = 0u;       // bit b: parity to wait for on bar[b] (b = 3: staging)
   uint32_t inflight = 0u;    // bit b: a copy into buffer b is in flight (issuing thread)
   bool trip_next = false;
   bool aborted = false;
@@ -663,11 +663,11 @@ __global__ void __launch_bounds__(224, 3)
   if (sidx >= a.nseg) break;
   load_segment(sh, a.seg, a.reps, sidx);
   __syncthreads();
-  if (!stage_bulk(sh, a.posf, st, &bar[2], (phase >> 2) & 1u, a.status)) {
+  if (!stage_bulk(sh, a.posf, st, &bar[3], (phase >> 3) & 1u, a.status)) {
     aborted = true;
     break;
   }
-  phase ^= 4u;
+  phase ^= 8u;
   put_sentinel(st, sh.S.staged);
   if (tripped) fill_offsets(sh, a.start);
   __syncthreads();
@@ -935,7 +935,7 @@ __global__ void __launch_bounds__(224, 3)
       const int x0 = base & ~7;  // 16-byte aligned start of the tile
       const int col = live ? p - x0 : tid;
       if (tid == 0) {
-        for (int t = 0; t < 2 && t < T; t++) {
+        for (int t = 0; t < nbuf && t < T; t++) {
           fence_proxy_async();
           mbar_expect_tx(&bar[t], tile_bytes);
           tma_load_2d(tiles + t * tile_elems, &rmap, x0, t * kClusterTileSlots, &bar[t]);
@@ -943,8 +943,8 @@ __global__ void __launch_bounds__(224, 3)
         }
       }
       bool failed = false;
-      for (int t = 0; t < T; t++) {
-        const int b = t & 1;
+      int b = 0;  // buffer of tile t: t mod nbuf
+      for (int t = 0; t < T; t++, b = b + 1 == nbuf ? 0 : b + 1) {
         const bool got = mbar_wait(&bar[b], (phase >> b) & 1u, a.status);
         const int wrem = wmax - t * kClusterTileSlots;  // warp-uniform
         if (got) {
@@ -964,10 +964,10 @@ __global__ void __launch_bounds__(224, 3)
           failed = true;
           break;
         }
-        if (tid == 0 && t + 2 < T) {
+        if (tid == 0 && t + nbuf < T) {
           fence_proxy_async();
           mbar_expect_tx(&bar[b], tile_bytes);
-          tma_load_2d(tiles + b * tile_elems, &rmap, x0, (t + 2) * kClusterTileSlots, &bar[b]);
+          tma_load_2d(tiles + b * tile_elems, &rmap, x0, (t + nbuf) * kClusterTileSlots, &bar[b]);
           inflight |= 1u << b;
         }
       }
@@ -975,8 +975,8 @@ __global__ void __launch_bounds__(224, 3)
         // a bounded wait ran out: give copies still in flight a bounded
         // chance to land in this block's shared memory, then leave
         if (tid == 0)
-          for (int b = 0; b < 2; b++)
-            if ((inflight >> b) & 1u) mbar_wait(&bar[b], (phase >> b) & 1u, a.status);
+          for (int k = 0; k < nbuf; k++)
+            if ((inflight >> k) & 1u) mbar_wait(&bar[k], (phase >> k) & 1u, a.status);
         aborted = true;
         break;
       }
@@ -1164,7 +1164,7 @@ template <typename K>
 void allow_smem(K kern) {
   cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)(sizeof(float4) * (kClusterMaxStaged + 1) +
-                             std::max(2 * kClusterTileSlots * 256 * sizeof(uint16_t),
+                             std::max(3 * kClusterTileSlots * 256 * sizeof(uint16_t),
                                       (size_t)8 * 2 * kWarpTileBytes)));
 }
 
@@ -1387,9 +1387,11 @@ int cluster_build(ClusterList& cl, const std::vector<ClusterReplica>& reps_in, f
 void launch_lj_cluster(const ClusterForceArgs& f, bool energy, cudaStream_t st) {
   const ClusterList& cl = *f.cl;
   if (cl.nseg == 0) return;
+  const bool block_tiles = cl.row_loads == 1 || cl.row_loads == 4;
+  const int nbuf = cl.row_loads == 4 ? 3 : 2;
   const size_t tiles =
-      cl.row_loads == 1 ? 2 * kClusterTileSlots * (size_t)(cl.block + 8) * sizeof(uint16_t)
-                        : (cl.row_loads == 3 ? (size_t)(cl.block / 32) * 2 * kWarpTileBytes : 0);
+      block_tiles ? nbuf * kClusterTileSlots * (size_t)(cl.block + 8) * sizeof(uint16_t)
+                  : (cl.row_loads == 3 ? (size_t)(cl.block / 32) * 2 * kWarpTileBytes : 0);
   const size_t smem = tiles + stage_bytes(cl.max_staged);
   ClStep a;
   a.nseg = cl.nseg;
@@ -1406,7 +1408,7 @@ void launch_lj_cluster(const ClusterForceArgs& f, bool energy, cudaStream_t st) 
   a.cap = cl.cap;
   a.rv2 = cl.rv2;
   a.pos_build = cl.pos_build;
-  a.skin = cl.skin;
+  a.skin = f.skin ? f.skin : cl.skin;
   a.flag_read = f.step % 3;
   a.flag_set = (f.step + 1) % 3;
   a.flag_clear = (f.step + 2) % 3;
@@ -1416,6 +1418,7 @@ void launch_lj_cluster(const ClusterForceArgs& f, bool energy, cudaStream_t st) 
   a.status = f.status;
   if (f.gear) a.g = *f.gear;
   else memset(&a.g, 0, sizeof(a.g));
+  a.nbuf = nbuf;
   // persistent grid: as many blocks as fit on the GPU at once, at most one
   // per segment
   auto grid_for = [&](const void* kern) {
@@ -1437,7 +1440,7 @@ void launch_lj_cluster(const ClusterForceArgs& f, bool energy, cudaStream_t st) 
   k_lj_cl<E, A, G, T><<<grid_for((const void*)k_lj_cl<E, A, G, T>), cl.block, smem, st>>>( \
       M, a)
 #define MDGB_CL_LAUNCH(E, A, G)                  \
-  if (cl.row_loads == 1)                         \
+  if (block_tiles)                               \
     MDGB_CL_LAUNCH2(E, A, G, 0, cl.rmap);        \
   else if (cl.row_loads == 3)                    \
     MDGB_CL_LAUNCH2(E, A, G, 2, cl.rmap_w);      \

@@ -129,6 +129,7 @@ struct ClusterForceArgs {
   double* epart;     // 3 doubles per segment block (energy)
   int* status;       // ST_TMA_TIMEOUT / ST_NONFINITE
   const ClusterGearArgs* gear;  // NULL: forces only
+  int* skin = nullptr;          // skin flags (NULL: the list's own)
 };
 void launch_lj_cluster(const ClusterForceArgs& a, bool energy, cudaStream_t st);
 int cluster_blocks(const ClusterList& cl);

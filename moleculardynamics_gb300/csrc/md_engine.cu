@@ -835,7 +835,7 @@ md_status md_create(const md_config* cfg, md_ctx** out) {
   if (cfg->cluster_cells < 0 || cfg->cluster_cells > kClusterMaxZ) return MD_BAD_CONFIG;
   if (cfg->cluster_threads < 0 || cfg->cluster_threads > 224 || cfg->cluster_threads % 32)
     return MD_BAD_CONFIG;
-  if (cfg->cluster_row_loads < 0 || cfg->cluster_row_loads > 3) return MD_BAD_CONFIG;
+  if (cfg->cluster_row_loads < 0 || cfg->cluster_row_loads > 4) return MD_BAD_CONFIG;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= cfg->device || cfg->device < 0)
     return MD_NO_DEVICE;
@@ -1183,7 +1183,7 @@ md_status md_autotune(md_ctx* c, int evals, md_tune_result* out) {
   const std::vector<int> caps = {1152, 1536, kClusterMaxStaged};
   const std::vector<int> loads = c->cfg.cluster_row_loads > 0
                                      ? std::vector<int>{c->cfg.cluster_row_loads}
-                                     : std::vector<int>{1, 2, 3};
+                                     : std::vector<int>{1, 2, 3, 4};
   cudaEvent_t e0, e1;
   CK(cudaEventCreate(&e0), "autotune");
   CK(cudaEventCreate(&e1), "autotune");
@@ -1191,6 +1191,29 @@ md_status md_autotune(md_ctx* c, int evals, md_tune_result* out) {
   int best_t = c->cl.block, best_c = c->cl.stage_cap, best_l = c->cl.row_loads, tried = 0;
   std::vector<ClusterReplica> reps = cluster_reps(c);
   double** v3[5] = {&c->vel, &c->acc, &c->b, &c->c, &c->f3};
+  // Where steps fuse the Gear update into the force kernel, candidates are
+  // timed as that kernel, on a scratch copy of the Gear state and scratch
+  // skin flags (the timing leaves the trajectory untouched).
+  const bool fused = c->mixed() && !c->walls();
+  const size_t n3 = 3 * (size_t)c->n;
+  double* gs = nullptr;
+  int* skin_s = nullptr;
+  if (fused) {
+    CK(cudaMalloc(&gs, sizeof(double) * 4 * n3), "autotune scratch");
+    if (cudaMalloc(&skin_s, sizeof(int) * 8) != cudaSuccess) {
+      cudaFree(gs);
+      return cuda_fail(c, cudaErrorMemoryAllocation, "autotune scratch");
+    }
+  }
+  ClusterGearArgs cg;
+  auto launch = [&]() {
+    ClusterForceArgs a = cl_args(c, c->f3_tmp, nullptr);
+    if (fused) {
+      a.gear = &cg;
+      a.skin = skin_s;
+    }
+    launch_lj_cluster(a, false, c->st);
+  };
   auto build = [&](int t, int cap, int ld) -> md_status {
     c->cl.block = t;
     c->cl.stage_cap = cap;
@@ -1210,10 +1233,27 @@ md_status md_autotune(md_ctx* c, int evals, md_tune_result* out) {
   for (const int3& k3 : cand) {
       const int ld = k3.x, t = k3.y, cap = k3.z;
       if ((s = build(t, cap, ld)) != MD_OK) break;
-      launch_lj_cluster(cl_args(c, c->f3_tmp, nullptr), false, c->st);  // warm
+      if (fused) {
+        // the build put the state in cell order: copy it after each build
+        double* src[4] = {c->vel, c->acc, c->b, c->c};
+        for (int k = 0; k < 4; k++)
+          cudaMemcpyAsync(gs + k * n3, src[k], sizeof(double) * n3, cudaMemcpyDeviceToDevice,
+                          c->st);
+        cudaMemsetAsync(skin_s, 0, sizeof(int) * 8, c->st);
+        GearArgs g = gear_args(c, c->t + 1);
+        cg.pos_next = c->pos_alt;
+        cg.posf_next = c->posf_alt;
+        cg.vel = gs;
+        cg.acc = gs + n3;
+        cg.b = gs + 2 * n3;
+        cg.c = gs + 3 * n3;
+        cg.k = c->gear;
+        for (int k = 0; k < 3; k++) cg.inv_mass[k] = g.inv_mass[k];
+        cg.trip2 = g.trip2;
+      }
+      launch();  // warm
       cudaEventRecord(e0, c->st);
-      for (int k = 0; k < evals; k++)
-        launch_lj_cluster(cl_args(c, c->f3_tmp, nullptr), false, c->st);
+      for (int k = 0; k < evals; k++) launch();
       cudaEventRecord(e1, c->st);
       cudaError_t ce = cudaEventSynchronize(e1);
       float ms = 0;
@@ -1232,6 +1272,11 @@ md_status md_autotune(md_ctx* c, int evals, md_tune_result* out) {
     }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
+  if (fused) {
+    cudaStreamSynchronize(c->st);
+    cudaFree(gs);
+    cudaFree(skin_s);
+  }
   if (s != MD_OK) return s;
   if ((s = build(best_t, best_c, best_l)) != MD_OK) return s;
   c->stats.cluster_segments = c->cl.nseg;

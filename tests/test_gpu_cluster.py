@@ -80,7 +80,8 @@ def test_cluster_independent_of_tiling(eng):
     n = len(pos)
     ref = None
     for cells, threads, loads in [(0, 0, 1), (1, 32, 2), (3, 224, 1), (64, 64, 2), (0, 0, 2),
-                                  (0, 0, 3), (2, 224, 3), (0, 32, 3)]:
+                                  (0, 0, 3), (2, 224, 3), (0, 32, 3), (0, 0, 4), (2, 224, 4),
+                                  (1, 32, 4)]:
         with _engine(eng, n, L, lj_kernel=eng.LJ_CLUSTER, cluster_cells=cells,
                      cluster_threads=threads, cluster_row_loads=loads) as e:
             e.upload(pos, vel)
@@ -179,5 +180,5 @@ def test_autotune_keeps_forces(eng):
         f1, _ = e.compute_forces()
         e.step(10)
     assert r["candidates"] >= 1 and r["threads"] in (64, 96, 128, 160, 192)
-    assert r["row_loads"] in (1, 2, 3)
+    assert r["row_loads"] in (1, 2, 3, 4)
     assert np.array_equal(f0, f1)
