@@ -352,10 +352,40 @@ int mdgb_last_status(void);
  * Optional extension keys: Periodic, Box, Precision, Species, Device. */
 md_status md_read_config(const char* path, md_config* cfg, char* strings, double* extra,
                          char* err, int err_len);
-/* Writes the .dat/.txt result pair of common/Results.cpp:120-229. */
+/* Writes the .dat/.txt result pair of common/Results.cpp:120-229; the
+ * many-body pair list of the .txt (tailResults, common/Results.cpp:88-118)
+ * is computed on the host from pos4. */
 md_status md_write_results(const char* filename, const md_config* cfg, float vxcm,
                            float elapsed_ms, const md_thermo* records, int nrec,
                            const double* pos4);
+/* The same files with the pair list given: pairs[2k], pairs[2k + 1] for
+ * k < npairs (from md_tail_pairs). */
+md_status md_write_results_pairs(const char* filename, const md_config* cfg, float vxcm,
+                                 float elapsed_ms, const md_thermo* records, int nrec,
+                                 const int* pairs, int npairs);
+
+/* ---- run outputs on the device (common/Results.cpp) ---- */
+/* Animation frames (pushAnim and writeAnimationBinaryData,
+ * common/Results.cpp:12-31,51-86).  every >= 0 captures a frame at md_begin
+ * and then at steps every, 2 every, ... (every = 0: one more frame at step 0,
+ * as cpu/cpumd/Host.cpp:83,126,188-192 behave); every < 0 stops capturing.
+ * A frame is the state converted to float on the device and copied to
+ * pinned host memory on a copy stream, so capturing does not stop the step
+ * loop; frames_hint sizes the first pinned block (more are allocated when a
+ * run outgrows it).  md_begin starts a new set of frames. */
+md_status md_set_animation(md_ctx* ctx, int every, int frames_hint);
+int md_animation_count(const md_ctx* ctx);
+/* frame k: n x float4 positions (x, y, z, type) and n x float3 velocities
+ * in the caller's numbering (either pointer may be NULL) */
+md_status md_get_animation_frame(md_ctx* ctx, int k, float* pos4, float* vel3);
+/* writes "<anim_file>(vxcm-<vxcm>).anm": int atoms, int animation steps,
+ * int frames, every frame's positions, then every frame's velocities */
+md_status md_write_animation(md_ctx* ctx, const char* anim_file, float vxcm);
+/* tailResults on the device: pairs i < j of the first n_mb atoms of
+ * different species closer than 2 reNO (FP64, the reference's arithmetic),
+ * in the reference's order; the first `capacity` pairs into pairs[2k],
+ * pairs[2k + 1], their total into *count. */
+md_status md_tail_pairs(md_ctx* ctx, int* pairs, int capacity, int* count);
 
 #ifdef __cplusplus
 }

@@ -18,7 +18,7 @@ BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libmdgb.so")
 RUN = os.path.join(PKG, "mdgb_run")
 
-CU_SOURCES = ["md_neighbor.cu", "md_forces.cu", "md_cluster.cu", "md_surrogate.cu", "md_integrate.cu", "md_engine.cu",
+CU_SOURCES = ["md_neighbor.cu", "md_forces.cu", "md_cluster.cu", "md_surrogate.cu", "md_integrate.cu", "md_output.cu", "md_engine.cu",
               "md_refshim.cu", "md_static.cu"]
 CPP_SOURCES = ["md_io.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -13,6 +13,7 @@
 // (the wall flag, as the reference's CUDA host also reads it every step) and
 // at the end of md_step.  The periodic mode has no walls and no per-step
 // host round trip.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -24,6 +25,7 @@
 #include "md_forces.h"
 #include "md_integrate.h"
 #include "md_neighbor.cuh"
+#include "md_output.h"
 #include "md_surrogate.h"
 
 using namespace mdgb;
@@ -156,6 +158,17 @@ struct md_ctx {
   std::vector<int> pending_weight;  // launches each pending interval stands for
   double kt_ms[kKernels] = {0, 0, 0, 0, 0, 0, 0};
   long long kt_n[kKernels] = {0, 0, 0, 0, 0, 0, 0};
+
+  // animation frames (cpu/cpumd/Host.cpp:83,126,188-192): converted on the
+  // device into one of two slots and streamed to pinned host blocks on
+  // io_st; a slot is reused only after its copy completed (a stream wait,
+  // not a host wait)
+  int anim_every = -1, anim_next = 0, anim_frames = 0, anim_slot = 0, anim_per_block = 1;
+  float* anim_dev = nullptr;  // 2 slots of 7 floats per atom
+  cudaStream_t io_st = nullptr;
+  cudaEvent_t anim_ready[2] = {nullptr, nullptr}, anim_done[2] = {nullptr, nullptr};
+  bool anim_busy[2] = {false, false};
+  std::vector<float*> anim_blocks;  // pinned host memory, anim_per_block frames each
 
   bool mixed() const { return cfg.precision == MD_PREC_MIXED; }
   bool permuted() const { return cluster && cl.built; }
@@ -605,6 +618,35 @@ md_status push_record(md_ctx* c, int t) {
   return s;
 }
 
+// One animation frame of the current state (pushAnim, common/Results.cpp:12-31).
+md_status capture_frame(md_ctx* c) {
+  const size_t per = 7 * (size_t)c->n;
+  const size_t fb = sizeof(float) * per;
+  const int s = c->anim_slot;
+  c->anim_slot ^= 1;
+  if (c->anim_busy[s]) CK(cudaStreamWaitEvent(c->st, c->anim_done[s], 0), "animation");
+  float* slot = c->anim_dev + (size_t)s * per;
+  launch_anim_pack(c->pos, c->vel, c->permuted() ? c->cl.orig : nullptr, c->n, slot, c->st);
+  c->stats.launches++;
+  CK(cudaEventRecord(c->anim_ready[s], c->st), "animation");
+  const size_t blk = (size_t)(c->anim_frames / c->anim_per_block);
+  while (c->anim_blocks.size() <= blk) {
+    float* h = nullptr;
+    CK(cudaHostAlloc((void**)&h, fb * (size_t)c->anim_per_block, cudaHostAllocDefault),
+       "animation frames");
+    c->anim_blocks.push_back(h);
+  }
+  float* host = c->anim_blocks[blk] + (size_t)(c->anim_frames % c->anim_per_block) * per;
+  CK(cudaStreamWaitEvent(c->io_st, c->anim_ready[s], 0), "animation");
+  CK(cudaMemcpyAsync(host, slot, fb, cudaMemcpyDeviceToHost, c->io_st), "animation");
+  CK(cudaEventRecord(c->anim_done[s], c->io_st), "animation");
+  c->anim_busy[s] = true;
+  c->anim_frames++;
+  return MD_OK;
+}
+
+bool anim_due(const md_ctx* c, int t) { return c->anim_every >= 0 && c->anim_next == t; }
+
 bool due(const md_ctx* c, int t) {
   return (c->cfg.use_lj && c->lj_next == t) || (c->cfg.use_mb && c->mb_next == t);
 }
@@ -650,6 +692,7 @@ bool window_ok(const md_ctx* c, int s, int nsteps) {
   const int t = c->t;
   for (int u = 0; u < kGraphSteps; u++) {
     if (c->cfg.output_timesteps > 0 && c->printout == t + u) return false;
+    if (anim_due(c, t + u)) return false;
     if (due(c, t + u + 1)) return false;
   }
   return true;
@@ -741,7 +784,8 @@ md_status step_once(md_ctx* c, bool last) {
   }
   c->predicted = false;
   const bool output = c->cfg.output_timesteps > 0 && c->printout == t;
-  const bool fuse = c->mixed() && !c->walls() && !last && !output && !due(c, t + 1);
+  const bool anim = anim_due(c, t);
+  const bool fuse = c->mixed() && !c->walls() && !last && !output && !anim && !due(c, t + 1);
   if (c->cluster && fuse) {
     {
       Timed tm(c, 6);
@@ -780,6 +824,11 @@ md_status step_once(md_ctx* c, bool last) {
     md_status s = push_record(c, t);
     if (s != MD_OK) return s;
     c->printout += c->cfg.output_timesteps;
+  }
+  if (anim) {
+    md_status s = capture_frame(c);
+    if (s != MD_OK) return s;
+    c->anim_next += c->anim_every;
   }
   c->t++;
   c->stats.steps++;
@@ -893,6 +942,16 @@ md_status md_create(const md_config* cfg, md_ctx** out) {
 void md_destroy(md_ctx* c) {
   if (!c) return;
   if (c->st) cudaStreamSynchronize(c->st);
+  if (c->io_st) {
+    cudaStreamSynchronize(c->io_st);
+    cudaStreamDestroy(c->io_st);
+  }
+  for (float* h : c->anim_blocks) cudaFreeHost(h);
+  for (int k = 0; k < 2; k++) {
+    if (c->anim_ready[k]) cudaEventDestroy(c->anim_ready[k]);
+    if (c->anim_done[k]) cudaEventDestroy(c->anim_done[k]);
+  }
+  if (c->anim_dev) cudaFree(c->anim_dev);
   list_free(c->lj);
   list_free(c->mb);
   cluster_free(c->cl);
@@ -1003,6 +1062,14 @@ md_status md_begin(md_ctx* c, float vxcm) {
   if (c->cfg.output_timesteps > 0) {
     s = push_record(c, 0);
     if (s != MD_OK) return s;
+  }
+  // the frames of a run start with the state before its first step
+  // (cpu/cpumd/Host.cpp:126-127; flushVectors clears them per run)
+  c->anim_frames = 0;
+  if (c->anim_every >= 0) {
+    s = capture_frame(c);
+    if (s != MD_OK) return s;
+    c->anim_next = c->anim_every;
   }
   forces(c, c->f3);
   launch_accel(c->pos, c->acc, c->f3, c->n, c->sp, c->st);
@@ -1289,6 +1356,90 @@ md_status md_autotune(md_ctx* c, int evals, md_tune_result* out) {
     out->best_ms = best / evals;
   }
   return check_status(c);
+}
+
+md_status md_set_animation(md_ctx* c, int every, int frames_hint) {
+  if (!c) return MD_BAD_ARGUMENT;
+  if (every < 0) {
+    c->anim_every = -1;
+    return MD_OK;
+  }
+  const size_t fb = sizeof(float) * 7 * (size_t)c->n;
+  if (!c->anim_dev) {
+    CK(cudaMalloc(&c->anim_dev, 2 * fb), "animation");
+    CK(cudaStreamCreateWithFlags(&c->io_st, cudaStreamNonBlocking), "animation");
+    for (int k = 0; k < 2; k++) {
+      CK(cudaEventCreateWithFlags(&c->anim_ready[k], cudaEventDisableTiming), "animation");
+      CK(cudaEventCreateWithFlags(&c->anim_done[k], cudaEventDisableTiming), "animation");
+    }
+  }
+  if (c->anim_blocks.empty()) {
+    // the first pinned block holds frames_hint frames (at most 1 GB), so
+    // runs within the hint never allocate while stepping
+    const size_t cap = std::max<size_t>(1, ((size_t)1 << 30) / fb);
+    c->anim_per_block = (int)std::max<size_t>(
+        1, std::min<size_t>(frames_hint > 0 ? (size_t)frames_hint : 16, cap));
+    float* h = nullptr;
+    CK(cudaHostAlloc((void**)&h, fb * (size_t)c->anim_per_block, cudaHostAllocDefault),
+       "animation frames");
+    c->anim_blocks.push_back(h);
+  }
+  c->anim_every = every;
+  return MD_OK;
+}
+
+int md_animation_count(const md_ctx* c) { return c ? c->anim_frames : 0; }
+
+md_status md_get_animation_frame(md_ctx* c, int k, float* pos4, float* vel3) {
+  if (!c || k < 0 || k >= c->anim_frames || (!pos4 && !vel3)) return MD_BAD_ARGUMENT;
+  CK(cudaStreamSynchronize(c->io_st), "animation");
+  const size_t n = (size_t)c->n;
+  const float* f = c->anim_blocks[k / c->anim_per_block] + (size_t)(k % c->anim_per_block) * 7 * n;
+  if (pos4) memcpy(pos4, f, sizeof(float) * 4 * n);
+  if (vel3) memcpy(vel3, f + 4 * n, sizeof(float) * 3 * n);
+  return MD_OK;
+}
+
+// common/Results.cpp:51-86: header (atoms, animation timesteps, frames), every
+// frame's positions, then every frame's velocities
+md_status md_write_animation(md_ctx* c, const char* anim_file, float vxcm) {
+  if (!c || !anim_file) return MD_BAD_ARGUMENT;
+  if (c->io_st) CK(cudaStreamSynchronize(c->io_st), "animation");
+  std::string name = std::string(anim_file) + "(vxcm-";
+  {
+    char buf[64];
+    // the reference streams the float with the default ostream format
+    std::snprintf(buf, sizeof(buf), "%g", (double)vxcm);
+    name += buf;
+  }
+  name += ").anm";
+  FILE* fp = std::fopen(name.c_str(), "wb");
+  if (!fp) return fail(c, MD_BAD_ARGUMENT, "cannot open " + name);
+  const int nop = c->n, every = c->anim_every, count = c->anim_frames;
+  bool ok = std::fwrite(&nop, sizeof(int), 1, fp) == 1 &&
+            std::fwrite(&every, sizeof(int), 1, fp) == 1 &&
+            std::fwrite(&count, sizeof(int), 1, fp) == 1;
+  const size_t n = (size_t)c->n;
+  for (int part = 0; part < 2 && ok; part++)
+    for (int k = 0; k < count && ok; k++) {
+      const float* f =
+          c->anim_blocks[k / c->anim_per_block] + (size_t)(k % c->anim_per_block) * 7 * n;
+      const size_t m = part == 0 ? 4 * n : 3 * n;
+      ok = std::fwrite(part == 0 ? f : f + 4 * n, sizeof(float), m, fp) == m;
+    }
+  ok = std::fclose(fp) == 0 && ok;
+  return ok ? MD_OK : fail(c, MD_BAD_ARGUMENT, "error writing " + name);
+}
+
+md_status md_tail_pairs(md_ctx* c, int* pairs, int capacity, int* count) {
+  if (!c || !count || capacity < 0 || (capacity > 0 && !pairs)) return MD_BAD_ARGUMENT;
+  *count = 0;
+  // many-body atoms are the first n_mb in the caller's numbering; the cell
+  // order of the cluster path only exists without them
+  if (c->cfg.n_mb < 2 || c->permuted()) return MD_OK;
+  int r = tail_pairs(c->pos, c->cfg.n_mb, pairs, capacity, count, c->st);
+  if (r) return cuda_fail(c, (cudaError_t)r, "tail pairs");
+  return MD_OK;
 }
 
 md_status md_set_graphs(md_ctx* c, int on) {

@@ -17,6 +17,7 @@
 #include <sstream>
 #include <string>
 #include <unordered_map>
+#include <vector>
 
 #include "../../include/mdgb.h"
 
@@ -230,27 +231,20 @@ extern "C" md_status md_read_config(const char* path, md_config* cfg, char* stri
   return MD_OK;
 }
 
-extern "C" md_status md_write_results(const char* filename, const md_config* cfg, float vxcm,
-                                      float elapsed, const md_thermo* recs, int nrec,
-                                      const double* pos4) {
-  if (!filename || !cfg || (nrec > 0 && !recs)) return MD_BAD_ARGUMENT;
-  // common/Results.cpp:88-118 tailResults
+namespace {
+
+// common/Results.cpp:88-118 tailResults: the text of the pair list
+std::string tail_text(const int* pairs, int npairs) {
   std::stringstream ssPairs, tail;
-  int pairs = 0;
   tail << "ManyBody Pairs:\n";
-  for (int i = 0; pos4 && i < cfg->n_mb; i++)
-    for (int j = i + 1; j < cfg->n_mb; j++) {
-      if ((int)pos4[4 * i + 3] == (int)pos4[4 * j + 3]) continue;
-      double dx = pos4[4 * i] - pos4[4 * j];
-      double dy = pos4[4 * i + 1] - pos4[4 * j + 1];
-      double dz = pos4[4 * i + 2] - pos4[4 * j + 2];
-      double dist = sqrt(dx * dx + dy * dy + dz * dz);
-      if (dist < 2 * 1.15f) {
-        pairs++;
-        ssPairs << "[" << i << ", " << j << "] ";
-      }
-    }
-  tail << "Amount: " << pairs << "\n" << ssPairs.str();
+  for (int k = 0; k < npairs; k++) ssPairs << "[" << pairs[2 * k] << ", " << pairs[2 * k + 1] << "] ";
+  tail << "Amount: " << npairs << "\n" << ssPairs.str();
+  return tail.str();
+}
+
+// common/Results.cpp:120-229 writeResults with the tail text given
+md_status write_results(const char* filename, const md_config* cfg, float vxcm, float elapsed,
+                        const md_thermo* recs, int nrec, const std::string& tail_str) {
   std::stringstream rf, lf;
   rf << filename << "(vxcm-" << vxcm << ").dat";
   lf << filename << "(vxcm-" << vxcm << ").txt";
@@ -298,7 +292,39 @@ extern "C" md_status md_write_results(const char* filename, const md_config* cfg
         << "\t" << r.momentum_z;
     log << std::fixed;
   }
-  log << "\n\n" << tail.str();
+  log << "\n\n" << tail_str;
   if (result.fail() || log.fail()) return MD_BAD_ARGUMENT;
   return MD_OK;
+}
+
+}  // namespace
+
+extern "C" md_status md_write_results(const char* filename, const md_config* cfg, float vxcm,
+                                      float elapsed, const md_thermo* recs, int nrec,
+                                      const double* pos4) {
+  if (!filename || !cfg || (nrec > 0 && !recs)) return MD_BAD_ARGUMENT;
+  // common/Results.cpp:88-118 tailResults over the many-body atoms
+  std::vector<int> pairs;
+  for (int i = 0; pos4 && i < cfg->n_mb; i++)
+    for (int j = i + 1; j < cfg->n_mb; j++) {
+      if ((int)pos4[4 * i + 3] == (int)pos4[4 * j + 3]) continue;
+      double dx = pos4[4 * i] - pos4[4 * j];
+      double dy = pos4[4 * i + 1] - pos4[4 * j + 1];
+      double dz = pos4[4 * i + 2] - pos4[4 * j + 2];
+      double dist = sqrt(dx * dx + dy * dy + dz * dz);
+      if (dist < 2 * 1.15f) {
+        pairs.push_back(i);
+        pairs.push_back(j);
+      }
+    }
+  return write_results(filename, cfg, vxcm, elapsed, recs, nrec,
+                       tail_text(pairs.data(), (int)pairs.size() / 2));
+}
+
+extern "C" md_status md_write_results_pairs(const char* filename, const md_config* cfg,
+                                            float vxcm, float elapsed, const md_thermo* recs,
+                                            int nrec, const int* pairs, int npairs) {
+  if (!filename || !cfg || (nrec > 0 && !recs) || npairs < 0 || (npairs > 0 && !pairs))
+    return MD_BAD_ARGUMENT;
+  return write_results(filename, cfg, vxcm, elapsed, recs, nrec, tail_text(pairs, npairs));
 }

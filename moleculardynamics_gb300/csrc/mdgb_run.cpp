@@ -46,11 +46,18 @@ int main(int argc, char** argv) {
     std::cerr << err << std::endl;
     return EXIT_FAILURE;
   }
-  const std::string input = strs, output = strs + 512, filename = strs + 1024;
+  const std::string input = strs, output = strs + 512, filename = strs + 1024,
+                    animfile = strs + 1536;
+  const int animts = (int)extra[5];
   std::cout << "Molecular::Dynamics\n";
   md_ctx* ctx = nullptr;
   md_status s = md_create(&cfg, &ctx);
   if (s != MD_OK) die(std::string("engine: ") + md_status_string(s));
+  // animation frames while animts > -1 (cpu/cpumd/Host.cpp:126,188,212)
+  if (animts > -1) {
+    const int frames = animts > 0 ? cfg.timesteps / animts + 2 : 2;
+    if ((s = md_set_animation(ctx, animts, frames)) != MD_OK) die(md_last_error(ctx));
+  }
   const int n = cfg.n_lj + cfg.n_mb;
   std::vector<double> pos(4 * (size_t)n), vel(3 * (size_t)n);
   const float vfrom = (float)extra[1], vto = (float)extra[2], vstep = (float)extra[3];
@@ -91,9 +98,17 @@ int main(int argc, char** argv) {
       if (!out.good()) die("Error writing to output file file.");
     }
     out.close();
-    if (md_write_results(filename.c_str(), &cfg, vxcm, elapsed, recs.data(), (int)recs.size(),
-                         pos.data()) != MD_OK)
+    // the many-body pair list of the .txt, on the device
+    int npairs = 0;
+    if ((s = md_tail_pairs(ctx, nullptr, 0, &npairs)) != MD_OK) die(md_last_error(ctx));
+    std::vector<int> pairs(2 * (size_t)npairs);
+    if (npairs > 0 && (s = md_tail_pairs(ctx, pairs.data(), npairs, &npairs)) != MD_OK)
+      die(md_last_error(ctx));
+    if (md_write_results_pairs(filename.c_str(), &cfg, vxcm, elapsed, recs.data(),
+                               (int)recs.size(), pairs.data(), npairs) != MD_OK)
       die("Error writing to result file.");
+    if (animts > -1 && md_write_animation(ctx, animfile.c_str(), vxcm) != MD_OK)
+      die(md_last_error(ctx));
     if (!(vstep > 0)) break;  // the reference loops forever on a zero step
   }
   md_destroy(ctx);

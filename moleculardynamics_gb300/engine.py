@@ -97,7 +97,9 @@ EXPORTS = ["md_create", "md_destroy", "md_status_string", "md_last_error", "md_u
            "mdgb_lennard_jones_forces", "mdgb_many_body_forces", "mdgb_calculate_accelerations",
            "mdgb_build_neighbor_list", "mdgb_free", "mdgb_perform_calculations",
            "mdgb_calculate_potential", "mdgb_set_species", "mdgb_last_status", "md_read_config",
-           "md_write_results", "md_host_alloc", "md_host_free",
+           "md_write_results", "md_write_results_pairs", "md_host_alloc", "md_host_free",
+           "md_set_animation", "md_animation_count", "md_get_animation_frame",
+           "md_write_animation", "md_tail_pairs",
            "mdgb_many_body_forces_static", "md_autotune", "md_set_graphs", "md_batch_create",
            "md_batch_size", "md_batch_records", "mdgb_tc_selftest", "mdgb_conv_selftest",
            "md_surrogate_create",
@@ -191,6 +193,14 @@ def load(path: str | None = None) -> C.CDLL:
                                  C.c_char_p, C.c_int]
     L.md_write_results.argtypes = [C.c_char_p, P(MdConfig), C.c_float, C.c_float,
                                    C.c_void_p, C.c_int, C.c_void_p]
+    L.md_write_results_pairs.argtypes = [C.c_char_p, P(MdConfig), C.c_float, C.c_float,
+                                         C.c_void_p, C.c_int, C.c_void_p, C.c_int]
+    L.md_set_animation.argtypes = [C.c_void_p, C.c_int, C.c_int]
+    L.md_animation_count.restype = C.c_int
+    L.md_animation_count.argtypes = [C.c_void_p]
+    L.md_get_animation_frame.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
+    L.md_write_animation.argtypes = [C.c_void_p, C.c_char_p, C.c_float]
+    L.md_tail_pairs.argtypes = [C.c_void_p, C.c_void_p, C.c_int, P(C.c_int)]
     if path is None:
         _lib = L
     return L
@@ -329,6 +339,35 @@ class Engine:
 
     def set_graphs(self, on: bool):
         self._ck(self.lib.md_set_graphs(self.h, int(on)), "md_set_graphs")
+
+    def set_animation(self, every: int, frames_hint: int = 0):
+        """Animation frames every `every` steps from md_begin on (-1: off)."""
+        self._ck(self.lib.md_set_animation(self.h, every, frames_hint), "md_set_animation")
+
+    def animation_count(self) -> int:
+        return self.lib.md_animation_count(self.h)
+
+    def animation_frame(self, k: int):
+        """(positions n x 4 float32, velocities n x 3 float32) of frame k."""
+        p = np.zeros((self.n, 4), np.float32)
+        v = np.zeros((self.n, 3), np.float32)
+        self._ck(self.lib.md_get_animation_frame(self.h, k, p.ctypes.data, v.ctypes.data),
+                 "md_get_animation_frame")
+        return p, v
+
+    def write_animation(self, anim_file: str, vxcm: float = 0.0):
+        self._ck(self.lib.md_write_animation(self.h, anim_file.encode(), vxcm),
+                 "md_write_animation")
+
+    def tail_pairs(self) -> np.ndarray:
+        """Many-body pairs closer than 2 reNO (k x 2, the reference's order)."""
+        cnt = C.c_int(0)
+        self._ck(self.lib.md_tail_pairs(self.h, None, 0, C.byref(cnt)), "md_tail_pairs")
+        out = np.zeros((max(cnt.value, 1), 2), np.int32)
+        if cnt.value:
+            self._ck(self.lib.md_tail_pairs(self.h, out.ctypes.data, cnt.value, C.byref(cnt)),
+                     "md_tail_pairs")
+        return out[:cnt.value]
 
 
 class Surrogate:

@@ -69,6 +69,41 @@ def test_results_files_are_byte_identical(eng, tmp_path):
         assert mine == ref, ext
 
 
+def test_results_files_from_a_pair_list(eng, tmp_path):
+    """md_write_results_pairs (the pair list given, as md_tail_pairs returns
+    it) writes the same bytes as the reference's writeResults."""
+    import ctypes as C
+    recs = np.load(os.path.join(GOLD, "results_records.npy"))
+    gold = np.load(os.path.join(GOLD, "reference_fixtures.npz"))
+    pos = np.ascontiguousarray(gold["bo_no/pos"])
+    n = len(pos)
+    cfg = eng.make_config(n_lj=0, n_mb=n, dt=2.0, timesteps=200, lj_rs=9.0, lj_rcut=8.0,
+                          use_lj=0, use_mb=1, mb_rs=3.5, mb_rcut=3.0)
+    # tailResults restated (common/Results.cpp:88-118)
+    lim = float(np.float32(2) * np.float32(1.15))
+    pairs = []
+    for i in range(n):
+        for j in range(i + 1, n):
+            if int(pos[i, 3]) == int(pos[j, 3]):
+                continue
+            dx, dy, dz = pos[i, :3] - pos[j, :3]
+            if np.sqrt(dx * dx + dy * dy + dz * dz) < lim:
+                pairs += [i, j]
+    flat = np.ascontiguousarray(np.array(pairs, np.int32))
+    th = np.zeros((3, 16))
+    th[:, :11] = recs
+    th = np.ascontiguousarray(th)
+    stem = str(tmp_path / "res")
+    L = eng.load()
+    s = L.md_write_results_pairs(stem.encode(), C.byref(cfg), 0.5, 123.0, th.ctypes.data, 3,
+                                 flat.ctypes.data, len(flat) // 2)
+    assert s == 0
+    for ext in ("dat", "txt"):
+        mine = open(f"{stem}(vxcm-0.5).{ext}", "rb").read()
+        ref = open(os.path.join(GOLD, f"results_vxcm-0.5.{ext}"), "rb").read()
+        assert mine == ref, ext
+
+
 def test_input_output_text_format(tmp_path, reference):
     """lattice.write_input writes what the reference's readInput reads."""
     from moleculardynamics_gb300 import lattice as lat
