@@ -381,6 +381,24 @@ md_status md_get_animation_frame(md_ctx* ctx, int k, float* pos4, float* vel3);
 /* writes "<anim_file>(vxcm-<vxcm>).anm": int atoms, int animation steps,
  * int frames, every frame's positions, then every frame's velocities */
 md_status md_write_animation(md_ctx* ctx, const char* anim_file, float vxcm);
+/* ---- equi: initial velocities (cpu/equi/Host.cpp:416-572) ---- */
+/* chooseVelocities on the device state: Maxwell-Boltzmann draws at
+ * temperature (kelvin; x 8.314e-7 as equi's rb) from a counter-based
+ * generator (splitmix64 of seed, atom, component; uniforms on (0, 1) with
+ * 2^32 levels in place of rand()), inverse error function (CUDA erfinv),
+ * momentum removal to 1e-15 and rescaling to the temperature.  Kept from the
+ * reference: many-body atoms i, i + 1 (i even, i < n_mb) share one draw made
+ * with atom i's mass; the momentum sums before the removal count such a pair
+ * once, and so does the total mass; the z draw applies the inverse error
+ * function before the affine map.  Where the reference's removal loop would
+ * never converge (the pairs' second atoms weigh as much as totalm or more,
+ * e.g. N-N pairs only), MD_BAD_ARGUMENT. */
+md_status md_choose_velocities(md_ctx* ctx, double temperature, unsigned long long seed);
+/* equi's schedule (cpu/equi/Host.cpp:174-175): after every step t with
+ * t % every == 0 (every = 50 in the reference) new velocities as
+ * md_choose_velocities, each from a new stream of seed; every <= 0: off. */
+md_status md_set_equilibration(md_ctx* ctx, double temperature, unsigned long long seed,
+                               int every);
 /* tailResults on the device: pairs i < j of the first n_mb atoms of
  * different species closer than 2 reNO (FP64, the reference's arithmetic),
  * in the reference's order; the first `capacity` pairs into pairs[2k],

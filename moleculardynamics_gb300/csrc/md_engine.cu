@@ -169,6 +169,11 @@ struct md_ctx {
   cudaEvent_t anim_ready[2] = {nullptr, nullptr}, anim_done[2] = {nullptr, nullptr};
   bool anim_busy[2] = {false, false};
   std::vector<float*> anim_blocks;  // pinned host memory, anim_per_block frames each
+  // equilibration (cpu/equi/Host.cpp:174-175): new Maxwell-Boltzmann
+  // velocities after every equi_every-th step
+  int equi_every = 0;
+  double equi_temp = 0;
+  unsigned long long equi_seed = 0, equi_draws = 0;
 
   bool mixed() const { return cfg.precision == MD_PREC_MIXED; }
   bool permuted() const { return cluster && cl.built; }
@@ -647,6 +652,25 @@ md_status capture_frame(md_ctx* c) {
 
 bool anim_due(const md_ctx* c, int t) { return c->anim_every >= 0 && c->anim_next == t; }
 
+bool equi_due(const md_ctx* c, int t) { return c->equi_every > 0 && t % c->equi_every == 0; }
+
+// chooseVelocities (cpu/equi/Host.cpp:416-572) on the current state;
+// temperature in kelvin (times rb = 8.314e-7, :85-86)
+md_status choose_velocities(md_ctx* c, double temperature, unsigned long long seed) {
+  int it = 0;
+  const int r = equi_velocities(c->pos, c->vel, c->permuted() ? c->cl.orig : nullptr, c->n,
+                                c->cfg.n_mb, c->sp, temperature * 8.314e-7, seed, c->sc.dpart,
+                                &it, c->st);
+  c->stats.launches += 2 * it + 6;
+  if (r == -1)
+    return fail(c, MD_BAD_ARGUMENT,
+                "momentum removal does not converge: the many-body pairs enter the total mass "
+                "once (cpu/equi/Host.cpp:474-478), so each shift overshoots at least as far "
+                "as it corrects");
+  if (r) return cuda_fail(c, (cudaError_t)r, "choose velocities");
+  return MD_OK;
+}
+
 bool due(const md_ctx* c, int t) {
   return (c->cfg.use_lj && c->lj_next == t) || (c->cfg.use_mb && c->mb_next == t);
 }
@@ -693,6 +717,7 @@ bool window_ok(const md_ctx* c, int s, int nsteps) {
   for (int u = 0; u < kGraphSteps; u++) {
     if (c->cfg.output_timesteps > 0 && c->printout == t + u) return false;
     if (anim_due(c, t + u)) return false;
+    if (equi_due(c, t + u)) return false;
     if (due(c, t + u + 1)) return false;
   }
   return true;
@@ -785,7 +810,9 @@ md_status step_once(md_ctx* c, bool last) {
   c->predicted = false;
   const bool output = c->cfg.output_timesteps > 0 && c->printout == t;
   const bool anim = anim_due(c, t);
-  const bool fuse = c->mixed() && !c->walls() && !last && !output && !anim && !due(c, t + 1);
+  const bool equi = equi_due(c, t);
+  const bool fuse =
+      c->mixed() && !c->walls() && !last && !output && !anim && !equi && !due(c, t + 1);
   if (c->cluster && fuse) {
     {
       Timed tm(c, 6);
@@ -829,6 +856,12 @@ md_status step_once(md_ctx* c, bool last) {
     md_status s = capture_frame(c);
     if (s != MD_OK) return s;
     c->anim_next += c->anim_every;
+  }
+  if (equi) {
+    // a new stream of draws for every reassignment
+    md_status s = choose_velocities(c, c->equi_temp, c->equi_seed + 0x632BE59BD9B4E019ull *
+                                                                      ++c->equi_draws);
+    if (s != MD_OK) return s;
   }
   c->t++;
   c->stats.steps++;
@@ -1389,6 +1422,23 @@ md_status md_set_animation(md_ctx* c, int every, int frames_hint) {
 }
 
 int md_animation_count(const md_ctx* c) { return c ? c->anim_frames : 0; }
+
+md_status md_choose_velocities(md_ctx* c, double temperature, unsigned long long seed) {
+  if (!c || !(temperature >= 0)) return MD_BAD_ARGUMENT;
+  md_status s = choose_velocities(c, temperature, seed);
+  if (s != MD_OK) return s;
+  return check_status(c);
+}
+
+md_status md_set_equilibration(md_ctx* c, double temperature, unsigned long long seed,
+                               int every) {
+  if (!c || !(temperature >= 0)) return MD_BAD_ARGUMENT;
+  c->equi_every = every > 0 ? every : 0;
+  c->equi_temp = temperature;
+  c->equi_seed = seed;
+  c->equi_draws = 0;
+  return MD_OK;
+}
 
 md_status md_get_animation_frame(md_ctx* c, int k, float* pos4, float* vel3) {
   if (!c || k < 0 || k >= c->anim_frames || (!pos4 && !vel3)) return MD_BAD_ARGUMENT;

@@ -477,6 +477,92 @@ __global__ void __launch_bounds__(kRedThreads)
 
 inline int nblk(long long n, int t) { return (int)((n + t - 1) / t); }
 
+
+// ---- equi: Maxwell-Boltzmann velocities (cpu/equi/Host.cpp:416-572) ----
+
+// splitmix64 finaliser (Vigna): one 64-bit hash per (seed, atom, component)
+__device__ __forceinline__ unsigned long long mix64(unsigned long long x) {
+  x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+  x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+  return x ^ (x >> 31);
+}
+
+// uniform on the open interval (0, 1) with 2^32 levels, as (rand() + 1) /
+// (RAND_MAX + 2) of cpu/equi/Host.h:26
+__device__ __forceinline__ double equi_uniform(unsigned long long seed, int atom, int comp) {
+  const unsigned long long z =
+      mix64(seed + (3ull * (unsigned long long)atom + (unsigned long long)comp + 1ull) *
+                       0x9E3779B97F4A7C15ull);
+  return ((double)(unsigned)(z >> 32) + 1.0) / 4294967297.0;
+}
+
+// Draws of :438-472 and the momentum sums of :474-478.  Many-body atoms come
+// in pairs (i, i + 1), i even and below n_mb, that share one draw made with
+// the first atom's mass; the sums count a pair once, with that mass, so
+// totalm leaves out the second atoms' masses.  The z draw applies inverf
+// before the affine map (:457-461).
+__global__ void k_equi_sample(const md_double4* __restrict__ pos, double* __restrict__ vel,
+                              const int* __restrict__ orig, int n, int n_mb, Species sp,
+                              double temp, unsigned long long seed, double* part) {
+  double v[4] = {0, 0, 0, 0};
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+    const int i = orig ? orig[p] : p;
+    const bool second = i >= 1 && i - 1 < n_mb && ((i - 1) & 1) == 0;
+    const bool first = i < n_mb && (i & 1) == 0 && i + 1 < n;
+    const int key = second ? i - 1 : i;
+    // many-body atoms exist only without the cell order, so p - 1 is i - 1
+    const double m = mass_of((int)pos[second ? p - 1 : p].w, sp);
+    const double sc = sqrt(2.0 * temp / m);
+    const double vx = erfinv(2.0 * equi_uniform(seed, key, 0) - 1.0) * sc;
+    const double vy = erfinv(2.0 * equi_uniform(seed, key, 1) - 1.0) * sc;
+    const double vz = (2.0 * erfinv(equi_uniform(seed, key, 2)) - 1.0) * sc;
+    vel[3 * (size_t)p] = vx;
+    vel[3 * (size_t)p + 1] = vy;
+    vel[3 * (size_t)p + 2] = vz;
+    if (!first) {
+      v[0] += m * vx;
+      v[1] += m * vy;
+      v[2] += m * vz;
+      v[3] += m;
+    }
+  }
+  block_store<4>(v, part);
+}
+
+// :480-484 the shift; :490-512 the sums that follow it (every atom's own mass)
+__global__ void k_equi_shift(const md_double4* __restrict__ pos, double* __restrict__ vel, int n,
+                             Species sp, double cx, double cy, double cz, double* part) {
+  double v[3] = {0, 0, 0};
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+    const double m = mass_of((int)pos[p].w, sp);
+    const double vx = vel[3 * (size_t)p] - cx, vy = vel[3 * (size_t)p + 1] - cy,
+                 vz = vel[3 * (size_t)p + 2] - cz;
+    vel[3 * (size_t)p] = vx;
+    vel[3 * (size_t)p + 1] = vy;
+    vel[3 * (size_t)p + 2] = vz;
+    v[0] += vx * m;
+    v[1] += vy * m;
+    v[2] += vz * m;
+  }
+  block_store<3>(v, part);
+}
+
+// :519-538 sum m v^2 (the products in the reference's order)
+__global__ void k_equi_ke(const md_double4* __restrict__ pos, const double* __restrict__ vel,
+                          int n, Species sp, double* part) {
+  double v[1] = {0};
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+    const double m = mass_of((int)pos[p].w, sp);
+    v[0] += m * norm2_exact(vel[3 * (size_t)p], vel[3 * (size_t)p + 1], vel[3 * (size_t)p + 2]);
+  }
+  block_store<1>(v, part);
+}
+
+__global__ void k_equi_scale(double* __restrict__ vel, int n3, double s) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n3; k += gridDim.x * blockDim.x)
+    vel[k] *= s;
+}
+
 }  // namespace
 
 void launch_predict(const GearArgs& a, cudaStream_t st) {
@@ -527,6 +613,56 @@ void launch_thermo(const md_double4* pos, const double* vel, int n, Species sp, 
   k_sum_partials<<<1, kRedThreads, 0, st>>>(part, B, 1, t1);
   k_thermo_final<<<1, 32, 0, st>>>(s8, t1, n, out);
 }
+
+int equi_velocities(const md_double4* pos, double* vel, const int* orig, int n, int n_mb,
+                    Species sp, double temp, unsigned long long seed, double* part,
+                    int* iterations, cudaStream_t st) {
+  int B = nblk(n, kRedThreads);
+  if (B > kRedBlocks) B = kRedBlocks;
+  if (B < 1) B = 1;
+  double* sums = part + 4 * kRedBlocks;
+  double h[4];
+  auto reduce = [&](int nv) -> cudaError_t {
+    k_sum_partials<<<1, kRedThreads, 0, st>>>(part, B, nv, sums);
+    cudaError_t e = cudaMemcpyAsync(h, sums, sizeof(double) * nv, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    return e;
+  };
+  k_equi_sample<<<B, kRedThreads, 0, st>>>(pos, vel, orig, n, n_mb, sp, temp, seed, part);
+  cudaError_t e = reduce(4);
+  if (e != cudaSuccess) return (int)e;
+  const double totalm = h[3];
+  double cx = h[0] / totalm, cy = h[1] / totalm, cz = h[2] / totalm;
+  // :480-515 until every component is within 1e-15.  The pairs' missing
+  // masses make each shift overshoot by the ratio of the second atoms' mass
+  // to totalm: the loop converges slowly while that ratio is below 1 and
+  // never otherwise (the reference then loops forever).  A shift that does
+  // not shrink the largest component ends the loop with an error.
+  int it = 0;
+  double prev = 1e300;
+  while (fabs(cx) > 1.0e-15 || fabs(cy) > 1.0e-15 || fabs(cz) > 1.0e-15) {
+    const double big = fmax(fabs(cx), fmax(fabs(cy), fabs(cz)));
+    if (++it > 100000 || !(big < prev)) {
+      *iterations = it;
+      return -1;
+    }
+    prev = big;
+    k_equi_shift<<<B, kRedThreads, 0, st>>>(pos, vel, n, sp, cx, cy, cz, part);
+    if ((e = reduce(3)) != cudaSuccess) return (int)e;
+    cx = h[0] / totalm;
+    cy = h[1] / totalm;
+    cz = h[2] / totalm;
+  }
+  *iterations = it;
+  // :519-546 rescale to temp
+  k_equi_ke<<<B, kRedThreads, 0, st>>>(pos, vel, n, sp, part);
+  if ((e = reduce(1)) != cudaSuccess) return (int)e;
+  const double t = h[0] / (3.0 * (double)n);
+  const double scalev = sqrt(temp / t);
+  k_equi_scale<<<nblk(3 * n, 256), 256, 0, st>>>(vel, 3 * n, scalev);
+  return (int)cudaGetLastError();
+}
+
 void launch_rep_records(const md_double4* pos, const double* vel, const int* ranges, int nrep,
                         Species sp, const double* e3, double time, double step, double* rec,
                         cudaStream_t st) {

@@ -47,6 +47,14 @@ void launch_ready(const md_double4* pos, const double* vel, int n, unsigned long
                   int* status, cudaStream_t st);
 // PerformCalculations (common/DebugCalculations.cpp:46-124) into out[0..7]:
 // com x,y,z, kinetic, momentum x,y,z, temperature.  part: >= 8 * 1024 doubles.
+// chooseVelocities (cpu/equi/Host.cpp:416-572) on the device state (orig:
+// caller's numbering of the stored atoms, NULL when stored in it); temp in
+// the reference's energy units (kelvin x 8.314e-7); part as for
+// launch_thermo.  Returns 0, a CUDA error code, or -1 when a momentum-removal
+// shift does not shrink the centre-of-mass velocity (the reference loops on).
+int equi_velocities(const md_double4* pos, double* vel, const int* orig, int n, int n_mb,
+                    Species sp, double temp, unsigned long long seed, double* part,
+                    int* iterations, cudaStream_t st);
 void launch_thermo(const md_double4* pos, const double* vel, int n, Species sp, double* part,
                    double* out, cudaStream_t st);
 // Deterministic sum of nv-vectors over nblocks partials: out[k] = sum_b part[nv*b + k].

@@ -99,7 +99,8 @@ EXPORTS = ["md_create", "md_destroy", "md_status_string", "md_last_error", "md_u
            "mdgb_calculate_potential", "mdgb_set_species", "mdgb_last_status", "md_read_config",
            "md_write_results", "md_write_results_pairs", "md_host_alloc", "md_host_free",
            "md_set_animation", "md_animation_count", "md_get_animation_frame",
-           "md_write_animation", "md_tail_pairs",
+           "md_write_animation", "md_tail_pairs", "md_choose_velocities",
+           "md_set_equilibration",
            "mdgb_many_body_forces_static", "md_autotune", "md_set_graphs", "md_batch_create",
            "md_batch_size", "md_batch_records", "mdgb_tc_selftest", "mdgb_conv_selftest",
            "md_surrogate_create",
@@ -201,6 +202,8 @@ def load(path: str | None = None) -> C.CDLL:
     L.md_get_animation_frame.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
     L.md_write_animation.argtypes = [C.c_void_p, C.c_char_p, C.c_float]
     L.md_tail_pairs.argtypes = [C.c_void_p, C.c_void_p, C.c_int, P(C.c_int)]
+    L.md_choose_velocities.argtypes = [C.c_void_p, C.c_double, C.c_ulonglong]
+    L.md_set_equilibration.argtypes = [C.c_void_p, C.c_double, C.c_ulonglong, C.c_int]
     if path is None:
         _lib = L
     return L
@@ -358,6 +361,15 @@ class Engine:
     def write_animation(self, anim_file: str, vxcm: float = 0.0):
         self._ck(self.lib.md_write_animation(self.h, anim_file.encode(), vxcm),
                  "md_write_animation")
+
+    def choose_velocities(self, temperature: float, seed: int):
+        """equi's chooseVelocities on the device state (kelvin)."""
+        self._ck(self.lib.md_choose_velocities(self.h, temperature, seed),
+                 "md_choose_velocities")
+
+    def set_equilibration(self, temperature: float, seed: int, every: int = 50):
+        self._ck(self.lib.md_set_equilibration(self.h, temperature, seed, every),
+                 "md_set_equilibration")
 
     def tail_pairs(self) -> np.ndarray:
         """Many-body pairs closer than 2 reNO (k x 2, the reference's order)."""
