@@ -628,6 +628,8 @@ __global__ void __launch_bounds__(224, 3)
   const int BX = blockDim.x + 8;
   uint16_t* tiles = (uint16_t*)dyn;
   const int nbuf = a.nbuf;  // block tiles in flight (ROWS 0): 2 or 3
+  const uint32_t tile_elems = kClusterTileSlots * BX;
+  const uint32_t tile_bytes = tile_elems * sizeof(uint16_t);
   const int tile_region =
       ROWS == 0 ? nbuf * kClusterTileSlots * BX * (int)sizeof(uint16_t)
                 : (ROWS == 2 ? (int)(blockDim.x >> 5) * 2 * kWarpTileBytes : 0);
@@ -663,7 +665,20 @@ __global__ void __launch_bounds__(224, 3)
   if (sidx >= a.nseg) break;
   load_segment(sh, a.seg, a.reps, sidx);
   __syncthreads();
+  // block tiles: the first two row tiles of the segment's first atoms go out
+  // with the staging copies, so their latency overlaps the staging's
+  const int npre = (ROWS == 0 && !tripped) ? min(nbuf, 2) : 0;
+  if (tid == 0)
+    for (int t = 0; t < npre; t++) {
+      fence_proxy_async();
+      mbar_expect_tx(&bar[t], tile_bytes);
+      tma_load_2d(tiles + t * tile_elems, &rmap, sh.S.p0 & ~7, t * kClusterTileSlots, &bar[t]);
+      inflight |= 1u << t;
+    }
   if (!stage_bulk(sh, a.posf, st, &bar[3], (phase >> 3) & 1u, a.status)) {
+    // copies still in flight land (or time out) before the block leaves
+    if (tid == 0)
+      for (int t = 0; t < npre; t++) mbar_wait(&bar[t], (phase >> t) & 1u, a.status);
     aborted = true;
     break;
   }
@@ -683,8 +698,6 @@ __global__ void __launch_bounds__(224, 3)
   const float s2_ng = a.sp.sig[2] * a.sp.sig[2], c_ng = 24.0f * a.sp.eps[2];
   const float s2_n = a.sp.sig[0] * a.sp.sig[0], c_n = 24.0f * a.sp.eps[0];
   const float s2_o = a.sp.sig[1] * a.sp.sig[1], c_o = 24.0f * a.sp.eps[1];
-  const uint32_t tile_elems = kClusterTileSlots * BX;
-  const uint32_t tile_bytes = tile_elems * sizeof(uint16_t);
   double ev[3] = {0.0, 0.0, 0.0};
   const int p0 = sh.S.p0, p1 = sh.S.p1;
   for (int base = p0; base < p1; base += blockDim.x) {
@@ -934,8 +947,9 @@ __global__ void __launch_bounds__(224, 3)
       const int T = (maxl + kClusterTileSlots - 1) / kClusterTileSlots;
       const int x0 = base & ~7;  // 16-byte aligned start of the tile
       const int col = live ? p - x0 : tid;
+      const int issued = base == p0 ? npre : 0;  // tiles already on their way
       if (tid == 0) {
-        for (int t = 0; t < nbuf && t < T; t++) {
+        for (int t = issued; t < nbuf && t < T; t++) {
           fence_proxy_async();
           mbar_expect_tx(&bar[t], tile_bytes);
           tma_load_2d(tiles + t * tile_elems, &rmap, x0, t * kClusterTileSlots, &bar[t]);
@@ -970,6 +984,17 @@ __global__ void __launch_bounds__(224, 3)
           tma_load_2d(tiles + b * tile_elems, &rmap, x0, (t + nbuf) * kClusterTileSlots, &bar[b]);
           inflight |= 1u << b;
         }
+      }
+      // tiles sent ahead that these rows did not need still complete their
+      // barrier phase before the buffers are reused
+      for (int t = T; !failed && t < issued; t++) {
+        const bool got = mbar_wait(&bar[t], (phase >> t) & 1u, a.status);
+        if (!__syncthreads_and(got)) {
+          failed = true;
+          break;
+        }
+        phase ^= 1u << t;
+        inflight &= ~(1u << t);
       }
       if (failed) {
         // a bounded wait ran out: give copies still in flight a bounded
@@ -1133,6 +1158,37 @@ __global__ void k_unpermute(const double* __restrict__ in, double* __restrict__ 
   if (p >= n) return;
   const size_t o = (size_t)orig[p];
   for (int d = 0; d < width; d++) out[width * o + d] = in[(size_t)width * p + d];
+}
+
+__global__ void k_invert(const int* __restrict__ orig, int* __restrict__ inv, int n) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p < n) inv[orig[p]] = p;
+}
+
+// one element per thread in the caller's order: the host side is read or
+// written in whole consecutive lines
+__global__ void k_gather_host(const double* __restrict__ host, double* __restrict__ dst,
+                              const int* __restrict__ inv, long long m, int width) {
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < m;
+       k += (long long)gridDim.x * blockDim.x) {
+    const long long i = k / width;
+    dst[(long long)width * inv[i] + (k - i * width)] = host[k];
+  }
+}
+
+__global__ void k_scatter_host(const double* __restrict__ src, double* __restrict__ host,
+                               const int* __restrict__ inv, long long m, int width) {
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < m;
+       k += (long long)gridDim.x * blockDim.x) {
+    const long long i = k / width;
+    host[k] = src[(long long)width * inv[i] + (k - i * width)];
+  }
+}
+
+__global__ void k_species_check(const md_double4* __restrict__ pos, int n, int* flag) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool other = p < n && (int)pos[p].w != SP_NG;
+  if (__any_sync(0xffffffffu, other) && (threadIdx.x & 31) == 0) atomicOr(flag, 1);
 }
 
 __global__ void k_permute_in(const double* __restrict__ in, double* __restrict__ out,
@@ -1381,6 +1437,7 @@ int cluster_build(ClusterList& cl, const std::vector<ClusterReplica>& reps_in, f
   cl.trip_dist = 0.5 * ((double)rv - rcut) - (double)margin;
   cudaMemsetAsync(cl.skin, 0, sizeof(int) * 4, st);  // trip flags and overflow
   cl.built = true;
+  cl.version++;
   return (int)cudaGetLastError();
 }
 
@@ -1505,6 +1562,26 @@ void launch_unpermute(const double* in, double* out, const int* orig, int n, int
 void launch_permute_in(const double* in, double* out, const int* orig, int n, int width,
                        cudaStream_t st) {
   if (n > 0) k_permute_in<<<nb(n, 256), 256, 0, st>>>(in, out, orig, n, width);
+}
+
+void launch_invert(const int* orig, int* inv, int n, cudaStream_t st) {
+  if (n > 0) k_invert<<<nb(n, 256), 256, 0, st>>>(orig, inv, n);
+}
+
+void launch_gather_host(const double* host, double* dst, const int* inv, int n, int width,
+                        cudaStream_t st) {
+  const long long m = (long long)n * width;
+  if (m > 0) k_gather_host<<<(int)std::min<long long>(nb(m, 256), 8 * 1024), 256, 0, st>>>(host, dst, inv, m, width);
+}
+
+void launch_scatter_host(const double* src, double* host, const int* inv, int n, int width,
+                         cudaStream_t st) {
+  const long long m = (long long)n * width;
+  if (m > 0) k_scatter_host<<<(int)std::min<long long>(nb(m, 256), 8 * 1024), 256, 0, st>>>(src, host, inv, m, width);
+}
+
+void launch_species_check(const md_double4* pos, int n, int* flag, cudaStream_t st) {
+  if (n > 0) k_species_check<<<nb(n, 256), 256, 0, st>>>(pos, n, flag);
 }
 
 void cluster_free(ClusterList& cl) {

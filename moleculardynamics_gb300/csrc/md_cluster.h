@@ -92,6 +92,7 @@ struct ClusterList {
   int* counters = nullptr;                        // device: max staged, max len, entries, max cell
   int* sched = nullptr;                           // device: persistent kernel's work counters
   bool built = false;
+  int version = 0;  // counts builds (each may change the order)
 };
 
 // Builds (or rebuilds) the structure for the replicas in `reps` (n and L
@@ -132,6 +133,18 @@ struct ClusterForceArgs {
   int* skin = nullptr;          // skin flags (NULL: the list's own)
 };
 void launch_lj_cluster(const ClusterForceArgs& a, bool energy, cudaStream_t st);
+// inv[orig[p]] = p
+void launch_invert(const int* orig, int* inv, int n, cudaStream_t st);
+// Transfers between the cell-ordered state and a caller array in its own
+// order that the device reaches directly (pinned host memory), element by
+// element in the caller's order: dst[width inv[i] + d] = host[width i + d],
+// and back.
+void launch_gather_host(const double* host, double* dst, const int* inv, int n, int width,
+                        cudaStream_t st);
+void launch_scatter_host(const double* src, double* host, const int* inv, int n, int width,
+                         cudaStream_t st);
+// flag |= 1 when some atom is not of the NG species
+void launch_species_check(const md_double4* pos, int n, int* flag, cudaStream_t st);
 int cluster_blocks(const ClusterList& cl);
 
 // Reference-layout rows (common/NeighborList.cpp:119-177) of atoms in their

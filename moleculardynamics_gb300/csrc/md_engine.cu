@@ -107,6 +107,8 @@ struct md_ctx {
   bool cluster = false;
   ClusterList cl;
   double* io = nullptr;  // 4 doubles per atom: permuted transfers
+  int* inv = nullptr;    // caller's index -> stored position (cell order)
+  int inv_version = -1;  // cl.version that inv was computed for
   md_double4* pos_alt = nullptr;  // next positions of the fused force + Gear kernel
   float4* posf_alt = nullptr;
   // independent periodic replicas (batched form): atoms of replica k are
@@ -989,7 +991,7 @@ void md_destroy(md_ctx* c) {
   list_free(c->mb);
   cluster_free(c->cl);
   if (c->gexec) cudaGraphExecDestroy(c->gexec);
-  void* ptrs[] = {c->sur_fx, c->sur_fs, c->rep_ranges, c->rep_buf, c->io, c->pos_alt, c->posf_alt, c->pos, c->vel, c->acc, c->b, c->c, c->f3, c->f3_tmp, c->posf, c->mb_sl,
+  void* ptrs[] = {c->inv, c->sur_fx, c->sur_fs, c->rep_ranges, c->rep_buf, c->io, c->pos_alt, c->posf_alt, c->pos, c->vel, c->acc, c->b, c->c, c->f3, c->f3_tmp, c->posf, c->mb_sl,
                   c->mb_slen, c->xsi, c->xsj, c->va, c->status, c->epart, c->dsc, c->rec,
                   c->sc.dpart, c->sc.umax, c->sc.counts, c->sc.block_sums};
   for (void* p : ptrs)
@@ -1008,10 +1010,39 @@ md_status md_upload(md_ctx* c, const double* pos4, const double* vel3) {
 }
 
 // host -> device array of `width` doubles per atom, in the caller's numbering
+// the device address of a caller buffer the GPU reaches directly (pinned
+// host memory, e.g. from md_host_alloc), else NULL
+const void* device_view(const void* p) {
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
+}
+
+md_status ensure_inv(md_ctx* c) {
+  if (!c->inv) CK(cudaMalloc(&c->inv, sizeof(int) * (size_t)c->n), "inverse order");
+  if (c->inv_version != c->cl.version) {
+    launch_invert(c->cl.orig, c->inv, c->n, c->st);
+    c->inv_version = c->cl.version;
+  }
+  return MD_OK;
+}
+
+// Caller -> device.  In cell order, a pinned caller array is read by the
+// device in place (whole lines over the host link, no staging copy);
+// other memory goes through the staging buffer.  The caller synchronises.
 md_status put_array(md_ctx* c, double* dst, const double* src, int width) {
   const size_t B = sizeof(double) * (size_t)width * (size_t)c->n;
   if (!c->permuted()) {
     CK(cudaMemcpyAsync(dst, src, B, cudaMemcpyHostToDevice, c->st), "upload");
+    return MD_OK;
+  }
+  if (const double* hv = (const double*)device_view(src)) {
+    md_status s = ensure_inv(c);
+    if (s != MD_OK) return s;
+    launch_gather_host(hv, dst, c->inv, c->n, width, c->st);
     return MD_OK;
   }
   CK(cudaMemcpyAsync(c->io, src, B, cudaMemcpyHostToDevice, c->st), "upload");
@@ -1027,6 +1058,12 @@ md_status get_array(md_ctx* c, double* dst, const double* src, int width) {
     CK(cudaMemcpyAsync(dst, src, B, cudaMemcpyDeviceToHost, c->st), "download");
     return MD_OK;
   }
+  if (double* hv = (double*)device_view(dst)) {
+    md_status s = ensure_inv(c);
+    if (s != MD_OK) return s;
+    launch_scatter_host(src, hv, c->inv, c->n, width, c->st);
+    return MD_OK;
+  }
   launch_unpermute(src, c->io, c->cl.orig, c->n, width, c->st);
   CK(cudaMemcpyAsync(dst, c->io, B, cudaMemcpyDeviceToHost, c->st), "download");
   CK(cudaStreamSynchronize(c->st), "download");
@@ -1036,20 +1073,22 @@ md_status get_array(md_ctx* c, double* dst, const double* src, int width) {
 md_status md_upload_state(md_ctx* c, const double* pos4, const double* vel3, const double* a3,
                           const double* b3, const double* c3) {
   if (!c) return MD_BAD_ARGUMENT;
-  const size_t N = (size_t)c->n;
   md_status s = MD_OK;
+  int* other = c->status + 3;  // some atom is not of the NG species
   if (pos4) {
-    int all = 1;
-    for (size_t i = 0; i < N && all; i++) all = (int)pos4[4 * i + 3] == SP_NG;
-    c->all_ng = all;
     if ((s = put_array(c, (double*)c->pos, pos4, 4)) != MD_OK) return s;
+    CK(cudaMemsetAsync(other, 0, sizeof(int), c->st), "upload");
+    launch_species_check(c->pos, c->n, other, c->st);
   }
   if (vel3 && (s = put_array(c, c->vel, vel3, 3)) != MD_OK) return s;
   if (a3 && (s = put_array(c, c->acc, a3, 3)) != MD_OK) return s;
   if (b3 && (s = put_array(c, c->b, b3, 3)) != MD_OK) return s;
   if (c3 && (s = put_array(c, c->c, c3, 3)) != MD_OK) return s;
   if (c->mixed() && pos4) launch_posf(c->pos, c->posf, c->n, c->st);
+  int flag = 0;
+  if (pos4) CK(cudaMemcpyAsync(&flag, other, sizeof(int), cudaMemcpyDeviceToHost, c->st), "upload");
   CK(cudaStreamSynchronize(c->st), "upload");
+  if (pos4) c->all_ng = flag == 0;
   return MD_OK;
 }
 

@@ -154,6 +154,42 @@ def test_cluster_state_round_trip(eng):
     assert np.array_equal(st["c"], c3)
 
 
+def test_cluster_pinned_transfers(eng):
+    """Pinned caller arrays are read and written by the device in place (no
+    staging copy); the result equals the staged path's, and the species
+    check done on the device keeps the all-argon fast path."""
+    pos, vel, L = argon_fcc(8, noise=0.1)
+    n = len(pos)
+    rng = np.random.default_rng(6)
+    a3, b3, c3 = (rng.standard_normal((n, 3)) for _ in range(3))
+    hp, hv = eng.pinned((n, 4)), eng.pinned((n, 3))
+    ha, hb, hc = (eng.pinned((n, 3)) for _ in range(3))
+    with _engine(eng, n, L, lj_kernel=eng.LJ_CLUSTER) as e:
+        e.upload(pos, vel)
+        e.begin(0.0)
+        e.step(7)
+        p0, v0 = e.download()
+        s0 = e.download_state()
+        # device -> pinned
+        e.lib.md_download(e.h, hp, hv)
+        e.lib.md_download_state(e.h, ha.ctypes.data, hb.ctypes.data, hc.ctypes.data, None)
+        assert np.array_equal(hp, p0) and np.array_equal(hv, v0)
+        assert np.array_equal(ha, s0["acc"]) and np.array_equal(hb, s0["b"])
+        assert np.array_equal(hc, s0["c"])
+        # pinned -> device
+        hp[:], hv[:], ha[:], hb[:], hc[:] = pos, vel, a3, b3, c3
+        e.upload_state(hp, hv, ha, hb, hc)
+        p1, v1 = e.download()
+        s1 = e.download_state()
+        f1, _ = e.compute_forces()
+        e.upload_state(pos, vel, a3, b3, c3)
+        f2, _ = e.compute_forces()
+    assert np.array_equal(p1, pos) and np.array_equal(v1, vel)
+    assert np.array_equal(s1["acc"], a3) and np.array_equal(s1["b"], b3)
+    assert np.array_equal(s1["c"], c3)
+    assert np.array_equal(f1, f2)
+
+
 def test_cluster_energy_conservation(eng):
     pos, vel, L = argon_fcc(8, seed=9)
     n = len(pos)
