@@ -167,6 +167,22 @@ def drift_per_1000(recs: np.ndarray, n: int, first_step: int) -> float:
     return float((e[-1] - e[0]) / n / EPS / steps * 1000.0)
 
 
+def fp32_roofline(entries: int, launch_s: float, peaks: dict) -> dict:
+    """FP32 arithmetic of one LJ force evaluation against the FP32 pipe's
+    nominal peak: 8 flops per row entry (3 differences, r^2 as a product
+    and two FMAs) and 15 per pair inside the cutoff (reciprocal, the r^-6
+    chain and force scalar, three FMAs into the sums), FMA = 2 flops; the
+    pairs inside the cutoff are (2.5 / 2.8)^3 of the entries (uniform
+    density).  The peak is 152 SMs x 128 FP32 lanes x 2 flops x the maximum
+    SM clock (no measured FP32 figure)."""
+    inside = entries * (2.5 / 2.8) ** 3
+    flops = 8.0 * entries + 15.0 * inside
+    achieved = flops / launch_s / 1e12
+    peak = 152 * 128 * 2 * peaks.get("sm_max_mhz", 2070.0) * 1e6 / 1e12
+    return {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+            "frac": achieved / peak, "peak_source": "nominal", "flops_alg_per_launch": flops}
+
+
 def roofline_traffic(workload: str, kernel: str = "lj_force"):
     """dram bytes per launch of the LJ kernel from the committed ncu summary."""
     path = os.path.join(ROOT, "profiles", f"{kernel}_{workload}.md")
@@ -552,6 +568,7 @@ def run_gb300(args, rank, world):
                             "traffic": roofline_traffic(args.workload, "lj_cluster_fused"),
                             "bytes_alg_per_launch": bytes_alg,
                             "avg_launch_ms": fu_ms / fu_n}
+        line["roofline_fp32"] = fp32_roofline(entries, avg_s, peaks)
     elif lj_n:
         entries = s1["lj_list_entries"]
         if s1["lj_cluster"]:
@@ -575,6 +592,8 @@ def run_gb300(args, rank, world):
                             "traffic": traffic,
                             "bytes_alg_per_launch": bytes_alg,
                             "avg_launch_ms": lj_ms / lj_n}
+        if precision == eng.PREC_MIXED:
+            line["roofline_fp32"] = fp32_roofline(entries, avg_s, peaks)
 
     if rank == 0 and not args.no_compare:
         # plain FP64 GPU path on the same workload (fewer steps: it is slow)
