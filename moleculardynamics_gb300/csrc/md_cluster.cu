@@ -1166,22 +1166,22 @@ __global__ void k_invert(const int* __restrict__ orig, int* __restrict__ inv, in
 }
 
 // one element per thread in the caller's order: the host side is read or
-// written in whole consecutive lines
+// written in whole consecutive lines (W is 3 or 4; W n < 2^31)
+template <int W>
 __global__ void k_gather_host(const double* __restrict__ host, double* __restrict__ dst,
-                              const int* __restrict__ inv, long long m, int width) {
-  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < m;
-       k += (long long)gridDim.x * blockDim.x) {
-    const long long i = k / width;
-    dst[(long long)width * inv[i] + (k - i * width)] = host[k];
+                              const int* __restrict__ inv, int m) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < m; k += gridDim.x * blockDim.x) {
+    const int i = k / W;
+    dst[(size_t)W * inv[i] + (k - i * W)] = host[k];
   }
 }
 
+template <int W>
 __global__ void k_scatter_host(const double* __restrict__ src, double* __restrict__ host,
-                               const int* __restrict__ inv, long long m, int width) {
-  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < m;
-       k += (long long)gridDim.x * blockDim.x) {
-    const long long i = k / width;
-    host[k] = src[(long long)width * inv[i] + (k - i * width)];
+                               const int* __restrict__ inv, int m) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < m; k += gridDim.x * blockDim.x) {
+    const int i = k / W;
+    host[k] = src[(size_t)W * inv[i] + (k - i * W)];
   }
 }
 
@@ -1570,14 +1570,24 @@ void launch_invert(const int* orig, int* inv, int n, cudaStream_t st) {
 
 void launch_gather_host(const double* host, double* dst, const int* inv, int n, int width,
                         cudaStream_t st) {
-  const long long m = (long long)n * width;
-  if (m > 0) k_gather_host<<<(int)std::min<long long>(nb(m, 256), 8 * 1024), 256, 0, st>>>(host, dst, inv, m, width);
+  const int m = n * width;
+  if (m <= 0) return;
+  const int g = std::min(nb(m, 256), 16 * 1024);
+  if (width == 4)
+    k_gather_host<4><<<g, 256, 0, st>>>(host, dst, inv, m);
+  else
+    k_gather_host<3><<<g, 256, 0, st>>>(host, dst, inv, m);
 }
 
 void launch_scatter_host(const double* src, double* host, const int* inv, int n, int width,
                          cudaStream_t st) {
-  const long long m = (long long)n * width;
-  if (m > 0) k_scatter_host<<<(int)std::min<long long>(nb(m, 256), 8 * 1024), 256, 0, st>>>(src, host, inv, m, width);
+  const int m = n * width;
+  if (m <= 0) return;
+  const int g = std::min(nb(m, 256), 16 * 1024);
+  if (width == 4)
+    k_scatter_host<4><<<g, 256, 0, st>>>(src, host, inv, m);
+  else
+    k_scatter_host<3><<<g, 256, 0, st>>>(src, host, inv, m);
 }
 
 void launch_species_check(const md_double4* pos, int n, int* flag, cudaStream_t st) {
