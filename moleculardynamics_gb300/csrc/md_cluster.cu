@@ -76,9 +76,18 @@ __global__ void k_cl_assign(md_double4* __restrict__ pos, int n, const ClusterRe
   bool bad = false;
 #pragma unroll
   for (int d = 0; d < 3; d++) {
-    const double q = floor(xdiv(xadd(x[d], h), r.L));
+    // floor((x + h) / L) and trunc((x + h) / cs) with the exact divisions,
+    // which GB300's narrow FP64 pipe makes costly: a product with the
+    // reciprocal (within 2 ulp of the quotient) decides unless the quotient
+    // lies within 1e-12 of an integer
+    const double xa = xadd(x[d], h);
+    const double qa = xa * r.invL;
+    const double q = fabs(qa - rint(qa)) > 1e-12 * fmax(1.0, fabs(qa)) ? floor(qa)
+                                                                         : floor(xdiv(xa, r.L));
     x[d] = xsub(x[d], xmul(q, r.L));
-    double s = xdiv(xadd(x[d], h), r.cs);
+    const double xb = q == 0.0 ? xa : xadd(x[d], h);
+    const double sa = xb * r.invcs;
+    double s = fabs(sa - rint(sa)) > 1e-12 * fmax(1.0, fabs(sa)) ? sa : xdiv(xb, r.cs);
     if (!(s >= 0.0 && s < 2.0e9)) {
       bad = true;
       s = 0.0;
@@ -1251,6 +1260,8 @@ int cluster_build(ClusterList& cl, const std::vector<ClusterReplica>& reps_in, f
     r.G = G;
     r.pad = 0;
     r.cs = r.L / G;
+    r.invL = 1.0 / r.L;
+    r.invcs = 1.0 / r.cs;
     r.Lf = (float)r.L;
     r.Llo = (float)(r.L - (double)r.Lf);
     r.cell0 = cell0;

@@ -31,6 +31,7 @@ struct ClusterReplica {
   int G;             // cells per edge (1: one cell, minimum image)
   int pad;
   double L, cs;      // box edge and cell size
+  double invL, invcs;  // their reciprocals (screening of the cell divisions)
   float Lf, Llo;     // L = Lf + Llo
 };
 
