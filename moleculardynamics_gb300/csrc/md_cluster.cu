@@ -674,20 +674,7 @@ __global__ void __launch_bounds__(224, 3)
   if (sidx >= a.nseg) break;
   load_segment(sh, a.seg, a.reps, sidx);
   __syncthreads();
-  // block tiles: the first two row tiles of the segment's first atoms go out
-  // with the staging copies, so their latency overlaps the staging's
-  const int npre = (ROWS == 0 && !tripped) ? min(nbuf, 2) : 0;
-  if (tid == 0)
-    for (int t = 0; t < npre; t++) {
-      fence_proxy_async();
-      mbar_expect_tx(&bar[t], tile_bytes);
-      tma_load_2d(tiles + t * tile_elems, &rmap, sh.S.p0 & ~7, t * kClusterTileSlots, &bar[t]);
-      inflight |= 1u << t;
-    }
   if (!stage_bulk(sh, a.posf, st, &bar[3], (phase >> 3) & 1u, a.status)) {
-    // copies still in flight land (or time out) before the block leaves
-    if (tid == 0)
-      for (int t = 0; t < npre; t++) mbar_wait(&bar[t], (phase >> t) & 1u, a.status);
     aborted = true;
     break;
   }
@@ -956,9 +943,8 @@ __global__ void __launch_bounds__(224, 3)
       const int T = (maxl + kClusterTileSlots - 1) / kClusterTileSlots;
       const int x0 = base & ~7;  // 16-byte aligned start of the tile
       const int col = live ? p - x0 : tid;
-      const int issued = base == p0 ? npre : 0;  // tiles already on their way
       if (tid == 0) {
-        for (int t = issued; t < nbuf && t < T; t++) {
+        for (int t = 0; t < nbuf && t < T; t++) {
           fence_proxy_async();
           mbar_expect_tx(&bar[t], tile_bytes);
           tma_load_2d(tiles + t * tile_elems, &rmap, x0, t * kClusterTileSlots, &bar[t]);
@@ -993,17 +979,6 @@ __global__ void __launch_bounds__(224, 3)
           tma_load_2d(tiles + b * tile_elems, &rmap, x0, (t + nbuf) * kClusterTileSlots, &bar[b]);
           inflight |= 1u << b;
         }
-      }
-      // tiles sent ahead that these rows did not need still complete their
-      // barrier phase before the buffers are reused
-      for (int t = T; !failed && t < issued; t++) {
-        const bool got = mbar_wait(&bar[t], (phase >> t) & 1u, a.status);
-        if (!__syncthreads_and(got)) {
-          failed = true;
-          break;
-        }
-        phase ^= 1u << t;
-        inflight &= ~(1u << t);
       }
       if (failed) {
         // a bounded wait ran out: give copies still in flight a bounded

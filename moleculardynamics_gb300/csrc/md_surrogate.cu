@@ -263,6 +263,21 @@ __device__ __forceinline__ void pair_of(int k, int S, int& a, int& b) {
   b = k - off(aa) + aa + 1;
 }
 
+// k-th pair (a < b) of S neighbours in diagonal order: pairs (a, a + d) for
+// d = 1, 2, ... in turn, so consecutive k have distinct a and distinct b
+// (lanes of a warp update distinct neighbours' force sums)
+__device__ __forceinline__ void pair_of_diag(int k, int S, int& a, int& b) {
+  // offset of diagonal d: (d - 1) S - (d - 1) d / 2
+  auto off = [&](int d) { return (d - 1) * S - (d - 1) * d / 2; };
+  const float m = (float)(2 * S - 1);
+  int d = 1 + (int)(0.5f * (m - sqrtf(fmaxf(m * m - 8.f * (float)k, 0.f))));
+  d = max(1, min(d, S - 1));
+  while (d > 1 && off(d) > k) d--;
+  while (d + 1 <= S - 1 && off(d + 1) <= k) d++;
+  a = k - off(d);
+  b = a + d;
+}
+
 // sum over the warp of 32 per-lane vectors: lane f ends with component f
 __device__ __forceinline__ float warp_reduce_scatter32(float (&v)[32]) {
   const int lane = threadIdx.x & 31;
@@ -330,11 +345,18 @@ __global__ void __launch_bounds__(128)
   __shared__ NbrSm nb[4];
   __shared__ float fn[4][3][kSgMax];
   __shared__ float gs[4][kDesc];
+  __shared__ float gz[4][kAng];  // g_f pref_f zeta_f lambda_f of the angular functions
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int i = blockIdx.x * 4 + warp;
   if (i >= n) return;  // whole warp
   NbrSm& N = nb[warp];
-  gs[warp][lane] = gcoef[(size_t)i * kDesc + lane];
+  {
+    const float gv = gcoef[(size_t)i * kDesc + lane];
+    // angular coefficients carry their prefactor 2^(1 - zeta)
+    const int f = lane - kRad;
+    gs[warp][lane] = f >= 0 ? gv * P.pref[f] : gv;
+    if (f >= 0) gz[warp][f] = gv * P.pref[f] * (float)P.zeta[f] * P.lam[f];
+  }
   for (int s = lane; s < kSgMax; s += 32) fn[warp][0][s] = fn[warp][1][s] = fn[warp][2][s] = 0.f;
   const int S = warp_load_nbrs(i, pos, sl, slen, box, P.rc, N);  // ends with __syncwarp
   const float* g = gs[warp];
@@ -357,27 +379,43 @@ __global__ void __launch_bounds__(128)
     fiz += gz;
   }
   __syncwarp();
+  const float* gzw = gz[warp];
   const int npair = S * (S - 1) / 2;
   for (int k = lane; k < npair; k += 32) {
     int a, b;
-    pair_of(k, S, a, b);
+    pair_of_diag(k, S, a, b);
     const float ra = N.r[a], rb = N.r[b], rab = ra * rb;
     const float c = (N.dx[a] * N.dx[b] + N.dy[a] * N.dy[b] + N.dz[a] * N.dz[b]) / rab;
     const float q = ra * ra + rb * rb;
     const float fca = N.fc[a], fcb = N.fc[b], dfa = N.dfc[a], dfb = N.dfc[b];
-    float A = 0.f, Ba = 0.f, Bb = 0.f;
     AngPair T;
     ang_pair(c, q, P, T);
+    // the sums over f = 8 e + 4 l + z factor per eta index e:
+    //   A  = fca fcb sum_e ex_e sum_lz g' zeta lambda b^(zeta-1)
+    //   Ba = fcb sum_e ex_e (-2 eta_e ra fca + dfa) sum_lz g' b^zeta, Bb likewise
+    float A = 0.f, Ba = 0.f, Bb = 0.f;
 #pragma unroll
-    for (int f = 0; f < kAng; f++) {
-      const int e = f >> 3, l = (f >> 2) & 1, z = f & 3;
-      if (T.b[l] <= 0.f) continue;
-      const float pz1 = T.pz1[l][z], pz = T.pz[l][z], ex = T.ex[e];
-      const float gf = g[kRad + f] * P.pref[f];
-      A += gf * (float)P.zeta[f] * P.lam[f] * pz1 * ex * fca * fcb;
-      Ba += gf * pz * ex * fcb * (-2.f * P.eta_a[f] * ra * fca + dfa);
-      Bb += gf * pz * ex * fca * (-2.f * P.eta_a[f] * rb * fcb + dfb);
+    for (int e = 0; e < 2; e++) {
+      float se = 0.f, ae = 0.f;
+#pragma unroll
+      for (int l = 0; l < 2; l++) {
+        const float on = T.b[l] > 0.f ? 1.f : 0.f;  // (1 + lambda cos) clipped at 0
+#pragma unroll
+        for (int z = 0; z < 4; z++) {
+          const int f = 8 * e + 4 * l + z;
+          se = fmaf(on * g[kRad + f], T.pz[l][z], se);
+          ae = fmaf(on * gzw[f], T.pz1[l][z], ae);
+        }
+      }
+      const float eta = P.eta_a[8 * e];
+      A = fmaf(ae, T.ex[e], A);
+      se *= T.ex[e];
+      Ba = fmaf(se, fmaf(-2.f * eta * ra, fca, dfa), Ba);
+      Bb = fmaf(se, fmaf(-2.f * eta * rb, fcb, dfb), Bb);
     }
+    A *= fca * fcb;
+    Ba *= fcb;
+    Bb *= fca;
     const float ia = 1.f / ra, ib = 1.f / rb;
     // dc/dd_a = d_b / (ra rb) - c d_a / ra^2
     const float gax = A * (N.dx[b] / rab - c * N.dx[a] * ia * ia) + Ba * N.dx[a] * ia;
