@@ -253,6 +253,12 @@ md_status md_surrogate_report(const md_ctx* ctx, md_surrogate_stats* out);
 md_status md_surrogate_forces(md_surrogate* s, md_ctx* ctx, double* force3, double* energy);
 /* descriptors (n_mb x 32): raw, or normalised as the network sees them */
 md_status md_surrogate_descriptors(md_surrogate* s, md_ctx* ctx, float* g, int normalised);
+/* q[i][f] = sum_j (e_j - e_i) . dG_if/dd_j: the derivative of the raw
+ * descriptors of the first n_mb atoms when every atom moves along e3
+ * (n_mb x 3); q is n_mb x 32.  The force-matching gradient applies this
+ * product to the force residual. */
+md_status md_surrogate_desc_directional(md_surrogate* s, md_ctx* ctx, const double* e3,
+                                        double* q);
 /* FP32 parameters: W1 [64][32], b1 [64], W2 [64][64], b2 [64], w3 [64], b3 */
 md_status md_surrogate_params(md_surrogate* s, float* params, int set);
 /* input normalisation (x = (g - mean) * istd) and target scaling

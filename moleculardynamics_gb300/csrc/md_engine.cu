@@ -1752,6 +1752,19 @@ md_status md_surrogate_forces(md_surrogate* s, md_ctx* c, double* f3, double* en
   return check_status(c);
 }
 
+md_status md_surrogate_desc_directional(md_surrogate* s, md_ctx* c, const double* e3,
+                                        double* q) {
+  if (!s || !c || !e3 || !q) return MD_BAD_ARGUMENT;
+  if (!c->begun) return fail(c, MD_BAD_ARGUMENT, "md_begin has not been called");
+  if (!c->cfg.use_mb || c->cfg.n_mb < 1) return fail(c, MD_BAD_ARGUMENT, "no bond-order atoms");
+  const int n = c->cfg.n_mb;
+  const RowWalker w = make_walker(c->mb);
+  int r = sur_descriptors(*s, c->pos, n, w, false, c->status, c->st);
+  if (!r) r = sur_directional(*s, c->pos, n, w.g.box, e3, q, c->st);
+  if (r) return cuda_fail(c, (cudaError_t)r, "surrogate directional derivative");
+  return check_status(c);
+}
+
 md_status md_surrogate_descriptors(md_surrogate* s, md_ctx* c, float* g, int normalised) {
   if (!s || !c || !g) return MD_BAD_ARGUMENT;
   if (!c->begun) return fail(c, MD_BAD_ARGUMENT, "md_begin has not been called");

@@ -789,61 +789,83 @@ __global__ void __launch_bounds__(128, 1)
 }
 
 // q_if = sum_j (e_j - e_i) . dG_if/dd_j for the force residual e (n x 3),
-// written as v_if = scale * istd_f * q_if (the loss' sensitivity to dt/dx)
+// written as v_if = scale * istd_f * q_if (the loss' sensitivity to dt/dx;
+// istd NULL: 1).  One warp per atom as k_sg_desc: lanes over neighbours,
+// then over neighbour pairs, each lane summing all 32 components, one
+// reduce-scatter at the end.  Per pair the 16 angular terms share
+//   K1 = fc_a fc_b (dc/dd_a . de_a + dc/dd_b . de_b) and, per eta index e,
+//   K2_e = fc_b (-2 eta_e r_a fc_a + dfc_a) u_a + fc_a (-2 eta_e r_b fc_b + dfc_b) u_b,
+// so q_f += pref_f ex_e (zeta_f lambda_f b^(zeta-1) K1 + b^zeta K2_e).
 __global__ void __launch_bounds__(128)
     k_sg_ctrans(const md_double4* __restrict__ pos, int n, const uint32_t* __restrict__ sl,
                 const int* __restrict__ slen, double box, DescParams P,
                 const float* __restrict__ e3, float scale, const float* __restrict__ istd,
                 float* __restrict__ V) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  float3 d[kSgMax];
-  float r[kSgMax];
-  int idx[kSgMax];
-  const int S = load_nbrs(i, pos, sl, slen, box, d, r, idx);
-  float q[kDesc];
-  for (int f = 0; f < kDesc; f++) q[f] = 0.f;
+  __shared__ NbrSm nb[4];
+  __shared__ float dex[4][kSgMax], dey[4][kSgMax], dez[4][kSgMax];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int i = blockIdx.x * 4 + warp;
+  if (i >= n) return;  // whole warp
+  NbrSm& N = nb[warp];
+  const int S = warp_load_nbrs(i, pos, sl, slen, box, P.rc, N);  // ends with __syncwarp
   const float eix = e3[3 * i], eiy = e3[3 * i + 1], eiz = e3[3 * i + 2];
-  float fc[kSgMax], dfc[kSgMax];
-  float3 de[kSgMax];
-  for (int s = 0; s < S; s++) {
-    fcut(r[s], P.rc, fc[s], dfc[s]);
-    de[s] = make_float3(e3[3 * idx[s]] - eix, e3[3 * idx[s] + 1] - eiy, e3[3 * idx[s] + 2] - eiz);
-    const float ir = 1.f / r[s];
-    const float ud = (d[s].x * de[s].x + d[s].y * de[s].y + d[s].z * de[s].z) * ir;  // u . de
+  float v[32];
+#pragma unroll
+  for (int f = 0; f < 32; f++) v[f] = 0.f;
+  for (int s = lane; s < S; s += 32) {
+    const int j = N.idx[s];
+    const float ex = e3[3 * j] - eix, ey = e3[3 * j + 1] - eiy, ez = e3[3 * j + 2] - eiz;
+    dex[warp][s] = ex;
+    dey[warp][s] = ey;
+    dez[warp][s] = ez;
+    const float ud = (N.dx[s] * ex + N.dy[s] * ey + N.dz[s] * ez) / N.r[s];  // u . de
+#pragma unroll
     for (int k = 0; k < kRad; k++) {
-      const float t = r[s] - P.rs[k];
-      const float ex = __expf(-P.eta_r * t * t);
-      q[k] += ex * (-2.f * P.eta_r * t * fc[s] + dfc[s]) * ud;
+      const float t = N.r[s] - P.rs[k];
+      v[k] += __expf(-P.eta_r * t * t) * (-2.f * P.eta_r * t * N.fc[s] + N.dfc[s]) * ud;
     }
   }
-  for (int a = 0; a < S; a++)
-    for (int b = a + 1; b < S; b++) {
-      const float rab = r[a] * r[b];
-      const float c = (d[a].x * d[b].x + d[a].y * d[b].y + d[a].z * d[b].z) / rab;
-      const float q2 = r[a] * r[a] + r[b] * r[b];
-      const float ia = 1.f / r[a], ib = 1.f / r[b];
-      // (dc/dd_a) . de_a + (dc/dd_b) . de_b, and the radial projections
-      const float dca = (d[b].x * de[a].x + d[b].y * de[a].y + d[b].z * de[a].z) / rab -
-                        c * (d[a].x * de[a].x + d[a].y * de[a].y + d[a].z * de[a].z) * ia * ia;
-      const float dcb = (d[a].x * de[b].x + d[a].y * de[b].y + d[a].z * de[b].z) / rab -
-                        c * (d[b].x * de[b].x + d[b].y * de[b].y + d[b].z * de[b].z) * ib * ib;
-      const float ua = (d[a].x * de[a].x + d[a].y * de[a].y + d[a].z * de[a].z) * ia;
-      const float ub = (d[b].x * de[b].x + d[b].y * de[b].y + d[b].z * de[b].z) * ib;
-      AngPair T;
-      ang_pair(c, q2, P, T);
+  __syncwarp();
+  const int npair = S * (S - 1) / 2;
+  for (int k = lane; k < npair; k += 32) {
+    int a, b;
+    pair_of(k, S, a, b);
+    const float ra = N.r[a], rb = N.r[b], rab = ra * rb;
+    const float ia = 1.f / ra, ib = 1.f / rb;
+    const float dax = N.dx[a], day = N.dy[a], daz = N.dz[a];
+    const float dbx = N.dx[b], dby = N.dy[b], dbz = N.dz[b];
+    const float eax = dex[warp][a], eay = dey[warp][a], eaz = dez[warp][a];
+    const float ebx = dex[warp][b], eby = dey[warp][b], ebz = dez[warp][b];
+    const float c = (dax * dbx + day * dby + daz * dbz) / rab;
+    const float q2 = ra * ra + rb * rb;
+    const float pa = dax * eax + day * eay + daz * eaz;  // d_a . de_a
+    const float pb = dbx * ebx + dby * eby + dbz * ebz;
+    const float dca = (dbx * eax + dby * eay + dbz * eaz) / rab - c * pa * ia * ia;
+    const float dcb = (dax * ebx + day * eby + daz * ebz) / rab - c * pb * ib * ib;
+    const float ua = pa * ia, ub = pb * ib;
+    const float fca = N.fc[a], fcb = N.fc[b], dfa = N.dfc[a], dfb = N.dfc[b];
+    AngPair T;
+    ang_pair(c, q2, P, T);
+    const float K1 = fca * fcb * (dca + dcb);
 #pragma unroll
-      for (int f = 0; f < kAng; f++) {
-        const int e = f >> 3, l = (f >> 2) & 1, z = f & 3;
-        if (T.b[l] <= 0.f) continue;
-        const float pz1 = T.pz1[l][z], pz = T.pz[l][z], ex = T.ex[e];
-        const float A = P.pref[f] * (float)P.zeta[f] * P.lam[f] * pz1 * ex * fc[a] * fc[b];
-        const float Ba = P.pref[f] * pz * ex * fc[b] * (-2.f * P.eta_a[f] * r[a] * fc[a] + dfc[a]);
-        const float Bb = P.pref[f] * pz * ex * fc[a] * (-2.f * P.eta_a[f] * r[b] * fc[b] + dfc[b]);
-        q[kRad + f] += A * (dca + dcb) + Ba * ua + Bb * ub;
+    for (int e = 0; e < 2; e++) {
+      const float eta = P.eta_a[8 * e];
+      const float K2 = fcb * fmaf(-2.f * eta * ra, fca, dfa) * ua +
+                       fca * fmaf(-2.f * eta * rb, fcb, dfb) * ub;
+#pragma unroll
+      for (int l = 0; l < 2; l++) {
+        const float on = T.b[l] > 0.f ? T.ex[e] : 0.f;  // (1 + lambda cos) clipped at 0
+#pragma unroll
+        for (int z = 0; z < 4; z++) {
+          const int f = 8 * e + 4 * l + z;
+          const float zl = (float)P.zeta[f] * P.lam[f];
+          v[kRad + f] += P.pref[f] * on * fmaf(zl * T.pz1[l][z], K1, T.pz[l][z] * K2);
+        }
       }
     }
-  for (int f = 0; f < kDesc; f++) V[(size_t)i * kDesc + f] = scale * istd[f] * q[f];
+  }
+  const float q = warp_reduce_scatter32(v);
+  V[(size_t)i * kDesc + lane] = scale * (istd ? istd[lane] : 1.f) * q;
 }
 
 // e = F_pred - F_exact (FP32) and sum e^2 into acc[0]
@@ -1226,6 +1248,32 @@ int sur_get_params(const Surrogate& s, float* P, cudaStream_t st) {
 int sur_param_count() { return kParams; }
 
 // neighbours, then descriptors (normalised when `normalised`) for atoms [0, n)
+// q_if = sum_j (e_j - e_i) . dG_if/dd_j for host e3 (n x 3) on the short
+// lists of the last sur_descriptors call; q_host n x 32
+int sur_directional(Surrogate& s, const md_double4* pos, int n, double box, const double* e3,
+                    double* q_host, cudaStream_t st) {
+  if (n <= 0) return 0;
+  std::vector<float> he(3 * (size_t)n);
+  for (size_t k = 0; k < he.size(); k++) he[k] = (float)e3[k];
+  float *de = nullptr, *dv = nullptr;
+  cudaError_t e = cudaMalloc(&de, sizeof(float) * he.size());
+  if (e == cudaSuccess) e = cudaMalloc(&dv, sizeof(float) * kDesc * (size_t)n);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(de, he.data(), sizeof(float) * he.size(), cudaMemcpyHostToDevice, st);
+  std::vector<float> hv(kDesc * (size_t)n);
+  if (e == cudaSuccess) {
+    k_sg_ctrans<<<sblocks(n, 4), 128, 0, st>>>(pos, n, s.sl, s.slen, box, s.P, de, 1.f, nullptr,
+                                               dv);
+    e = cudaMemcpyAsync(hv.data(), dv, sizeof(float) * hv.size(), cudaMemcpyDeviceToHost, st);
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e == cudaSuccess)
+    for (size_t k = 0; k < hv.size(); k++) q_host[k] = hv[k];
+  if (de) cudaFree(de);
+  if (dv) cudaFree(dv);
+  return (int)e;
+}
+
 int sur_descriptors(Surrogate& s, const md_double4* pos, int n, const RowWalker& w,
                     bool normalised, int* d_status, cudaStream_t st) {
   cudaError_t e;
@@ -1579,7 +1627,7 @@ int sur_train_fm(Surrogate& s, int steps, float lr, double* loss_e, double* loss
     k_fm_resid<<<sblocks(3LL * n, 256), 256, 0, st>>>(s.F32, c.fx, 3 * n, s.E3, s.scratch);
     // dL_F/d(dt/dx) = -2 kappa sigma istd q with kappa = w_force / (3 n var_F)
     const float kappa = (float)(s.w_force / (3.0 * n * s.force_var));
-    k_sg_ctrans<<<sblocks(n, 128), 128, 0, st>>>(c.pos, n, c.sl, c.slen, c.box, s.P, s.E3,
+    k_sg_ctrans<<<sblocks(n, 4), 128, 0, st>>>(c.pos, n, c.sl, c.slen, c.box, s.P, s.E3,
                                                  (float)(-2.0 * kappa * s.sigma), s.istd_d, s.V);
     cudaMemsetAsync(s.G_d, 0, sizeof(float) * kParams, st);
     cudaMemsetAsync(s.loss_d, 0, sizeof(double), st);

@@ -94,6 +94,8 @@ int sur_set_params(Surrogate& s, const float* P, cudaStream_t st);
 int sur_get_params(const Surrogate& s, float* P, cudaStream_t st);
 int sur_param_count();
 // neighbours within rc, then descriptors of atoms [0, n) into s.X
+int sur_directional(Surrogate& s, const md_double4* pos, int n, double box, const double* e3,
+                    double* q_host, cudaStream_t st);
 int sur_descriptors(Surrogate& s, const md_double4* pos, int n, const RowWalker& w,
                     bool normalised, int* d_status, cudaStream_t st);
 // appends atoms offset, offset + stride, ... of the last raw descriptors

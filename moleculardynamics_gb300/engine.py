@@ -108,7 +108,8 @@ EXPORTS = ["md_create", "md_destroy", "md_status_string", "md_last_error", "md_u
            "md_surrogate_samples", "md_surrogate_train", "md_surrogate_attach",
            "md_surrogate_report", "md_surrogate_forces", "md_surrogate_descriptors",
            "md_surrogate_params", "md_surrogate_normalisation", "md_surrogate_loss_grad",
-           "md_surrogate_net", "md_surrogate_train_forces", "md_surrogate_force_grad"]
+           "md_surrogate_net", "md_surrogate_train_forces", "md_surrogate_force_grad",
+           "md_surrogate_desc_directional"]
 
 
 def load(path: str | None = None) -> C.CDLL:
@@ -158,6 +159,7 @@ def load(path: str | None = None) -> C.CDLL:
     L.md_surrogate_report.argtypes = [C.c_void_p, P(MdSurrogateStats)]
     L.md_surrogate_forces.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, P(C.c_double)]
     L.md_surrogate_descriptors.argtypes = [C.c_void_p, C.c_void_p, _fp, C.c_int]
+    L.md_surrogate_desc_directional.argtypes = [C.c_void_p, C.c_void_p, _dp, _dp]
     L.md_surrogate_params.argtypes = [C.c_void_p, _fp, C.c_int]
     L.md_surrogate_normalisation.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                              C.c_int]
@@ -465,6 +467,17 @@ class Surrogate:
         if s != 0:
             raise EngineError(s, "md_surrogate_forces: " + self.lib.md_last_error(e.h).decode())
         return f, en.value
+
+    def desc_directional(self, e: "Engine", e3: np.ndarray) -> np.ndarray:
+        """sum_j (e_j - e_i) . dG_if/dd_j for the first n_mb atoms (n_mb x 32)."""
+        n = e.cfg.n_mb
+        e3 = np.ascontiguousarray(e3, np.float64).reshape(n, 3)
+        q = np.zeros((n, 32))
+        s = self.lib.md_surrogate_desc_directional(self.h, e.h, e3, q)
+        if s != 0:
+            raise EngineError(s, "md_surrogate_desc_directional: " +
+                              self.lib.md_last_error(e.h).decode())
+        return q
 
     def descriptors(self, e: "Engine", normalised: bool = False) -> np.ndarray:
         g = np.zeros((e.cfg.n_mb, 32), np.float32)

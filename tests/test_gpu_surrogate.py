@@ -57,6 +57,26 @@ def test_descriptors_vs_oracle(eng):
     assert np.abs((g - ref) / scale).max() < 2e-4
 
 
+def test_desc_directional_vs_oracle(eng):
+    """The force-matching transpose (k_sg_ctrans): the derivative of every
+    atom's descriptors when all atoms move along e equals the central finite
+    difference of the CPU restatement's descriptors."""
+    from oracle import surrogate_ref as sref
+    pos, vel, L = nitrogen_diamond(4, noise=0.05)
+    n = len(pos)
+    e3 = np.random.default_rng(8).standard_normal((n, 3)) * 0.1
+    with _mb_engine(eng, pos, vel, L) as e, eng.Surrogate(cutoff=MB_RC) as s:
+        q = s.desc_directional(e, e3)
+        p, _ = e.download()
+    h = 1e-4
+    pp, pm = p.copy(), p.copy()
+    pp[:, :3] += h * e3
+    pm[:, :3] -= h * e3
+    ref = (sref.descriptors(pp, L, MB_RC) - sref.descriptors(pm, L, MB_RC)) / (2 * h)
+    scale = np.abs(ref).max(0) + 1e-12
+    assert np.abs((q - ref) / scale).max() < 2e-3
+
+
 def test_network_vs_oracle(eng):
     from oracle import surrogate_ref as sref
     with eng.Surrogate(cutoff=MB_RC) as s:
