@@ -550,14 +550,14 @@ __global__ void __launch_bounds__(128)
       T va = 0, dva = 0, vr = 0, dvr = 0, vdw, dvdw, bo = 0;
       T dbx = 0, dby = 0, dbz = 0;
       T fcut, dfcut;
-      cutoff<T>(rij / 10, fcut, dfcut);
+      cutoff<T>(fdiv<T>(rij, 10), fcut, dfcut);
       T xs_i = nanv, xs_j = nanv;
       if (fcut > 0) {
         const T de = get_de<T>(ti, tj), re = get_re<T>(ti, tj), beta = get_beta<T>(ti, tj);
         attractive<T>(va, dva, rij, de, beta, re);
         repulsive<T>(vr, dvr, rij, de, beta, re);
         // BondOrderFuncs.h:12-143 bondOrder1
-        const T drijx = ijx / rij, drijy = ijy / rij, drijz = ijz / rij;
+        const T drijx = fdiv<T>(ijx, rij), drijy = fdiv<T>(ijy, rij), drijz = fdiv<T>(ijz, rij);
         const T E = md_exp((T)MD_LAMDA3 * (rij - re));
         T xsi = 0, xsj = 0;
         T dxsix = 0, dxsiy = 0, dxsiz = 0, dxsjx = 0, dxsjy = 0, dxsjz = 0;
@@ -576,37 +576,37 @@ __global__ void __launch_bounds__(128)
           T fci, dfci, fcj, dfcj;
           cutoff<T>(rim, fci, dfci);
           cutoff<T>(rjm, fcj, dfcj);
-          const T drimx = imx / rim, drimy = imy / rim, drimz = imz / rim;
+          const T drimx = fdiv<T>(imx, rim), drimy = fdiv<T>(imy, rim), drimz = fdiv<T>(imz, rim);
           if (fci > 0) {
             const T num2 = rij * rij + rim * rim - rjm * rjm;
-            const T icos = num2 / (2.0f * rij * rim);
+            const T icos = fdiv<T>(num2, 2.0f * rij * rim);
             T gth, gpre;
             angular<T>(icos, gth, gpre);
             xsi += fci * gth * E;
             const T den = 4.0f * rij * rij * rim * rim;
-            const T dcx = ((2.0f * rij * drijx + 2.0f * rim * drimx) * 2.0f * rij * rim -
-                           (2.0f * rim * drijx + 2.0f * rij * drimx) * num2) / den;
-            const T dcy = ((2.0f * rij * drijy + 2.0f * rim * drimy) * 2.0f * rij * rim -
-                           (2.0f * rim * drijy + 2.0f * rij * drimy) * num2) / den;
-            const T dcz = ((2.0f * rij * drijz + 2.0f * rim * drimz) * 2.0f * rij * rim -
-                           (2.0f * rim * drijz + 2.0f * rij * drimz) * num2) / den;
+            const T dcx = fdiv<T>(((2.0f * rij * drijx + 2.0f * rim * drimx) * 2.0f * rij * rim -
+                           (2.0f * rim * drijx + 2.0f * rij * drimx) * num2), den);
+            const T dcy = fdiv<T>(((2.0f * rij * drijy + 2.0f * rim * drimy) * 2.0f * rij * rim -
+                           (2.0f * rim * drijy + 2.0f * rij * drimy) * num2), den);
+            const T dcz = fdiv<T>(((2.0f * rij * drijz + 2.0f * rim * drimz) * 2.0f * rij * rim -
+                           (2.0f * rim * drijz + 2.0f * rij * drimz) * num2), den);
             dxsix += dfci * drimx * gth * E + fci * (gpre * dcx) * E + fci * gth * MD_LAMDA3 * E * drijx;
             dxsiy += dfci * drimy * gth * E + fci * (gpre * dcy) * E + fci * gth * MD_LAMDA3 * E * drijy;
             dxsiz += dfci * drimz * gth * E + fci * (gpre * dcz) * E + fci * gth * MD_LAMDA3 * E * drijz;
           }
           if (fcj > 0) {
             const T num2 = rij * rij + rjm * rjm - rim * rim;
-            const T jcos = num2 / (2.0f * rij * rjm);
+            const T jcos = fdiv<T>(num2, 2.0f * rij * rjm);
             T gth, gpre;
             angular<T>(jcos, gth, gpre);
             xsj += fcj * gth * E;
             const T den = 4.0f * rij * rij * rjm * rjm;
-            const T dcx = ((2.0f * rij * drijx - 2.0f * rim * drimx) * 2.0f * rij * rjm -
-                           2.0f * rjm * drijx * num2) / den;
-            const T dcy = ((2.0f * rij * drijy - 2.0f * rim * drimy) * 2.0f * rij * rjm -
-                           2.0f * rjm * drijy * num2) / den;
-            const T dcz = ((2.0f * rij * drijz - 2.0f * rim * drimz) * 2.0f * rij * rjm -
-                           2.0f * rjm * drijz * num2) / den;
+            const T dcx = fdiv<T>(((2.0f * rij * drijx - 2.0f * rim * drimx) * 2.0f * rij * rjm -
+                           2.0f * rjm * drijx * num2), den);
+            const T dcy = fdiv<T>(((2.0f * rij * drijy - 2.0f * rim * drimy) * 2.0f * rij * rjm -
+                           2.0f * rjm * drijy * num2), den);
+            const T dcz = fdiv<T>(((2.0f * rij * drijz - 2.0f * rim * drimz) * 2.0f * rij * rjm -
+                           2.0f * rjm * drijz * num2), den);
             dxsjx += fcj * ((gpre * dcx) * E + MD_LAMDA3 * E * drijx * gth);
             dxsjy += fcj * ((gpre * dcy) * E + MD_LAMDA3 * E * drijy * gth);
             dxsjz += fcj * ((gpre * dcz) * E + MD_LAMDA3 * E * drijz * gth);
@@ -614,8 +614,8 @@ __global__ void __launch_bounds__(128)
         }
         xs_i = xsi;
         xs_j = xsj;
-        const T bij = 1.0f / (1.0f + xsi), pbi = 1.0f / ((1.0f + xsi) * (1.0f + xsi));
-        const T bji = 1.0f / (1.0f + xsj), pbj = 1.0f / ((1.0f + xsj) * (1.0f + xsj));
+        const T bij = fdiv<T>(1.0f, 1.0f + xsi), pbi = fdiv<T>(1.0f, (1.0f + xsi) * (1.0f + xsi));
+        const T bji = fdiv<T>(1.0f, 1.0f + xsj), pbj = fdiv<T>(1.0f, (1.0f + xsj) * (1.0f + xsj));
         bo = 0.5f * (bij + bji);
         dbx = 0.5f * (pbi * dxsix + pbj * dxsjx);
         dby = 0.5f * (pbi * dxsiy + pbj * dxsjy);
@@ -626,9 +626,9 @@ __global__ void __launch_bounds__(128)
       va_s[slot] = va;
       vander_waals<T>(vdw, dvdw, rij, get_r0v<T>(ti, tj));
       const T fij = dvr - bo * dva + dvdw;
-      fx += fij * ijx / rij - dbx * va;
-      fy += fij * ijy / rij - dby * va;
-      fz += fij * ijz / rij - dbz * va;
+      fx += fdiv<T>(fij * ijx, rij) - dbx * va;
+      fy += fdiv<T>(fij * ijy, rij) - dby * va;
+      fz += fdiv<T>(fij * ijz, rij) - dbz * va;
       if (ENERGY) ev[0] += (double)(0.5f * ((vr - bo * va) + vdw));
     }
     double sx = warp_sum((double)fx), sy = warp_sum((double)fy), sz = warp_sum((double)fz);
@@ -690,7 +690,7 @@ __global__ void __launch_bounds__(128)
       const T rik = md_sqrt(ikx * ikx + iky * iky + ikz * ikz);
       T fci, dfci;
       cutoff<T>(rik, fci, dfci);
-      const T drikx = ikx / rik, driky = iky / rik, drikz = ikz / rik;
+      const T drikx = fdiv<T>(ikx, rik), driky = fdiv<T>(iky, rik), drikz = fdiv<T>(ikz, rik);
       const int Si = slen[ip];
       for (int sj = 0; sj < Si; sj++) {
         const size_t q = (size_t)sj * n + ip;
@@ -732,35 +732,35 @@ __global__ void __launch_bounds__(128)
         // BondOrderFuncs.h:148-237 bondOrder2 (k third body of pair ip, jp)
         const T jkx = pjx - xk, jky = pjy - yk, jkz = pjz - zk;
         const T rjk = md_sqrt(jkx * jkx + jky * jky + jkz * jkz);
-        const T drjkx = -jkx / rjk, drjky = -jky / rjk, drjkz = -jkz / rjk;
+        const T drjkx = fdiv<T>(-jkx, rjk), drjky = fdiv<T>(-jky, rjk), drjkz = fdiv<T>(-jkz, rjk);
         T fcj, dfcj;
         cutoff<T>(rjk, fcj, dfcj);
         const T E = md_exp((T)MD_LAMDA3 * (rij - re));
         T dbx = 0, dby = 0, dbz = 0;
         if (fci > 0) {
           const T num2 = rij * rij + rik * rik - rjk * rjk;
-          const T icos = num2 / (2.0f * rij * rik);
+          const T icos = fdiv<T>(num2, 2.0f * rij * rik);
           T gth, gpre;
           angular<T>(icos, gth, gpre);
           const T den = 4.0f * rij * rij * rik * rik;
-          const T dcx = ((2.0f * rik * drikx - 2.0f * rjk * drjkx) * 2.0f * rij * rik - (2.0f * rij * drikx) * num2) / den;
-          const T dcy = ((2.0f * rik * driky - 2.0f * rjk * drjky) * 2.0f * rij * rik - (2.0f * rij * driky) * num2) / den;
-          const T dcz = ((2.0f * rik * drikz - 2.0f * rjk * drjkz) * 2.0f * rij * rik - (2.0f * rij * drikz) * num2) / den;
-          const T p = 1.0f / ((1.0f + xs_i) * (1.0f + xs_i));
+          const T dcx = fdiv<T>(((2.0f * rik * drikx - 2.0f * rjk * drjkx) * 2.0f * rij * rik - (2.0f * rij * drikx) * num2), den);
+          const T dcy = fdiv<T>(((2.0f * rik * driky - 2.0f * rjk * drjky) * 2.0f * rij * rik - (2.0f * rij * driky) * num2), den);
+          const T dcz = fdiv<T>(((2.0f * rik * drikz - 2.0f * rjk * drjkz) * 2.0f * rij * rik - (2.0f * rij * drikz) * num2), den);
+          const T p = fdiv<T>(1.0f, (1.0f + xs_i) * (1.0f + xs_i));
           dbx += 0.5f * (p * (dfci * drikx * gth * E + fci * (gpre * dcx) * E));
           dby += 0.5f * (p * (dfci * driky * gth * E + fci * (gpre * dcy) * E));
           dbz += 0.5f * (p * (dfci * drikz * gth * E + fci * (gpre * dcz) * E));
         }
         if (fcj > 0) {
           const T num2 = rij * rij + rjk * rjk - rik * rik;
-          const T jcos = num2 / (2.0f * rij * rjk);
+          const T jcos = fdiv<T>(num2, 2.0f * rij * rjk);
           T gth, gpre;
           angular<T>(jcos, gth, gpre);
           const T den = 4.0f * rij * rij * rjk * rjk;
-          const T dcx = ((2.0f * rjk * drjkx - 2.0f * rik * drikx) * 2.0f * rij * rjk - (2.0f * rij * drjkx) * num2) / den;
-          const T dcy = ((2.0f * rjk * drjky - 2.0f * rik * driky) * 2.0f * rij * rjk - (2.0f * rij * drjky) * num2) / den;
-          const T dcz = ((2.0f * rjk * drjkz - 2.0f * rik * drikz) * 2.0f * rij * rjk - (2.0f * rij * drjkz) * num2) / den;
-          const T p = 1.0f / ((1.0f + xs_j) * (1.0f + xs_j));
+          const T dcx = fdiv<T>(((2.0f * rjk * drjkx - 2.0f * rik * drikx) * 2.0f * rij * rjk - (2.0f * rij * drjkx) * num2), den);
+          const T dcy = fdiv<T>(((2.0f * rjk * drjky - 2.0f * rik * driky) * 2.0f * rij * rjk - (2.0f * rij * drjky) * num2), den);
+          const T dcz = fdiv<T>(((2.0f * rjk * drjkz - 2.0f * rik * drikz) * 2.0f * rij * rjk - (2.0f * rij * drjkz) * num2), den);
+          const T p = fdiv<T>(1.0f, (1.0f + xs_j) * (1.0f + xs_j));
           dbx += 0.5f * (p * (dfcj * drjkx * gth * E + fcj * (gpre * dcx) * E));
           dby += 0.5f * (p * (dfcj * drjky * gth * E + fcj * (gpre * dcy) * E));
           dbz += 0.5f * (p * (dfcj * drjkz * gth * E + fcj * (gpre * dcz) * E));

@@ -9,12 +9,27 @@
 
 namespace mdgb {
 
+// FP64: the library functions (the reference's expressions).  FP32 (the
+// precision form, within 1e-4 of FP64 by requirement): the hardware
+// approximations, a few ulp each -- exp by ex2.approx, tanh from it as
+// 1 - 2 / (e^2x + 1) (absolute error about 1e-7), sqrt as x rsqrt(x) (the
+// bond-order distances are never 0), quotients by __fdividef.
 __device__ __forceinline__ double md_exp(double x) { return exp(x); }
-__device__ __forceinline__ float md_exp(float x) { return expf(x); }
+__device__ __forceinline__ float md_exp(float x) { return __expf(x); }
 __device__ __forceinline__ double md_tanh(double x) { return tanh(x); }
-__device__ __forceinline__ float md_tanh(float x) { return tanhf(x); }
+__device__ __forceinline__ float md_tanh(float x) {
+  return 1.0f - __fdividef(2.0f, __expf(2.0f * x) + 1.0f);
+}
 __device__ __forceinline__ double md_sqrt(double x) { return sqrt(x); }
-__device__ __forceinline__ float md_sqrt(float x) { return sqrtf(x); }
+__device__ __forceinline__ float md_sqrt(float x) { return x * rsqrtf(x); }
+template <typename T>
+__device__ __forceinline__ T fdiv(T a, T b) {
+  return a / b;
+}
+template <>
+__device__ __forceinline__ float fdiv<float>(float a, float b) {
+  return __fdividef(a, b);
+}
 
 // common/Getters.cpp:29-78
 template <typename T>
@@ -74,8 +89,8 @@ template <typename T>
 __device__ __forceinline__ void angular(T costhe, T& g, T& gpre) {
   T hc = MD_H - costhe;
   T q = MD_D + hc * hc;
-  g = 1.0f + MD_C / MD_D - MD_C / q;
-  gpre = -MD_C / (q * q) * 2.0f * hc;
+  g = 1.0f + MD_C / MD_D - fdiv<T>(MD_C, q);
+  gpre = -fdiv<T>(MD_C, q * q) * 2.0f * hc;
 }
 
 // LennardJones.h:65-86: parameters of an NG pair, selected by the other type
