@@ -412,7 +412,7 @@ def surrogate_form(eng, device, train_steps: int, run_steps: int, seed: int = 5)
         # the same precision with lists built at the final positions, as the
         # FP64 judge's are: the arithmetic's own error, without the list state
         same = None
-        if precision != eng.PREC_FP64:
+        if precision != eng.PREC_FP64 and threshold is None:
             ef = engine(p1, v1, L, precision)
             same = rel(ef.compute_forces()[0])
             ef.close()
