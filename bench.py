@@ -650,6 +650,41 @@ def run_gb300(args, rank, world):
     return 0
 
 
+def bond_order_lattice(eng, T: float, seed: int, precision, device: int = 0, ncell: int = 16):
+    """Nitrogen on an ncell^3 diamond lattice (nearest neighbour 1.5 A, 0.02 A
+    noise) in its periodic box, bond order only (rs 3.5 A, rcut 3.0 A, dt
+    0.5 fs); returns a begun engine."""
+    from moleculardynamics_gb300 import lattice as lat
+    a = 4 * 1.5 / np.sqrt(3.0)
+    pos, vel, L = lat.make_system("diamond", ncell, T, seed=seed, a=a, noise=0.02,
+                                  species=lat.SPECIES_N, mass_table="neon")
+    cfg = eng.make_config(n_mb=len(pos), use_lj=0, use_mb=1, mb_rs=3.5, mb_rcut=3.0, dt=0.5,
+                          periodic=1, box=L, species=eng.SPECIES_NEON, device=device,
+                          precision=precision)
+    e = eng.Engine(cfg)
+    e.upload(pos, vel)
+    e.begin(0.0)
+    return e
+
+
+def run_case(args) -> int:
+    """Profiling cases (one process, one GPU, no JSON contract line)."""
+    from moleculardynamics_gb300 import build as b
+    from moleculardynamics_gb300 import engine as eng
+    b.build()
+    eng.load()
+    if args.case == "bo32k":
+        e = bond_order_lattice(eng, 900.0, 15, eng.PREC_MIXED)
+        e.set_timing(True)
+        e.step(args.steps)
+        e.synchronize()
+        ms, _ = e.kernel_time(eng.KERNEL_STEP)
+        e.close()
+        print(json.dumps({"case": "bo32k", "atoms": 32768, "md_steps": args.steps,
+                          "ms_per_step": ms / max(args.steps, 1)}))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -675,8 +710,14 @@ def main():
     ap.add_argument("--batch-loop-steps", type=int, default=10)
     ap.add_argument("--sur-train-steps", type=int, default=20000)
     ap.add_argument("--sur-run-steps", type=int, default=200)
+    ap.add_argument("--case", default=None, choices=["bo32k"],
+                    help="a profiling case instead of the benchmark: bo32k runs the "
+                         "32,768-atom bond-order lattice in the precision form for --steps "
+                         "MD steps and prints its step time")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.case:
+        return run_case(args)
     rank, world, _ = dist_env()
     if args.impl == "reference":
         return run_reference_arm(args, rank, world)
