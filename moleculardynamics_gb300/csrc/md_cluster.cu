@@ -700,6 +700,16 @@ __global__ void __launch_bounds__(224, 3)
     const int p = base + tid;
     const bool live = p < p1;
     const int self = live ? self_offset(sh, p) : 0;
+    if (GEAR && live) {
+      // the Gear state of this atom is read after the force loop: ask L2
+      // for its lines now
+      prefetch_l2(a.pos + p);
+      prefetch_l2(a.g.vel + 3 * (size_t)p);
+      prefetch_l2(a.g.acc + 3 * (size_t)p);
+      prefetch_l2(a.g.b + 3 * (size_t)p);
+      prefetch_l2(a.g.c + 3 * (size_t)p);
+      prefetch_l2(a.pos_build + p);
+    }
     const float4 pi = st[self];
     const int ti = __float_as_int(pi.w);
     float hx = 0.f, hy = 0.f, hz = 0.f, lx = 0.f, ly = 0.f, lz = 0.f;
