@@ -674,6 +674,12 @@ __global__ void __launch_bounds__(224, 3)
   if (sidx >= a.nseg) break;
   load_segment(sh, a.seg, a.reps, sidx);
   __syncthreads();
+  // block tiles: the segment's first two row tiles go to L2 while the
+  // neighbourhood streams in (no completion to wait for)
+  if (ROWS == 0 && !tripped && tid == 0) {
+    tma_prefetch_2d(&rmap, sh.S.p0 & ~7, 0);
+    tma_prefetch_2d(&rmap, sh.S.p0 & ~7, kClusterTileSlots);
+  }
   if (!stage_bulk(sh, a.posf, st, &bar[3], (phase >> 3) & 1u, a.status)) {
     aborted = true;
     break;

@@ -77,6 +77,15 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* s
   return false;
 }
 
+// L2 prefetch of one box of a tiled tensor map (coordinates as for
+// tma_load_2d; no shared memory, no barrier, no completion to wait for)
+__device__ __forceinline__ void tma_prefetch_2d(const CUtensorMap* map, int x, int y) {
+  asm volatile("cp.async.bulk.prefetch.tensor.2d.L2.global.tile [%0, {%1, %2}];" ::"l"(
+                   (unsigned long long)map),
+               "r"(x), "r"(y)
+               : "memory");
+}
+
 // L2 prefetch of the line holding p (no register result, no wait)
 __device__ __forceinline__ void prefetch_l2(const void* p) {
   asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
