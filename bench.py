@@ -401,7 +401,7 @@ def surrogate_form(eng, device, train_steps: int, run_steps: int, seed: int = 5)
         # network's when it computed any step, else the exact kernel's
         if threshold is None or not rep or rep["surrogate_steps"] == 0:
             es0, es1 = ex0, en[3]
-        # the exact FP64 forces at the final positions judge every variant
+        # the exact FP64 forces at the final positions are the reference for every variant
         e64 = engine(p1, v1, L)
         fx, _ = e64.compute_forces()
         e64.close()
@@ -410,7 +410,7 @@ def surrogate_form(eng, device, train_steps: int, run_steps: int, seed: int = 5)
             return float(np.sqrt(((fa - fx) ** 2).sum(1).mean() / (fx ** 2).sum(1).mean()))
 
         # the same precision with lists built at the final positions, as the
-        # FP64 judge's are: the arithmetic's own error, without the list state
+        # FP64 reference's are: the arithmetic's own error, without the list state
         same = None
         if precision != eng.PREC_FP64 and threshold is None:
             ef = engine(p1, v1, L, precision)
@@ -426,7 +426,7 @@ def surrogate_form(eng, device, train_steps: int, run_steps: int, seed: int = 5)
 
     exact = run(None)
     exact32 = run(None, eng.PREC_MIXED)
-    # the surrogate runs beside the precision form: its judge and fallback
+    # the surrogate runs beside the precision form: its error check and fallback
     # is the exact kernel of the context (FP32 pairs, FP64 Gear)
     strict = run(1e-4, eng.PREC_MIXED)
     loose = run(1.0, eng.PREC_MIXED)

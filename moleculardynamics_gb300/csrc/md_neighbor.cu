@@ -248,7 +248,7 @@ inline int blocks(long long n, int t) { return (int)((n + t - 1) / t); }
 
 }  // namespace
 
-// cuTensorMapEncodeTiled from the driver, looked up once through the runtime
+// cuTensorMapEncodeTiled of the CUDA driver API, looked up once through the runtime
 typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
                                   const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
                                   const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
