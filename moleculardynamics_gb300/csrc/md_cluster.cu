@@ -21,6 +21,7 @@
 #include <cfloat>
 #include <cmath>
 #include <cstring>
+#include <type_traits>
 
 #include "md_cluster.h"
 #include "md_gear.cuh"
@@ -485,7 +486,50 @@ __global__ void __launch_bounds__(256)
     const int p = base + threadIdx.x;
     const bool live = p < sh.S.p1;
     int kept = 0;
-    if (live) {
+    if (live && !minimg) {
+      // the 9 column groups in row order, four independent distance tests
+      // per step; only the centre group holds the atom itself
+      const int self = self_offset(sh, p);
+      const float4 pi = st[self];
+      const int zspan = sh.S.cz1 - sh.S.cz0 + 3;
+      int w = 1;
+      while (w < zspan - 2 && sh.off[4][w + 1] <= self) w++;
+      const int u = w - 1;
+      auto near = [&](int q) {
+        const float4 pj = st[q];
+        const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+        return dx * dx + dy * dy + dz * dz < rv2;
+      };
+      auto take = [&](int q, bool in) {
+        if (in) {
+          if (MODE != 0 && kept < cap) rows[(size_t)kept * ld + p] = (uint16_t)q;
+          kept++;
+        }
+      };
+      auto group = [&](int g, auto centre) {
+        const int qa = sh.off[g][u], qb = sh.off[g][u + 3];
+        int q = qa;
+        for (; q + 4 <= qb; q += 4) {
+          bool i0 = near(q), i1 = near(q + 1), i2 = near(q + 2), i3 = near(q + 3);
+          if (decltype(centre)::value) {
+            i0 = i0 && q != self;
+            i1 = i1 && q + 1 != self;
+            i2 = i2 && q + 2 != self;
+            i3 = i3 && q + 3 != self;
+          }
+          take(q, i0);
+          take(q + 1, i1);
+          take(q + 2, i2);
+          take(q + 3, i3);
+        }
+        for (; q < qb; q++) take(q, near(q) && (!decltype(centre)::value || q != self));
+      };
+#pragma unroll 1
+      for (int g = 0; g < 4; g++) group(g, std::false_type());
+      group(4, std::true_type());
+#pragma unroll 1
+      for (int g = 5; g < 9; g++) group(g, std::false_type());
+    } else if (live) {
       const int self = self_offset(sh, p);
       const float4 pi = st[self];
       walk_staged(sh, self, [&](int q) {
@@ -719,6 +763,19 @@ __global__ void __launch_bounds__(224, 3)
     const float4 pi = st[self];
     const int ti = __float_as_int(pi.w);
     float hx = 0.f, hy = 0.f, hz = 0.f, lx = 0.f, ly = 0.f, lz = 0.f;
+    // energies (ENERGY): E, shifted E and the virial of the atom's pairs,
+    // summed like the forces (FP32 within a 16-slot chunk, compensated
+    // across chunks, widened to FP64 once per atom)
+    float ce = 0.f, cs = 0.f, cw = 0.f;
+    float eh = 0.f, el = 0.f, sh2 = 0.f, sl2 = 0.f, wh = 0.f, wl = 0.f;
+    auto fold_energy = [&]() {
+      if (ENERGY) {
+        kahan_add(eh, el, ce);
+        kahan_add(sh2, sl2, cs);
+        kahan_add(wh, wl, cw);
+        ce = cs = cw = 0.f;
+      }
+    };
     // candidate q into the running sums (cx, cy, cz); `valid` false
     // evaluates a harmless dummy (no branch)
     auto pair = [&](int q, bool valid, float& cx, float& cy, float& cz) {
@@ -750,14 +807,14 @@ __global__ void __launch_bounds__(224, 3)
       cx = fmaf(dx, fij, cx);
       cy = fmaf(dy, fij, cy);
       cz = fmaf(dz, fij, cz);
-      if (ENERGY && in) {
+      if (ENERGY) {
         const float src2 = s2 / rc2;
         const float src6 = src2 * src2 * src2;
         const float eps = c24 * (1.0f / 24.0f);
         const float e = 2.0f * eps * (sr6 * sr6 - sr6);
-        ev[0] += (double)e;
-        ev[1] += (double)e - (double)(2.0f * eps * (src6 * src6 - src6));
-        ev[2] += 0.5 * (double)(r2 * fij);
+        ce += in ? e : 0.0f;
+        cs += in ? e - 2.0f * eps * (src6 * src6 - src6) : 0.0f;
+        cw += r2 * fij;  // fij is zero outside the cutoff
       }
     };
     // 16 row slots: even and odd slots in two sums (two independent FMA
@@ -789,6 +846,7 @@ __global__ void __launch_bounds__(224, 3)
       kahan_add(hx, lx, ax + bx);
       kahan_add(hy, ly, ay + by);
       kahan_add(hz, lz, az + bz);
+      fold_energy();
     };
     // The padded-row form of a pair: no validity test, and the FP64 decision
     // near the cutoff is deferred: `band` records that some pair of the
@@ -1016,6 +1074,7 @@ __global__ void __launch_bounds__(224, 3)
           kahan_add(hx, lx, cx);
           kahan_add(hy, ly, cy);
           kahan_add(hz, lz, cz);
+          fold_energy();
           cx = cy = cz = 0.f;
           inchunk = 0;
         }
@@ -1034,6 +1093,7 @@ __global__ void __launch_bounds__(224, 3)
       kahan_add(hx, lx, cx);
       kahan_add(hy, ly, cy);
       kahan_add(hz, lz, cz);
+      fold_energy();
       if (kept > a.cap) atomicOr(&a.skin[3], 1);
       a.len[p] = (uint16_t)(kept < a.cap ? kept : a.cap);
       kept_new = kept;
@@ -1045,6 +1105,11 @@ __global__ void __launch_bounds__(224, 3)
       // combined in FP64
       const double f[3] = {widen_exact(hx) - widen_exact(lx), widen_exact(hy) - widen_exact(ly),
                            widen_exact(hz) - widen_exact(lz)};
+      if (ENERGY) {
+        ev[0] += (double)eh - (double)el;
+        ev[1] += (double)sh2 - (double)sl2;
+        ev[2] += 0.5 * ((double)wh - (double)wl);
+      }
       if (!GEAR) {
         a.f3[3 * p] = f[0];
         a.f3[3 * p + 1] = f[1];
@@ -1396,10 +1461,10 @@ int cluster_build(ClusterList& cl, const std::vector<ClusterReplica>& reps_in, f
   const bool have_rows = cl.rows && cl.cap > 0 && (long long)cl.cap * cl.ld <= cl.rows_elems;
   if (cl.nseg > 0) {
     if (have_rows)
-      k_cl_rows<2><<<cl.nseg, 256, smem, st>>>(cl.seg, cl.rep, cl.start, cl.pos_build, cl.rv2,
+      k_cl_rows<2><<<cl.nseg, cl.block, smem, st>>>(cl.seg, cl.rep, cl.start, cl.pos_build, cl.rv2,
                                                cl.rows, cl.len, cl.ld, cl.cap, cl.counters);
     else
-      k_cl_rows<0><<<cl.nseg, 256, smem, st>>>(cl.seg, cl.rep, cl.start, cl.pos_build, cl.rv2,
+      k_cl_rows<0><<<cl.nseg, cl.block, smem, st>>>(cl.seg, cl.rep, cl.start, cl.pos_build, cl.rv2,
                                                nullptr, cl.len, cl.ld, 0, cl.counters);
   }
   cudaMemcpyAsync(hc, cl.counters, sizeof(hc), cudaMemcpyDeviceToHost, st);
@@ -1434,7 +1499,7 @@ int cluster_build(ClusterList& cl, const std::vector<ClusterReplica>& reps_in, f
     return -1;
   }
   if (!fits && cl.nseg > 0)
-    k_cl_rows<1><<<cl.nseg, 256, smem, st>>>(cl.seg, cl.rep, cl.start, cl.pos_build, cl.rv2,
+    k_cl_rows<1><<<cl.nseg, cl.block, smem, st>>>(cl.seg, cl.rep, cl.start, cl.pos_build, cl.rv2,
                                              cl.rows, cl.len, cl.ld, cl.cap, cl.counters);
   cl.trip_dist = 0.5 * ((double)rv - rcut) - (double)margin;
   cudaMemsetAsync(cl.skin, 0, sizeof(int) * 4, st);  // trip flags and overflow
