@@ -149,11 +149,11 @@ def make_workload(name: str, seed: int = 2024):
 
 
 def engine_for(eng, n, L, precision, device, output=MD_PER_BENCH_STEP, lj_kernel=0, threads=0,
-               row_loads=0):
+               row_loads=0, stage_cap=0):
     cfg = eng.make_config(n_lj=n, dt=2.0, lj_rs=2.8 * SIGMA, lj_rcut=2.5 * SIGMA, periodic=1,
                           box=L, precision=precision, species=eng.SPECIES_ARGON, device=device,
                           output_timesteps=output, lj_kernel=lj_kernel, cluster_threads=threads,
-                          cluster_row_loads=row_loads)
+                          cluster_row_loads=row_loads, cluster_stage_cap=stage_cap)
     return eng.Engine(cfg)
 
 
@@ -469,7 +469,7 @@ def run_gb300(args, rank, world):
     precision = eng.PREC_MIXED if prec_name == "mixed" else eng.PREC_FP64
     lj_kernel = {"auto": eng.LJ_AUTO, "rows": eng.LJ_ROWS, "cluster": eng.LJ_CLUSTER}[args.lj_kernel]
     e = engine_for(eng, n, L, precision, device, lj_kernel=lj_kernel, threads=args.threads,
-                   row_loads=args.row_loads)
+                   row_loads=args.row_loads, stage_cap=args.stage_cap)
     e.upload(pos, vel)
     e.begin(0.0)
     # tiles are tuned on the thermalised state (on the initial lattice every
@@ -705,6 +705,8 @@ def main():
                     help="cluster row scheme: 1 block TMA tiles, 2 register prefetch, "
                          "3 per-warp TMA tiles, 4 block TMA tiles three deep "
                          "(0: the autotuner chooses)")
+    ap.add_argument("--stage-cap", type=int, default=0,
+                    help="cluster staged atoms per segment (0: the autotuner chooses)")
     ap.add_argument("--no-forms", action="store_true", help="skip the batched/surrogate forms")
     ap.add_argument("--batch-steps", type=int, default=1000)
     ap.add_argument("--batch-loop-steps", type=int, default=10)

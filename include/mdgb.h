@@ -76,6 +76,8 @@ typedef struct md_config {
   int cluster_row_loads;   /* rows of the cluster kernel: 0 default / autotuned, 1 TMA tiles of
                               the block in shared memory (two in flight), 2 per-lane register
                               prefetch, 3 TMA tiles of each warp, 4 as 1 with three in flight */
+  int cluster_stage_cap;   /* staged atoms per segment of the cluster kernel (0: default /
+                              autotuned; otherwise 64 .. 11264) */
 } md_config;
 
 /* LJ kernel of the precision form.  ROWS: compact rows of packed atom

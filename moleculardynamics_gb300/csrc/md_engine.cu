@@ -920,6 +920,9 @@ md_status md_create(const md_config* cfg, md_ctx** out) {
   if (cfg->cluster_threads < 0 || cfg->cluster_threads > 224 || cfg->cluster_threads % 32)
     return MD_BAD_CONFIG;
   if (cfg->cluster_row_loads < 0 || cfg->cluster_row_loads > 4) return MD_BAD_CONFIG;
+  if (cfg->cluster_stage_cap != 0 &&
+      (cfg->cluster_stage_cap < 64 || cfg->cluster_stage_cap > kClusterMaxStaged))
+    return MD_BAD_CONFIG;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= cfg->device || cfg->device < 0)
     return MD_NO_DEVICE;
@@ -930,6 +933,7 @@ md_status md_create(const md_config* cfg, md_ctx** out) {
   if (cfg->cluster_cells > 0) c->cl.Z = cfg->cluster_cells;
   if (cfg->cluster_threads > 0) c->cl.block = cfg->cluster_threads;
   if (cfg->cluster_row_loads > 0) c->cl.row_loads = cfg->cluster_row_loads;
+  if (cfg->cluster_stage_cap > 0) c->cl.stage_cap = cfg->cluster_stage_cap;
   c->n = (int)n;
   c->sp = species_table(cfg->species);
   c->gear = gear_coef((double)cfg->dt);
@@ -1319,7 +1323,9 @@ md_status md_autotune(md_ctx* c, int evals, md_tune_result* out) {
   const bool fixed_threads = c->cfg.cluster_threads > 0;
   std::vector<int> threads = fixed_threads ? std::vector<int>{c->cl.block}
                                            : std::vector<int>{64, 96, 128, 160, 192};
-  const std::vector<int> caps = {1152, 1536, kClusterMaxStaged};
+  const std::vector<int> caps = c->cfg.cluster_stage_cap > 0
+                                    ? std::vector<int>{c->cfg.cluster_stage_cap}
+                                    : std::vector<int>{1152, 1536, kClusterMaxStaged};
   const std::vector<int> loads = c->cfg.cluster_row_loads > 0
                                      ? std::vector<int>{c->cfg.cluster_row_loads}
                                      : std::vector<int>{1, 2, 3, 4};

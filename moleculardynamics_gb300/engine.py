@@ -44,7 +44,7 @@ class MdConfig(C.Structure):
                 ("box", C.c_double), ("precision", C.c_int), ("species", C.c_int),
                 ("device", C.c_int), ("reference_energy", C.c_int), ("lj_kernel", C.c_int),
                 ("cluster_cells", C.c_int), ("cluster_threads", C.c_int),
-                ("cluster_row_loads", C.c_int)]
+                ("cluster_row_loads", C.c_int), ("cluster_stage_cap", C.c_int)]
 
 
 THERMO_FIELDS = ["time", "temperature", "e", "ek", "eu", "com_x", "com_y", "com_z",
@@ -215,11 +215,11 @@ def make_config(n_lj=0, n_mb=0, dt=2.0, timesteps=0, lj_rs=9.534, lj_rcut=8.5125
                 mb_rcut=3.0, use_lj=1, use_mb=0, output_timesteps=0, energy_loss=1.0,
                 periodic=0, box=0.0, precision=PREC_FP64, species=SPECIES_ARGON, device=0,
                 reference_energy=0, lj_kernel=0, cluster_cells=0,
-                cluster_threads=0, cluster_row_loads=0) -> MdConfig:
+                cluster_threads=0, cluster_row_loads=0, cluster_stage_cap=0) -> MdConfig:
     return MdConfig(n_lj, n_mb, dt, timesteps, lj_rs, lj_rcut, mb_rs, mb_rcut, use_lj, use_mb,
                     output_timesteps, energy_loss, periodic, box, precision, species, device,
                     reference_energy, lj_kernel, cluster_cells, cluster_threads,
-                    cluster_row_loads)
+                    cluster_row_loads, cluster_stage_cap)
 
 
 class Engine:

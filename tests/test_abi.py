@@ -80,7 +80,9 @@ def test_bad_configs_are_rejected(eng):
                 eng.make_config(n_lj=10, dt=0.0),
                 eng.make_config(n_lj=10, periodic=1, box=10.0),
                 eng.make_config(n_lj=10, precision=7),
-                eng.make_config(n_mb=10, use_lj=0, use_mb=1, mb_rs=3.0, mb_rcut=3.5)):
+                eng.make_config(n_mb=10, use_lj=0, use_mb=1, mb_rs=3.0, mb_rcut=3.5),
+                eng.make_config(n_lj=10, cluster_stage_cap=32),
+                eng.make_config(n_lj=10, cluster_stage_cap=20000)):
         assert lib.md_create(C.byref(cfg), C.byref(h)) == 1
 
 

@@ -79,11 +79,14 @@ def test_cluster_independent_of_tiling(eng):
     pos, vel, L = argon_fcc(12, noise=0.1)
     n = len(pos)
     ref = None
-    for cells, threads, loads in [(0, 0, 1), (1, 32, 2), (3, 224, 1), (64, 64, 2), (0, 0, 2),
-                                  (0, 0, 3), (2, 224, 3), (0, 32, 3), (0, 0, 4), (2, 224, 4),
-                                  (1, 32, 4)]:
+    for cells, threads, loads, cap in [(0, 0, 1, 0), (1, 32, 2, 0), (3, 224, 1, 0),
+                                       (64, 64, 2, 0), (0, 0, 2, 0), (0, 0, 3, 0),
+                                       (2, 224, 3, 0), (0, 32, 3, 0), (0, 0, 4, 0),
+                                       (2, 224, 4, 0), (1, 32, 4, 0), (0, 128, 1, 64),
+                                       (0, 96, 2, 1152)]:
         with _engine(eng, n, L, lj_kernel=eng.LJ_CLUSTER, cluster_cells=cells,
-                     cluster_threads=threads, cluster_row_loads=loads) as e:
+                     cluster_threads=threads, cluster_row_loads=loads,
+                     cluster_stage_cap=cap) as e:
             e.upload(pos, vel)
             e.begin(0.0)
             e.step(20)
