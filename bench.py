@@ -496,6 +496,7 @@ def run_gb300(args, rank, world):
     co_ms, co_n = e.kernel_time(eng.KERNEL_CORRECT)
     li_ms, li_n = e.kernel_time(eng.KERNEL_LIST)
     fu_ms, fu_n = e.kernel_time(eng.KERNEL_FUSED)
+    fc_ms, fc_n = e.kernel_time(eng.KERNEL_FUSED_CORRECT)
     s1 = e.stats()
     e.set_timing(False)
     t_max = dist.max(step_ms)
@@ -554,9 +555,11 @@ def run_gb300(args, rank, world):
             "lj_force": lj_ms / max(lj_n, 1), "predict": pr_ms / max(pr_n, 1),
             "correct": co_ms / max(co_n, 1),
             "fused_force_gear": fu_ms / max(fu_n, 1),
+            "fused_force_correct": fc_ms / max(fc_n, 1),
             "list_build_amortised": li_ms / md_steps},
         "kernel_launches": {"lj_force": lj_n, "predict": pr_n, "correct": co_n,
-                            "fused_force_gear": fu_n, "list_build": li_n},
+                            "fused_force_gear": fu_n, "fused_force_correct": fc_n,
+                            "list_build": li_n},
         "accuracy": {"energy_drift_eps_per_atom_per_1000_steps": drift},
     }
     peaks = measured_peaks()

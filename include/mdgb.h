@@ -166,7 +166,8 @@ md_status md_get_stats(const md_ctx* ctx, md_stats* out);
 /* Per-kernel device timing with CUDA events on the engine's stream.
  * kernel: 0 = LJ force, 1 = bond order, 2 = predict, 3 = correct, 4 = list build,
  * 5 = whole md_step calls (first launch to last), 6 = cluster force kernel with the
- * Gear correct + predict fused in (precision form, periodic). */
+ * Gear correct + predict fused in (precision form, periodic), 7 = the same kernel with
+ * the correct only (the steps before a list build, a record or the call's end). */
 md_status md_set_timing(md_ctx* ctx, int on);
 md_status md_kernel_time(const md_ctx* ctx, int kernel, double* total_ms, long long* launches);
 /* Autotuner of the cluster kernel (precision form, periodic): times `evals`

@@ -662,8 +662,10 @@ struct ClStep {
 
 // FP32 LJ force, persistent: each block takes segments from a shared
 // counter until none is left.  ev: E, E_shifted, W per segment (as md_forces.cu).
-// GEAR: the Gear correct of this step and predict of the next follow for each
-// atom in the same thread (cpu/common/Device.cpp:17-85 in FP64 with FMAs).
+// GEAR 1: the Gear correct of this step and predict of the next follow for each
+// atom in the same thread (cpu/common/Device.cpp:17-85 in FP64 with FMAs);
+// GEAR 2: the correct only (a list build, a record or the call's end follows),
+// forces also stored.
 // Dynamic shared memory: two row tiles [16][blockDim + 8] of uint16 (TMA
 // destinations), then the staged positions.
 // Row loads: ROWS 0, tiles of the whole block by TMA into shared memory
@@ -673,7 +675,7 @@ struct ClStep {
 constexpr int kWarpTileAtoms = 40;  // 32 atoms + up to 8 for the 16-byte start
 constexpr int kWarpTileBytes = kWarpTileAtoms * kClusterTileSlots * 2;
 
-template <bool ENERGY, bool ALL_NG, bool GEAR, int ROWS>
+template <bool ENERGY, bool ALL_NG, int GEAR, int ROWS>
 __global__ void __launch_bounds__(224, 3)
     k_lj_cl(const __grid_constant__ CUtensorMap rmap, const ClStep a) {
   extern __shared__ __align__(128) unsigned char dyn[];
@@ -693,7 +695,9 @@ __global__ void __launch_bounds__(224, 3)
   __shared__ int s_max[8];
   __shared__ int s_trip;
   if (tid == 0) {
-    s_trip = (a.skin[a.flag_read] | a.skin[3]) != 0;
+    // an energy evaluation follows a correct-only launch of the same step,
+    // which records a trip of the corrected positions in the next step's flag
+    s_trip = (a.skin[a.flag_read] | a.skin[3] | (ENERGY ? a.skin[a.flag_set] : 0)) != 0;
     for (int k = 0; k < 4; k++) mbar_init(&bar[k], 1);
     if (ROWS == 2)
       for (int w = 0; w < (int)(blockDim.x >> 5); w++) {
@@ -1110,11 +1114,12 @@ __global__ void __launch_bounds__(224, 3)
         ev[1] += (double)sh2 - (double)sl2;
         ev[2] += 0.5 * ((double)wh - (double)wl);
       }
-      if (!GEAR) {
+      if (GEAR != 1) {
         a.f3[3 * p] = f[0];
         a.f3[3 * p + 1] = f[1];
         a.f3[3 * p + 2] = f[2];
-      } else {
+      }
+      if (GEAR) {
         const md_double4 r = a.pos[p];
         const int type = ti;  // the staged copy carries the species as an integer
         GearAtom s;
@@ -1131,7 +1136,7 @@ __global__ void __launch_bounds__(224, 3)
         const double im = type == SP_N ? a.g.inv_mass[0]
                                        : (type == SP_O ? a.g.inv_mass[1] : a.g.inv_mass[2]);
         gear_correct_fma(s, f, im, a.g.k);
-        gear_predict_fma(s, a.g.k);
+        if (GEAR == 1) gear_predict_fma(s, a.g.k);
 #pragma unroll
         for (int d = 0; d < 3; d++) {
           a.g.vel[3 * p + d] = s.v[d];
@@ -1148,7 +1153,7 @@ __global__ void __launch_bounds__(224, 3)
         const float4 pf = make_float4(narrow_rn(s.r[0]), narrow_rn(s.r[1]), narrow_rn(s.r[2]),
                                       __int_as_float(type));
         // a non-finite force, velocity or derivative reaches the predicted
-        // position: one FP32 test covers the whole state
+        // (corrected) position: one FP32 test covers the whole state
         if (!(fabsf(pf.x) <= FLT_MAX && fabsf(pf.y) <= FLT_MAX && fabsf(pf.z) <= FLT_MAX))
           atomicOr(a.status, ST_NONFINITE);
         a.g.posf_next[p] = pf;
@@ -1430,24 +1435,30 @@ int cluster_build(ClusterList& cl, const std::vector<ClusterReplica>& reps_in, f
     allow_smem(k_cl_rows<0>);
     allow_smem(k_cl_rows<1>);
     allow_smem(k_cl_rows<2>);
-    allow_smem(k_lj_cl<false, false, false, 0>);
-    allow_smem(k_lj_cl<false, true, false, 0>);
-    allow_smem(k_lj_cl<true, false, false, 0>);
-    allow_smem(k_lj_cl<true, true, false, 0>);
-    allow_smem(k_lj_cl<false, false, true, 0>);
-    allow_smem(k_lj_cl<false, true, true, 0>);
-    allow_smem(k_lj_cl<false, false, false, 1>);
-    allow_smem(k_lj_cl<false, true, false, 1>);
-    allow_smem(k_lj_cl<true, false, false, 1>);
-    allow_smem(k_lj_cl<true, true, false, 1>);
-    allow_smem(k_lj_cl<false, false, true, 1>);
-    allow_smem(k_lj_cl<false, true, true, 1>);
-    allow_smem(k_lj_cl<false, false, false, 2>);
-    allow_smem(k_lj_cl<false, true, false, 2>);
-    allow_smem(k_lj_cl<true, false, false, 2>);
-    allow_smem(k_lj_cl<true, true, false, 2>);
-    allow_smem(k_lj_cl<false, false, true, 2>);
-    allow_smem(k_lj_cl<false, true, true, 2>);
+    allow_smem(k_lj_cl<false, false, 0, 0>);
+    allow_smem(k_lj_cl<false, true, 0, 0>);
+    allow_smem(k_lj_cl<true, false, 0, 0>);
+    allow_smem(k_lj_cl<true, true, 0, 0>);
+    allow_smem(k_lj_cl<false, false, 1, 0>);
+    allow_smem(k_lj_cl<false, true, 1, 0>);
+    allow_smem(k_lj_cl<false, false, 2, 0>);
+    allow_smem(k_lj_cl<false, true, 2, 0>);
+    allow_smem(k_lj_cl<false, false, 0, 1>);
+    allow_smem(k_lj_cl<false, true, 0, 1>);
+    allow_smem(k_lj_cl<true, false, 0, 1>);
+    allow_smem(k_lj_cl<true, true, 0, 1>);
+    allow_smem(k_lj_cl<false, false, 1, 1>);
+    allow_smem(k_lj_cl<false, true, 1, 1>);
+    allow_smem(k_lj_cl<false, false, 2, 1>);
+    allow_smem(k_lj_cl<false, true, 2, 1>);
+    allow_smem(k_lj_cl<false, false, 0, 2>);
+    allow_smem(k_lj_cl<false, true, 0, 2>);
+    allow_smem(k_lj_cl<true, false, 0, 2>);
+    allow_smem(k_lj_cl<true, true, 0, 2>);
+    allow_smem(k_lj_cl<false, false, 1, 2>);
+    allow_smem(k_lj_cl<false, true, 1, 2>);
+    allow_smem(k_lj_cl<false, false, 2, 2>);
+    allow_smem(k_lj_cl<false, true, 2, 2>);
     attrs = true;
   }
   const float margin = (float)(1e-6 * (reps.empty() ? 0.0 : reps.back().L + rv) + 1e-6);
@@ -1571,11 +1582,13 @@ void launch_lj_cluster(const ClusterForceArgs& f, bool energy, cudaStream_t st) 
   else                                           \
     MDGB_CL_LAUNCH2(E, A, G, 1, cl.rmap)
   if (energy) {
-    if (f.all_ng) { MDGB_CL_LAUNCH(true, true, false); } else { MDGB_CL_LAUNCH(true, false, false); }
+    if (f.all_ng) { MDGB_CL_LAUNCH(true, true, 0); } else { MDGB_CL_LAUNCH(true, false, 0); }
+  } else if (f.gear && f.gear->correct_only) {
+    if (f.all_ng) { MDGB_CL_LAUNCH(false, true, 2); } else { MDGB_CL_LAUNCH(false, false, 2); }
   } else if (f.gear) {
-    if (f.all_ng) { MDGB_CL_LAUNCH(false, true, true); } else { MDGB_CL_LAUNCH(false, false, true); }
+    if (f.all_ng) { MDGB_CL_LAUNCH(false, true, 1); } else { MDGB_CL_LAUNCH(false, false, 1); }
   } else {
-    if (f.all_ng) { MDGB_CL_LAUNCH(false, true, false); } else { MDGB_CL_LAUNCH(false, false, false); }
+    if (f.all_ng) { MDGB_CL_LAUNCH(false, true, 0); } else { MDGB_CL_LAUNCH(false, false, 0); }
   }
 #undef MDGB_CL_LAUNCH
 #undef MDGB_CL_LAUNCH2

@@ -117,13 +117,14 @@ struct ClusterGearArgs {
   GearCoef k;
   double inv_mass[3];
   float trip2;       // squared skin displacement (< 0: trip every step)
+  bool correct_only = false;  // stop after the correct (forces also go to f3)
 };
 
 struct ClusterForceArgs {
   const ClusterList* cl;
   const float4* posf;
   const md_double4* pos;
-  double* f3;        // forces out (unused when gear is set)
+  double* f3;        // forces out (unused when gear is set, unless correct_only)
   int step;          // MD step t of this evaluation (skin flag rotation)
   double rcutsq;
   Species sp;

@@ -67,7 +67,7 @@ int next_build(float maxnlmove, double vmax, double dt, int t) {
   return nb > 2147483647LL ? 2147483647 : (int)nb;
 }
 
-constexpr int kKernels = 7;  // timing ids of md_kernel_time
+constexpr int kKernels = 8;  // timing ids of md_kernel_time
 
 __global__ void k_begin(md_double4* pos, double* vel, int n, double half_box, int clamp,
                         double vxcm) {
@@ -117,9 +117,13 @@ struct md_ctx {
   std::vector<ClusterReplica> reps_in;
   int* rep_ranges = nullptr;    // device: (first atom, atoms) per replica
   double* rep_buf = nullptr;    // device: 3 energies + 16 record doubles per replica
-  // CUDA graph of a window of fused steps (replayed while nothing else is due)
+  // CUDA graphs of a window of fused steps (replayed while nothing else is
+  // due): two slots, since a correct-only step swaps the position buffers
+  // once and windows then start from either buffer order
   bool graphs = false;
-  cudaGraphExec_t gexec = nullptr;
+  cudaGraphExec_t gexec[2] = {nullptr, nullptr};
+  std::vector<unsigned char> gsig[2];
+  int glast = 0;  // slot replayed last
   // learned surrogate of the bond-order term (not owned): used while its
   // force error, measured by the exact kernel every sur_every steps, stays
   // within sur_threshold; otherwise the exact kernel computes the forces
@@ -129,7 +133,6 @@ struct md_ctx {
   bool sur_use = false;
   long long sur_steps = 0, sur_exact_steps = 0, sur_checks = 0, sur_rejects = 0;
   double *sur_fx = nullptr, *sur_fs = nullptr;  // check buffers (3 doubles per many-body atom)
-  std::vector<unsigned char> gsig;
   long long graph_windows = 0;
   // bond-order scratch
   uint32_t* mb_sl = nullptr;
@@ -158,8 +161,8 @@ struct md_ctx {
   std::vector<cudaEvent_t> ev_pool;
   std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> pending;
   std::vector<int> pending_weight;  // launches each pending interval stands for
-  double kt_ms[kKernels] = {0, 0, 0, 0, 0, 0, 0};
-  long long kt_n[kKernels] = {0, 0, 0, 0, 0, 0, 0};
+  double kt_ms[kKernels] = {};
+  long long kt_n[kKernels] = {};
 
   // animation frames (cpu/cpumd/Host.cpp:83,126,188-192): converted on the
   // device into one of two slots and streamed to pinned host blocks on
@@ -678,8 +681,10 @@ bool due(const md_ctx* c, int t) {
 }
 
 // Forces of step t, correct of step t and predict of step t + 1 in one
-// kernel (cluster path); the next positions go to the other buffer.
-void launch_fused(md_ctx* c) {
+// kernel (cluster path); the next positions go to the other buffer.  With
+// predict false the kernel stops after the correct and also stores the forces
+// in f3: the other buffer then holds the corrected state of step t.
+void launch_fused(md_ctx* c, bool predict = true) {
   GearArgs g = gear_args(c, c->t + 1);
   ClusterGearArgs cg;
   cg.pos_next = c->pos_alt;
@@ -691,7 +696,8 @@ void launch_fused(md_ctx* c) {
   cg.k = c->gear;
   for (int k = 0; k < 3; k++) cg.inv_mass[k] = g.inv_mass[k];
   cg.trip2 = g.trip2;
-  ClusterForceArgs a = cl_args(c, nullptr, nullptr);
+  cg.correct_only = !predict;
+  ClusterForceArgs a = cl_args(c, predict ? nullptr : c->f3, nullptr);
   a.gear = &cg;
   launch_lj_cluster(a, false, c->st);
 }
@@ -747,9 +753,13 @@ md_status run_window(md_ctx* c) {
   memcpy(sig.ptr, ptrs, sizeof(ptrs));
   memcpy(sig.rmap, &c->cl.rmap, sizeof(CUtensorMap));
   const unsigned char* sb = (const unsigned char*)&sig;
-  const bool same = c->gexec && c->gsig.size() == sizeof(sig) &&
-                    memcmp(c->gsig.data(), sb, sizeof(sig)) == 0;
-  if (!same) {
+  int slot = -1;
+  for (int k = 0; k < 2; k++)
+    if (c->gexec[k] && c->gsig[k].size() == sizeof(sig) &&
+        memcmp(c->gsig[k].data(), sb, sizeof(sig)) == 0)
+      slot = k;
+  if (slot < 0) {
+    slot = c->gexec[c->glast] ? 1 - c->glast : c->glast;  // the slot not replayed last
     // capture the window's launches (the host state is restored afterwards)
     const int t0 = c->t;
     const md_stats st0 = c->stats;
@@ -763,30 +773,33 @@ md_status run_window(md_ctx* c) {
     c->t = t0;
     c->stats = st0;  // kGraphSteps swaps: buffers are back in place
     if (e != cudaSuccess) return cuda_fail(c, e, "graph capture");
+    cudaGraphExec_t& x = c->gexec[slot];
     bool updated = false;
-    if (c->gexec) {
+    if (x) {
       cudaGraphExecUpdateResultInfo info;
-      updated = cudaGraphExecUpdate(c->gexec, g, &info) == cudaSuccess;
+      updated = cudaGraphExecUpdate(x, g, &info) == cudaSuccess;
       if (!updated) {
         cudaGetLastError();
-        cudaGraphExecDestroy(c->gexec);
-        c->gexec = nullptr;
+        cudaGraphExecDestroy(x);
+        x = nullptr;
       }
     }
     if (!updated) {
-      e = cudaGraphInstantiate(&c->gexec, g, 0);
+      e = cudaGraphInstantiate(&x, g, 0);
       if (e != cudaSuccess) {
         cudaGraphDestroy(g);
-        c->gexec = nullptr;
+        x = nullptr;
+        c->gsig[slot].clear();
         return cuda_fail(c, e, "graph instantiate");
       }
     }
     cudaGraphDestroy(g);
-    c->gsig.assign(sb, sb + sizeof(sig));
+    c->gsig[slot].assign(sb, sb + sizeof(sig));
   }
+  c->glast = slot;
   {
     Timed tm(c, 6, kGraphSteps);
-    CK(cudaGraphLaunch(c->gexec, c->st), "graph launch");
+    CK(cudaGraphLaunch(c->gexec[slot], c->st), "graph launch");
   }
   for (int u = 0; u < kGraphSteps; u++) advance_fused(c);
   c->graph_windows++;
@@ -823,20 +836,32 @@ md_status step_once(md_ctx* c, bool last) {
     advance_fused(c);
     return MD_OK;
   }
-  {
-    md_status fs = forces(c, c->f3, true);
-    if (fs != MD_OK) return fs;
-  }
-  if (c->walls()) CK(cudaMemsetAsync(c->wall_flag, 0, sizeof(int), c->st), "wall flag");
-  {
-    Timed tm(c, 3);
-    if (fuse) {
-      launch_correct_predict(gear_args(c, t + 1), c->st);
-      c->predicted = true;
-    } else {
-      launch_correct(gear_args(c, t), c->st);
+  if (c->cluster) {
+    // forces and correct of step t in one kernel, without the predict (a list
+    // build, a record, a frame, new velocities or the call's end follows)
+    {
+      Timed tm(c, 7);
+      launch_fused(c, false);
     }
+    std::swap(c->pos, c->pos_alt);
+    std::swap(c->posf, c->posf_alt);
     c->stats.launches++;
+  } else {
+    {
+      md_status fs = forces(c, c->f3, true);
+      if (fs != MD_OK) return fs;
+    }
+    if (c->walls()) CK(cudaMemsetAsync(c->wall_flag, 0, sizeof(int), c->st), "wall flag");
+    {
+      Timed tm(c, 3);
+      if (fuse) {
+        launch_correct_predict(gear_args(c, t + 1), c->st);
+        c->predicted = true;
+      } else {
+        launch_correct(gear_args(c, t), c->st);
+      }
+      c->stats.launches++;
+    }
   }
   if (c->walls()) {
     int flag = 0;
@@ -994,7 +1019,8 @@ void md_destroy(md_ctx* c) {
   list_free(c->lj);
   list_free(c->mb);
   cluster_free(c->cl);
-  if (c->gexec) cudaGraphExecDestroy(c->gexec);
+  for (cudaGraphExec_t x : c->gexec)
+    if (x) cudaGraphExecDestroy(x);
   void* ptrs[] = {c->inv, c->sur_fx, c->sur_fs, c->rep_ranges, c->rep_buf, c->io, c->pos_alt, c->posf_alt, c->pos, c->vel, c->acc, c->b, c->c, c->f3, c->f3_tmp, c->posf, c->mb_sl,
                   c->mb_slen, c->xsi, c->xsj, c->va, c->status, c->epart, c->dsc, c->rec,
                   c->sc.dpart, c->sc.umax, c->sc.counts, c->sc.block_sums};

@@ -27,7 +27,7 @@ PREC_FP64, PREC_MIXED = 0, 1
 LJ_AUTO, LJ_ROWS, LJ_CLUSTER = 0, 1, 2
 SPECIES_NEON, SPECIES_ARGON = 0, 1
 (KERNEL_LJ, KERNEL_MB, KERNEL_PREDICT, KERNEL_CORRECT, KERNEL_LIST, KERNEL_STEP,
- KERNEL_FUSED) = range(7)
+ KERNEL_FUSED, KERNEL_FUSED_CORRECT) = range(8)
 
 
 class EngineError(RuntimeError):
