@@ -453,6 +453,24 @@ md_status check_status(md_ctx* c) {
   return MD_OK;
 }
 
+// The cluster build put the state in its cell order: back to the caller's
+// numbering, and the row-list kernel takes over from here on.
+void leave_cluster(md_ctx* c) {
+  launch_unpermute((const double*)c->pos, (double*)c->pos_alt, c->cl.orig, c->n, 4, c->st);
+  std::swap(c->pos, c->pos_alt);
+  double** v3[5] = {&c->vel, &c->acc, &c->b, &c->c, &c->f3};
+  for (int k = 0; k < 5; k++)
+    if (*v3[k] && c->cl.v3_tmp[k]) {
+      launch_unpermute(*v3[k], c->cl.v3_tmp[k], c->cl.orig, c->n, 3, c->st);
+      std::swap(*v3[k], c->cl.v3_tmp[k]);
+    }
+  c->stats.launches += 6;
+  c->cluster = false;
+  c->graphs = false;
+  c->predicted = false;
+  c->stats.lj_cluster = 0;
+}
+
 // readyList + buildList for the lists due at step t (Host.cpp:143-152)
 md_status rebuild(md_ctx* c, int t) {
   Timed tm(c, 4);
@@ -486,21 +504,28 @@ md_status rebuild(md_ctx* c, int t) {
     int r = cluster_build(c->cl, reps, c->cfg.lj_rs, sqrt((double)c->lj_rcutsq), &c->pos, v3,
                           c->posf, c->sc, c->status, c->st, e);
     c->stats.launches += 17;
-    if (r != 0) {
-      if (r == -1) return fail(c, e.find("non-finite") != std::string::npos ? MD_NONFINITE : MD_BAD_CONFIG, e);
-      return cuda_fail(c, (cudaError_t)r, "LJ cluster build");
+    if (r == -1 && c->cfg.lj_kernel == MD_LJ_AUTO && !c->batch &&
+        e.find("shared-memory stage") != std::string::npos) {
+      // a neighbourhood too dense for the staged shared memory: the row-list
+      // kernel takes over (the state goes back to the caller's numbering)
+      leave_cluster(c);  // the row-list build below runs instead
+    } else {
+      if (r != 0) {
+        if (r == -1) return fail(c, e.find("non-finite") != std::string::npos ? MD_NONFINITE : MD_BAD_CONFIG, e);
+        return cuda_fail(c, (cudaError_t)r, "LJ cluster build");
+      }
+      c->lj_next = next_build(c->lj_maxnlmove, vmax, dt, t);
+      c->stats.list_builds++;
+      c->stats.lj_max_row = c->cl.maxlen;
+      c->stats.lj_nlargest = 0;
+      c->stats.lj_cells = c->cl.h_rep[0].G;
+      c->stats.lj_list_entries = c->cl.entries;
+      c->stats.lj_tma = 0;
+      c->stats.lj_cluster = 1;
+      c->stats.cluster_segments = c->cl.nseg;
+      c->stats.cluster_max_staged = c->cl.max_staged;
+      return MD_OK;
     }
-    c->lj_next = next_build(c->lj_maxnlmove, vmax, dt, t);
-    c->stats.list_builds++;
-    c->stats.lj_max_row = c->cl.maxlen;
-    c->stats.lj_nlargest = 0;
-    c->stats.lj_cells = c->cl.h_rep[0].G;
-    c->stats.lj_list_entries = c->cl.entries;
-    c->stats.lj_tma = 0;
-    c->stats.lj_cluster = 1;
-    c->stats.cluster_segments = c->cl.nseg;
-    c->stats.cluster_max_staged = c->cl.max_staged;
-    return MD_OK;
   }
   if (c->cfg.use_lj && (c->lj_next == t || both)) {
     if (c->lj.skin) {

@@ -221,3 +221,39 @@ def test_autotune_keeps_forces(eng):
     assert r["candidates"] >= 1 and r["threads"] in (64, 96, 128, 160, 192)
     assert r["row_loads"] in (1, 2, 3, 4)
     assert np.array_equal(f0, f1)
+
+
+def test_dense_neighbourhood_falls_back_to_rows(eng):
+    """12,167 argon atoms 1.2 A apart in a 27.6 A box (one cell with minimum
+    images): more atoms than a segment can stage.  AUTO hands the system to the
+    row-list kernel (the state is mapped back to the caller's numbering) and
+    runs as LJ_ROWS does, bit for bit; LJ_CLUSTER reports the limit."""
+    m, a = 23, 1.2
+    L = m * a
+    g = (np.arange(m) + 0.5) * a - L / 2
+    x, y, z = np.meshgrid(g, g, g, indexing="ij")
+    n = m ** 3
+    rng = np.random.default_rng(3)
+    pos = np.zeros((n, 4))
+    pos[:, 0], pos[:, 1], pos[:, 2] = x.ravel(), y.ravel(), z.ravel()
+    pos[:, :3] += rng.uniform(-0.01, 0.01, (n, 3))
+    pos[:, 3] = 2
+    vel = rng.normal(0.0, 1e-4, (n, 3))
+    out = {}
+    for k in (eng.LJ_ROWS, eng.LJ_AUTO):
+        with _engine(eng, n, L, lj_kernel=k, dt=0.01) as e:
+            e.upload(pos, vel)
+            e.begin(0.0)
+            f0 = e.compute_forces()[0]
+            e.step(4)
+            p, v = e.download()
+            st = e.stats()
+        assert st["lj_cluster"] == 0
+        assert np.isfinite(p).all() and np.isfinite(f0).all()
+        out[k] = (f0, p, v)
+    for a_, b_ in zip(out[eng.LJ_ROWS], out[eng.LJ_AUTO]):
+        assert np.array_equal(a_, b_)
+    with _engine(eng, n, L, lj_kernel=eng.LJ_CLUSTER, dt=0.01) as e:
+        e.upload(pos, vel)
+        with pytest.raises(eng.EngineError, match="shared-memory stage"):
+            e.begin(0.0)
