@@ -463,6 +463,8 @@ __device__ __forceinline__ void put_sentinel(float4* st, int staged) {
   if (threadIdx.x == 0) st[staged] = make_float4(1e18f, 1e18f, 1e18f, __int_as_float(SP_NG));
 }
 
+constexpr int kRowStep = 8;  // staged candidates tested per step of the row walk
+
 // 4. compact rows from the build-time positions (MODE 0: count, 1: write,
 // 2: both, rows longer than cap truncated and reported through the counters)
 template <int MODE>
@@ -487,8 +489,8 @@ __global__ void __launch_bounds__(256)
     const bool live = p < sh.S.p1;
     int kept = 0;
     if (live && !minimg) {
-      // the 9 column groups in row order, four independent distance tests
-      // per step; only the centre group holds the atom itself
+      // the 9 column groups in row order, kRowStep independent distance
+      // tests per step; only the centre group holds the atom itself
       const int self = self_offset(sh, p);
       const float4 pi = st[self];
       const int zspan = sh.S.cz1 - sh.S.cz0 + 3;
@@ -509,18 +511,13 @@ __global__ void __launch_bounds__(256)
       auto group = [&](int g, auto centre) {
         const int qa = sh.off[g][u], qb = sh.off[g][u + 3];
         int q = qa;
-        for (; q + 4 <= qb; q += 4) {
-          bool i0 = near(q), i1 = near(q + 1), i2 = near(q + 2), i3 = near(q + 3);
-          if (decltype(centre)::value) {
-            i0 = i0 && q != self;
-            i1 = i1 && q + 1 != self;
-            i2 = i2 && q + 2 != self;
-            i3 = i3 && q + 3 != self;
-          }
-          take(q, i0);
-          take(q + 1, i1);
-          take(q + 2, i2);
-          take(q + 3, i3);
+        for (; q + kRowStep <= qb; q += kRowStep) {
+          bool in[kRowStep];
+#pragma unroll
+          for (int u = 0; u < kRowStep; u++)
+            in[u] = near(q + u) && (!decltype(centre)::value || q + u != self);
+#pragma unroll
+          for (int u = 0; u < kRowStep; u++) take(q + u, in[u]);
         }
         for (; q < qb; q++) take(q, near(q) && (!decltype(centre)::value || q != self));
       };
