@@ -196,26 +196,6 @@ __global__ void __launch_bounds__(128)
   }
 }
 
-// offsets d_j = r_j - r_i (FP32) of i's neighbours
-__device__ __forceinline__ int load_nbrs(int i, const md_double4* pos, const uint32_t* sl,
-                                         const int* slen, double box, float3* d, float* r,
-                                         int* idx) {
-  const md_double4 pi = pos[i];
-  const int S = slen[i];
-  for (int s = 0; s < S; s++) {
-    const uint32_t e = sl[(size_t)i * kSgMax + s];
-    const int j = entry_index(e);
-    const md_double4 pj = pos[j];
-    const double dx = pj.x + entry_img(e, 0) * box - pi.x;
-    const double dy = pj.y + entry_img(e, 1) * box - pi.y;
-    const double dz = pj.z + entry_img(e, 2) * box - pi.z;
-    d[s] = make_float3((float)dx, (float)dy, (float)dz);
-    r[s] = sqrtf(d[s].x * d[s].x + d[s].y * d[s].y + d[s].z * d[s].z);
-    idx[s] = j;
-  }
-  return S;
-}
-
 // ---- warp-per-atom descriptor and force kernels (4 atoms per block) ----
 struct NbrSm {
   float dx[kSgMax], dy[kSgMax], dz[kSgMax], r[kSgMax], fc[kSgMax], dfc[kSgMax];
