@@ -17,6 +17,7 @@
 //           loops over j of i's short list that lie in k's candidate row and
 //           adds k's third-body force (BondOrderFuncs.h:148-237, 339-393).
 // Lane sums are combined with warp shuffles.
+#include <type_traits>
 #include <cmath>
 
 #include "md_forces.h"
@@ -520,6 +521,8 @@ __global__ void __launch_bounds__(128)
   const int warps = blockDim.x >> 5;
   const int i = blockIdx.x * warps + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
+  // FP32: the angle derivatives in a shorter, algebraically equal form
+  constexpr bool kFast = std::is_same<T, float>::value;
   double ev[2] = {0.0, 0.0};
   if (i < n) {
     T xi, yi, zi;
@@ -559,6 +562,7 @@ __global__ void __launch_bounds__(128)
         // BondOrderFuncs.h:12-143 bondOrder1
         const T drijx = fdiv<T>(ijx, rij), drijy = fdiv<T>(ijy, rij), drijz = fdiv<T>(ijz, rij);
         const T E = md_exp((T)MD_LAMDA3 * (rij - re));
+        const T inv_rij = fdiv<T>(1.0f, rij), half_inv_rij = 0.5f * inv_rij;
         T xsi = 0, xsj = 0;
         T dxsix = 0, dxsiy = 0, dxsiz = 0, dxsjx = 0, dxsjy = 0, dxsjz = 0;
         for (int m = 0; m < S; m++) {
@@ -577,7 +581,22 @@ __global__ void __launch_bounds__(128)
           cutoff<T>(rim, fci, dfci);
           cutoff<T>(rjm, fcj, dfcj);
           const T drimx = fdiv<T>(imx, rim), drimy = fdiv<T>(imy, rim), drimz = fdiv<T>(imz, rim);
-          if (fci > 0) {
+          if (kFast && fci > 0) {
+            // d cos / d r_i = drij (1/rim - cos/rij) + drim (1/rij - cos/rim):
+            // the reference's quotient below, two scalars per triplet
+            const T inv_rim = fdiv<T>(1.0f, rim);
+            const T num2 = rij * rij + rim * rim - rjm * rjm;
+            const T icos = num2 * half_inv_rij * inv_rim;
+            T gth, gpre;
+            angular<T>(icos, gth, gpre);
+            xsi += fci * gth * E;
+            const T fE = fci * E;
+            const T cm = dfci * gth * E + fE * gpre * (inv_rij - icos * inv_rim);
+            const T cj = fE * (gpre * (inv_rim - icos * inv_rij) + gth * (T)MD_LAMDA3);
+            dxsix = fma(drimx, cm, fma(drijx, cj, dxsix));
+            dxsiy = fma(drimy, cm, fma(drijy, cj, dxsiy));
+            dxsiz = fma(drimz, cm, fma(drijz, cj, dxsiz));
+          } else if (fci > 0) {
             const T num2 = rij * rij + rim * rim - rjm * rjm;
             const T icos = fdiv<T>(num2, 2.0f * rij * rim);
             T gth, gpre;
@@ -594,7 +613,21 @@ __global__ void __launch_bounds__(128)
             dxsiy += dfci * drimy * gth * E + fci * (gpre * dcy) * E + fci * gth * MD_LAMDA3 * E * drijy;
             dxsiz += dfci * drimz * gth * E + fci * (gpre * dcz) * E + fci * gth * MD_LAMDA3 * E * drijz;
           }
-          if (fcj > 0) {
+          if (kFast && fcj > 0) {
+            // d cos / d r_i = drij (1/rjm - cos/rij) - drim rim / (rij rjm)
+            const T inv_rjm = fdiv<T>(1.0f, rjm);
+            const T num2 = rij * rij + rjm * rjm - rim * rim;
+            const T jcos = num2 * half_inv_rij * inv_rjm;
+            T gth, gpre;
+            angular<T>(jcos, gth, gpre);
+            xsj += fcj * gth * E;
+            const T fE = fcj * E;
+            const T cj = fE * (gpre * (inv_rjm - jcos * inv_rij) + (T)MD_LAMDA3 * gth);
+            const T cm = -fE * gpre * rim * inv_rij * inv_rjm;
+            dxsjx = fma(drijx, cj, fma(drimx, cm, dxsjx));
+            dxsjy = fma(drijy, cj, fma(drimy, cm, dxsjy));
+            dxsjz = fma(drijz, cj, fma(drimz, cm, dxsjz));
+          } else if (fcj > 0) {
             const T num2 = rij * rij + rjm * rjm - rim * rim;
             const T jcos = fdiv<T>(num2, 2.0f * rij * rjm);
             T gth, gpre;
@@ -669,6 +702,8 @@ __global__ void __launch_bounds__(128)
   const int warps = blockDim.x >> 5;
   const int k = blockIdx.x * warps + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
+  // FP32: the angle derivatives in a shorter, algebraically equal form
+  constexpr bool kFast = std::is_same<T, float>::value;
   double ev[1] = {0.0};
   if (k < n) {
     T xk, yk, zk;
@@ -691,6 +726,7 @@ __global__ void __launch_bounds__(128)
       T fci, dfci;
       cutoff<T>(rik, fci, dfci);
       const T drikx = fdiv<T>(ikx, rik), driky = fdiv<T>(iky, rik), drikz = fdiv<T>(ikz, rik);
+      const T inv_rik = fdiv<T>(1.0f, rik);
       const int Si = slen[ip];
       for (int sj = 0; sj < Si; sj++) {
         const size_t q = (size_t)sj * n + ip;
@@ -736,8 +772,23 @@ __global__ void __launch_bounds__(128)
         T fcj, dfcj;
         cutoff<T>(rjk, fcj, dfcj);
         const T E = md_exp((T)MD_LAMDA3 * (rij - re));
+        const T half_inv_rij = fdiv<T>(0.5f, rij), inv_rij = 2.0f * half_inv_rij;
+        const T inv_rjk = fdiv<T>(1.0f, rjk);
         T dbx = 0, dby = 0, dbz = 0;
-        if (fci > 0) {
+        if (kFast && fci > 0) {
+          // d cos / d r_k = drik (1/rij - cos/rik) - drjk rjk / (rij rik)
+          const T num2 = rij * rij + rik * rik - rjk * rjk;
+          const T icos = num2 * half_inv_rij * inv_rik;
+          T gth, gpre;
+          angular<T>(icos, gth, gpre);
+          const T p = fdiv<T>(1.0f, (1.0f + xs_i) * (1.0f + xs_i));
+          const T pE = 0.5f * p * E;
+          const T ck = pE * (dfci * gth + fci * gpre * (inv_rij - icos * inv_rik));
+          const T cj = -pE * fci * gpre * rjk * inv_rij * inv_rik;
+          dbx = fma(drikx, ck, fma(drjkx, cj, dbx));
+          dby = fma(driky, ck, fma(drjky, cj, dby));
+          dbz = fma(drikz, ck, fma(drjkz, cj, dbz));
+        } else if (fci > 0) {
           const T num2 = rij * rij + rik * rik - rjk * rjk;
           const T icos = fdiv<T>(num2, 2.0f * rij * rik);
           T gth, gpre;
@@ -751,7 +802,20 @@ __global__ void __launch_bounds__(128)
           dby += 0.5f * (p * (dfci * driky * gth * E + fci * (gpre * dcy) * E));
           dbz += 0.5f * (p * (dfci * drikz * gth * E + fci * (gpre * dcz) * E));
         }
-        if (fcj > 0) {
+        if (kFast && fcj > 0) {
+          // d cos / d r_k = drjk (1/rij - cos/rjk) - drik rik / (rij rjk)
+          const T num2 = rij * rij + rjk * rjk - rik * rik;
+          const T jcos = num2 * half_inv_rij * inv_rjk;
+          T gth, gpre;
+          angular<T>(jcos, gth, gpre);
+          const T p = fdiv<T>(1.0f, (1.0f + xs_j) * (1.0f + xs_j));
+          const T pE = 0.5f * p * E;
+          const T cj = pE * (dfcj * gth + fcj * gpre * (inv_rij - jcos * inv_rjk));
+          const T ck = -pE * fcj * gpre * rik * inv_rij * inv_rjk;
+          dbx = fma(drjkx, cj, fma(drikx, ck, dbx));
+          dby = fma(drjky, cj, fma(driky, ck, dby));
+          dbz = fma(drjkz, cj, fma(drikz, ck, dbz));
+        } else if (fcj > 0) {
           const T num2 = rij * rij + rjk * rjk - rik * rik;
           const T jcos = fdiv<T>(num2, 2.0f * rij * rjk);
           T gth, gpre;
