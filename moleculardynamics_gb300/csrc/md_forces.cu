@@ -476,8 +476,11 @@ __global__ void __launch_bounds__(128)
     k_mb_short(const md_double4* __restrict__ pos, const float4* __restrict__ posf, int n,
                int ld, const uint32_t* __restrict__ list, const int* __restrict__ len, Grid g,
                double rcutsq, uint32_t* __restrict__ sl, int* __restrict__ slen) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+  // one warp per atom, lanes over its row: the kept entries in row order
+  // (ballot prefix), 32 candidates tested at a time
+  const int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (i >= n) return;  // whole warp
   T xi, yi, zi;
   int ti;
   PosT<T>::load(pos, posf, i, xi, yi, zi, ti);
@@ -485,30 +488,37 @@ __global__ void __launch_bounds__(128)
   const T band = (T)1e-5 * rc2;
   int cnt = 0;
   const int L = len[i];
-  for (int k = 0; k < L; k++) {
-    const uint32_t e = list[(size_t)k * ld + i];
-    const int j = entry_index(e);
-    T xj, yj, zj;
-    int tj;
-    PosT<T>::load(pos, posf, j, xj, yj, zj, tj);
-    PosT<T>::image(xj, yj, zj, e, g);
-    T r2;
-    if (sizeof(T) == 8)
-      r2 = (T)norm2_exact((double)(xi - xj), (double)(yi - yj), (double)(zi - zj));
-    else
-      r2 = (xi - xj) * (xi - xj) + (yi - yj) * (yi - yj) + (zi - zj) * (zi - zj);
-    bool keep = r2 < rc2;
-    if (sizeof(T) == 4 && r2 > rc2 - band && r2 < rc2 + band) {
-      double a[3], b[3];
-      int t0;
-      PosT<double>::load(pos, posf, i, a[0], a[1], a[2], t0);
-      PosT<double>::load(pos, posf, j, b[0], b[1], b[2], t0);
-      PosT<double>::image(b[0], b[1], b[2], e, g);
-      keep = norm2_exact(xsub(a[0], b[0]), xsub(a[1], b[1]), xsub(a[2], b[2])) < rcutsq;
+  for (int k0 = 0; k0 < L; k0 += 32) {
+    const int k = k0 + lane;
+    bool keep = false;
+    uint32_t e = 0;
+    if (k < L) {
+      e = list[(size_t)k * ld + i];
+      const int j = entry_index(e);
+      T xj, yj, zj;
+      int tj;
+      PosT<T>::load(pos, posf, j, xj, yj, zj, tj);
+      PosT<T>::image(xj, yj, zj, e, g);
+      T r2;
+      if (sizeof(T) == 8)
+        r2 = (T)norm2_exact((double)(xi - xj), (double)(yi - yj), (double)(zi - zj));
+      else
+        r2 = (xi - xj) * (xi - xj) + (yi - yj) * (yi - yj) + (zi - zj) * (zi - zj);
+      keep = r2 < rc2;
+      if (sizeof(T) == 4 && r2 > rc2 - band && r2 < rc2 + band) {
+        double a[3], b[3];
+        int t0;
+        PosT<double>::load(pos, posf, i, a[0], a[1], a[2], t0);
+        PosT<double>::load(pos, posf, j, b[0], b[1], b[2], t0);
+        PosT<double>::image(b[0], b[1], b[2], e, g);
+        keep = norm2_exact(xsub(a[0], b[0]), xsub(a[1], b[1]), xsub(a[2], b[2])) < rcutsq;
+      }
     }
-    if (keep) sl[(size_t)(cnt++) * n + i] = e;
+    const unsigned mask = __ballot_sync(0xffffffffu, keep);
+    if (keep) sl[(size_t)(cnt + __popc(mask & ((1u << lane) - 1u))) * n + i] = e;
+    cnt += __popc(mask);
   }
-  slen[i] = cnt;
+  if (lane == 0) slen[i] = cnt;
 }
 
 template <typename T, bool ENERGY>
@@ -897,8 +907,8 @@ int mb_blocks(int n) { return nblk(n, 4); }
 template <typename T>
 static void launch_mb_t(const MbArgs& a, bool energy, cudaStream_t st) {
   if (a.n <= 0) return;
-  k_mb_short<T><<<nblk(a.n, 128), 128, 0, st>>>(a.pos, a.posf, a.n, a.ld, a.list, a.len, a.grid,
-                                                a.rcutsq, a.sl, a.slen);
+  k_mb_short<T><<<nblk(a.n, 4), 128, 0, st>>>(a.pos, a.posf, a.n, a.ld, a.list, a.len, a.grid,
+                                              a.rcutsq, a.sl, a.slen);
   const int B = nblk(a.n, 4);
   T* xsi = (T*)a.xsi;
   T* xsj = (T*)a.xsj;

@@ -150,46 +150,71 @@ __global__ void __launch_bounds__(128)
   const float boxf = (float)w.g.box;
   const int cx = w.cell3[3 * i], cy = w.cell3[3 * i + 1], cz = w.cell3[3 * i + 2];
   const int cells = w.g.cells;
-  int cnt = 0;
-  for (int dx = -1; dx < 2; dx++)
-    for (int dy = -1; dy < 2; dy++)
-      for (int dz = -1; dz < 2; dz++) {
-        int nc[3] = {cx + dx, cy + dy, cz + dz};
-        int im[3] = {0, 0, 0};
-        bool out = false;
+  // lane c < 27 looks up cell c of the 27 (dx slowest, dz fastest) with its image
+  int cs = 0, cn = 0, im[3] = {0, 0, 0};
+  if (lane < 27) {
+    int nc[3] = {cx + lane / 9 - 1, cy + (lane / 3) % 3 - 1, cz + lane % 3 - 1};
+    bool out = false;
 #pragma unroll
-        for (int d = 0; d < 3; d++) {
-          if (!w.g.periodic) {
-            if (nc[d] >= cells || nc[d] < 0) out = true;
-          } else {
-            if (nc[d] < 0) { nc[d] += cells; im[d] = -1; }
-            if (nc[d] >= cells) { nc[d] -= cells; im[d] = 1; }
-          }
-        }
-        if (out) continue;
-        const int slot = table_find(w.keys, w.cap, cell_key(nc[0], nc[1], nc[2]));
-        if (slot < 0) continue;
-        const int a = w.start[slot], b = a + w.count[slot];
-        for (int q0 = a; q0 < b; q0 += 32) {
-          const int q = q0 + lane;
-          bool keep = false;
-          int m = 0;
-          if (q < b) {
-            m = w.sorted[q];
-            if (m != i) {
-              const float4 pm = pos[m];
-              const float ddx = fmaf((float)im[0], boxf, pm.x) - pi.x;
-              const float ddy = fmaf((float)im[1], boxf, pm.y) - pi.y;
-              const float ddz = fmaf((float)im[2], boxf, pm.z) - pi.z;
-              keep = ddx * ddx + ddy * ddy + ddz * ddz < rc2;
-            }
-          }
-          const unsigned mask = __ballot_sync(0xffffffffu, keep);
-          const int at = cnt + __popc(mask & ((1u << lane) - 1u));
-          if (keep && at < kSgMax) sl[(size_t)i * kSgMax + at] = pack_entry(m, im[0], im[1], im[2]);
-          cnt += __popc(mask);
-        }
+    for (int d = 0; d < 3; d++) {
+      if (!w.g.periodic) {
+        if (nc[d] >= cells || nc[d] < 0) out = true;
+      } else {
+        if (nc[d] < 0) { nc[d] += cells; im[d] = -1; }
+        if (nc[d] >= cells) { nc[d] -= cells; im[d] = 1; }
       }
+    }
+    if (!out) {
+      const int slot = table_find(w.keys, w.cap, cell_key(nc[0], nc[1], nc[2]));
+      if (slot >= 0) {
+        cs = w.start[slot];
+        cn = w.count[slot];
+      }
+    }
+  }
+  // the cells' atoms as one list in cell order: inclusive prefix of the counts
+  int incl = cn;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int t = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += t;
+  }
+  const int total = __shfl_sync(0xffffffffu, incl, 31);
+  const int excl = incl - cn;
+  int cnt = 0;
+  for (int v0 = 0; v0 < total; v0 += 32) {
+    const int v = v0 + lane;
+    // cell of candidate v: the first c with incl_c > v (27 cells: five halvings)
+    int lo = 0, hi = 26;
+#pragma unroll
+    for (int it = 0; it < 5; it++) {
+      const int mid = (lo + hi) >> 1;
+      if (__shfl_sync(0xffffffffu, incl, mid) > v)
+        hi = mid;
+      else
+        lo = mid + 1;
+    }
+    const int c = min(lo, 26);
+    const int base = __shfl_sync(0xffffffffu, cs, c) - __shfl_sync(0xffffffffu, excl, c);
+    const int ix = __shfl_sync(0xffffffffu, im[0], c), iy = __shfl_sync(0xffffffffu, im[1], c),
+              iz = __shfl_sync(0xffffffffu, im[2], c);
+    bool keep = false;
+    int m = 0;
+    if (v < total) {
+      m = w.sorted[base + v];
+      if (m != i) {
+        const float4 pm = pos[m];
+        const float ddx = fmaf((float)ix, boxf, pm.x) - pi.x;
+        const float ddy = fmaf((float)iy, boxf, pm.y) - pi.y;
+        const float ddz = fmaf((float)iz, boxf, pm.z) - pi.z;
+        keep = ddx * ddx + ddy * ddy + ddz * ddz < rc2;
+      }
+    }
+    const unsigned mask = __ballot_sync(0xffffffffu, keep);
+    const int at = cnt + __popc(mask & ((1u << lane) - 1u));
+    if (keep && at < kSgMax) sl[(size_t)i * kSgMax + at] = pack_entry(m, ix, iy, iz);
+    cnt += __popc(mask);
+  }
   if (lane == 0) {
     if (cnt > kSgMax) atomicOr(status, ST_CELL_OVERFLOW);
     slen[i] = cnt < kSgMax ? cnt : kSgMax;
