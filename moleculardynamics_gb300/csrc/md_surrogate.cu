@@ -135,8 +135,8 @@ __device__ __forceinline__ void ang_pair(float c, float q, const DescParams& P, 
 
 // neighbours of i within rc (from the bond-order candidate rows: the 27
 // build-time cells around i, as walk_row visits them), as packed entries
-// with their periodic image; one warp per atom, lanes over a cell's atoms,
-// kept entries compacted in candidate order with a ballot
+// with their periodic image; one warp per atom, lanes over the cells' atoms
+// joined into one list, kept entries compacted in candidate order with a ballot
 // (distances in FP32 from an FP32 copy of the positions: a neighbour at the
 // cutoff enters the descriptors with weight fc(rc) = 0 either way)
 __global__ void __launch_bounds__(128)
@@ -223,7 +223,7 @@ __global__ void __launch_bounds__(128)
 
 // ---- warp-per-atom descriptor and force kernels (4 atoms per block) ----
 struct NbrSm {
-  float dx[kSgMax], dy[kSgMax], dz[kSgMax], r[kSgMax], fc[kSgMax], dfc[kSgMax];
+  float dx[kSgMax], dy[kSgMax], dz[kSgMax], r[kSgMax], ir[kSgMax], fc[kSgMax], dfc[kSgMax];
   int idx[kSgMax];
 };
 
@@ -248,6 +248,7 @@ __device__ __forceinline__ int warp_load_nbrs(int i, const md_double4* pos, cons
     N.dy[s] = dy;
     N.dz[s] = dz;
     N.r[s] = r;
+    N.ir[s] = 1.f / r;  // the pair terms multiply by it instead of dividing
     N.fc[s] = fc;
     N.dfc[s] = dfc;
     N.idx[s] = j;
@@ -325,7 +326,7 @@ __global__ void __launch_bounds__(128)
   for (int k = lane; k < npair; k += 32) {
     int a, b;
     pair_of(k, S, a, b);
-    const float c = (N.dx[a] * N.dx[b] + N.dy[a] * N.dy[b] + N.dz[a] * N.dz[b]) / (N.r[a] * N.r[b]);
+    const float c = (N.dx[a] * N.dx[b] + N.dy[a] * N.dy[b] + N.dz[a] * N.dz[b]) * (N.ir[a] * N.ir[b]);
     const float q = N.r[a] * N.r[a] + N.r[b] * N.r[b];
     const float ff = N.fc[a] * N.fc[b];
     AngPair T;
@@ -373,7 +374,7 @@ __global__ void __launch_bounds__(128)
       const float t = N.r[s] - P.rs[k];
       sum += g[k] * __expf(-P.eta_r * t * t) * (-2.f * P.eta_r * t * N.fc[s] + N.dfc[s]);
     }
-    const float ir = 1.f / N.r[s];
+    const float ir = N.ir[s];
     const float gx = sum * N.dx[s] * ir, gy = sum * N.dy[s] * ir, gz = sum * N.dz[s] * ir;
     // dG/dr_j = +grad, dG/dr_i = -grad; F = -dE/dr
     fn[warp][0][s] -= gx;
@@ -389,8 +390,9 @@ __global__ void __launch_bounds__(128)
   for (int k = lane; k < npair; k += 32) {
     int a, b;
     pair_of_diag(k, S, a, b);
-    const float ra = N.r[a], rb = N.r[b], rab = ra * rb;
-    const float c = (N.dx[a] * N.dx[b] + N.dy[a] * N.dy[b] + N.dz[a] * N.dz[b]) / rab;
+    const float ra = N.r[a], rb = N.r[b];
+    const float ia = N.ir[a], ib = N.ir[b], irab = ia * ib;
+    const float c = (N.dx[a] * N.dx[b] + N.dy[a] * N.dy[b] + N.dz[a] * N.dz[b]) * irab;
     const float q = ra * ra + rb * rb;
     const float fca = N.fc[a], fcb = N.fc[b], dfa = N.dfc[a], dfb = N.dfc[b];
     AngPair T;
@@ -421,14 +423,13 @@ __global__ void __launch_bounds__(128)
     A *= fca * fcb;
     Ba *= fcb;
     Bb *= fca;
-    const float ia = 1.f / ra, ib = 1.f / rb;
     // dc/dd_a = d_b / (ra rb) - c d_a / ra^2
-    const float gax = A * (N.dx[b] / rab - c * N.dx[a] * ia * ia) + Ba * N.dx[a] * ia;
-    const float gay = A * (N.dy[b] / rab - c * N.dy[a] * ia * ia) + Ba * N.dy[a] * ia;
-    const float gaz = A * (N.dz[b] / rab - c * N.dz[a] * ia * ia) + Ba * N.dz[a] * ia;
-    const float gbx = A * (N.dx[a] / rab - c * N.dx[b] * ib * ib) + Bb * N.dx[b] * ib;
-    const float gby = A * (N.dy[a] / rab - c * N.dy[b] * ib * ib) + Bb * N.dy[b] * ib;
-    const float gbz = A * (N.dz[a] / rab - c * N.dz[b] * ib * ib) + Bb * N.dz[b] * ib;
+    const float gax = A * (N.dx[b] * irab - c * N.dx[a] * ia * ia) + Ba * N.dx[a] * ia;
+    const float gay = A * (N.dy[b] * irab - c * N.dy[a] * ia * ia) + Ba * N.dy[a] * ia;
+    const float gaz = A * (N.dz[b] * irab - c * N.dz[a] * ia * ia) + Ba * N.dz[a] * ia;
+    const float gbx = A * (N.dx[a] * irab - c * N.dx[b] * ib * ib) + Bb * N.dx[b] * ib;
+    const float gby = A * (N.dy[a] * irab - c * N.dy[b] * ib * ib) + Bb * N.dy[b] * ib;
+    const float gbz = A * (N.dz[a] * irab - c * N.dz[b] * ib * ib) + Bb * N.dz[b] * ib;
     atomicAdd(&fn[warp][0][a], -gax);
     atomicAdd(&fn[warp][1][a], -gay);
     atomicAdd(&fn[warp][2][a], -gaz);
@@ -823,7 +824,7 @@ __global__ void __launch_bounds__(128)
     dex[warp][s] = ex;
     dey[warp][s] = ey;
     dez[warp][s] = ez;
-    const float ud = (N.dx[s] * ex + N.dy[s] * ey + N.dz[s] * ez) / N.r[s];  // u . de
+    const float ud = (N.dx[s] * ex + N.dy[s] * ey + N.dz[s] * ez) * N.ir[s];  // u . de
 #pragma unroll
     for (int k = 0; k < kRad; k++) {
       const float t = N.r[s] - P.rs[k];
@@ -835,18 +836,18 @@ __global__ void __launch_bounds__(128)
   for (int k = lane; k < npair; k += 32) {
     int a, b;
     pair_of(k, S, a, b);
-    const float ra = N.r[a], rb = N.r[b], rab = ra * rb;
-    const float ia = 1.f / ra, ib = 1.f / rb;
+    const float ra = N.r[a], rb = N.r[b];
+    const float ia = N.ir[a], ib = N.ir[b], irab = ia * ib;
     const float dax = N.dx[a], day = N.dy[a], daz = N.dz[a];
     const float dbx = N.dx[b], dby = N.dy[b], dbz = N.dz[b];
     const float eax = dex[warp][a], eay = dey[warp][a], eaz = dez[warp][a];
     const float ebx = dex[warp][b], eby = dey[warp][b], ebz = dez[warp][b];
-    const float c = (dax * dbx + day * dby + daz * dbz) / rab;
+    const float c = (dax * dbx + day * dby + daz * dbz) * irab;
     const float q2 = ra * ra + rb * rb;
     const float pa = dax * eax + day * eay + daz * eaz;  // d_a . de_a
     const float pb = dbx * ebx + dby * eby + dbz * ebz;
-    const float dca = (dbx * eax + dby * eay + dbz * eaz) / rab - c * pa * ia * ia;
-    const float dcb = (dax * ebx + day * eby + daz * ebz) / rab - c * pb * ib * ib;
+    const float dca = (dbx * eax + dby * eay + dbz * eaz) * irab - c * pa * ia * ia;
+    const float dcb = (dax * ebx + day * eby + daz * ebz) * irab - c * pb * ib * ib;
     const float ua = pa * ia, ub = pb * ib;
     const float fca = N.fc[a], fcb = N.fc[b], dfa = N.dfc[a], dfb = N.dfc[b];
     AngPair T;
