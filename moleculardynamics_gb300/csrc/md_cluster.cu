@@ -82,10 +82,12 @@ __global__ void k_cl_assign(md_double4* __restrict__ pos, int n, const ClusterRe
     // reciprocal (within 2 ulp of the quotient) decides unless the quotient
     // lies within 1e-12 of an integer
     const double xa = xadd(x[d], h);
-    const double qa = xa * r.invL;
-    const double q = fabs(qa - rint(qa)) > 1e-12 * fmax(1.0, fabs(qa)) ? floor(qa)
-                                                                         : floor(xdiv(xa, r.L));
-    x[d] = xsub(x[d], xmul(q, r.L));
+    double q = 0.0;  // 0 <= x + L/2 < L: the rounded quotient lies in [0, 1)
+    if (!(xa >= 0.0 && xa < r.L)) {
+      const double qa = xa * r.invL;
+      q = fabs(qa - rint(qa)) > 1e-12 * fmax(1.0, fabs(qa)) ? floor(qa) : floor(xdiv(xa, r.L));
+      x[d] = xsub(x[d], xmul(q, r.L));
+    }
     const double xb = q == 0.0 ? xa : xadd(x[d], h);
     const double sa = xb * r.invcs;
     double s = fabs(sa - rint(sa)) > 1e-12 * fmax(1.0, fabs(sa)) ? sa : xdiv(xb, r.cs);
