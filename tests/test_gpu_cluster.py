@@ -207,6 +207,31 @@ def test_cluster_energy_conservation(eng):
     assert drift < 1e-4, drift
 
 
+def test_records_leave_the_trajectory_unchanged(eng):
+    """A record after every step makes every step a correct-only launch
+    followed by the energy launch and a separate predict; the trajectory is
+    that of the fused steps, bit for bit, across list builds, and the last
+    record's energy is that of an energy evaluation at the final state."""
+    pos, vel, L = argon_fcc(8, noise=0.1, seed=4)
+    n = len(pos)
+    out = {}
+    for every in (0, 1):
+        with _engine(eng, n, L, lj_kernel=eng.LJ_CLUSTER, output_timesteps=every) as e:
+            e.upload(pos, vel)
+            e.begin(0.0)
+            e.step(120)
+            out[every] = e.download()
+            st = e.stats()
+            if every:
+                rec = e.records()
+                assert len(rec) >= 120
+                _, en = e.compute_forces()
+                # the last record holds the final state's shifted LJ energy
+                assert abs(rec[-1, 12] - en[1]) <= 1e-6 * abs(en[1])
+        assert st["list_builds"] > 2
+    assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
+
+
 def test_autotune_keeps_forces(eng):
     """The autotuner only changes tiling: forces stay bit-identical."""
     pos, vel, L = argon_fcc(12, noise=0.1)
