@@ -521,6 +521,16 @@ __global__ void __launch_bounds__(128)
   if (lane == 0) slen[i] = cnt;
 }
 
+// Third bodies m of the warp's atom i (pass 1, FP32): what depends on i and
+// m only, computed once per warp instead of once per pair i-j
+constexpr int kThirdMax = 64;
+struct ThirdSm {
+  float x[kThirdMax], y[kThirdMax], z[kThirdMax];  // position at its image
+  float r[kThirdMax], fc[kThirdMax], dfc[kThirdMax];
+  float ux[kThirdMax], uy[kThirdMax], uz[kThirdMax];  // (r_i - r_m) / r_im
+  int id[kThirdMax];                                  // atom, -1 for an NG atom
+};
+
 template <typename T, bool ENERGY>
 __global__ void __launch_bounds__(128)
     k_mb_pass1(const md_double4* __restrict__ pos, const float4* __restrict__ posf,
@@ -534,6 +544,8 @@ __global__ void __launch_bounds__(128)
   // FP32: the angle derivatives in a shorter, algebraically equal form
   constexpr bool kFast = std::is_same<T, float>::value;
   double ev[2] = {0.0, 0.0};
+  __shared__ ThirdSm third_sm[4];
+  ThirdSm& TS = third_sm[(threadIdx.x >> 5) & 3];
   if (i < n) {
     T xi, yi, zi;
     int ti;
@@ -542,6 +554,32 @@ __global__ void __launch_bounds__(128)
     T fx = 0, fy = 0, fz = 0;
     const T cut_rijsq = (T)MD_CUTOFF_RIJSQ;
     const T nanv = (T)NAN;
+    const bool staged = kFast && S <= kThirdMax && blockDim.x <= 128;  // warp-uniform
+    if (staged) {
+      for (int m = lane; m < S; m += 32) {
+        const uint32_t em = sl[(size_t)m * n + i];
+        const int mp = entry_index(em);
+        T xm, ym, zm;
+        int tm;
+        PosT<T>::load(pos, posf, mp, xm, ym, zm, tm);
+        PosT<T>::image(xm, ym, zm, em, g);
+        const T imx = xi - xm, imy = yi - ym, imz = zi - zm;
+        const T rim = md_sqrt(imx * imx + imy * imy + imz * imz);
+        T fci, dfci;
+        cutoff<T>(rim, fci, dfci);
+        TS.id[m] = tm == SP_NG ? -1 : mp;
+        TS.x[m] = (float)xm;
+        TS.y[m] = (float)ym;
+        TS.z[m] = (float)zm;
+        TS.r[m] = (float)rim;
+        TS.fc[m] = (float)fci;
+        TS.dfc[m] = (float)dfci;
+        TS.ux[m] = (float)fdiv<T>(imx, rim);
+        TS.uy[m] = (float)fdiv<T>(imy, rim);
+        TS.uz[m] = (float)fdiv<T>(imz, rim);
+      }
+      __syncwarp();
+    }
     for (int s = lane; s < S; s += 32) {
       const uint32_t e = sl[(size_t)s * n + i];
       const int j = entry_index(e);
@@ -576,21 +614,37 @@ __global__ void __launch_bounds__(128)
         T xsi = 0, xsj = 0;
         T dxsix = 0, dxsiy = 0, dxsiz = 0, dxsjx = 0, dxsjy = 0, dxsjz = 0;
         for (int m = 0; m < S; m++) {
-          const uint32_t em = sl[(size_t)m * n + i];
-          const int mp = entry_index(em);
-          T xm, ym, zm;
-          int tm;
-          PosT<T>::load(pos, posf, mp, xm, ym, zm, tm);
-          if (tm == SP_NG || mp == j) continue;
-          PosT<T>::image(xm, ym, zm, em, g);
-          const T imx = xi - xm, imy = yi - ym, imz = zi - zm;
-          const T rim = md_sqrt(imx * imx + imy * imy + imz * imz);
+          T xm, ym, zm, rim, fci, dfci, drimx, drimy, drimz;
+          if (staged) {
+            const int mp = TS.id[m];
+            if (mp < 0 || mp == j) continue;
+            xm = TS.x[m];
+            ym = TS.y[m];
+            zm = TS.z[m];
+            rim = TS.r[m];
+            fci = TS.fc[m];
+            dfci = TS.dfc[m];
+            drimx = TS.ux[m];
+            drimy = TS.uy[m];
+            drimz = TS.uz[m];
+          } else {
+            const uint32_t em = sl[(size_t)m * n + i];
+            const int mp = entry_index(em);
+            int tm;
+            PosT<T>::load(pos, posf, mp, xm, ym, zm, tm);
+            if (tm == SP_NG || mp == j) continue;
+            PosT<T>::image(xm, ym, zm, em, g);
+            const T imx = xi - xm, imy = yi - ym, imz = zi - zm;
+            rim = md_sqrt(imx * imx + imy * imy + imz * imz);
+            cutoff<T>(rim, fci, dfci);
+            drimx = fdiv<T>(imx, rim);
+            drimy = fdiv<T>(imy, rim);
+            drimz = fdiv<T>(imz, rim);
+          }
           const T jmx = xj - xm, jmy = yj - ym, jmz = zj - zm;
           const T rjm = md_sqrt(jmx * jmx + jmy * jmy + jmz * jmz);
-          T fci, dfci, fcj, dfcj;
-          cutoff<T>(rim, fci, dfci);
+          T fcj, dfcj;
           cutoff<T>(rjm, fcj, dfcj);
-          const T drimx = fdiv<T>(imx, rim), drimy = fdiv<T>(imy, rim), drimz = fdiv<T>(imz, rim);
           if (kFast && fci > 0) {
             // d cos / d r_i = drij (1/rim - cos/rij) + drim (1/rij - cos/rim):
             // the reference's quotient below, two scalars per triplet
