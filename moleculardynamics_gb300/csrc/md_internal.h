@@ -35,7 +35,7 @@ struct NeighborList {
   Grid grid{};
   CellTable table;
   int* atom_slot = nullptr;    // table slot of each atom's cell
-  int* cell3 = nullptr;        // build-time cell coordinates (3 per atom)
+  int* cell3 = nullptr;        // build-time cell coordinates (x, y, z, unused: 4 ints per atom)
   int* unsorted = nullptr;
   int* sorted = nullptr;       // atoms grouped by slot, ascending inside a cell
   uint32_t* list = nullptr;

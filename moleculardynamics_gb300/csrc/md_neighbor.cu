@@ -60,8 +60,9 @@ __global__ void k_cell_assign(md_double4* __restrict__ pos, int n, Grid g, int* 
       if (c[d] >= g.cells) c[d] = g.cells - 1;
       if (c[d] < 0) c[d] = 0;
     }
-    cell3[3 * i + d] = c[d];
   }
+  // one 16-byte row per atom: x, y, z and an unused fourth int
+  reinterpret_cast<int4*>(cell3)[i] = make_int4(c[0], c[1], c[2], 0);
   if (bad) atomicOr(status, isfinite(p.x + p.y + p.z) ? ST_CELL_OVERFLOW : ST_NONFINITE);
   unsigned long long key = cell_key(c[0], c[1], c[2]);
   unsigned h = (unsigned)(mix64(key) & (unsigned long long)(cap - 1));
@@ -376,7 +377,7 @@ int list_build(NeighborList& nl, md_double4* pos, int n, const Grid& g, int comp
       if ((e = cudaMalloc(p, sizeof(int) * need)) != cudaSuccess) return e;
     }
     if (nl.cell3) cudaFree(nl.cell3);
-    if ((e = cudaMalloc(&nl.cell3, sizeof(int) * 3 * need)) != cudaSuccess) return e;
+    if ((e = cudaMalloc(&nl.cell3, sizeof(int) * 4 * need)) != cudaSuccess) return e;
     if (nl.len) cudaFree(nl.len);
     if ((e = cudaMalloc(&nl.len, sizeof(int) * need)) != cudaSuccess) return e;
     if (nl.pos_build) cudaFree(nl.pos_build);

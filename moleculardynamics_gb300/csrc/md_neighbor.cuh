@@ -50,7 +50,8 @@ __device__ __forceinline__ void walk_row(const RowWalker& w, const md_double4* p
     }
     return;
   }
-  const int cx = w.cell3[3 * i], cy = w.cell3[3 * i + 1], cz = w.cell3[3 * i + 2];
+  const int4 c4 = reinterpret_cast<const int4*>(w.cell3)[i];
+  const int cx = c4.x, cy = c4.y, cz = c4.z;
   const int cells = w.g.cells;
   for (int dx = -1; dx < 2; dx++)
     for (int dy = -1; dy < 2; dy++)
@@ -84,9 +85,11 @@ __device__ __forceinline__ void walk_row(const RowWalker& w, const md_double4* p
 __device__ __forceinline__ bool in_row(const int* cell3, const Grid& g, int k, int j,
                                        int* img) {
   if (j == k) return false;
+  const int4 k4 = reinterpret_cast<const int4*>(cell3)[k], j4 = reinterpret_cast<const int4*>(cell3)[j];
+  const int ck3[3] = {k4.x, k4.y, k4.z}, cj3[3] = {j4.x, j4.y, j4.z};
 #pragma unroll
   for (int d = 0; d < 3; d++) {
-    int ck = cell3[3 * k + d], cj = cell3[3 * j + d];
+    int ck = ck3[d], cj = cj3[d];
     img[d] = 0;
     if (!g.periodic) {
       int dd = cj - ck;

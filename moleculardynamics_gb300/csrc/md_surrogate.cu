@@ -148,7 +148,8 @@ __global__ void __launch_bounds__(128)
   const float4 pi = pos[i];
   const float rc2 = rc * rc;
   const float boxf = (float)w.g.box;
-  const int cx = w.cell3[3 * i], cy = w.cell3[3 * i + 1], cz = w.cell3[3 * i + 2];
+  const int4 c4 = reinterpret_cast<const int4*>(w.cell3)[i];
+  const int cx = c4.x, cy = c4.y, cz = c4.z;
   const int cells = w.g.cells;
   // lane c < 27 looks up cell c of the 27 (dx slowest, dz fastest) with its image
   int cs = 0, cn = 0, im[3] = {0, 0, 0};
