@@ -167,20 +167,86 @@ def drift_per_1000(recs: np.ndarray, n: int, first_step: int) -> float:
     return float((e[-1] - e[0]) / n / EPS / steps * 1000.0)
 
 
-def fp32_roofline(entries: int, launch_s: float, peaks: dict) -> dict:
-    """FP32 arithmetic of one LJ force evaluation against the FP32 pipe's
-    nominal peak: 8 flops per row entry (3 differences, r^2 as a product
-    and two FMAs) and 15 per pair inside the cutoff (reciprocal, the r^-6
-    chain and force scalar, three FMAs into the sums), FMA = 2 flops; the
-    pairs inside the cutoff are (2.5 / 2.8)^3 of the entries (uniform
-    density).  The peak is 152 SMs x 128 FP32 lanes x 2 flops x the maximum
-    SM clock (no measured FP32 figure)."""
+# FP64 operations per atom of the fused Gear update: correct 6 per component
+# (a = F/m, the difference, four FMAs), predict 10 per component (4 + 3 + 2 + 1
+# FMAs), and the compensated force widened with one subtraction per component
+GEAR_FP64_OPS_PER_ATOM = 3 * (6 + 10 + 1)
+
+
+def fp32_roofline(entries: int, launch_s: float, arith: dict) -> dict:
+    """FP32 arithmetic of one LJ force evaluation against the FP32 rate
+    measured on this device (md_measure_arith_peaks: FMA chains on every SM):
+    8 flops per row entry (3 differences, r^2 as a product and two FMAs) and
+    15 per pair inside the cutoff (reciprocal, the r^-6 chain and force
+    scalar, three FMAs into the sums), FMA = 2 flops; the pairs inside the
+    cutoff are (2.5 / 2.8)^3 of the entries (uniform density)."""
     inside = entries * (2.5 / 2.8) ** 3
     flops = 8.0 * entries + 15.0 * inside
     achieved = flops / launch_s / 1e12
-    peak = 152 * 128 * 2 * peaks.get("sm_max_mhz", 2070.0) * 1e6 / 1e12
+    peak = arith["fp32_gflops"] / 1e3
     return {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-            "frac": achieved / peak, "peak_source": "nominal", "flops_alg_per_launch": flops}
+            "frac": achieved / peak, "peak_source": "measured (FMA chains on this device)",
+            "flops_alg_per_launch": flops}
+
+
+def fp64_lj_roofline(entries: int, launch_s: float, arith: dict) -> dict:
+    """The plain FP64 LJ kernel (k_lj_fp64) against the FP64 rate measured
+    on this device.  Operations of the reference's formula as the kernel
+    evaluates it (no FMA contraction, for bit-exact parity;
+    cpu/common/LennardJones.h:12-30): per row entry 3 differences, r^2 (3
+    products, 2 sums) and the cutoff test = 8; per pair inside the cutoff
+    a square root, 4 divisions, 10 products and sums and 3 FMA-free updates
+    of the sums (6) = 21, each counted as one flop.  Divisions and square
+    roots take many FP64 pipe slots each, so this count sits well below
+    the pipe's occupancy."""
+    inside = entries * (2.5 / 2.8) ** 3
+    flops = 8.0 * entries + 21.0 * inside
+    achieved = flops / launch_s / 1e12
+    peak = arith["fp64_gflops"] / 1e3
+    return {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+            "frac": achieved / peak, "peak_source": "measured (FMA chains on this device)",
+            "flops_alg_per_launch": flops,
+            "divisions_and_sqrt_per_launch": 5.0 * inside}
+
+
+# FP32 flops of the bond-order force evaluation (k_mb_short + k_mb_pass1 +
+# k_mb_pass2), counted from the kernels' FP32 expressions with FMA = 2 and a
+# reciprocal, square root, exponential or tanh = 1: per pair within the cutoff
+# (attractive, repulsive and van der Waals terms, the pair cutoff, the bond
+# order from xi, the force) 75; per pass-1 triplet (i, j, m), both sides of
+# the angle term with their derivatives, 110; per pass-2 triplet (k, i, j)
+# 130.  The FP64 instantiation evaluates the reference's own expressions
+# (more operations, divisions in place of products); the same counts are used
+# for it, so its fraction is a lower bound.
+MB_FLOPS_PAIR, MB_FLOPS_TRIPLET1, MB_FLOPS_TRIPLET2 = 75.0, 110.0, 130.0
+
+
+def bond_order_counts(pos: np.ndarray, L: float, rcut: float = 3.0) -> dict:
+    """Pairs and triplets the bond-order passes evaluate at these positions:
+    c_i neighbours of atom i within rcut (minimum image); pass 1 takes every
+    pair (i, j) with every other m of i's neighbours, pass 2 every (k, i) with
+    every other j of i's neighbours (an upper bound: it keeps only j in k's
+    candidate row)."""
+    from scipy.spatial import cKDTree
+    x = np.mod(pos[:, :3] + 0.5 * L, L)
+    tree = cKDTree(x, boxsize=L)
+    c = np.array([len(v) - 1 for v in tree.query_ball_point(x, rcut)], dtype=np.float64)
+    pairs = float(c.sum())
+    trip = float((c * (c - 1)).sum())
+    return {"pairs": pairs, "triplets_pass1": trip, "triplets_pass2": trip,
+            "mean_neighbours": float(c.mean())}
+
+
+def bond_order_roofline(counts: dict, launch_s: float, arith: dict, fp64: bool) -> dict:
+    flops = (MB_FLOPS_PAIR * counts["pairs"] + MB_FLOPS_TRIPLET1 * counts["triplets_pass1"]
+             + MB_FLOPS_TRIPLET2 * counts["triplets_pass2"])
+    achieved = flops / launch_s / 1e12
+    peak = (arith["fp64_gflops"] if fp64 else arith["fp32_gflops"]) / 1e3
+    return {"kernel": "k_mb_short + k_mb_pass1 + k_mb_pass2" + ("<double>" if fp64 else "<float>"),
+            "bound": "fp64" if fp64 else "fp32", "achieved": achieved, "peak": peak,
+            "unit": "TFLOP/s", "frac": achieved / peak,
+            "peak_source": "measured (FMA chains on this device)",
+            "flops_alg_per_launch": flops, "avg_launch_ms": launch_s * 1e3, "counts": counts}
 
 
 def roofline_traffic(workload: str, kernel: str = "lj_force"):
@@ -334,7 +400,8 @@ def batched_form(eng, device, steps: int, loop_steps: int, seed: int = 4096) -> 
     }
 
 
-def surrogate_form(eng, device, train_steps: int, run_steps: int, seed: int = 5) -> dict:
+def surrogate_form(eng, device, train_steps: int, run_steps: int, arith: dict,
+                   seed: int = 5) -> dict:
     """The learned bond-order surrogate on the 32,768-atom nitrogen diamond
     (16^3 cells, nearest neighbour 1.5 A, 0.02 A noise).  Training data:
     trajectories of the exact FP64 method at 300, 700, 1100 and 1500 K on
@@ -390,6 +457,7 @@ def surrogate_form(eng, device, train_steps: int, run_steps: int, seed: int = 5)
         e.step(run_steps)
         e.synchronize()
         ms, _ = e.kernel_time(eng.KERNEL_STEP)
+        mb_ms, mb_n = e.kernel_time(eng.KERNEL_MB)
         e.set_timing(False)
         th1 = e.thermo_now()
         fk, en = e.compute_forces()
@@ -417,7 +485,12 @@ def surrogate_form(eng, device, train_steps: int, run_steps: int, seed: int = 5)
             same = rel(ef.compute_forces()[0])
             ef.close()
         drift = ((th1["ek"] + es1) - (th0["ek"] + es0)) / n / run_steps * 1000.0
+        roof = None
+        if threshold is None and mb_n:
+            roof = bond_order_roofline(bond_order_counts(p1, L), mb_ms / mb_n / 1e3, arith,
+                                       precision == eng.PREC_FP64)
         return {"ms_per_step": ms / run_steps, "value": n * run_steps / (ms / 1e3),
+                "roofline": roof,
                 "force_rms_rel_vs_exact_same_lists": same,
                 "force_rms_rel_vs_exact": rel(fs if threshold is not None and rep and
                                               rep["surrogate_steps"] > 0 else fk),
@@ -464,6 +537,10 @@ def run_gb300(args, rank, world):
     b.build()
     eng.load()
     device = int(os.environ.get("LOCAL_RANK", "0"))
+    # FP64 and FP32 rates of this device (FMA chains), the denominators of
+    # the FP64 and FP32 rooflines below
+    arith = eng.measure_arith_peaks(device)
+    arith["sms"] = eng.device_sm_count(device)
     pos, vel, L, prec_name = make_workload(args.workload)
     n = len(pos)
     precision = eng.PREC_MIXED if prec_name == "mixed" else eng.PREC_FP64
@@ -504,6 +581,13 @@ def run_gb300(args, rank, world):
     value = world * n * md_steps / (t_max / 1e3)
     recs = e.records()
     drift = drift_per_1000(recs, n, warm_steps)
+    # energy drift over the full run length of the workload (10,000 MD steps),
+    # continued from the timed state; records every 100 steps
+    t_drift0 = int(recs[-1, 15]) if len(recs) else 0
+    for _ in range(max(args.drift_steps, 0) // MD_PER_BENCH_STEP):
+        e.step(MD_PER_BENCH_STEP)
+    e.synchronize()
+    drift_long = drift_per_1000(e.records(), n, t_drift0) if args.drift_steps > 0 else None
 
     # end to end through the C ABI: the caller owns the Gear state in pinned
     # host memory; every bench step copies it in, runs, and copies it back
@@ -567,7 +651,11 @@ def run_gb300(args, rank, world):
         "kernel_launches": {"lj_force": lj_n, "predict": pr_n, "correct": co_n,
                             "fused_force_gear": fu_n, "fused_force_correct": fc_n,
                             "list_build": li_n},
-        "accuracy": {"energy_drift_eps_per_atom_per_1000_steps": drift},
+        "accuracy": {"energy_drift_eps_per_atom_per_1000_steps": drift,
+                     "energy_drift_eps_per_atom_per_1000_steps_long": drift_long,
+                     "drift_leg_md_steps": args.drift_steps},
+        "arith_peaks": dict(arith, how="md_measure_arith_peaks: 8 dependent FMA chains per "
+                                        "thread, 2048 threads per SM, best of 3, FMA = 2 flops"),
     }
     peaks = measured_peaks()
     if fu_n:
@@ -586,7 +674,14 @@ def run_gb300(args, rank, world):
                             "traffic": roofline_traffic(args.workload, "lj_cluster_fused"),
                             "bytes_alg_per_launch": bytes_alg,
                             "avg_launch_ms": fu_ms / fu_n}
-        line["roofline_fp32"] = fp32_roofline(entries, avg_s, peaks)
+        line["roofline_fp32"] = fp32_roofline(entries, avg_s, arith)
+        # the FP64 pipe's share: the Gear update alone at the measured FP64 rate
+        floor_ms = n * GEAR_FP64_OPS_PER_ATOM / (arith["fp64_gflops"] * 1e9 / 2.0) * 1e3
+        line["roofline"]["fp64_gear_floor_ms"] = floor_ms
+        line["roofline"]["fp64_gear_ops_per_atom"] = GEAR_FP64_OPS_PER_ATOM
+        line["roofline"]["fp64_gear_floor_share_of_launch"] = floor_ms / (fu_ms / fu_n)
+        line["roofline"]["launch_ms_at_60pct_hbm"] = bytes_alg / (0.6 * line["roofline"]["peak"]
+                                                                  * 1e9) * 1e3
     elif lj_n:
         entries = s1["lj_list_entries"]
         if s1["lj_cluster"]:
@@ -611,7 +706,7 @@ def run_gb300(args, rank, world):
                             "bytes_alg_per_launch": bytes_alg,
                             "avg_launch_ms": lj_ms / lj_n}
         if precision == eng.PREC_MIXED:
-            line["roofline_fp32"] = fp32_roofline(entries, avg_s, peaks)
+            line["roofline_fp32"] = fp32_roofline(entries, avg_s, arith)
 
     if rank == 0 and not args.no_compare:
         # plain FP64 GPU path on the same workload (fewer steps: it is slow)
@@ -626,6 +721,7 @@ def run_gb300(args, rank, world):
         f64.synchronize()
         ms64, _ = f64.kernel_time(eng.KERNEL_STEP)
         lj64_ms, lj64_n = f64.kernel_time(eng.KERNEL_LJ)
+        ent64 = f64.stats()["lj_list_entries"]
         v64 = n * k64 / (ms64 / 1e3)
         # force error of the chosen form at the same positions
         pnow, vnow = e.download()
@@ -636,14 +732,18 @@ def run_gb300(args, rank, world):
         f64.close()
         rms = float(np.sqrt(((fb - fa) ** 2).sum(1).mean()) / np.sqrt((fa ** 2).sum(1).mean()))
         line["plain_fp64"] = {"value": v64, "unit": "atom-steps/s", "md_steps": k64,
-                              "lj_force_ms": lj64_ms / max(lj64_n, 1)}
+                              "lj_force_ms": lj64_ms / max(lj64_n, 1),
+                              "roofline": dict(fp64_lj_roofline(ent64, lj64_ms / max(lj64_n, 1)
+                                                                / 1e3, arith),
+                                               kernel="k_lj_fp64",
+                                               avg_launch_ms=lj64_ms / max(lj64_n, 1))}
         line["speedup_vs_plain_fp64"] = value / world / v64
         line["accuracy"]["force_rms_rel_vs_fp64"] = rms
     if rank == 0 and not args.no_forms:
         line["forms"] = {"batched": batched_form(eng, device, args.batch_steps,
                                                   args.batch_loop_steps),
                          "surrogate": surrogate_form(eng, device, args.sur_train_steps,
-                                                     args.sur_run_steps)}
+                                                     args.sur_run_steps, arith)}
     if rank == 0 and world == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1
         csteps = args.cpu_md_steps
@@ -653,6 +753,13 @@ def run_gb300(args, rank, world):
                                 "sample": f"{n} atoms, {csteps} MD steps after the list build, "
                                           f"{threads} OpenMP threads, C restatement of the "
                                           "reference step (oracle/mdoracle.c)"}
+        # the reference as shipped runs on one core
+        ms1, kind1 = cpu_baseline(pos, vel, L, args.cpu_1t_steps, 1)
+        line["cpu_baseline_1thread"] = {
+            "value": n * args.cpu_1t_steps / (ms1 / 1e3), "unit": "atom-steps/s", "cores": 1,
+            "kind": kind1,
+            "sample": f"{n} atoms, {args.cpu_1t_steps} MD step(s) after the list build, one "
+                      "thread, C restatement of the reference step (oracle/mdoracle.c)"}
     e.close()
     dist.close()
     if rank == 0:
@@ -706,6 +813,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--fp64-steps", type=int, default=100)
     ap.add_argument("--cpu-md-steps", type=int, default=5)
+    ap.add_argument("--cpu-1t-steps", type=int, default=1)
+    ap.add_argument("--drift-steps", type=int, default=10000,
+                    help="MD steps of the energy-drift leg after the timed loop")
     ap.add_argument("--ref-md-steps", type=int, default=2)
     ap.add_argument("--lj-kernel", default="auto", choices=["auto", "rows", "cluster"])
     ap.add_argument("--no-tune", action="store_true", help="skip the cluster autotuner")
@@ -718,7 +828,7 @@ def main():
     ap.add_argument("--stage-cap", type=int, default=0,
                     help="cluster staged atoms per segment (0: the autotuner chooses)")
     ap.add_argument("--no-forms", action="store_true", help="skip the batched/surrogate forms")
-    ap.add_argument("--batch-steps", type=int, default=1000)
+    ap.add_argument("--batch-steps", type=int, default=5000)
     ap.add_argument("--batch-loop-steps", type=int, default=10)
     ap.add_argument("--sur-train-steps", type=int, default=20000)
     ap.add_argument("--sur-run-steps", type=int, default=200)

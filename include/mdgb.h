@@ -18,8 +18,9 @@
  *     common/NeighborList.h and common/DebugCalculations.h with the same
  *     arguments and meaning, operating on host arrays (each call copies in,
  *     computes on the GPU, copies out).  A C++ file that forwards the
- *     reference names to these is all cpumd needs.  They
- *     return void like the reference; mdgb_last_status() reports failures.
+ *     reference names to these (refshim/cpumd_device_gb300.cpp in this
+ *     package) is all cpumd needs.  They return void like the reference;
+ *     mdgb_last_status() reports failures.
  *
  * Units are the reference's: angstrom, femtosecond, g/mol, energy 1e7 J/mol.
  */
@@ -191,6 +192,21 @@ md_status md_autotune(md_ctx* ctx, int evals, md_tune_result* out);
 /* CUDA graphs for the cluster path (default on): windows of fused steps
  * with nothing else due are replayed as one captured graph. */
 md_status md_set_graphs(md_ctx* ctx, int on);
+/* Bounded device waits of the LJ kernels: a wait on an mbarrier for a TMA
+ * row tile or a staged neighbourhood gives up after `tries` polls, the call
+ * returns MD_TIMEOUT, and the kernel leaves once the copies it still has in
+ * flight have landed (those last waits keep the default limit, so no copy
+ * outlives its block).  Default 1 << 20; tries = 0 gives up at the first
+ * wait (for tests of the timeout path).  The surrogate's tensor-core commit
+ * waits always use the default.  The state after MD_TIMEOUT is undefined:
+ * upload it again before stepping on. */
+md_status md_set_wait_limit(md_ctx* ctx, int tries);
+
+/* Arithmetic peaks of a device measured with CUDA events: dependent FMA
+ * chains on every SM, FMA = 2 flops (the roofline denominators of the FP64
+ * and FP32 kernels).  Takes about 0.1 s. */
+md_status md_measure_arith_peaks(int device, double* fp64_gflops, double* fp32_gflops);
+md_status md_device_sm_count(int device, int* sms);
 
 /* ---- batched form: many independent periodic replicas in one context ----
  * Replica k has natoms[k] atoms in a cubic periodic box of edge boxes[k];
@@ -336,18 +352,23 @@ void mdgb_calculate_potential(const double* pos4, double* vib_lj, double* vib_mb
  * direct cudaMalloc/cudaFree, or a time-critical loop that cannot take the
  * synchronisation an allocation may cause.  Inputs and the output are the
  * caller's device arrays: d_pos4 (n x real4, 32-byte aligned), d_list (rows in
- * the reference layout), d_f3 (n x real3, accumulated into when ljexist).
- * Scratch lives in one fixed array of about 33 MB inside the library, held on
- * every GPU that loads it until the process exits; sizes above 16384 atoms or
- * 1048576 atom x row-slot pairs (n * nlargestsize) are rejected with
- * MD_BAD_ARGUMENT and a message in err.  The first call on a device looks up
- * the array's address; make that first call before any stream capture.  All
- * calls share the array: calls that overlap on the GPU race, so serialise
- * them.  stream is a cudaStream_t (NULL: the default stream); the work is
- * queued on it and the function returns without waiting.  Returns md_status. */
+ * the reference layout), d_f3 (n x real3; overwritten when ljexist is 0,
+ * accumulated into when it is 1).  d_missing_xi (device int, may be NULL)
+ * receives the number of third-body reads of a xi that pass 1 did not make
+ * (a list built at other positions; those xi count as 0), as the regular
+ * path reports missing_xi.  Scratch lives in one fixed array of about 33 MB
+ * inside the library, held on every GPU that loads it until the process
+ * exits; sizes above 16384 atoms or 1048576 atom x row-slot pairs
+ * (n * nlargestsize) are rejected with MD_BAD_ARGUMENT and a message in err.
+ * Each call looks up the array's address on the current device (no
+ * allocation); the first call on a device also loads the library's device
+ * image there, so make that first call before any stream capture.  All calls
+ * share the array: calls that overlap on the GPU race, so serialise them.
+ * stream is a cudaStream_t (NULL: the default stream); the work is queued on
+ * it and the function returns without waiting.  Returns md_status. */
 int mdgb_many_body_forces_static(const double* d_pos4, double* d_f3, int n, int nlargestsize,
                                  int nlistsize, const int* d_list, double rcutsq, int ljexist,
-                                 void* stream, char* err, int err_len);
+                                 int* d_missing_xi, void* stream, char* err, int err_len);
 /* species table of the mdgb_* layer: MD_SPECIES_NEON (default, the reference's) */
 void mdgb_set_species(int species);
 /* status of the last mdgb_* call on this thread (MD_OK or the failure) */

@@ -19,7 +19,7 @@ LIB = os.path.join(PKG, "libmdgb.so")
 RUN = os.path.join(PKG, "mdgb_run")
 
 CU_SOURCES = ["md_neighbor.cu", "md_forces.cu", "md_cluster.cu", "md_surrogate.cu", "md_integrate.cu", "md_output.cu", "md_engine.cu",
-              "md_refshim.cu", "md_static.cu"]
+              "md_refshim.cu", "md_static.cu", "md_diag.cu"]
 CPP_SOURCES = ["md_io.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "--extended-lambda", "-Xcompiler", "-fPIC",

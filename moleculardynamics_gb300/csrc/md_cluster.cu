@@ -345,7 +345,7 @@ __device__ __forceinline__ void stage(const SegShared& sh, const float4* __restr
 // out; the caller then leaves after the copies land or time out.
 __device__ __forceinline__ bool stage_bulk(const SegShared& sh, const float4* __restrict__ src,
                                            float4* st, uint64_t* bar, uint32_t parity,
-                                           int* status) {
+                                           int* status, int limit) {
   const ClusterSegment& S = sh.S;
   if (threadIdx.x == 0) {
     fence_proxy_async();  // earlier generic accesses to the stage come first
@@ -356,9 +356,9 @@ __device__ __forceinline__ bool stage_bulk(const SegShared& sh, const float4* __
         bulk_load(st + pc.dst, src + pc.src, (uint32_t)pc.count * (uint32_t)sizeof(float4), bar);
     }
   }
-  const bool got = mbar_wait(bar, parity, status);
+  const bool got = mbar_wait(bar, parity, status, limit);
   if (!__syncthreads_and(got)) {
-    if (threadIdx.x == 0) mbar_wait(bar, parity, status);
+    if (threadIdx.x == 0) mbar_drain(bar, parity, status);
     return false;
   }
   const float Lf = sh.r.Lf, Llo = sh.r.Llo;
@@ -657,6 +657,7 @@ struct ClStep {
   int* status;
   ClusterGearArgs g;
   int nbuf;  // row tiles in flight in the block-tile scheme (2 or 3)
+  int wait_limit;  // polls of a bounded mbarrier wait
 };
 
 // FP32 LJ force, persistent: each block takes segments from a shared
@@ -727,7 +728,7 @@ __global__ void __launch_bounds__(224, 3)
     tma_prefetch_2d(&rmap, sh.S.p0 & ~7, 0);
     tma_prefetch_2d(&rmap, sh.S.p0 & ~7, kClusterTileSlots);
   }
-  if (!stage_bulk(sh, a.posf, st, &bar[3], (phase >> 3) & 1u, a.status)) {
+  if (!stage_bulk(sh, a.posf, st, &bar[3], (phase >> 3) & 1u, a.status, a.wait_limit)) {
     aborted = true;
     break;
   }
@@ -942,7 +943,8 @@ __global__ void __launch_bounds__(224, 3)
       bool wfailed = false;
       for (int t = 0; t < Tw; t++) {
         const int b = t & 1;
-        const bool got = __all_sync(0xffffffffu, mbar_wait(&wb2[b], (phase >> b) & 1u, a.status));
+        const bool got = __all_sync(
+            0xffffffffu, mbar_wait(&wb2[b], (phase >> b) & 1u, a.status, a.wait_limit));
         if (!got) {
           wfailed = true;
           break;
@@ -969,7 +971,7 @@ __global__ void __launch_bounds__(224, 3)
         // time out) before the block leaves
         if (lane == 0)
           for (int b = 0; b < 2; b++)
-            if ((inflight >> b) & 1u) mbar_wait(&wb2[b], (phase >> b) & 1u, a.status);
+            if ((inflight >> b) & 1u) mbar_drain(&wb2[b], (phase >> b) & 1u, a.status);
         aborted = true;
         break;
       }
@@ -1031,7 +1033,7 @@ __global__ void __launch_bounds__(224, 3)
       bool failed = false;
       int b = 0;  // buffer of tile t: t mod nbuf
       for (int t = 0; t < T; t++, b = b + 1 == nbuf ? 0 : b + 1) {
-        const bool got = mbar_wait(&bar[b], (phase >> b) & 1u, a.status);
+        const bool got = mbar_wait(&bar[b], (phase >> b) & 1u, a.status, a.wait_limit);
         const int wrem = wmax - t * kClusterTileSlots;  // warp-uniform
         if (got) {
           phase ^= 1u << b;
@@ -1062,7 +1064,7 @@ __global__ void __launch_bounds__(224, 3)
         // chance to land in this block's shared memory, then leave
         if (tid == 0)
           for (int k = 0; k < nbuf; k++)
-            if ((inflight >> k) & 1u) mbar_wait(&bar[k], (phase >> k) & 1u, a.status);
+            if ((inflight >> k) & 1u) mbar_drain(&bar[k], (phase >> k) & 1u, a.status);
         aborted = true;
         break;
       }
@@ -1553,6 +1555,7 @@ void launch_lj_cluster(const ClusterForceArgs& f, bool energy, cudaStream_t st) 
   if (f.gear) a.g = *f.gear;
   else memset(&a.g, 0, sizeof(a.g));
   a.nbuf = nbuf;
+  a.wait_limit = f.wait_limit;
   // persistent grid: as many blocks as fit on the GPU at once, at most one
   // per segment
   auto grid_for = [&](const void* kern) {

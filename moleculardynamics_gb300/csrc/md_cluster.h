@@ -133,6 +133,7 @@ struct ClusterForceArgs {
   int* status;       // ST_TMA_TIMEOUT / ST_NONFINITE
   const ClusterGearArgs* gear;  // NULL: forces only
   int* skin = nullptr;          // skin flags (NULL: the list's own)
+  int wait_limit = 1 << 20;     // polls of a bounded mbarrier wait (0: give up at once)
 };
 void launch_lj_cluster(const ClusterForceArgs& a, bool energy, cudaStream_t st);
 // inv[orig[p]] = p

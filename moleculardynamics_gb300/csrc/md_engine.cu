@@ -141,6 +141,7 @@ struct md_ctx {
   long long mb_elems = 0;
   // flags and reductions
   int* status = nullptr;
+  int wait_limit = 1 << 20;  // polls of a bounded mbarrier wait (md_set_wait_limit)
   int* wall_flag = nullptr;
   int* missing = nullptr;
   Scratch sc;
@@ -297,6 +298,7 @@ ForceArgs lj_args(md_ctx* c, double* f3, double* epart) {
   a.rcutsq = (double)c->lj_rcutsq;
   a.sp = c->sp;
   a.epart = epart;
+  a.wait_limit = c->wait_limit;
   return a;
 }
 
@@ -352,6 +354,7 @@ ClusterForceArgs cl_args(md_ctx* c, double* f3, double* epart) {
   a.epart = epart;
   a.status = c->status;
   a.gear = nullptr;
+  a.wait_limit = c->wait_limit;
   return a;
 }
 
@@ -758,7 +761,7 @@ bool window_ok(const md_ctx* c, int s, int nsteps) {
 
 md_status run_window(md_ctx* c) {
   struct Sig {
-    int t6, nseg, max_staged, block, all_ng, cap, ld;
+    int t6, nseg, max_staged, block, all_ng, cap, ld, wait_limit;
     float trip2;
     const void* ptr[14];
     unsigned char rmap[sizeof(CUtensorMap)];
@@ -771,6 +774,7 @@ md_status run_window(md_ctx* c) {
   sig.all_ng = c->all_ng;
   sig.cap = c->cl.cap;
   sig.ld = c->cl.ld;
+  sig.wait_limit = c->wait_limit;
   sig.trip2 = gear_args(c, c->t + 1).trip2;
   const void* ptrs[14] = {c->pos, c->pos_alt, c->posf, c->posf_alt, c->vel, c->acc, c->b, c->c,
                           c->cl.seg, c->cl.rows, c->cl.len, c->cl.pos_build, c->cl.skin,
@@ -1591,6 +1595,12 @@ md_status md_tail_pairs(md_ctx* c, int* pairs, int capacity, int* count) {
 md_status md_set_graphs(md_ctx* c, int on) {
   if (!c) return MD_BAD_ARGUMENT;
   c->graphs = on && c->cluster;
+  return MD_OK;
+}
+
+md_status md_set_wait_limit(md_ctx* c, int tries) {
+  if (!c || tries < 0) return MD_BAD_ARGUMENT;
+  c->wait_limit = tries;
   return MD_OK;
 }
 

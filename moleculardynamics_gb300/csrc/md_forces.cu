@@ -302,7 +302,7 @@ __global__ void __launch_bounds__(kListTileAtoms, 8)
              const md_double4* __restrict__ pos, double* __restrict__ f3, int n, int ld,
              uint32_t* __restrict__ list, int* __restrict__ len, RowWalker w, int* skin,
              int parity, int cap, float rv2, float4* __restrict__ pos_build, double rcutsq,
-             Species sp, int* status) {
+             Species sp, int* status, int wait_limit) {
   __shared__ __align__(128) uint32_t tile[2][kListTileSlots][kListTileAtoms];
   __shared__ __align__(8) uint64_t bar[2];
   __shared__ int s_max[kListTileAtoms / 32];
@@ -353,10 +353,13 @@ __global__ void __launch_bounds__(kListTileAtoms, 8)
   const float s2_o = sp.sig[1] * sp.sig[1], c_o = 24.0f * sp.eps[1];
   float hx = 0.f, hy = 0.f, hz = 0.f, lx = 0.f, ly = 0.f, lz = 0.f;
   bool ok = true;
+  int failed_at = 0;
   for (int t = 0; t < T; t++) {
     const int b = t & 1;
-    if (!mbar_wait(&bar[b], (uint32_t)((t >> 1) & 1), status)) {
+    // the outcome is made block-uniform, so every thread leaves together
+    if (!__syncthreads_and(mbar_wait(&bar[b], (uint32_t)((t >> 1) & 1), status, wait_limit))) {
       ok = false;
+      failed_at = t;
       break;
     }
     const int kmax = min(kListTileSlots, L - t * kListTileSlots);
@@ -411,8 +414,11 @@ __global__ void __launch_bounds__(kListTileAtoms, 8)
     }
   }
   if (!ok) {
-    // give copies still in flight a bounded chance to land, then leave
-    for (int t = 0; t < 2 && t < T; t++) mbar_wait(&bar[t], 0, status);
+    // tiles failed_at and failed_at + 1 may still be in flight: they land in
+    // this block's shared memory before it leaves
+    if (tid == 0)
+      for (int t = failed_at; t < failed_at + 2 && t < T; t++)
+        mbar_drain(&bar[t & 1], (uint32_t)((t >> 1) & 1), status);
     return;
   }
   if (i < n) {
@@ -937,12 +943,12 @@ void launch_lj(const ForceArgs& a, bool fp32, bool energy, cudaStream_t st) {
       k_lj_tma<true><<<TB, kListTileAtoms, 0, st>>>(*a.tmap, a.posf, a.pos, a.f3, a.n, a.ld,
                                                     a.list, a.len, a.walker, a.skin, a.parity,
                                                     a.cap, a.rv2, a.pos_build, a.rcutsq, a.sp,
-                                                    a.status);
+                                                    a.status, a.wait_limit);
     else
       k_lj_tma<false><<<TB, kListTileAtoms, 0, st>>>(*a.tmap, a.posf, a.pos, a.f3, a.n, a.ld,
                                                      a.list, a.len, a.walker, a.skin, a.parity,
                                                      a.cap, a.rv2, a.pos_build, a.rcutsq, a.sp,
-                                                     a.status);
+                                                     a.status, a.wait_limit);
   } else {
     if (energy)
       k_lj_fp32<true><<<B, T, 0, st>>>(a.posf, a.pos, a.f3, a.n, a.ld, a.list, a.len, a.walker,

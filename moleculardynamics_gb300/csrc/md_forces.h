@@ -24,6 +24,7 @@ struct ForceArgs {
   double rcutsq;
   Species sp;
   double* epart;        // 3 doubles per block when energy is requested
+  int wait_limit = 1 << 20;  // polls of a bounded mbarrier wait (0: give up at once)
 };
 
 struct MbArgs {

@@ -496,6 +496,112 @@ __device__ __forceinline__ double equi_uniform(unsigned long long seed, int atom
   return ((double)(unsigned)(z >> 32) + 1.0) / 4294967297.0;
 }
 
+// ---- the reference's inverse error function (cpu/equi/Statistics.cpp) ----
+// The same steps as the reference, so that velocities drawn here match
+// equi's for the same uniforms: Newton iterations on the file's own erf and
+// erfc (not CUDA's), every product and sum rounded on its own (no FMA
+// contraction), the library's exp, log and sqrt.  The reference's erf stops
+// its series after two terms for negative arguments (its stopping test
+// divides by the negative sum), so inverf is inaccurate below zero; kept.
+// Each loop also stops after kRefIters rounds, which the reference's
+// convergence tests reach long before.
+constexpr int kRefIters = 400;
+
+// Statistics.cpp:175-196, |x| <= 2.2: the Taylor series
+__device__ double ref_erf_series(double x) {
+  const double two_sqrtpi = 1.128379167095512574;
+  double sum = x, term = x;
+  const double xsqr = xmul(x, x);
+  int j = 1;
+  for (int it = 0; it < kRefIters; it++) {
+    term = xmul(term, xdiv(xsqr, (double)j));
+    sum = xsub(sum, xdiv(term, (double)(2 * j + 1)));
+    ++j;
+    term = xmul(term, xdiv(xsqr, (double)j));
+    sum = xadd(sum, xdiv(term, (double)(2 * j + 1)));
+    ++j;
+    if (!(xdiv(fabs(term), sum) > 1e-12)) break;
+  }
+  return xmul(two_sqrtpi, sum);
+}
+
+// Statistics.cpp:209-227, x >= 2.2: the continued fraction
+__device__ double ref_erfc_cf(double x) {
+  const double one_sqrtpi = 0.564189583547756287;
+  double a = 1, b = x, c = x, d = xadd(xmul(x, x), 0.5), q1, q2 = xdiv(b, d), nn = 1.0, t;
+  for (int it = 0; it < kRefIters; it++) {
+    t = xadd(xmul(a, nn), xmul(b, x));
+    a = b;
+    b = t;
+    t = xadd(xmul(c, nn), xmul(d, x));
+    c = d;
+    d = t;
+    nn = xadd(nn, 0.5);
+    q1 = q2;
+    q2 = xdiv(b, d);
+    if (!(xdiv(fabs(xsub(q1, q2)), q2) > 1e-12)) break;
+  }
+  return xmul(xmul(one_sqrtpi, exp(xmul(-x, x))), q2);
+}
+
+// Statistics.cpp:199-208 erfc
+__device__ double ref_erfc(double x) {
+  if (fabs(x) < 2.2) return xsub(1.0, ref_erf_series(x));
+  if (x < 0) return xsub(2.0, ref_erfc_cf(-x));
+  return ref_erfc_cf(x);
+}
+
+// Statistics.cpp:175-180 erf
+__device__ double ref_erf(double x) {
+  if (fabs(x) > 2.2) return xsub(1.0, ref_erfc(x));
+  return ref_erf_series(x);
+}
+
+// Statistics.cpp:25-41
+__device__ double ref_inv_erf_small(double z) {
+  const double c = 1.1283791670955125738961589;
+  double f = -z, f1 = c;
+  double q = xdiv(f, f1), x = -q, x0 = 0;
+  for (int it = 0; it < kRefIters && fabs(xsub(x, x0)) > 1e-12 && fabs(f) > 1e-14; it++) {
+    x0 = x;
+    f = xsub(ref_erf(x), z);
+    f1 = xmul(c, exp(xmul(-x, x)));
+    q = xdiv(f, f1);
+    x = xsub(x, xmul(q, xsub(1.0, xmul(x, q))));
+  }
+  return x;
+}
+
+// Statistics.cpp:58-64 and :74-95
+__device__ double ref_inv_erfc_small(double z) {
+  const double c = 1.7724538509055160272981675;
+  double f = 1;
+  const double logz = log(xdiv(1.0, xmul(c, z)));
+  const double slz = sqrt(logz);
+  const double a = xsub(slz, xdiv(xmul(0.25, log(logz)), slz));
+  double x = xdiv(ref_erfc(a), xmul(xmul(xmul(c, a), z), z)), x0 = 0;
+  for (int it = 0; it < kRefIters && fabs(xsub(x, x0)) > xmul(1e-12, x) &&
+                   fabs(f) > xmul(1e-15, z);
+       it++) {
+    x0 = x;
+    const double slx = sqrt(log(x));
+    f = xsub(z, ref_erfc(slx));
+    const double f1i = xmul(xmul(xmul(c, x), x), slx);
+    x = xsub(x, xmul(xmul(f, f1i),
+                     xsub(1.0, xmul(xmul(xmul(c, f), x), xadd(slx, xdiv(0.25, slx))))));
+  }
+  return sqrt(log(x));
+}
+
+// Statistics.cpp:115-140 inverf
+__device__ double ref_inverf(double z) {
+  const double az = fabs(z);
+  if (az >= 1) return z == 1 ? (double)INFINITY : (z == -1 ? -(double)INFINITY : (double)NAN);
+  if (az < 0.8125) return ref_inv_erf_small(z);
+  if (z > 0) return ref_inv_erfc_small(xsub(1.0, z));
+  return -ref_inv_erfc_small(xadd(z, 1.0));
+}
+
 // Draws of :438-472 and the momentum sums of :474-478.  Many-body atoms come
 // in pairs (i, i + 1), i even and below n_mb, that share one draw made with
 // the first atom's mass; the sums count a pair once, with that mass, so
@@ -512,10 +618,10 @@ __global__ void k_equi_sample(const md_double4* __restrict__ pos, double* __rest
     const int key = second ? i - 1 : i;
     // many-body atoms exist only without the cell order, so p - 1 is i - 1
     const double m = mass_of((int)pos[second ? p - 1 : p].w, sp);
-    const double sc = sqrt(2.0 * temp / m);
-    const double vx = erfinv(2.0 * equi_uniform(seed, key, 0) - 1.0) * sc;
-    const double vy = erfinv(2.0 * equi_uniform(seed, key, 1) - 1.0) * sc;
-    const double vz = (2.0 * erfinv(equi_uniform(seed, key, 2)) - 1.0) * sc;
+    const double sc = sqrt(xdiv(xmul(2.0, temp), m));
+    const double vx = xmul(ref_inverf(xsub(xmul(2.0, equi_uniform(seed, key, 0)), 1.0)), sc);
+    const double vy = xmul(ref_inverf(xsub(xmul(2.0, equi_uniform(seed, key, 1)), 1.0)), sc);
+    const double vz = xmul(xsub(xmul(2.0, ref_inverf(equi_uniform(seed, key, 2))), 1.0), sc);
     vel[3 * (size_t)p] = vx;
     vel[3 * (size_t)p + 1] = vy;
     vel[3 * (size_t)p + 2] = vz;
@@ -634,15 +740,16 @@ int equi_velocities(const md_double4* pos, double* vel, const int* orig, int n, 
   const double totalm = h[3];
   double cx = h[0] / totalm, cy = h[1] / totalm, cz = h[2] / totalm;
   // :480-515 until every component is within 1e-15.  The pairs' missing
-  // masses make each shift overshoot by the ratio of the second atoms' mass
-  // to totalm: the loop converges slowly while that ratio is below 1 and
-  // never otherwise (the reference then loops forever).  A shift that does
-  // not shrink the largest component ends the loop with an error.
+  // masses leave a residue after the first shift; from then on each shift
+  // scales the remainder by minus the ratio of the second atoms' mass to
+  // totalm: the loop converges while that ratio is below 1 and never
+  // otherwise (the reference then loops forever).  A shift after the second
+  // that does not shrink the largest component ends the loop with an error.
   int it = 0;
   double prev = 1e300;
   while (fabs(cx) > 1.0e-15 || fabs(cy) > 1.0e-15 || fabs(cz) > 1.0e-15) {
     const double big = fmax(fabs(cx), fmax(fabs(cy), fabs(cz)));
-    if (++it > 100000 || !(big < prev)) {
+    if (++it > 100000 || (it > 2 && !(big < prev))) {
       *iterations = it;
       return -1;
     }

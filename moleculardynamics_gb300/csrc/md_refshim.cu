@@ -340,7 +340,10 @@ int* mdgb_build_neighbor_list(const double* pos4, mdgb_list_settings* ls, double
   Grid g = make_grid_reference(box, ls->rs);
   int r = list_build(s.nl, s.pos, n, g, 0, 0.f, (double)ls->rcut, s.sc, s.flags, s.st, err);
   if (r != 0) {
-    g_last = r == -1 ? MD_CELL_OVERFLOW : MD_CUDA_ERROR;
+    if (r == -1)
+      g_last = err.find("non-finite") != std::string::npos ? MD_NONFINITE : MD_CELL_OVERFLOW;
+    else
+      g_last = MD_CUDA_ERROR;
     return nullptr;
   }
   ls->nlistsize = s.nl.nlistsize;

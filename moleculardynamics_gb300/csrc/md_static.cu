@@ -16,7 +16,6 @@
 // keeps the last call's contents, so calls that overlap on the GPU (two
 // streams, two host threads) race on it: serialise them.
 #include <cstring>
-#include <mutex>
 
 #include "../../include/mdgb.h"
 #include "md_forces.h"
@@ -42,11 +41,6 @@ constexpr size_t kStaticBytes = kOffFlags + 256;
 
 static __device__ __align__(256) unsigned char g_static_scratch[kStaticBytes];
 
-// device address of g_static_scratch per device, looked up once per device
-constexpr int kMaxDevices = 64;
-std::mutex g_setup_mutex;
-unsigned char* g_scratch_addr[kMaxDevices] = {nullptr};
-
 // reference rows (i * nlistsize + k, -1 padded) -> ELL slot-major rows
 __global__ void k_static_rows(const int* __restrict__ list, int n, int nlargest, int nls,
                               uint32_t* __restrict__ ell, int* __restrict__ len) {
@@ -70,7 +64,8 @@ void put_err(char* err, int err_len, const char* msg) {
 extern "C" int mdgb_many_body_forces_static(const double* d_pos4, double* d_f3, int n,
                                             int nlargestsize, int nlistsize,
                                             const int* d_list, double rcutsq, int ljexist,
-                                            void* stream, char* err, int err_len) {
+                                            int* d_missing_xi, void* stream, char* err,
+                                            int err_len) {
   if (n < 0 || nlistsize < 0 || nlargestsize < 0 || nlargestsize > nlistsize) {
     put_err(err, err_len, "bad size argument");
     return MD_BAD_ARGUMENT;
@@ -91,27 +86,19 @@ extern "C" int mdgb_many_body_forces_static(const double* d_pos4, double* d_f3, 
             "atom x row-slot pairs (n * nlargestsize)");
     return MD_BAD_ARGUMENT;
   }
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
-    put_err(err, err_len, "no current CUDA device");
-    return MD_NO_DEVICE;
+  // The array's device address on the current device, looked up on every
+  // call: the lookup allocates nothing, and an address kept from an earlier
+  // call would be stale after the application reset the device (the
+  // library's device image is then loaded again, possibly elsewhere).  The
+  // first call on a device also loads that image.
+  void* p = nullptr;
+  cudaError_t e0 = cudaGetSymbolAddress(&p, g_static_scratch);
+  if (e0 != cudaSuccess || !p) {
+    put_err(err, err_len, e0 != cudaSuccess ? cudaGetErrorString(e0) : "no device address");
+    return e0 == cudaErrorNoDevice || e0 == cudaErrorInvalidDevice ? MD_NO_DEVICE
+                                                                     : MD_CUDA_ERROR;
   }
-  unsigned char* base;
-  {
-    // first call on this device: look up the array's device address with the
-    // device current; later calls reuse it
-    std::lock_guard<std::mutex> lock(g_setup_mutex);
-    if (!g_scratch_addr[dev]) {
-      void* p = nullptr;
-      cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
-      if (e != cudaSuccess || !p) {
-        put_err(err, err_len, cudaGetErrorString(e));
-        return MD_CUDA_ERROR;
-      }
-      g_scratch_addr[dev] = (unsigned char*)p;
-    }
-    base = g_scratch_addr[dev];
-  }
+  unsigned char* base = (unsigned char*)p;
   cudaStream_t st = (cudaStream_t)stream;
   int* flags = (int*)(base + kOffFlags);
   // only the missing-xi counter must start at zero; every other part of the
@@ -146,6 +133,14 @@ extern "C" int mdgb_many_body_forces_static(const double* d_pos4, double* d_f3, 
   a.va = base + kOffVa;
   a.missing = flags;
   launch_mb(a, false, false, st);
+  // pass 2's count of xi reads that pass 1 never made (the regular entry
+  // point reports it in its stats): copied on the caller's stream
+  if (d_missing_xi &&
+      cudaMemcpyAsync(d_missing_xi, flags, sizeof(int), cudaMemcpyDeviceToDevice, st) !=
+          cudaSuccess) {
+    put_err(err, err_len, "cudaMemcpyAsync failed");
+    return MD_CUDA_ERROR;
+  }
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {
     put_err(err, err_len, cudaGetErrorString(e));

@@ -67,14 +67,23 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   return ok != 0;
 }
 
-// Bounded wait for phase `parity` of bar.  Returns false (and flags the
-// status word) when the limit runs out.
+// Bounded wait for phase `parity` of bar: at most `limit` polls (a kernel
+// argument; 0 gives up at once).  Returns false (and flags the status word)
+// when the limit runs out.
 constexpr int kWaitLimit = 1 << 20;
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* status) {
-  for (int it = 0; it < kWaitLimit; it++)
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* status,
+                                          int limit = kWaitLimit) {
+  for (int it = 0; it < limit; it++)
     if (mbar_try_wait(bar, parity)) return true;
   atomicOr(status, ST_TMA_TIMEOUT);
   return false;
+}
+
+// After a wait gave up: the copies this block still has in flight land in
+// its shared memory before it leaves.  Always the default limit, whatever
+// limit the failed wait had, so that no copy outlives the block.
+__device__ __forceinline__ bool mbar_drain(uint64_t* bar, uint32_t parity, int* status) {
+  return mbar_wait(bar, parity, status, kWaitLimit);
 }
 
 // L2 prefetch of one box of a tiled tensor map (coordinates as for

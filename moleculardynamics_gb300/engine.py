@@ -109,7 +109,8 @@ EXPORTS = ["md_create", "md_destroy", "md_status_string", "md_last_error", "md_u
            "md_surrogate_report", "md_surrogate_forces", "md_surrogate_descriptors",
            "md_surrogate_params", "md_surrogate_normalisation", "md_surrogate_loss_grad",
            "md_surrogate_net", "md_surrogate_train_forces", "md_surrogate_force_grad",
-           "md_surrogate_desc_directional"]
+           "md_surrogate_desc_directional", "md_set_wait_limit", "md_measure_arith_peaks",
+           "md_device_sm_count"]
 
 
 def load(path: str | None = None) -> C.CDLL:
@@ -147,6 +148,9 @@ def load(path: str | None = None) -> C.CDLL:
     L.md_synchronize.argtypes = [C.c_void_p]
     L.md_autotune.argtypes = [C.c_void_p, C.c_int, P(MdTuneResult)]
     L.md_set_graphs.argtypes = [C.c_void_p, C.c_int]
+    L.md_set_wait_limit.argtypes = [C.c_void_p, C.c_int]
+    L.md_measure_arith_peaks.argtypes = [C.c_int, P(C.c_double), P(C.c_double)]
+    L.md_device_sm_count.argtypes = [C.c_int, P(C.c_int)]
     L.mdgb_tc_selftest.argtypes = [_fp, _fp, _fp, C.c_int, C.c_int]
     L.mdgb_conv_selftest.argtypes = [_fp, _dp, C.c_int, _dp, _dp, _fp, _fp]
     L.md_surrogate_create.argtypes = [C.c_int, C.c_ulonglong, C.c_float, P(C.c_void_p)]
@@ -190,7 +194,7 @@ def load(path: str | None = None) -> C.CDLL:
     L.mdgb_many_body_forces_static.restype = C.c_int
     L.mdgb_many_body_forces_static.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int,
                                                C.c_int, C.c_void_p, C.c_double, C.c_int,
-                                               C.c_void_p, C.c_char_p, C.c_int]
+                                               C.c_void_p, C.c_void_p, C.c_char_p, C.c_int]
     L.mdgb_last_status.restype = C.c_int
     L.md_read_config.argtypes = [C.c_char_p, P(MdConfig), C.c_char_p, P(C.c_double),
                                  C.c_char_p, C.c_int]
@@ -341,6 +345,9 @@ class Engine:
 
     def synchronize(self):
         self._ck(self.lib.md_synchronize(self.h), "md_synchronize")
+
+    def set_wait_limit(self, tries: int):
+        self._ck(self.lib.md_set_wait_limit(self.h, int(tries)), "md_set_wait_limit")
 
     def set_graphs(self, on: bool):
         self._ck(self.lib.md_set_graphs(self.h, int(on)), "md_set_graphs")
@@ -699,3 +706,22 @@ def read_config(path: str):
     extras = dict(zip(["Temperature", "VXCMFROM", "VXCMTO", "VXCMSTEP", "CUDA Blocks",
                        "AnimationTimesteps"], list(extra)))
     return cfg, strings, extras
+
+
+def measure_arith_peaks(device: int = 0) -> dict:
+    """FP64 and FP32 FMA-chain rates of the device (GFLOP/s, FMA = 2)."""
+    lib = load()
+    f64, f32 = C.c_double(), C.c_double()
+    s = lib.md_measure_arith_peaks(device, C.byref(f64), C.byref(f32))
+    if s != 0:
+        raise EngineError(s, "md_measure_arith_peaks")
+    return {"fp64_gflops": f64.value, "fp32_gflops": f32.value}
+
+
+def device_sm_count(device: int = 0) -> int:
+    lib = load()
+    n = C.c_int()
+    s = lib.md_device_sm_count(device, C.byref(n))
+    if s != 0:
+        raise EngineError(s, "md_device_sm_count")
+    return n.value

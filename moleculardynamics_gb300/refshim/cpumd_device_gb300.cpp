@@ -82,17 +82,41 @@ int* buildNeighborList(real4* posArray, listSettings* listsettings, real boxSize
   return list;
 }
 
-// common/NeighborList.cpp:161: the GPU build needs no bucket hash; kept so
-// that code calling it still links.  Returns the first-hash bucket index.
+// common/NeighborList.cpp:161-207 computeBucket, for code that calls it
+// directly (the GPU build itself keeps cells in its own table and never
+// calls it).  Same open-addressing scheme and results: the first hash
+// H1 cx + H2 cy + H3 cz, on a collision the second hash H1 cx ^ H2 cy ^ H3 cz
+// followed by a linear probe; pop = true looks a cell up (-1 if absent),
+// pop = false claims its bucket.  The products keep the reference's C
+// integer types: H1 does not fit an int, so H1 * c is a 64-bit product, while
+// H2 * c and H3 * c are int products that wrap; the combined value is
+// truncated to int before the modulo.
+namespace {
+long long ref_hash_term(long long h, int c) {
+  if (h > 0x7fffffffLL) return h * (long long)c;  // long operand: 64-bit product
+  return (long long)(int)((unsigned)h * (unsigned)c);  // int product, wrapped
+}
+int ref_bucket_mod(long long v, int buckets) {
+  int n = (int)(unsigned)(unsigned long long)v;  // int n = <long expression>
+  n %= buckets;
+  return n < 0 ? n + buckets : n;
+}
+bool cell_is(const int3& b, int cx, int cy, int cz) {
+  return b.x == cx && b.y == cy && b.z == cz;
+}
+}  // namespace
+
 int computeBucket(int cx, int cy, int cz, int3* bucketlist, int buckets, bool pop) {
-  int n = (int)((long long)H1 * cx + (long long)H2 * cy + (long long)H3 * cz);
-  n = n % buckets;
-  if (n < 0) n += buckets;
+  const long long t1 = ref_hash_term(H1, cx), t2 = ref_hash_term(H2, cy),
+                  t3 = ref_hash_term(H3, cz);
+  int n = ref_bucket_mod(t1 + t2 + t3, buckets);
   if (pop && bucketlist[n].x == -1) return -1;
-  if (!pop) {
-    bucketlist[n].x = cx;
-    bucketlist[n].y = cy;
-    bucketlist[n].z = cz;
+  if (bucketlist[n].x != -1 && !cell_is(bucketlist[n], cx, cy, cz)) {
+    // taken by another cell: second hash, then the next free or matching bucket
+    n = ref_bucket_mod(t1 ^ t2 ^ t3, buckets);
+    if (pop && bucketlist[n].x == -1) return -1;
+    while (bucketlist[n].x != -1 && !cell_is(bucketlist[n], cx, cy, cz)) n = (n + 1) % buckets;
   }
+  if (!pop) bucketlist[n] = int3{cx, cy, cz};
   return n;
 }

@@ -1,7 +1,8 @@
 #!/usr/bin/env bash
 # Builds the reference CPU engine of vakuras/moleculardynamics IN PLACE from
-# its own sources (read-only tree given as $1, default /root/reference) into
-# oracle/_ref/.  Test infrastructure only: nothing here is shipped or timed as
+# its own sources (read-only tree given as the required argument $1) into
+# oracle/_ref/; the tree's location is recorded in oracle/_ref/source_root for
+# the tests that compile reference files themselves.  Test infrastructure only: nothing here is shipped or timed as
 # the product.
 #
 # The reference is Visual Studio 2008 code.  It compiles with g++ unmodified
@@ -22,7 +23,11 @@
 # runs of hostMain.  Precision: real = double (-DEQUI), which is how cpumd is
 # configured in cpu/cpumd/cpumd.vcproj:46.
 set -euo pipefail
-REF=${1:-/root/reference}
+if [ $# -lt 1 ]; then
+  echo "usage: build_ref.sh <reference source tree>" >&2
+  exit 2
+fi
+REF=$1
 HERE=$(cd "$(dirname "$0")" && pwd)
 OUT="$HERE/_ref"
 SHIM="$OUT/shim"
@@ -31,6 +36,7 @@ if [ ! -f "$REF/common/NeighborList.cpp" ]; then
   exit 2
 fi
 mkdir -p "$SHIM"
+printf '%s\n' "$REF" > "$OUT/source_root"
 
 cat > "$SHIM/windows.h" <<'EOF'
 #pragma once
@@ -92,6 +98,48 @@ build_variant() {  # build_variant <name> <extra flags>
   for o in $objs; do case "$o" in *ref_harness.o) ;; *) progobjs="$progobjs $o";; esac; done
   $CXX -o "$OUT/cpumd_$name" $progobjs "$obj/Main.o"
 }
+# equi (cpu/equi/Host.cpp, Statistics.cpp) for chooseVelocities and inverf.
+# Two more shims, force-included into those two files only:
+#   - RAND_MAX is the value of the platform the reference was written for
+#     (Visual C++: 0x7fff).  With glibc's 2^31 - 1, MD_RANDMAX = RAND_MAX + 2
+#     (cpu/equi/Host.h:26) overflows int and every draw comes out negative.
+#   - rand() replays a stream of draws the test supplies
+#     (ref_equi_harness.cpp), instead of the clock-seeded stream of :83.
+# <cfloat> is included for DBL_MAX (Statistics.cpp:121), which the Visual C++
+# headers provided indirectly.  -fno-builtin keeps the compiler from treating
+# the reference's own erf/erfc (Statistics.cpp:175-227) as the library's, and
+# -Bsymbolic binds the library's calls to them rather than to libm's.
+{
+  echo '#pragma once'
+  echo '#include <cstdlib>'
+  echo '#include <cfloat>'
+  echo '#undef RAND_MAX'
+  echo '#define RAND_MAX 0x7fff'
+  echo 'extern "C" int mdref_replay_rand(void);'
+  echo '#define rand() mdref_replay_rand()'
+} > "$SHIM/equi_shim.h"
+build_equi() {  # build_equi <name> <extra flags>
+  local name=$1; shift
+  local obj="$OUT/obj_$name"
+  local objs=""
+  for s in "$REF/cpu/equi/Host.cpp" "$REF/cpu/equi/Statistics.cpp"; do
+    local o="$obj/equi_$(basename "${s%.*}").o"
+    $CXX $FLAGS -fno-builtin -include "$SHIM/equi_shim.h" "$@" -c "$s" -o "$o" &
+    objs="$objs $o"
+  done
+  $CXX $FLAGS "$@" -c "$HERE/ref_equi_harness.cpp" -o "$obj/ref_equi_harness.o" &
+  wait
+  local common=""
+  for s in $SRCS; do
+    case "$s" in *cpumd/Host.cpp) ;; *) common="$common $obj/$(basename "${s%.*}").o";; esac
+  done
+  $CXX -shared -Wl,-Bsymbolic -o "$OUT/libmdref_equi_$name.so" $objs \
+      "$obj/ref_equi_harness.o" $common
+}
+
 build_variant neon
 build_variant argon -include "$HERE/argon_constants.h"
-echo "built $OUT/libmdref_neon.so $OUT/libmdref_argon.so $OUT/cpumd_neon $OUT/cpumd_argon"
+build_equi neon
+build_equi argon -include "$HERE/argon_constants.h"
+echo "built $OUT/libmdref_neon.so $OUT/libmdref_argon.so $OUT/cpumd_neon $OUT/cpumd_argon" \
+     "$OUT/libmdref_equi_neon.so $OUT/libmdref_equi_argon.so"

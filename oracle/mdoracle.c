@@ -1068,3 +1068,193 @@ int orc_run(const orc_run_params* p, double* pos4, double* vel3, double* acc3, d
   orc_free_list(mbl);
   return nrec;
 }
+
+/* ---- equi: the reference's inverse error function and velocity draw ---- */
+
+/* cpu/equi/Statistics.cpp:175-196 erf: the Taylor series for |x| <= 2.2 with
+ * the reference's stopping test |term| / sum > 1e-12.  For x < 0 the sum is
+ * negative, the test fails at once and the series stops after its first two
+ * terms: the reference's erf, and so its inverf, is inaccurate for negative
+ * arguments; that is kept.  Beyond 2.2, 1 - erfc(x). */
+static double ref_erfc(double x);
+static double ref_erf(double x) {
+  const double two_sqrtpi = 1.128379167095512574;
+  if (fabs(x) > 2.2) return 1.0 - ref_erfc(x);
+  double sum = x, term = x, xsqr = x * x;
+  int j = 1;
+  do {
+    term *= xsqr / j;
+    sum -= term / (2 * j + 1);
+    ++j;
+    term *= xsqr / j;
+    sum += term / (2 * j + 1);
+    ++j;
+  } while (fabs(term) / sum > 1e-12);
+  return two_sqrtpi * sum;
+}
+
+/* Statistics.cpp:199-227 erfc: 1 - erf(x) for |x| < 2.2, 2 - erfc(-x) for
+ * x < 0, else the continued fraction until two convergents agree to 1e-12. */
+static double ref_erfc(double x) {
+  const double one_sqrtpi = 0.564189583547756287;
+  if (fabs(x) < 2.2) return 1.0 - ref_erf(x);
+  if (x < 0) return 2.0 - ref_erfc(-x);
+  double a = 1, b = x, c = x, d = x * x + 0.5, q1, q2 = b / d, nn = 1.0, t;
+  do {
+    t = a * nn + b * x;
+    a = b;
+    b = t;
+    t = c * nn + d * x;
+    c = d;
+    d = t;
+    nn += 0.5;
+    q1 = q2;
+    q2 = b / d;
+  } while (fabs(q1 - q2) / q2 > 1e-12);
+  return one_sqrtpi * exp(-x * x) * q2;
+}
+
+/* Statistics.cpp:25-41: second-order Newton steps on erf(x) - z from x = 0 */
+static double inv_erf_small(double z) {
+  const double c = 1.1283791670955125738961589; /* 2 / sqrt(pi) */
+  double f = -z, f1 = c;
+  double q = f / f1, x = -q, x0 = 0;
+  while (fabs(x - x0) > 1e-12 && fabs(f) > 1e-14) {
+    x0 = x;
+    f = ref_erf(x) - z;
+    f1 = c * exp(-x * x);
+    q = f / f1;
+    x -= q * (1 - x * q);
+  }
+  return x;
+}
+
+/* Statistics.cpp:58-64: the start value of inv_erfc_small */
+static double lambert_w2(double z) {
+  double logz = log(z);
+  double slz = sqrt(logz);
+  return slz - 0.25 * log(logz) / slz;
+}
+
+/* Statistics.cpp:74-95: Newton steps on erfc(sqrt(log(x))) - z */
+static double inv_erfc_small(double z) {
+  const double c = 1.7724538509055160272981675; /* sqrt(pi) */
+  double f = 1, f1i = 0;
+  double a = lambert_w2(1 / (c * z));
+  double x = ref_erfc(a) / (c * a * z * z), x0 = 0;
+  while (fabs(x - x0) > 1e-12 * x && fabs(f) > 1e-15 * z) {
+    double slx;
+    x0 = x;
+    slx = sqrt(log(x));
+    f = z - ref_erfc(slx);
+    f1i = c * x * x * slx;
+    x -= f * f1i * (1 - c * f * x * (slx + 0.25 / slx));
+  }
+  return sqrt(log(x));
+}
+
+/* cpu/equi/Statistics.cpp:115-140 inverf */
+double orc_inverf(double z) {
+  double az = fabs(z);
+  if (az >= 1) {
+    if (z == 1) return INFINITY;
+    if (z == -1) return -INFINITY;
+    return NAN;
+  }
+  if (az < 0.8125) return inv_erf_small(z);
+  if (z > 0) return inv_erfc_small(1 - z);
+  return -inv_erfc_small(z + 1);
+}
+
+/* cpu/equi/Host.cpp:416-572 chooseVelocities, with the uniforms y of
+ * (rand() + 1) / MD_RANDMAX given (three per draw: x, y, z, in the
+ * reference's order).  Many-body atoms i, i + 1 (i < n_mb) share one draw
+ * made with atom i's mass, and the sums before the momentum removal count
+ * such a pair once (:465-478); the z draw applies inverf before the affine
+ * map (:457-461).  The removal loop (:480-515) is the reference's; where a
+ * shift after the second does not shrink the largest momentum component (the
+ * reference would loop forever) or max_shifts are spent, returns -1.  Returns the number of
+ * uniforms used. */
+long orc_choose_velocities(const double* pos4, double* vel3, int n, int n_mb, double temp,
+                           int species, const double* u, long nu, long max_shifts,
+                           long* shifts) {
+  orc_species sp;
+  orc_species_get(species, &sp);
+  const double mass_of[3] = {sp.mN, sp.mO, sp.mNG};
+  double cmvx = 0, cmvy = 0, cmvz = 0, totalm = 0, t = 0;
+  long k = 0;
+  for (int i = 0; i < n; i++) {
+    double mass = mass_of[(int)pos4[4 * i + 3]];
+    double y = k < nu ? u[k] : 0;
+    k++;
+    y = 2.0 * y - 1.0;
+    y = orc_inverf(y);
+    vel3[3 * i] = y * sqrt(2.0 * temp / mass);
+    y = k < nu ? u[k] : 0;
+    k++;
+    y = 2.0 * y - 1.0;
+    y = orc_inverf(y);
+    vel3[3 * i + 1] = y * sqrt(2.0 * temp / mass);
+    y = k < nu ? u[k] : 0;
+    k++;
+    y = orc_inverf(y);
+    y = 2.0 * y - 1.0;
+    vel3[3 * i + 2] = y * sqrt(2.0 * temp / mass);
+    if (i < n_mb) {
+      vel3[3 * (i + 1)] = vel3[3 * i];
+      vel3[3 * (i + 1) + 1] = vel3[3 * i + 1];
+      vel3[3 * (i + 1) + 2] = vel3[3 * i + 2];
+      i++;
+    }
+    cmvx = cmvx + mass * vel3[3 * i];
+    cmvy = cmvy + mass * vel3[3 * i + 1];
+    cmvz = cmvz + mass * vel3[3 * i + 2];
+    totalm += mass;
+  }
+  cmvx = cmvx / totalm;
+  cmvy = cmvy / totalm;
+  cmvz = cmvz / totalm;
+  long s = 0;
+  double prev = INFINITY;
+  while ((fabs(cmvx) > 1.0e-15) || (fabs(cmvy) > 1.0e-15) || (fabs(cmvz) > 1.0e-15)) {
+    double big = fmax(fabs(cmvx), fmax(fabs(cmvy), fabs(cmvz)));
+    /* the first shift leaves the pairs' residue; from the second on each
+       shift scales the remainder by minus (second atoms' mass) / totalm */
+    if (++s > max_shifts || (s > 2 && !(big < prev))) {
+      if (shifts) *shifts = s;
+      return -1;
+    }
+    prev = big;
+    for (int i = 0; i < n; i++) {
+      vel3[3 * i] = vel3[3 * i] - cmvx;
+      vel3[3 * i + 1] = vel3[3 * i + 1] - cmvy;
+      vel3[3 * i + 2] = vel3[3 * i + 2] - cmvz;
+    }
+    cmvx = 0.0;
+    cmvy = 0.0;
+    cmvz = 0.0;
+    for (int i = 0; i < n; i++) {
+      double mass = mass_of[(int)pos4[4 * i + 3]];
+      cmvx = cmvx + vel3[3 * i] * mass;
+      cmvy = cmvy + vel3[3 * i + 1] * mass;
+      cmvz = cmvz + vel3[3 * i + 2] * mass;
+    }
+    cmvx = cmvx / totalm;
+    cmvy = cmvy / totalm;
+    cmvz = cmvz / totalm;
+  }
+  for (int i = 0; i < n; i++) {
+    double mass = mass_of[(int)pos4[4 * i + 3]];
+    t += mass * (vel3[3 * i] * vel3[3 * i] + vel3[3 * i + 1] * vel3[3 * i + 1] +
+                 vel3[3 * i + 2] * vel3[3 * i + 2]);
+  }
+  t = t / (3.0 * (double)n);
+  double scalev = sqrt(temp / t);
+  for (int i = 0; i < n; i++) {
+    vel3[3 * i] = vel3[3 * i] * scalev;
+    vel3[3 * i + 1] = vel3[3 * i + 1] * scalev;
+    vel3[3 * i + 2] = vel3[3 * i + 2] * scalev;
+  }
+  if (shifts) *shifts = s;
+  return k;
+}

@@ -104,6 +104,15 @@ int orc_run(const orc_run_params* p, double* pos4, double* vel3, double* acc3, d
 
 int orc_max_threads(void);
 
+/* cpu/equi/Statistics.cpp:115-140 inverf, with the file's own erf/erfc */
+double orc_inverf(double z);
+/* cpu/equi/Host.cpp:416-572 chooseVelocities with the uniforms given (three
+ * per draw); returns the uniforms used, or -1 where the momentum removal does
+ * not converge */
+long orc_choose_velocities(const double* pos4, double* vel3, int n, int n_mb, double temp,
+                           int species, const double* u, long nu, long max_shifts,
+                           long* shifts);
+
 #ifdef __cplusplus
 }
 #endif

@@ -51,9 +51,25 @@ def build_oracle(force: bool = False) -> str:
     return ORACLE_SO
 
 
-def build_reference(ref_root: str = "/root/reference") -> bool:
-    """Build oracle/_ref from the reference sources when they are present."""
-    if not os.path.isfile(os.path.join(ref_root, "common", "NeighborList.cpp")):
+def reference_source_root() -> str | None:
+    """Where oracle/_ref was built from (recorded by build_ref.sh), or the
+    MDGB_REFERENCE_SRC environment variable; None when neither is set."""
+    env = os.environ.get("MDGB_REFERENCE_SRC")
+    if env:
+        return env
+    rec = os.path.join(HERE, "_ref", "source_root")
+    if os.path.isfile(rec):
+        with open(rec) as f:
+            return f.read().strip() or None
+    return None
+
+
+def build_reference(ref_root: str | None = None) -> bool:
+    """Build oracle/_ref from the reference sources at ref_root (default: the
+    MDGB_REFERENCE_SRC environment variable or the recorded tree); False when
+    they are not present."""
+    ref_root = ref_root or reference_source_root()
+    if not ref_root or not os.path.isfile(os.path.join(ref_root, "common", "NeighborList.cpp")):
         return False
     subprocess.run(["bash", os.path.join(HERE, "build_ref.sh"), ref_root], check=True,
                    capture_output=True)
@@ -117,6 +133,11 @@ class Oracle:
         L.orc_ready_list.argtypes = [_dp, _dp, C.c_int, C.POINTER(C.c_double),
                                      C.POINTER(C.c_double)]
         L.orc_next_build.argtypes = [C.c_float, C.c_double, C.c_double, C.c_int]
+        L.orc_inverf.restype = C.c_double
+        L.orc_inverf.argtypes = [C.c_double]
+        L.orc_choose_velocities.restype = C.c_long
+        L.orc_choose_velocities.argtypes = [_dp, _dp, C.c_int, C.c_int, C.c_double, C.c_int,
+                                            _dp, C.c_long, C.c_long, C.POINTER(C.c_long)]
         L.orc_next_build.restype = C.c_int
         L.orc_list_settings.argtypes = [C.c_float, C.c_float] + [C.POINTER(C.c_float)] * 3
         L.orc_run.argtypes = [C.POINTER(OrcRunParams), _dp, _dp, _dp, _dp, _dp, _dp,
@@ -234,6 +255,63 @@ class Oracle:
 
     def max_threads(self) -> int:
         return self.lib.orc_max_threads()
+
+
+def _oracle_inverf(self, z: float) -> float:
+    """cpu/equi/Statistics.cpp:115-140 inverf (mdoracle.c restatement)."""
+    return self.lib.orc_inverf(float(z))
+
+
+def _oracle_choose_velocities(self, pos4, n_mb: int, temp: float, species: int, u,
+                              max_shifts: int = 100000):
+    """cpu/equi/Host.cpp:416-572 with the uniforms u given: (vel, uniforms
+    used, shifts); vel is None where the momentum removal does not converge."""
+    pos4 = np.ascontiguousarray(pos4, np.float64)
+    u = np.ascontiguousarray(u, np.float64)
+    vel = np.zeros((len(pos4), 3))
+    sh = C.c_long()
+    k = self.lib.orc_choose_velocities(pos4, vel, len(pos4), n_mb, temp, species, u, len(u),
+                                       max_shifts, C.byref(sh))
+    return (None if k < 0 else vel), k, sh.value
+
+
+Oracle.inverf = _oracle_inverf
+Oracle.choose_velocities = _oracle_choose_velocities
+
+
+class ReferenceEqui:
+    """The reference's equi velocity draw compiled in place
+    (oracle/_ref/libmdref_equi_<variant>.so), rand() replaying given draws."""
+
+    def __init__(self, path: str):
+        self.lib = C.CDLL(path)
+        L = self.lib
+        L.ref_equi_inverf.restype = C.c_double
+        L.ref_equi_inverf.argtypes = [C.c_double]
+        L.ref_equi_choose_velocities.restype = C.c_long
+        L.ref_equi_choose_velocities.argtypes = [_dp, _dp, C.c_int, C.c_int, C.c_double, _ip,
+                                                 C.c_long]
+
+    def inverf(self, z: float) -> float:
+        return self.lib.ref_equi_inverf(float(z))
+
+    def choose_velocities(self, pos4, n_lj: int, n_mb: int, temp: float, draws):
+        """(vel, draws used); draws are rand() values in [0, 0x7fff]."""
+        pos4 = np.ascontiguousarray(pos4, np.float64)
+        draws = np.ascontiguousarray(draws, np.int32)
+        vel = np.zeros((len(pos4), 3))
+        k = self.lib.ref_equi_choose_velocities(pos4, vel, n_lj, n_mb, temp, draws, len(draws))
+        return vel, k
+
+
+def load_reference_equi(variant: str = "argon") -> ReferenceEqui | None:
+    path = os.path.join(REF_DIR, f"libmdref_equi_{variant}.so")
+    if not os.path.exists(path):
+        return None
+    try:
+        return ReferenceEqui(path)
+    except OSError:
+        return None
 
 
 class Reference:

@@ -1,9 +1,13 @@
 """equi's initial velocities on the device (md_choose_velocities) against the
-CPU restatement (oracle/equi_ref.py, same counter-based generator):
+C restatement of the reference (oracle/mdoracle.c orc_choose_velocities,
+bit-exact to the reference compiled in place: tests/test_equi_pinned.py), fed
+the device generator's uniforms (oracle/equi_ref.py):
 
 * argon systems in both precisions (the cluster path stores atoms in cell
   order; the draws follow the caller's numbering): velocities within 1e-12
-  relative (CUDA erfinv against scipy's, parallel against sequential sums);
+  relative.  The device runs the reference's inverf step for step (its own
+  erf/erfc series, no FMA contraction); what differs is CUDA's exp, log and
+  sqrt against the host's, and parallel against sequential momentum sums;
 * a many-body + LJ system: the N-O pairs share one draw, the momentum sums
   count a pair once, and the result matches the restatement;
 * pure many-body systems: O-N pairs only match the restatement; O-N and
