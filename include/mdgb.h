@@ -70,7 +70,11 @@ typedef struct md_config {
   int species;             /* MD_SPECIES_NEON (reference table) or _ARGON (NG = argon) */
   int device;              /* CUDA device ordinal */
   int reference_energy;    /* 1: records use the reference's all-pairs energy
-                              (DebugCalculations.cpp:129-270, O(N^2)/O(N^3)) */
+                              (DebugCalculations.cpp:129-270, O(N^2)/O(N^3));
+                              2: the same, and every record quantity summed in the
+                              reference's order by one device thread (records
+                              bit-identical to the reference's for LJ systems; for
+                              small systems) */
   int lj_kernel;           /* MD_LJ_AUTO, MD_LJ_ROWS or MD_LJ_CLUSTER (precision form) */
   int cluster_cells;       /* cells per segment of the cluster kernel (0: default) */
   int cluster_threads;     /* threads per segment block (0: default; multiple of 32, <= 224) */

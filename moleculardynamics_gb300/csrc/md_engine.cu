@@ -68,6 +68,7 @@ int next_build(float maxnlmove, double vmax, double dt, int t) {
 }
 
 constexpr int kKernels = 8;  // timing ids of md_kernel_time
+constexpr long long kSeqTerms = 1LL << 21;  // pair terms per chunk of an in-order record
 
 __global__ void k_begin(md_double4* pos, double* vel, int n, double half_box, int clamp,
                         double vxcm) {
@@ -142,6 +143,7 @@ struct md_ctx {
   // flags and reductions
   int* status = nullptr;
   int wait_limit = 1 << 20;  // polls of a bounded mbarrier wait (md_set_wait_limit)
+  double* seq_buf = nullptr;  // pair terms of records in the reference's order (2 x kSeqTerms)
   int* wall_flag = nullptr;
   int* missing = nullptr;
   Scratch sc;
@@ -593,14 +595,30 @@ md_status rebuild(md_ctx* c, int t) {
   return MD_OK;
 }
 
+}  // namespace
+extern "C" md_status ensure_inv(md_ctx* c);
+namespace {
+
 // thermo + energies of the current state into a 16-double record at rec16
 md_status make_record(md_ctx* c, int t, double* rec16) {
   double* th8 = c->dsc;
   double* elj = c->dsc + 8;
   double* emb = c->dsc + 11;
   double* ref = c->dsc + 14;
-  launch_thermo(c->pos, c->vel, c->n, c->sp, c->sc.dpart, th8, c->st);
-  c->stats.launches += 5;
+  const bool seq = c->cfg.reference_energy == 2;  // the reference's summation order
+  const int* inv = nullptr;
+  if (seq && c->permuted()) {
+    md_status s = ensure_inv(c);
+    if (s != MD_OK) return s;
+    inv = c->inv;
+  }
+  if (seq) {
+    launch_thermo_seq(c->pos, c->vel, inv, c->n, c->sp, th8, c->st);
+    c->stats.launches += 1;
+  } else {
+    launch_thermo(c->pos, c->vel, c->n, c->sp, c->sc.dpart, th8, c->st);
+    c->stats.launches += 5;
+  }
   CK(cudaMemsetAsync(elj, 0, sizeof(double) * 8, c->st), "record");
   if (c->cfg.use_lj) {
     int B = c->cluster ? cluster_blocks(c->cl) : lj_blocks(c->n);
@@ -625,7 +643,12 @@ md_status make_record(md_ctx* c, int t, double* rec16) {
     launch_sum_partials(a.epart2, B, 1, emb + 2, c->st);
     c->stats.launches += 5;
   }
-  if (c->cfg.reference_energy) {
+  if (seq) {
+    if (!c->seq_buf) CK(cudaMalloc(&c->seq_buf, sizeof(double) * 2 * (size_t)kSeqTerms),
+                        "record terms");
+    c->stats.launches +=
+        launch_ref_potential_seq(c->pos, inv, c->n, c->sp, c->seq_buf, kSeqTerms, ref, c->st);
+  } else if (c->cfg.reference_energy) {
     md_status s = ensure_epart(c, 2LL * c->n);
     if (s != MD_OK) return s;
     launch_ref_potential(c->pos, c->n, c->sp, c->epart, ref, c->st);
@@ -1050,7 +1073,7 @@ void md_destroy(md_ctx* c) {
   cluster_free(c->cl);
   for (cudaGraphExec_t x : c->gexec)
     if (x) cudaGraphExecDestroy(x);
-  void* ptrs[] = {c->inv, c->sur_fx, c->sur_fs, c->rep_ranges, c->rep_buf, c->io, c->pos_alt, c->posf_alt, c->pos, c->vel, c->acc, c->b, c->c, c->f3, c->f3_tmp, c->posf, c->mb_sl,
+  void* ptrs[] = {c->seq_buf, c->inv, c->sur_fx, c->sur_fs, c->rep_ranges, c->rep_buf, c->io, c->pos_alt, c->posf_alt, c->pos, c->vel, c->acc, c->b, c->c, c->f3, c->f3_tmp, c->posf, c->mb_sl,
                   c->mb_slen, c->xsi, c->xsj, c->va, c->status, c->epart, c->dsc, c->rec,
                   c->sc.dpart, c->sc.umax, c->sc.counts, c->sc.block_sums};
   for (void* p : ptrs)

@@ -6,6 +6,7 @@
 // returns the same bits as the reference on the same forces.  Reductions are
 // deterministic: per-block partials in a fixed grid, then one block that sums
 // them in a fixed order.
+#include <algorithm>
 #include <cmath>
 
 #include "mdgb.h"
@@ -392,6 +393,135 @@ __global__ void k_ref_potential(const md_double4* __restrict__ pos, int n, Speci
     for (int w = 0; w < (int)(blockDim.x >> 5); w++) s += sm[threadIdx.x][w];
     part[2 * i + threadIdx.x] = s;
   }
+}
+
+// ---- records in the reference's summation order ----
+// PerformCalculations (common/DebugCalculations.cpp:46-124) by one thread,
+// atom after atom in the caller's numbering (inv: caller index -> stored
+// position, NULL when stored in it), every product and sum rounded on its
+// own: the reference's bits.  Output as k_thermo_final.
+__global__ void k_thermo_seq(const md_double4* __restrict__ pos, const double* __restrict__ vel,
+                             const int* __restrict__ inv, int n, Species sp, double* out) {
+  if (threadIdx.x || blockIdx.x) return;
+  double mass = 0, cmvx = 0, cmvy = 0, cmvz = 0, total = 0, ke = 0, temp = 0;
+  double cx = 0, cy = 0, cz = 0;
+  for (int i = 0; i < n; i++) {
+    const int p = inv ? inv[i] : i;
+    const md_double4 r = pos[p];
+    const int t = (int)r.w;
+    // :65-76, a switch without a default: another type keeps the last mass
+    if (t == SP_N || t == SP_O || t == SP_NG) mass = (double)sp.mass[t];
+    const double vx = vel[3 * (size_t)p], vy = vel[3 * (size_t)p + 1],
+                 vz = vel[3 * (size_t)p + 2];
+    ke = xadd(ke, xmul(mass, xadd(xadd(xmul(vx, vx), xmul(vy, vy)), xmul(vz, vz))));
+    cmvx = xadd(cmvx, xmul(mass, vx));
+    cmvy = xadd(cmvy, xmul(mass, vy));
+    cmvz = xadd(cmvz, xmul(mass, vz));
+    total = xadd(total, mass);
+    cx = xadd(cx, xmul(mass, r.x));
+    cy = xadd(cy, xmul(mass, r.y));
+    cz = xadd(cz, xmul(mass, r.z));
+  }
+  out[0] = xdiv(cx, total);
+  out[1] = xdiv(cy, total);
+  out[2] = xdiv(cz, total);
+  out[4] = cmvx;
+  out[5] = cmvy;
+  out[6] = cmvz;
+  cmvx = xdiv(cmvx, total);
+  cmvy = xdiv(cmvy, total);
+  cmvz = xdiv(cmvz, total);
+  for (int i = 0; i < n; i++) {
+    const int p = inv ? inv[i] : i;
+    const int t = (int)pos[p].w;
+    const double m = (double)sp.mass[t == SP_N ? SP_N : (t == SP_O ? SP_O : SP_NG)];
+    const double dx = xsub(vel[3 * (size_t)p], cmvx), dy = xsub(vel[3 * (size_t)p + 1], cmvy),
+                 dz = xsub(vel[3 * (size_t)p + 2], cmvz);
+    temp = xadd(temp, xmul(m, xadd(xadd(xmul(dx, dx), xmul(dy, dy)), xmul(dz, dz))));
+  }
+  out[7] = xdiv(temp, xmul(xmul(3.0, (double)n), (double)MD_KB));
+  out[3] = xdiv(ke, 2.0);
+}
+
+// The terms of calculatePotentional (common/DebugCalculations.cpp:129-270)
+// for the ordered pairs (i, j) of rows [row0, row0 + rows), j fastest, in
+// the caller's numbering: the LJ term with every rounding of the reference
+// (so an LJ system's sum is bit-identical), the bond-order term as
+// k_ref_potential computes it; 0 where the reference adds nothing (i = j,
+// a pair of the other kind, beyond CUTOFF_RIJ), which leaves a running sum
+// unchanged.
+__global__ void k_ref_terms(const md_double4* __restrict__ pos, const int* __restrict__ inv,
+                            int n, Species sp, int row0, int rows, double* __restrict__ tlj,
+                            double* __restrict__ tmb) {
+  const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= (long long)rows * n) return;
+  const int i = row0 + (int)(k / n), j = (int)(k % n);
+  double elj = 0.0, emb = 0.0;
+  if (i != j) {
+    const md_double4 pi = pos[inv ? inv[i] : i], pj = pos[inv ? inv[j] : j];
+    const int ti = (int)pi.w, tj = (int)pj.w;
+    const double ijx = xsub(pi.x, pj.x), ijy = xsub(pi.y, pj.y), ijz = xsub(pi.z, pj.z);
+    const double rijsq = norm2_exact(ijx, ijy, ijz);
+    if (tj == SP_NG || ti == SP_NG) {
+      const int sel = lj_select(ti, tj);
+      const double sig = sp.sig[sel], eps = sp.eps[sel];
+      const double sr2 = xdiv(xmul(sig, sig), rijsq);
+      const double sr6 = xmul(xmul(sr2, sr2), sr2);
+      elj = xmul(xmul(2.0, eps), xsub(xmul(sr6, sr6), sr6));
+    } else {
+      const double rij = sqrt(rijsq);
+      if (!(rij > MD_CUTOFF_RIJ)) {
+        double va = 0, dva, vr = 0, dvr, vdw, dvdw, bo = 0, fcut, dfcut;
+        cutoff<double>(rij / 10, fcut, dfcut);
+        if (fcut > 0) {
+          const double de = get_de<double>(ti, tj), re = get_re<double>(ti, tj),
+                       beta = get_beta<double>(ti, tj);
+          attractive<double>(va, dva, rij, de, beta, re);
+          repulsive<double>(vr, dvr, rij, de, beta, re);
+          const double E = exp(MD_LAMDA3 * (rij - re));
+          double xsi = 0, xsj = 0;
+          for (int m = 0; m < n; m++) {
+            const md_double4 pm = pos[inv ? inv[m] : m];
+            if ((int)pm.w == SP_NG || m == j || m == i) continue;
+            const double rim = sqrt(norm2_exact(pi.x - pm.x, pi.y - pm.y, pi.z - pm.z));
+            const double rjm = sqrt(norm2_exact(pj.x - pm.x, pj.y - pm.y, pj.z - pm.z));
+            double fci, dfci, fcj, dfcj;
+            cutoff<double>(rim, fci, dfci);
+            cutoff<double>(rjm, fcj, dfcj);
+            if (fci > 0) {
+              double g, gp;
+              angular<double>((rij * rij + rim * rim - rjm * rjm) / (2.0f * rij * rim), g, gp);
+              xsi += fci * g * E;
+            }
+            if (fcj > 0) {
+              double g, gp;
+              angular<double>((rij * rij + rjm * rjm - rim * rim) / (2.0f * rij * rjm), g, gp);
+              xsj += fcj * g * E;
+            }
+          }
+          bo = 0.5f * (1.0f / (1.0f + xsi) + 1.0f / (1.0f + xsj));
+        }
+        vander_waals<double>(vdw, dvdw, rij, get_r0v<double>(ti, tj));
+        emb = 0.5f * ((vr - bo * va) + vdw);
+      }
+    }
+  }
+  tlj[k] = elj;
+  tmb[k] = emb;
+}
+
+// The reference's running sums (*vibLJ += ..., *vibMB += ...) over a chunk of
+// terms in order, by one thread; out[0..1] carry from chunk to chunk.
+__global__ void k_ref_sum_seq(const double* __restrict__ tlj, const double* __restrict__ tmb,
+                              long long count, double* out) {
+  if (threadIdx.x || blockIdx.x) return;
+  double a = out[0], b = out[1];
+  for (long long k = 0; k < count; k++) {
+    a = xadd(a, tlj[k]);
+    b = xadd(b, tmb[k]);
+  }
+  out[0] = a;
+  out[1] = b;
 }
 
 __global__ void k_record(const double* __restrict__ th8, const double* __restrict__ elj,
@@ -788,6 +918,25 @@ void launch_ref_potential(const md_double4* pos, int n, Species sp, double* part
   }
   k_ref_potential<<<n, 128, 0, st>>>(pos, n, sp, part);
   k_sum_partials<<<1, kRedThreads, 0, st>>>(part, n, 2, out);
+}
+void launch_thermo_seq(const md_double4* pos, const double* vel, const int* inv, int n,
+                       Species sp, double* out, cudaStream_t st) {
+  k_thermo_seq<<<1, 32, 0, st>>>(pos, vel, inv, n, sp, out);
+}
+int launch_ref_potential_seq(const md_double4* pos, const int* inv, int n, Species sp,
+                             double* buf, long long buf_terms, double* out, cudaStream_t st) {
+  cudaMemsetAsync(out, 0, 2 * sizeof(double), st);
+  if (n <= 0) return 0;
+  const int rows = (int)std::max(1LL, std::min((long long)n, buf_terms / n));
+  int launches = 1;
+  for (int r0 = 0; r0 < n; r0 += rows) {
+    const int nr = std::min(rows, n - r0);
+    const long long terms = (long long)nr * n;
+    k_ref_terms<<<nblk(terms, 256), 256, 0, st>>>(pos, inv, n, sp, r0, nr, buf, buf + buf_terms);
+    k_ref_sum_seq<<<1, 32, 0, st>>>(buf, buf + buf_terms, terms, out);
+    launches += 2;
+  }
+  return launches;
 }
 void launch_record(const double* th8, const double* e_lj3, const double* e_mb3,
                    const double* ref2, int use_ref, double time, double step, double* rec16,

@@ -70,6 +70,17 @@ void launch_rep_records(const md_double4* pos, const double* vel, const int* ran
 // part: >= 2 * n doubles.
 void launch_ref_potential(const md_double4* pos, int n, Species sp, double* part, double* out,
                           cudaStream_t st);
+// PerformCalculations and calculatePotentional in the reference's summation
+// order (one device thread adds the terms in the reference's sequence), for
+// records bit-identical to the reference's: thermo into out8 (layout of
+// launch_thermo), the energies into out[0..1].  inv: caller index -> stored
+// position (NULL: stored in the caller's order).  buf holds 2 * buf_terms
+// doubles; the pair terms go through it in chunks of rows.  Returns the
+// number of kernels launched.
+void launch_thermo_seq(const md_double4* pos, const double* vel, const int* inv, int n,
+                       Species sp, double* out8, cudaStream_t st);
+int launch_ref_potential_seq(const md_double4* pos, const int* inv, int n, Species sp,
+                             double* buf, long long buf_terms, double* out, cudaStream_t st);
 // Assembles an md_thermo record (as 16 doubles) from device scalars:
 // th8 from launch_thermo, e_lj3 = (E, E_shifted, W), e_mb3 = (E, W1, W2).
 void launch_record(const double* th8, const double* e_lj3, const double* e_mb3,

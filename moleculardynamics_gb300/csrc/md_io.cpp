@@ -196,8 +196,10 @@ extern "C" md_status md_read_config(const char* path, md_config* cfg, char* stri
     set_err("bad value for Device");
     return MD_BAD_CONFIG;
   }
-  if (get_str(p, "ReferenceEnergy", sv) && !get_bool(p, "ReferenceEnergy", c.reference_energy)) {
-    set_err("bad value for ReferenceEnergy");
+  if (get_str(p, "ReferenceEnergy", sv) &&
+      (!get_num(p, "ReferenceEnergy", c.reference_energy) || c.reference_energy < 0 ||
+       c.reference_energy > 2)) {
+    set_err("bad value for ReferenceEnergy (0, 1 or 2)");
     return MD_BAD_CONFIG;
   }
   if (get_str(p, "LJKernel", sv)) {

@@ -1,0 +1,91 @@
+#!/usr/bin/env python3
+"""Generates tests/golden/dropin/: the files the reference's own cpumd writes
+for one run, to be compared byte for byte with what mdgb_run writes.
+
+Run where the reference sources exist: oracle/build_ref.sh builds the
+unmodified cpumd program (cpu/cpumd/Main.cpp + Host.cpp and the common
+files, argon in the NG slot) as oracle/_ref/cpumd_argon.  The run:
+  864 argon atoms, FCC 6^3 at rho* = 0.8442, Maxwell-Boltzmann at 94.4 K
+  (seeded), LJ rs 2.8 sigma / rcut 2.5 sigma, dt 2 fs, 200 steps, records
+  every 50 steps, animation frames every 50 steps, vxcm 0 and 0.001 (two
+  passes of the sweep, cpu/cpumd/Host.cpp:75), walls as the reference has
+  them (no periodic box).
+Committed: the configuration file, the input state (dropin_input.npz; the
+Input text file is written from it by input_text below), the .dat/.txt
+pair of every pass, and SHA-256 digests of the Output file and of the .anm
+animation of every pass (manifest.json).
+"""
+import hashlib
+import json
+import os
+import shutil
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+OUT = os.path.join(HERE, "dropin")
+sys.path.insert(0, ROOT)
+
+CONFIG = "dropin.cfg"
+VXCM = ("0", "0.001")
+
+
+def input_text(pos4: np.ndarray, vel3: np.ndarray) -> str:
+    """The Input file (common/Loader.cpp:125-155: x y z type vx vy vz per
+    atom, whitespace separated), every double written with 17 significant
+    digits so that it reads back exactly."""
+    rows = np.concatenate([pos4, vel3], axis=1)
+    return "".join(" ".join("%.17g" % v for v in r) + "\n" for r in rows)
+
+
+def sha256(path: str) -> str:
+    with open(path, "rb") as f:
+        return hashlib.sha256(f.read()).hexdigest()
+
+
+def outputs(run_dir: str):
+    """(name -> bytes of the .dat/.txt files, name -> digest of Output/.anm)"""
+    files, digests = {}, {}
+    for v in VXCM:
+        for ext in ("dat", "txt"):
+            name = f"results(vxcm-{v}).{ext}"
+            with open(os.path.join(run_dir, name), "rb") as f:
+                files[name] = f.read()
+        name = f"anim(vxcm-{v}).anm"
+        digests[name] = sha256(os.path.join(run_dir, name))
+    digests["output.txt"] = sha256(os.path.join(run_dir, "output.txt"))
+    return files, digests
+
+
+def main():
+    from moleculardynamics_gb300 import lattice as lat
+    from oracle.oracle import REF_DIR
+    exe = os.path.join(REF_DIR, "cpumd_argon")
+    if not os.path.exists(exe):
+        sys.exit("oracle/_ref/cpumd_argon not built (run oracle/build_ref.sh)")
+    os.makedirs(OUT, exist_ok=True)
+    pos, vel, _ = lat.make_system("fcc", 6, 94.4, seed=864)
+    np.savez(os.path.join(OUT, "dropin_input.npz"), pos=pos, vel=vel)
+    with tempfile.TemporaryDirectory() as d:
+        shutil.copy(os.path.join(OUT, CONFIG), d)
+        with open(os.path.join(d, "input.txt"), "w") as f:
+            f.write(input_text(pos, vel))
+        r = subprocess.run([exe, CONFIG], cwd=d, capture_output=True, text=True)
+        if r.returncode != 0:
+            sys.exit(r.stdout + r.stderr)
+        files, digests = outputs(d)
+    for name, data in files.items():
+        with open(os.path.join(OUT, name), "wb") as f:
+            f.write(data)
+    with open(os.path.join(OUT, "manifest.json"), "w") as f:
+        json.dump({"config": CONFIG, "vxcm": list(VXCM), "files": sorted(files),
+                   "sha256": digests}, f, indent=1, sort_keys=True)
+    print("wrote", OUT)
+
+
+if __name__ == "__main__":
+    main()

@@ -154,23 +154,27 @@ def test_mixed_lj_and_bond_order(eng, oracle):
 
 @pytest.mark.parametrize("periodic", [0, 1])
 def test_lj_trajectory_bit_exact(eng, oracle, periodic):
-    """300 steps of the full loop, list rebuilds included, equal to the bit."""
+    """The first workload at its stated length: 864 argon atoms (FCC 6^3,
+    rho* = 0.8442, 94.4 K), 1000 NVE steps of 2 fs in FP64, list rebuilds
+    included, equal to the bit; records every 100 steps, their energies
+    (and so the energy drift over the run) as the oracle's."""
     pos, vel, L = argon_fcc(6)
     n = len(pos)
     with _engine(eng, n_lj=n, lj_rs=RS, lj_rcut=RC, periodic=periodic, box=L,
                  output_timesteps=100) as e:
         e.upload(pos, vel)
         e.begin(0.0)
-        e.step(300)
+        e.step(1000)
         gp, gv = e.download()
         recs = e.records()
         st = e.stats()
-    ref = oracle.run(run_params(n_lj=n, timesteps=300, output_timesteps=100, periodic=periodic,
-                                box=L), pos, vel, thermo_records=10)
+    ref = oracle.run(run_params(n_lj=n, timesteps=1000, output_timesteps=100, periodic=periodic,
+                                box=L, threads=oracle.max_threads()), pos, vel,
+                     thermo_records=20)
     assert st["list_builds"] == ref["builds"]
     assert np.array_equal(gp, ref["pos"]) and np.array_equal(gv, ref["vel"])
     th = ref["thermo"]
-    assert len(recs) == len(th) == 3   # t = 0, 100, 200
+    assert len(recs) == len(th) == 10   # t = 0, 100, ..., 900
     for r, o in zip(recs, th):
         assert _rel(r[1], o[7]) < 1e-12          # temperature
         assert _rel(r[3], o[3]) < 1e-12          # kinetic energy
