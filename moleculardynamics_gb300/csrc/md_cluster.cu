@@ -254,6 +254,8 @@ __global__ void k_cl_segments(ClusterSegment* __restrict__ seg, const int* __res
     for (int g = 0; g < 10; g++) S.group[g] = g == 9 ? 1 : 0;
     S.npieces = 1;
     S.staged = pc.count;
+    S.self0 = 0;
+    S.img = 0;
     atomicMax(&counters[0], S.staged);
     return;
   }
@@ -287,6 +289,15 @@ __global__ void k_cl_segments(ClusterSegment* __restrict__ seg, const int* __res
   S.group[9] = np;
   S.npieces = np;
   S.staged = dst;
+  // own cells cz0..cz1 lie in the image-free piece of the (0, 0) group
+  int s0 = 0, img = 0;
+  for (int k = 0; k < np; k++) {
+    const ClusterPiece& pc = S.piece[k];
+    if (k >= S.group[4] && k < S.group[5] && pc.iz == 0) s0 = pc.dst + (S.p0 - pc.src);
+    img |= pc.ix | pc.iy | pc.iz;
+  }
+  S.self0 = s0;
+  S.img = img != 0;
   atomicMax(&counters[0], dst);
 }
 
@@ -308,14 +319,7 @@ __device__ __forceinline__ void load_segment(SegShared& sh, const ClusterSegment
   const int* rs = (const int*)&reps[sh.S.rep];
   int* rd = (int*)&sh.r;
   for (int k = threadIdx.x; k < (int)(sizeof(ClusterReplica) / 4); k += blockDim.x) rd[k] = rs[k];
-  if (threadIdx.x == 0) {
-    // own cells cz0..cz1 lie in the image-free piece of the (0, 0) group
-    int s0 = 0;
-    if (reps[sh.S.rep].G > 1)
-      for (int k = sh.S.group[4]; k < sh.S.group[5]; k++)
-        if (sh.S.piece[k].iz == 0) s0 = sh.S.piece[k].dst + (sh.S.p0 - sh.S.piece[k].src);
-    sh.self0 = s0;
-  }
+  if (threadIdx.x == 0) sh.self0 = sh.S.self0;  // computed at the build (k_cl_segments)
 }
 
 // staged copy of positions with the pieces' periodic images applied
@@ -347,20 +351,27 @@ __device__ __forceinline__ bool stage_bulk(const SegShared& sh, const float4* __
                                            float4* st, uint64_t* bar, uint32_t parity,
                                            int* status, int limit) {
   const ClusterSegment& S = sh.S;
-  if (threadIdx.x == 0) {
-    fence_proxy_async();  // earlier generic accesses to the stage come first
-    mbar_expect_tx(bar, (uint32_t)S.staged * (uint32_t)sizeof(float4));
-    for (int k = 0; k < S.npieces; k++) {
+  if (threadIdx.x < 32) {
+    // one lane announces the bytes, then up to 27 lanes issue a piece each
+    if (threadIdx.x == 0) {
+      fence_proxy_async();  // earlier generic accesses to the stage come first
+      mbar_expect_tx(bar, (uint32_t)S.staged * (uint32_t)sizeof(float4));
+    }
+    __syncwarp();
+    const int k = threadIdx.x;
+    if (k < S.npieces) {
       const ClusterPiece& pc = S.piece[k];
       if (pc.count > 0)
         bulk_load(st + pc.dst, src + pc.src, (uint32_t)pc.count * (uint32_t)sizeof(float4), bar);
     }
   }
-  const bool got = mbar_wait(bar, parity, status, limit);
+  // the warps sleep in the wait (suspend-time hint) rather than spin
+  const bool got = mbar_wait_sleep(bar, parity, status, limit);
   if (!__syncthreads_and(got)) {
     if (threadIdx.x == 0) mbar_drain(bar, parity, status);
     return false;
   }
+  if (!S.img) return true;
   const float Lf = sh.r.Lf, Llo = sh.r.Llo;
   for (int k = 0; k < S.npieces; k++) {
     const ClusterPiece& pc = S.piece[k];
@@ -461,6 +472,75 @@ __device__ __forceinline__ void pad_rows(uint16_t* __restrict__ rows, int ld, in
     for (int k = min(kept, cap); k < padded; k++) rows[(size_t)k * ld + p] = (uint16_t)sentinel;
 }
 
+// Grouped rows (the register-prefetch scheme): slots k of atom p in groups
+// of eight, one 16-byte word per atom and group, rows[((k / 8) ld + p) 8 +
+// k % 8], each entry the staged atom's byte offset 16 q (staged
+// neighbourhoods below 4,095 atoms), so that the force loop fetches eight
+// slots with one load and addresses the staged position without arithmetic.
+// Otherwise slot-major staged indices, rows[k ld + p].
+__device__ __forceinline__ size_t row_slot(int k, int p, int ld, int grouped) {
+  return grouped ? (((size_t)(k >> 3) * ld + p) << 3) + (k & 7) : (size_t)k * ld + p;
+}
+__device__ __forceinline__ uint16_t row_val(int q, int grouped) {
+  return (uint16_t)(grouped ? q << 4 : q);
+}
+
+// word k (0..7) of a row chunk held in registers, without indexing the
+// array at run time (which would place it in local memory)
+__device__ __forceinline__ uint32_t pick8(const uint32_t (&c)[8], int k) {
+  const uint32_t a = (k & 1) ? c[1] : c[0], b = (k & 1) ? c[3] : c[2];
+  const uint32_t d = (k & 1) ? c[5] : c[4], e = (k & 1) ? c[7] : c[6];
+  const uint32_t lo = (k & 2) ? b : a, hi = (k & 2) ? e : d;
+  return (k & 4) ? hi : lo;
+}
+
+// Appends a thread's grouped row entries eight at a time: entries shift into
+// a 128-bit register word from the top (funnel shifts), and every full word
+// is stored with one 16-byte store.  Entries past cap are counted, not stored.
+struct GroupWriter {
+  uint32_t w0 = 0, w1 = 0, w2 = 0, w3 = 0;
+  int n = 0;  // entries pushed
+  __device__ __forceinline__ void push(uint16_t* rows, int ld, int cap, int p, uint32_t e) {
+    w0 = __funnelshift_r(w0, w1, 16);
+    w1 = __funnelshift_r(w1, w2, 16);
+    w2 = __funnelshift_r(w2, w3, 16);
+    w3 = (w3 >> 16) | (e << 16);
+    ++n;
+    if ((n & 7) == 0 && n <= cap)
+      reinterpret_cast<uint4*>(rows)[(size_t)((n >> 3) - 1) * ld + p] = make_uint4(w0, w1, w2, w3);
+  }
+  // pads with the sentinel to `padded` slots (a multiple of 16, <= cap)
+  __device__ __forceinline__ void finish(uint16_t* rows, int ld, int cap, int p, int padded,
+                                         uint32_t sentinel) {
+    while ((n & 7) != 0 && n < padded) push(rows, ld, cap, p, sentinel);
+    const uint32_t s2 = sentinel | (sentinel << 16);
+    for (int g = (n + 7) >> 3; 8 * g < padded; g++)
+      reinterpret_cast<uint4*>(rows)[(size_t)g * ld + p] = make_uint4(s2, s2, s2, s2);
+  }
+};
+
+// warp-uniform padded length: the warp's longest kept row rounded up to
+// whole 16-slot tiles, at most cap
+__device__ __forceinline__ int padded_len(bool live, int kept, int cap) {
+  int wm = live ? min(kept, cap) : 0;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) wm = max(wm, __shfl_xor_sync(0xffffffffu, wm, o));
+  return min((wm + kClusterTileSlots - 1) / kClusterTileSlots * kClusterTileSlots, cap);
+}
+
+// pad_rows for either layout; warp-collective
+__device__ __forceinline__ void pad_rows_any(uint16_t* __restrict__ rows, int ld, int cap, int p,
+                                             bool live, int kept, int sentinel, int grouped) {
+  if (!grouped) {
+    pad_rows(rows, ld, cap, p, live, kept, sentinel);
+    return;
+  }
+  const int padded = padded_len(live, kept, cap);
+  if (live)
+    for (int k = min(kept, cap); k < padded; k++)
+      rows[row_slot(k, p, ld, 1)] = row_val(sentinel, 1);
+}
+
 __device__ __forceinline__ void put_sentinel(float4* st, int staged) {
   if (threadIdx.x == 0) st[staged] = make_float4(1e18f, 1e18f, 1e18f, __int_as_float(SP_NG));
 }
@@ -474,7 +554,7 @@ __global__ void __launch_bounds__(256)
     k_cl_rows(const ClusterSegment* __restrict__ seg, const ClusterReplica* __restrict__ reps,
               const int* __restrict__ start, const float4* __restrict__ pb, float rv2,
               uint16_t* __restrict__ rows, uint16_t* __restrict__ len, int ld, int cap,
-              int* __restrict__ counters) {
+              int* __restrict__ counters, int grouped) {
   extern __shared__ float4 st[];
   __shared__ SegShared sh;
   load_segment(sh, seg, reps, blockIdx.x);
@@ -490,6 +570,7 @@ __global__ void __launch_bounds__(256)
     const int p = base + threadIdx.x;
     const bool live = p < sh.S.p1;
     int kept = 0;
+    GroupWriter gw;
     if (live && !minimg) {
       // the 9 column groups in row order, kRowStep independent distance
       // tests per step; only the centre group holds the atom itself
@@ -506,7 +587,12 @@ __global__ void __launch_bounds__(256)
       };
       auto take = [&](int q, bool in) {
         if (in) {
-          if (MODE != 0 && kept < cap) rows[(size_t)kept * ld + p] = (uint16_t)q;
+          if (MODE != 0) {
+            if (grouped)
+              gw.push(rows, ld, cap, p, (uint32_t)q << 4);
+            else if (kept < cap)
+              rows[(size_t)kept * ld + p] = (uint16_t)q;
+          }
           kept++;
         }
       };
@@ -540,12 +626,24 @@ __global__ void __launch_bounds__(256)
           dz = min_img(dz, Lf, invL);
         }
         if (dx * dx + dy * dy + dz * dz < rv2) {
-          if (MODE != 0 && kept < cap) rows[(size_t)kept * ld + p] = (uint16_t)q;
+          if (MODE != 0) {
+            if (grouped)
+              gw.push(rows, ld, cap, p, (uint32_t)q << 4);
+            else if (kept < cap)
+              rows[(size_t)kept * ld + p] = (uint16_t)q;
+          }
           kept++;
         }
       });
     }
-    if (MODE != 0) pad_rows(rows, ld, cap, p, live, kept, sh.S.staged);
+    if (MODE != 0) {
+      if (grouped) {
+        const int padded = padded_len(live, kept, cap);
+        if (live) gw.finish(rows, ld, cap, p, padded, (uint32_t)sh.S.staged << 4);
+      } else {
+        pad_rows(rows, ld, cap, p, live, kept, sh.S.staged);
+      }
+    }
     if (MODE != 1 && live) {
       len[p] = (uint16_t)min(kept, 65535);
       mx = max(mx, kept);
@@ -634,6 +732,55 @@ __device__ __noinline__ bool band_inside(const SegShared& sh, const md_double4* 
   return norm2_exact(xsub(a.x, xj), xsub(a.y, yj), xsub(a.z, zj)) < rcutsq;
 }
 
+// LJ parameters of the force loops: one species (P, Q of the inv^4 form) or
+// the three NG pair kinds (sigma^2, 24 eps)
+struct LjParams {
+  float s2[3], c24[3];
+  float p, q;
+};
+
+// The padded-row loops decide pairs within 1e-5 of the cutoff afterwards:
+// the atom's row is walked again (entries from global memory, in row order),
+// and every pair in the band that the FP64 decision keeps is added, in row
+// order, to one FP32 sum, folded once into the compensated force.  Rare
+// (about one atom in 600 has such a pair).
+template <bool ALL_NG>
+__device__ __noinline__ float3 band_pass(const SegShared& sh, const float4* st,
+                                         const md_double4* pos, double rcutsq,
+                                         const uint16_t* rows, int ld, int grouped, int p, int L,
+                                         float4 pi, float rc_lo, float rc_hi, LjParams lp) {
+  float ex = 0.f, ey = 0.f, ez = 0.f;
+  const int ti = __float_as_int(pi.w);
+  for (int k = 0; k < L; k++) {
+    const int e = rows[row_slot(k, p, ld, grouped)];
+    const int q = grouped ? e >> 4 : e;
+    const float4 pj = st[q];
+    const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+    const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+    if (!(r2 > rc_lo && r2 < rc_hi)) continue;
+    float fij;
+    const float inv = rcp_approx(r2);
+    if (ALL_NG) {
+      const float inv2 = inv * inv;
+      fij = (inv2 * inv2) * fmaf(lp.p, inv2 * inv, -lp.q);
+    } else {
+      const int tj = __float_as_int(pj.w);
+      if (!(tj == SP_NG || ti == SP_NG)) continue;
+      const int sel = lj_select(ti, tj);
+      const float s2 = sel == SP_N ? lp.s2[0] : (sel == SP_O ? lp.s2[1] : lp.s2[2]);
+      const float c24 = sel == SP_N ? lp.c24[0] : (sel == SP_O ? lp.c24[1] : lp.c24[2]);
+      const float sr2 = s2 * inv;
+      const float sr6 = sr2 * sr2 * sr2;
+      fij = c24 * inv * sr6 * fmaf(2.0f, sr6, -1.0f);
+    }
+    if (!band_inside(sh, pos, p, q, rcutsq)) continue;
+    ex = fmaf(dx, fij, ex);
+    ey = fmaf(dy, fij, ey);
+    ez = fmaf(dz, fij, ez);
+  }
+  return make_float3(ex, ey, ez);
+}
+
 // Arguments of the segment force kernel (device copy of ClusterForceArgs).
 struct ClStep {
   int nseg;
@@ -658,6 +805,7 @@ struct ClStep {
   ClusterGearArgs g;
   int nbuf;  // row tiles in flight in the block-tile scheme (2 or 3)
   int wait_limit;  // polls of a bounded mbarrier wait
+  int grouped;     // rows grouped by eight slots, byte offsets (row_slot)
 };
 
 // FP32 LJ force, persistent: each block takes segments from a shared
@@ -748,6 +896,22 @@ __global__ void __launch_bounds__(224, 3)
   const float s2_ng = a.sp.sig[2] * a.sp.sig[2], c_ng = 24.0f * a.sp.eps[2];
   const float s2_n = a.sp.sig[0] * a.sp.sig[0], c_n = 24.0f * a.sp.eps[0];
   const float s2_o = a.sp.sig[1] * a.sp.sig[1], c_o = 24.0f * a.sp.eps[1];
+  // LJ factor F/r of a pair, inv = 1/r^2.  One species (ALL_NG):
+  // inv^4 (P inv^3 - Q), P = 48 eps sigma^12, Q = 24 eps sigma^6, in every
+  // row scheme and in the lean kernel (so that the scheme does not change a
+  // bit of the result); mixed species: 24 eps inv (sigma^2 inv)^3
+  // (2 (sigma^2 inv)^3 - 1) with the pair's parameters.
+  const float q6 = s2_ng * s2_ng * s2_ng;
+  const float lj_q = c_ng * q6, lj_p = 2.0f * c_ng * q6 * q6;
+  auto lj_factor = [&](float inv, float s2, float c24) {
+    if (ALL_NG) {
+      const float inv2 = inv * inv;
+      return (inv2 * inv2) * fmaf(lj_p, inv2 * inv, -lj_q);
+    }
+    const float sr2 = s2 * inv;
+    const float sr6 = sr2 * sr2 * sr2;
+    return c24 * inv * sr6 * fmaf(2.0f, sr6, -1.0f);
+  };
   double ev[3] = {0.0, 0.0, 0.0};
   const int p0 = sh.S.p0, p1 = sh.S.p1;
   for (int base = p0; base < p1; base += blockDim.x) {
@@ -767,6 +931,7 @@ __global__ void __launch_bounds__(224, 3)
     const float4 pi = st[self];
     const int ti = __float_as_int(pi.w);
     float hx = 0.f, hy = 0.f, hz = 0.f, lx = 0.f, ly = 0.f, lz = 0.f;
+    bool band_any = false;  // a padded-row chunk had a pair in the cutoff band
     // energies (ENERGY): E, shifted E and the virial of the atom's pairs,
     // summed like the forces (FP32 within a 16-slot chunk, compensated
     // across chunks, widened to FP64 once per atom)
@@ -802,8 +967,8 @@ __global__ void __launch_bounds__(224, 3)
       }
       const float inv = rcp_approx(r2);
       const float sr2 = s2 * inv;
-      const float sr6 = sr2 * sr2 * sr2;
-      float fij = c24 * inv * sr6 * fmaf(2.0f, sr6, -1.0f);
+      const float sr6 = sr2 * sr2 * sr2;  // the energy terms below
+      float fij = lj_factor(inv, s2, c24);
       bool in = r2 <= rc_lo;
       if (use && !in && r2 < rc_hi) in = band_inside(sh, a.pos, p, q, a.rcutsq);
       in = in && use;
@@ -868,10 +1033,7 @@ __global__ void __launch_bounds__(224, 3)
         s2 = sel == SP_N ? s2_n : (sel == SP_O ? s2_o : s2_ng);
         c24 = sel == SP_N ? c_n : (sel == SP_O ? c_o : c_ng);
       }
-      const float inv = rcp_approx(r2);
-      const float sr2 = s2 * inv;
-      const float sr6 = sr2 * sr2 * sr2;
-      float fij = c24 * inv * sr6 * fmaf(2.0f, sr6, -1.0f);
+      float fij = lj_factor(rcp_approx(r2), s2, c24);
       band |= use && fabsf(r2 - rc_mid) < rc_half;
       fij = use && r2 <= rc_lo ? fij : 0.0f;
       cx = fmaf(dx, fij, cx);
@@ -888,32 +1050,7 @@ __global__ void __launch_bounds__(224, 3)
         pair_fast(get(kk), ax, ay, az, band);
         pair_fast(get(kk + 1), bx, by, bz, band);
       }
-      if (band) {
-#pragma unroll 1
-        for (int kk = 0; kk < kClusterTileSlots; kk++) {
-          const int q = get(kk);
-          const float4 pj = st[q];
-          const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
-          const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-          if (!(r2 > rc_lo && r2 < rc_hi)) continue;
-          float s2 = s2_ng, c24 = c_ng;
-          if (!ALL_NG) {
-            const int tj = __float_as_int(pj.w);
-            if (!(tj == SP_NG || ti == SP_NG)) continue;
-            const int sel = lj_select(ti, tj);
-            s2 = sel == SP_N ? s2_n : (sel == SP_O ? s2_o : s2_ng);
-            c24 = sel == SP_N ? c_n : (sel == SP_O ? c_o : c_ng);
-          }
-          if (!band_inside(sh, a.pos, p, q, a.rcutsq)) continue;
-          const float inv = rcp_approx(r2);
-          const float sr2 = s2 * inv;
-          const float sr6 = sr2 * sr2 * sr2;
-          const float fij = c24 * inv * sr6 * fmaf(2.0f, sr6, -1.0f);
-          ax = fmaf(dx, fij, ax);
-          ay = fmaf(dy, fij, ay);
-          az = fmaf(dz, fij, az);
-        }
-      }
+      band_any |= band;  // decided after the row (band_pass)
       kahan_add(hx, lx, ax + bx);
       kahan_add(hy, ly, ay + by);
       kahan_add(hz, lz, az + bz);
@@ -976,34 +1113,33 @@ __global__ void __launch_bounds__(224, 3)
         break;
       }
     } else if (!tripped && ROWS == 1) {
+      // grouped rows (row_slot): each lane streams its own row, sixteen
+      // slots as two 16-byte loads, one chunk in flight while the previous
+      // one computes; whole padded tiles below the warp's longest row only
+      // (t0 is a multiple of 16: the test is warp-uniform)
       const int L = live ? (int)a.len[p] : 0;
       int wmax = L;
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) wmax = max(wmax, __shfl_xor_sync(0xffffffffu, wmax, o));
-      const uint16_t* rp = a.rows + (live ? p : 0);
-      // two entries per register; whole padded tiles below the warp's
-      // longest row only (t0 is a multiple of 16: the test is warp-uniform)
-      auto fetch = [&](int t0, uint32_t (&dst)[kClusterTileSlots / 2]) {
+      const uint4* rp = reinterpret_cast<const uint4*>(a.rows) + (live ? p : 0);
+      const size_t gs = (size_t)a.ld;  // 16-byte words between groups of a row
+      auto fetch = [&](int t0, uint4& d0, uint4& d1) {
         if (t0 < wmax) {
-#pragma unroll
-          for (int k = 0; k < kClusterTileSlots / 2; k++) {
-            const uint32_t lo = (uint32_t)__ldg(rp + (size_t)(t0 + 2 * k) * a.ld);
-            const uint32_t hi = (uint32_t)__ldg(rp + (size_t)(t0 + 2 * k + 1) * a.ld);
-            dst[k] = lo | (hi << 16);
-          }
+          d0 = __ldg(rp + (size_t)(t0 >> 3) * gs);
+          d1 = __ldg(rp + (size_t)((t0 >> 3) + 1) * gs);
         } else {
-#pragma unroll
-          for (int k = 0; k < kClusterTileSlots / 2; k++) dst[k] = 0u;
+          d0 = d1 = make_uint4(0u, 0u, 0u, 0u);
         }
       };
-      uint32_t nx[kClusterTileSlots / 2];
-      fetch(0, nx);
+      uint4 n0, n1;
+      fetch(0, n0, n1);
       for (int t0 = 0; t0 < wmax; t0 += kClusterTileSlots) {
-        uint32_t cu[kClusterTileSlots / 2];
-#pragma unroll
-        for (int k = 0; k < kClusterTileSlots / 2; k++) cu[k] = nx[k];
-        fetch(t0 + kClusterTileSlots, nx);  // next chunk in flight while this one computes
-        auto get = [&](int kk) { return (int)((cu[kk >> 1] >> ((kk & 1) * 16)) & 0xFFFFu); };
+        const uint32_t cu[8] = {n0.x, n0.y, n0.z, n0.w, n1.x, n1.y, n1.z, n1.w};
+        fetch(t0 + kClusterTileSlots, n0, n1);  // next chunk in flight
+        // entries are byte offsets of the staged positions (16 q)
+        auto get = [&](int kk) {
+          return (int)((pick8(cu, kk >> 1) >> ((kk & 1) * 16)) & 0xFFF0u) >> 4;
+        };
         if (!fast)
           chunk16(get, L - t0, wmax - t0);
         else if (live)
@@ -1091,7 +1227,7 @@ __global__ void __launch_bounds__(224, 3)
           dz = min_img(dz, Lf, invL);
         }
         if (dx * dx + dy * dy + dz * dz < a.rv2) {
-          if (kept < a.cap) a.rows[(size_t)kept * a.ld + p] = (uint16_t)q;
+          if (kept < a.cap) a.rows[row_slot(kept, p, a.ld, a.grouped)] = row_val(q, a.grouped);
           kept++;
         }
       });
@@ -1104,7 +1240,18 @@ __global__ void __launch_bounds__(224, 3)
       kept_new = kept;
       a.pos_build[p] = a.posf[p];
     }
-    if (tripped) pad_rows(a.rows, a.ld, a.cap, p, live, kept_new, sh.S.staged);
+    if (fast && !tripped && live && band_any) {
+      LjParams lp;
+      lp.s2[0] = s2_n, lp.s2[1] = s2_o, lp.s2[2] = s2_ng;
+      lp.c24[0] = c_n, lp.c24[1] = c_o, lp.c24[2] = c_ng;
+      lp.p = lj_p, lp.q = lj_q;
+      const float3 e = band_pass<ALL_NG>(sh, st, a.pos, a.rcutsq, a.rows, a.ld, a.grouped, p,
+                                         (int)a.len[p], pi, rc_lo, rc_hi, lp);
+      kahan_add(hx, lx, e.x);
+      kahan_add(hy, ly, e.y);
+      kahan_add(hz, lz, e.z);
+    }
+    if (tripped) pad_rows_any(a.rows, a.ld, a.cap, p, live, kept_new, sh.S.staged, a.grouped);
     if (live) {
       // the compensated sums widened exactly (integer operations) and
       // combined in FP64
@@ -1179,6 +1326,316 @@ __global__ void __launch_bounds__(224, 3)
   if (blockIdx.x == 0 && tid == 0) {
     if (tripped) atomicAdd(&a.skin[4], 1);
     a.skin[a.flag_clear] = 0;  // flag of step t + 2 starts clear
+  }
+}
+
+// ---- the lean kernel: one species, grouped rows, no energies ----
+// The launches that run every step of the precision form (one species,
+// grouped rows of the register-prefetch scheme, no energy terms) in a kernel
+// of their own, with the same arithmetic as k_lj_cl<false, true, GEAR, 1>
+// to the bit.  Only the padded-row pair loop and the Gear update are inline;
+// the rare paths (the full-row walk of a skin trip, the minimum-image loop
+// of one-cell replicas, the cutoff-band pass) are separate functions, so
+// that their registers do not weigh on the pair loop.
+
+struct LeanConst {
+  float rc_lo, rc_hi, rc_mid, rc_half, lj_p, lj_q;
+  float Lf, invL;
+};
+
+// F/r of one species, inv = 1/r^2: inv^4 (P inv^3 - Q) (k_lj_cl's lj_factor)
+__device__ __forceinline__ float lean_factor(float r2, const LeanConst& k) {
+  const float inv = rcp_approx(r2);
+  const float inv2 = inv * inv;
+  return (inv2 * inv2) * fmaf(k.lj_p, inv2 * inv, -k.lj_q);
+}
+
+struct LeanSum {
+  float hx, hy, hz, lx, ly, lz;
+  int kept;
+};
+
+// entry kk (0..15) of a 16-slot chunk held in two words of four
+__device__ __forceinline__ int lean_entry(uint4 w0, uint4 w1, int kk) {
+  const uint32_t c[8] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w};
+  return (int)((pick8(c, kk >> 1) >> ((kk & 1) * 16)) & 0xFFF0u) >> 4;
+}
+
+// one checked pair of the walks below (k_lj_cl's pair, one species)
+__device__ __forceinline__ void lean_checked(const SegShared& sh, const float4* st,
+                                             const md_double4* pos, double rcutsq, int p,
+                                             float4 pi, int q, bool valid, bool minimg,
+                                             const LeanConst& k, float& cx, float& cy,
+                                             float& cz) {
+  const float4 pj = st[q];
+  float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+  if (minimg) {
+    dx = min_img(dx, k.Lf, k.invL);
+    dy = min_img(dy, k.Lf, k.invL);
+    dz = min_img(dz, k.Lf, k.invL);
+  }
+  const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+  float fij = lean_factor(r2, k);
+  bool in = r2 <= k.rc_lo;
+  if (valid && !in && r2 < k.rc_hi) in = band_inside(sh, pos, p, q, rcutsq);
+  in = in && valid;
+  fij = in ? fij : 0.0f;
+  cx = fmaf(dx, fij, cx);
+  cy = fmaf(dy, fij, cy);
+  cz = fmaf(dz, fij, cz);
+}
+
+// skin exceeded: the full candidate row from the stage, and a fresh compact
+// row at the current positions (k_lj_cl's tripped path)
+__device__ __noinline__ LeanSum lean_refresh(const SegShared& sh, const float4* st, const ClStep& a,
+                                             int p, int self, float4 pi, LeanConst k) {
+  LeanSum s = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0};
+  const bool minimg = sh.r.G == 1;
+  int inchunk = 0;
+  float cx = 0.f, cy = 0.f, cz = 0.f;
+  walk_staged(sh, self, [&](int q) {
+    lean_checked(sh, st, a.pos, a.rcutsq, p, pi, q, true, minimg, k, cx, cy, cz);
+    if (++inchunk == kClusterTileSlots) {
+      kahan_add(s.hx, s.lx, cx);
+      kahan_add(s.hy, s.ly, cy);
+      kahan_add(s.hz, s.lz, cz);
+      cx = cy = cz = 0.f;
+      inchunk = 0;
+    }
+    const float4 pj = st[q];
+    float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+    if (minimg) {
+      dx = min_img(dx, k.Lf, k.invL);
+      dy = min_img(dy, k.Lf, k.invL);
+      dz = min_img(dz, k.Lf, k.invL);
+    }
+    if (dx * dx + dy * dy + dz * dz < a.rv2) {
+      if (s.kept < a.cap) a.rows[row_slot(s.kept, p, a.ld, 1)] = row_val(q, 1);
+      s.kept++;
+    }
+  });
+  kahan_add(s.hx, s.lx, cx);
+  kahan_add(s.hy, s.ly, cy);
+  kahan_add(s.hz, s.lz, cz);
+  if (s.kept > a.cap) atomicOr(&a.skin[3], 1);
+  a.len[p] = (uint16_t)(s.kept < a.cap ? s.kept : a.cap);
+  a.pos_build[p] = a.posf[p];
+  return s;
+}
+
+// one-cell replicas (minimum images): the checked loop over the grouped
+// row (k_lj_cl's chunk16), lanes of the warp in step; warp-collective
+__device__ __noinline__ LeanSum lean_minimg(const SegShared& sh, const float4* st, const ClStep& a,
+                                            int p, bool live, int self, float4 pi, LeanConst k) {
+  LeanSum s = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0};
+  const int L = live ? (int)a.len[p] : 0;
+  int wmax = L;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) wmax = max(wmax, __shfl_xor_sync(0xffffffffu, wmax, o));
+  const uint4* rp = reinterpret_cast<const uint4*>(a.rows) + (live ? p : 0);
+  for (int t0 = 0; t0 < wmax; t0 += kClusterTileSlots) {
+    const uint4 w0 = __ldg(rp + (size_t)(t0 >> 3) * a.ld);
+    const uint4 w1 = __ldg(rp + (size_t)((t0 >> 3) + 1) * a.ld);
+    const int rem = L - t0, wrem = wmax - t0;
+    float ax = 0.f, ay = 0.f, az = 0.f, bx = 0.f, by = 0.f, bz = 0.f;
+    for (int kk = 0; kk < kClusterTileSlots && kk < wrem; kk++) {
+      const bool valid = kk < rem;
+      const int q = valid ? lean_entry(w0, w1, kk) : self;
+      if (kk & 1)
+        lean_checked(sh, st, a.pos, a.rcutsq, p, pi, q, valid, true, k, bx, by, bz);
+      else
+        lean_checked(sh, st, a.pos, a.rcutsq, p, pi, q, valid, true, k, ax, ay, az);
+    }
+    kahan_add(s.hx, s.lx, ax + bx);
+    kahan_add(s.hy, s.ly, ay + by);
+    kahan_add(s.hz, s.lz, az + bz);
+  }
+  return s;
+}
+
+template <int GEAR>
+__global__ void __launch_bounds__(256, 4) k_lj_lean(const ClStep a) {
+  extern __shared__ __align__(128) unsigned char dyn[];
+  float4* st = reinterpret_cast<float4*>(dyn);
+  const int tid = threadIdx.x;
+  __shared__ SegShared sh;
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ int s_trip, s_seg;
+  if (tid == 0) {
+    s_trip = (a.skin[a.flag_read] | a.skin[3]) != 0;
+    mbar_init(&bar, 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  const bool tripped = s_trip != 0;
+  LeanConst k;
+  {
+    const float rc2 = (float)a.rcutsq;
+    k.rc_lo = rc2 * (1.0f - 1e-5f);
+    k.rc_hi = rc2 * (1.0f + 1e-5f);
+    k.rc_mid = 0.5f * (k.rc_lo + k.rc_hi);
+    k.rc_half = 0.5f * (k.rc_hi - k.rc_lo) * 1.001f;
+    const float s2 = a.sp.sig[2] * a.sp.sig[2], c24 = 24.0f * a.sp.eps[2];
+    const float q6 = s2 * s2 * s2;
+    k.lj_q = c24 * q6;
+    k.lj_p = 2.0f * c24 * q6 * q6;
+  }
+  uint32_t phase = 0u;
+  bool trip_next = false;
+  for (;;) {
+    if (tid == 0) s_seg = atomicAdd(&a.sched[0], 1);
+    __syncthreads();
+    const int sidx = s_seg;
+    if (sidx >= a.nseg) break;
+    load_segment(sh, a.seg, a.reps, sidx);
+    __syncthreads();
+    if (!stage_bulk(sh, a.posf, st, &bar, phase, a.status, a.wait_limit)) break;
+    phase ^= 1u;
+    put_sentinel(st, sh.S.staged);
+    if (tripped) fill_offsets(sh, a.start);
+    __syncthreads();
+    const bool minimg = sh.r.G == 1;
+    k.Lf = sh.r.Lf;
+    k.invL = 1.0f / sh.r.Lf;
+    const int p1 = sh.S.p1;
+    for (int base = sh.S.p0; base < p1; base += blockDim.x) {
+      const int p = base + tid;
+      const bool live = p < p1;
+      const int self = live ? self_offset(sh, p) : 0;
+      if (GEAR && live) {
+        prefetch_l2(a.pos + p);
+        prefetch_l2(a.g.vel + 3 * (size_t)p);
+        prefetch_l2(a.g.acc + 3 * (size_t)p);
+        prefetch_l2(a.g.b + 3 * (size_t)p);
+        prefetch_l2(a.g.c + 3 * (size_t)p);
+        prefetch_l2(a.pos_build + p);
+      }
+      const float4 pi = st[self];
+      float hx = 0.f, hy = 0.f, hz = 0.f, lx = 0.f, ly = 0.f, lz = 0.f;
+      if (tripped || minimg) {
+        const LeanSum r = tripped ? (live ? lean_refresh(sh, st, a, p, self, pi, k) : LeanSum{})
+                                  : lean_minimg(sh, st, a, p, live, self, pi, k);
+        hx = r.hx, hy = r.hy, hz = r.hz, lx = r.lx, ly = r.ly, lz = r.lz;
+        if (tripped) pad_rows_any(a.rows, a.ld, a.cap, p, live, r.kept, sh.S.staged, 1);
+      } else {
+        // the sentinel-padded rows: every slot below the warp's padded
+        // length holds a real or a sentinel entry
+        const int L = live ? (int)a.len[p] : 0;
+        int wmax = L;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) wmax = max(wmax, __shfl_xor_sync(0xffffffffu, wmax, o));
+        const uint4* rp = reinterpret_cast<const uint4*>(a.rows) + (live ? p : 0);
+        const size_t gs = (size_t)a.ld;
+        uint4 n0 = make_uint4(0u, 0u, 0u, 0u), n1 = n0;
+        if (wmax > 0) {
+          n0 = __ldg(rp);
+          n1 = __ldg(rp + gs);
+        }
+        const char* sb = reinterpret_cast<const char*>(st);
+        bool band_any = false;
+        for (int t0 = 0; t0 < wmax; t0 += kClusterTileSlots) {
+          const uint4 w0 = n0, w1 = n1;
+          if (t0 + kClusterTileSlots < wmax) {
+            n0 = __ldg(rp + (size_t)((t0 >> 3) + 2) * gs);
+            n1 = __ldg(rp + (size_t)((t0 >> 3) + 3) * gs);
+          }
+          if (!live) continue;
+          const uint32_t cw[8] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w};
+          float ax = 0.f, ay = 0.f, az = 0.f, bx = 0.f, by = 0.f, bz = 0.f;
+          bool band = false;
+          auto one = [&](uint32_t off, float& cx, float& cy, float& cz) {
+            const float4 pj = *reinterpret_cast<const float4*>(sb + off);
+            const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+            const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+            float fij = lean_factor(r2, k);
+            band |= fabsf(r2 - k.rc_mid) < k.rc_half;
+            fij = r2 <= k.rc_lo ? fij : 0.0f;
+            cx = fmaf(dx, fij, cx);
+            cy = fmaf(dy, fij, cy);
+            cz = fmaf(dz, fij, cz);
+          };
+#pragma unroll
+          for (int w = 0; w < 8; w++) {
+            one(cw[w] & 0xFFFFu, ax, ay, az);
+            one(cw[w] >> 16, bx, by, bz);
+          }
+          band_any |= band;
+          kahan_add(hx, lx, ax + bx);
+          kahan_add(hy, ly, ay + by);
+          kahan_add(hz, lz, az + bz);
+        }
+        if (live && band_any) {
+          LjParams lp;
+          lp.p = k.lj_p, lp.q = k.lj_q;
+          const float3 e = band_pass<true>(sh, st, a.pos, a.rcutsq, a.rows, a.ld, 1, p, L, pi,
+                                           k.rc_lo, k.rc_hi, lp);
+          kahan_add(hx, lx, e.x);
+          kahan_add(hy, ly, e.y);
+          kahan_add(hz, lz, e.z);
+        }
+      }
+      if (!live) continue;
+      const double f[3] = {widen_exact(hx) - widen_exact(lx), widen_exact(hy) - widen_exact(ly),
+                           widen_exact(hz) - widen_exact(lz)};
+      if (GEAR != 1) {
+        a.f3[3 * p] = f[0];
+        a.f3[3 * p + 1] = f[1];
+        a.f3[3 * p + 2] = f[2];
+      }
+      if (GEAR) {
+        const md_double4 r = a.pos[p];
+        const int type = __float_as_int(pi.w);
+        GearAtom s;
+        s.r[0] = r.x;
+        s.r[1] = r.y;
+        s.r[2] = r.z;
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+          s.v[d] = a.g.vel[3 * p + d];
+          s.a[d] = a.g.acc[3 * p + d];
+          s.b[d] = a.g.b[3 * p + d];
+          s.c[d] = a.g.c[3 * p + d];
+        }
+        const double im = type == SP_N ? a.g.inv_mass[0]
+                                       : (type == SP_O ? a.g.inv_mass[1] : a.g.inv_mass[2]);
+        gear_correct_fma(s, f, im, a.g.k);
+        if (GEAR == 1) gear_predict_fma(s, a.g.k);
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+          a.g.vel[3 * p + d] = s.v[d];
+          a.g.acc[3 * p + d] = s.a[d];
+          a.g.b[3 * p + d] = s.b[d];
+          a.g.c[3 * p + d] = s.c[d];
+        }
+        md_double4 rn;
+        rn.x = s.r[0];
+        rn.y = s.r[1];
+        rn.z = s.r[2];
+        rn.w = r.w;
+        a.g.pos_next[p] = rn;
+        const float4 pf = make_float4(narrow_rn(s.r[0]), narrow_rn(s.r[1]), narrow_rn(s.r[2]),
+                                      __int_as_float(type));
+        if (!(fabsf(pf.x) <= FLT_MAX && fabsf(pf.y) <= FLT_MAX && fabsf(pf.z) <= FLT_MAX))
+          atomicOr(a.status, ST_NONFINITE);
+        a.g.posf_next[p] = pf;
+        const float4 pb = a.pos_build[p];
+        const float ddx = pf.x - pb.x, ddy = pf.y - pb.y, ddz = pf.z - pb.z;
+        trip_next |= ddx * ddx + ddy * ddy + ddz * ddz > a.g.trip2;
+      }
+    }
+    __syncthreads();  // the next segment overwrites sh and the stage
+  }
+  if (tid == 0) {
+    __threadfence();
+    if (atomicAdd(&a.sched[1], 1) == (int)gridDim.x - 1) {
+      a.sched[0] = 0;
+      a.sched[1] = 0;
+    }
+  }
+  if (GEAR && trip_next) a.skin[a.flag_set] = 1;
+  if (blockIdx.x == 0 && tid == 0) {
+    if (tripped) atomicAdd(&a.skin[4], 1);
+    a.skin[a.flag_clear] = 0;
   }
 }
 
@@ -1460,7 +1917,19 @@ int cluster_build(ClusterList& cl, const std::vector<ClusterReplica>& reps_in, f
     allow_smem(k_lj_cl<false, true, 1, 2>);
     allow_smem(k_lj_cl<false, false, 2, 2>);
     allow_smem(k_lj_cl<false, true, 2, 2>);
+    allow_smem(k_lj_lean<0>);
+    allow_smem(k_lj_lean<1>);
+    allow_smem(k_lj_lean<2>);
     attrs = true;
+  }
+  // the register-prefetch scheme reads grouped rows of byte offsets, which
+  // address at most 4,094 staged atoms and the sentinel; denser
+  // neighbourhoods take the block-tile scheme
+  if (cl.row_loads == 2 && cl.max_staged >= 4095) cl.row_loads = 1;
+  const int grouped = cl.row_loads == 2 ? 1 : 0;
+  if (grouped != cl.grouped) {
+    cl.grouped = grouped;
+    cl.cap = 0;  // the old rows are in the other layout: rebuild them
   }
   const float margin = (float)(1e-6 * (reps.empty() ? 0.0 : reps.back().L + rv) + 1e-6);
   const float rv_keep = rv + margin;
@@ -1474,10 +1943,11 @@ int cluster_build(ClusterList& cl, const std::vector<ClusterReplica>& reps_in, f
   if (cl.nseg > 0) {
     if (have_rows)
       k_cl_rows<2><<<cl.nseg, cl.block, smem, st>>>(cl.seg, cl.rep, cl.start, cl.pos_build, cl.rv2,
-                                               cl.rows, cl.len, cl.ld, cl.cap, cl.counters);
+                                               cl.rows, cl.len, cl.ld, cl.cap, cl.counters,
+                                               cl.grouped);
     else
       k_cl_rows<0><<<cl.nseg, cl.block, smem, st>>>(cl.seg, cl.rep, cl.start, cl.pos_build, cl.rv2,
-                                               nullptr, cl.len, cl.ld, 0, cl.counters);
+                                               nullptr, cl.len, cl.ld, 0, cl.counters, 0);
   }
   cudaMemcpyAsync(hc, cl.counters, sizeof(hc), cudaMemcpyDeviceToHost, st);
   if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
@@ -1512,7 +1982,8 @@ int cluster_build(ClusterList& cl, const std::vector<ClusterReplica>& reps_in, f
   }
   if (!fits && cl.nseg > 0)
     k_cl_rows<1><<<cl.nseg, cl.block, smem, st>>>(cl.seg, cl.rep, cl.start, cl.pos_build, cl.rv2,
-                                             cl.rows, cl.len, cl.ld, cl.cap, cl.counters);
+                                             cl.rows, cl.len, cl.ld, cl.cap, cl.counters,
+                                             cl.grouped);
   cl.trip_dist = 0.5 * ((double)rv - rcut) - (double)margin;
   cudaMemsetAsync(cl.skin, 0, sizeof(int) * 4, st);  // trip flags and overflow
   cl.built = true;
@@ -1556,6 +2027,7 @@ void launch_lj_cluster(const ClusterForceArgs& f, bool energy, cudaStream_t st) 
   else memset(&a.g, 0, sizeof(a.g));
   a.nbuf = nbuf;
   a.wait_limit = f.wait_limit;
+  a.grouped = cl.grouped;
   // persistent grid: as many blocks as fit on the GPU at once, at most one
   // per segment
   auto grid_for = [&](const void* kern) {
@@ -1583,7 +2055,17 @@ void launch_lj_cluster(const ClusterForceArgs& f, bool energy, cudaStream_t st) 
     MDGB_CL_LAUNCH2(E, A, G, 2, cl.rmap_w);      \
   else                                           \
     MDGB_CL_LAUNCH2(E, A, G, 1, cl.rmap)
-  if (energy) {
+  if (cl.grouped && f.all_ng && !energy) {
+    // every-step launches of one species on grouped rows: the lean kernel
+    const int gear = !f.gear ? 0 : (f.gear->correct_only ? 2 : 1);
+    const size_t sm = stage_bytes(cl.max_staged);
+    if (gear == 1)
+      k_lj_lean<1><<<grid_for((const void*)k_lj_lean<1>), cl.block, sm, st>>>(a);
+    else if (gear == 2)
+      k_lj_lean<2><<<grid_for((const void*)k_lj_lean<2>), cl.block, sm, st>>>(a);
+    else
+      k_lj_lean<0><<<grid_for((const void*)k_lj_lean<0>), cl.block, sm, st>>>(a);
+  } else if (energy) {
     if (f.all_ng) { MDGB_CL_LAUNCH(true, true, 0); } else { MDGB_CL_LAUNCH(true, false, 0); }
   } else if (f.gear && f.gear->correct_only) {
     if (f.all_ng) { MDGB_CL_LAUNCH(false, true, 2); } else { MDGB_CL_LAUNCH(false, false, 2); }

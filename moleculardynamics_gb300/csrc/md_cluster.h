@@ -49,6 +49,8 @@ struct ClusterSegment {
   int p0, p1;        // sorted atoms of the segment's cells
   int staged;        // atoms staged in shared memory
   int npieces;
+  int self0;         // staged offset of the segment's first own atom
+  int img;           // some piece carries a periodic image
   int group[10];     // first piece of each (dx, dy) group (9 groups + end)
   ClusterPiece piece[kClusterMaxPieces];
 };
@@ -87,6 +89,9 @@ struct ClusterList {
   int stage_cap = kClusterMaxStaged;              // staged atoms per segment (soft cap)
   int row_loads = 1;                              // 1 block TMA tiles, 2 register prefetch,
                                                   // 3 per-warp TMA tiles
+  int grouped = 0;                                // rows grouped by eight slots with byte
+                                                  // offsets (the register-prefetch scheme):
+                                                  // rows[((k / 8) ld + p) 8 + k % 8] = 16 q
   CUtensorMap rmap;                               // TMA map of rows: {ld atoms, cap slots}
   CUtensorMap rmap_w;                             // the same with per-warp boxes
   int rmap_ok = 0;

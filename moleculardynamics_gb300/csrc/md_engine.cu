@@ -784,7 +784,7 @@ bool window_ok(const md_ctx* c, int s, int nsteps) {
 
 md_status run_window(md_ctx* c) {
   struct Sig {
-    int t6, nseg, max_staged, block, all_ng, cap, ld, wait_limit;
+    int t6, nseg, max_staged, block, all_ng, cap, ld, wait_limit, row_loads, grouped;
     float trip2;
     const void* ptr[14];
     unsigned char rmap[sizeof(CUtensorMap)];
@@ -798,6 +798,8 @@ md_status run_window(md_ctx* c) {
   sig.cap = c->cl.cap;
   sig.ld = c->cl.ld;
   sig.wait_limit = c->wait_limit;
+  sig.row_loads = c->cl.row_loads;
+  sig.grouped = c->cl.grouped;
   sig.trip2 = gear_args(c, c->t + 1).trip2;
   const void* ptrs[14] = {c->pos, c->pos_alt, c->posf, c->posf_alt, c->vel, c->acc, c->b, c->c,
                           c->cl.seg, c->cl.rows, c->cl.len, c->cl.pos_build, c->cl.skin,

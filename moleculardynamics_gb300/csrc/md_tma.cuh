@@ -79,6 +79,31 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* s
   return false;
 }
 
+// try_wait with a suspend-time hint: the warp may sleep up to hint_ns in the
+// instruction instead of returning at once, so a long wait issues few polls
+__device__ __forceinline__ bool mbar_try_wait_sleep(uint64_t* bar, uint32_t parity,
+                                                    uint32_t hint_ns) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n"
+      " selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(smem_addr(bar)), "r"(parity), "r"(hint_ns)
+      : "memory");
+  return ok != 0;
+}
+
+// mbar_wait with sleeping polls (waits of whole blocks on staged copies);
+// at most `limit` polls of up to kWaitHintNs each
+constexpr uint32_t kWaitHintNs = 2000;
+__device__ __forceinline__ bool mbar_wait_sleep(uint64_t* bar, uint32_t parity, int* status,
+                                                int limit = kWaitLimit) {
+  for (int it = 0; it < limit; it++)
+    if (mbar_try_wait_sleep(bar, parity, kWaitHintNs)) return true;
+  atomicOr(status, ST_TMA_TIMEOUT);
+  return false;
+}
+
 // After a wait gave up: the copies this block still has in flight land in
 // its shared memory before it leaves.  Always the default limit, whatever
 // limit the failed wait had, so that no copy outlives the block.
