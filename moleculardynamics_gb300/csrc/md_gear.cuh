@@ -52,6 +52,11 @@ __device__ __forceinline__ double widen_exact(float f) {
   return __hiloint2double((int)hi, (int)lo);
 }
 
+// The conversion instruction, in a function of its own: the compiler cannot
+// evaluate a call ahead of its branch, so the common path of narrow_rn issues
+// nothing on the FP64 pipe (a conversion there costs as much as an FMA).
+static __device__ __noinline__ float narrow_slow(double d) { return __double2float_rn(d); }
+
 // FP64 -> FP32 rounded to nearest, ties to even, by integer operations for
 // results in the normal FP32 range; zero, tiny, huge and non-finite values
 // take the conversion instruction.
@@ -59,7 +64,7 @@ __device__ __forceinline__ float narrow_rn(double d) {
   const uint64_t u = (uint64_t)__double_as_longlong(d);
   const uint32_t hi = (uint32_t)(u >> 32);
   const int e = (int)((hi >> 20) & 0x7FFu) - 896;  // FP32 biased exponent
-  if (e <= 0 || e >= 255) return __double2float_rn(d);
+  if (e <= 0 || e >= 255) return narrow_slow(d);
   const uint32_t mf = (uint32_t)(u >> 29) & 0x7FFFFFu;  // top 23 mantissa bits
   const uint32_t rest = (uint32_t)u & 0x1FFFFFFFu;      // the 29 dropped bits
   const uint32_t up = rest > 0x10000000u || (rest == 0x10000000u && (mf & 1u));
