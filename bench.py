@@ -169,7 +169,10 @@ def drift_per_1000(recs: np.ndarray, n: int, first_step: int) -> float:
 
 # FP64 operations per atom of the fused Gear update: correct 6 per component
 # (a = F/m, the difference, four FMAs), predict 10 per component (4 + 3 + 2 + 1
-# FMAs), and the compensated force widened with one subtraction per component
+# FMAs), and the compensated force widened with one subtraction per component.
+# Each takes one FP64 pipe slot (a warp-wide FP64 instruction per 64 cycles per
+# scheduler at GB300's measured rate), so n x 51 / (FMA rate) is the launch's
+# FP64 floor.
 GEAR_FP64_OPS_PER_ATOM = 3 * (6 + 10 + 1)
 
 
@@ -667,7 +670,9 @@ def run_gb300(args, rank, world):
         avg_s = fu_ms / fu_n / 1e3
         achieved = bytes_alg / avg_s / 1e9
         peak = peaks.get("hbm_gbs")
-        line["roofline"] = {"kernel": "k_lj_cl<fused Gear>", "bound": "hbm", "achieved": achieved,
+        kname = ("k_lj_lean<1> (force + Gear, fused)" if (tune or {}).get("row_loads") == 2
+                 or args.row_loads == 2 else "k_lj_cl<fused Gear>")
+        line["roofline"] = {"kernel": kname, "bound": "hbm", "achieved": achieved,
                             "peak": peak if peak else 6800.0, "unit": "GB/s",
                             "frac": achieved / (peak if peak else 6800.0),
                             "peak_source": "measured" if peak else "fallback",
