@@ -403,16 +403,48 @@ def batched_form(eng, device, steps: int, loop_steps: int, seed: int = 4096) -> 
     }
 
 
-def surrogate_form(eng, device, train_steps: int, run_steps: int, arith: dict,
-                   seed: int = 5) -> dict:
+# surrogate training data: temperatures of the exact trajectories and the MD
+# steps at which they are sampled (denser early, where the lattice's first
+# transient is); held-out states along a further trajectory
+SUR_TEMPS = (300.0, 600.0, 900.0, 1200.0, 1500.0)
+SUR_MARKS = (25, 50, 75, 100, 150, 200, 300, 400, 500, 700, 1000, 1500, 2000, 3000, 4000, 5000,
+             6500, 8000, 10000)
+SUR_HELDOUT = (5, 100, 400, 1000, 3000, 6000, 10000)
+# learning-rate schedule (fraction of the Adam steps, rate) of each model kind
+SUR_LR = {0: ((0.25, 2e-3), (0.25, 1e-3), (0.25, 3e-4), (0.25, 1e-4)),
+          1: ((0.25, 1e-3), (0.25, 5e-4), (0.25, 2e-4), (0.25, 5e-5))}
+# thresholds tried for the best accepted one (relative RMS force error)
+SUR_LADDER = (1e-4, 3e-4, 1e-3, 3e-3, 1e-2, 0.02, 0.03, 0.05, 0.07, 0.1, 0.15, 0.2, 0.3, 0.5, 1.0)
+
+
+def surrogate_form(eng, device, train_steps: int, run_steps: int, fp64_steps: int,
+                   arith: dict, sweep: bool = False, seed: int = 5) -> dict:
     """The learned bond-order surrogate on the 32,768-atom nitrogen diamond
-    (16^3 cells, nearest neighbour 1.5 A, 0.02 A noise).  Training data:
-    trajectories of the exact FP64 method at 300, 700, 1100 and 1500 K on
-    4,096-atom boxes of the same lattice, 50 snapshots = 204,800 atomic
-    environments; the network is trained by force matching with the
-    tensor-core kernels.  Then NVE runs of the 32,768-atom system with the
-    surrogate (exact-kernel checks every 10 steps) and with the exact method
-    alone are timed from the same state."""
+    (16^3 cells, nearest neighbour 1.5 A, 0.02 A noise).
+
+    Training data: trajectories of the 32,768-atom system from 300, 600, 900,
+    1200 and 1500 K, 10,000 steps each (the exact method in its precision
+    form), sampled at the SUR_MARKS steps; at each sample the exact FP64
+    bond-order forces are the labels: 95 snapshots = 3.1 M atomic
+    environments.  Both model kinds are force-matched on them for
+    `train_steps` Adam steps (one snapshot per step, four learning-rate stages):
+      * the per-atom energy network 32-64-64-1 (BF16 tcgen05), forces from its
+        gradient;
+      * the direct-force head 32-H-H-32 (FP32), forces from its outputs.
+    Their force error is taken at held-out states along a further 900 K
+    trajectory.  With `sweep`, also the head at H = 32 and 128 and the head
+    and the energy network on a quarter and a sixteenth of the snapshots:
+    the error against model size and data.
+
+    Then, with the model of the lower held-out error, NVE runs of the
+    32,768-atom system from one 900 K state: the exact FP64 method
+    (`fp64_steps`), the exact precision form and the surrogate at threshold
+    1e-4 (`run_steps` each, exact-kernel check every 10 steps; the 1e-4 run
+    reads the network's error at every check along what is then the exact
+    trajectory), and the surrogate at the best accepted threshold: the
+    smallest of SUR_LADDER that at least half of those checks pass.  Energy
+    drift is that of kinetic + exact bond-order energy (the head has no
+    energy of its own)."""
     from moleculardynamics_gb300 import lattice as lat
     a = 4 * 1.5 / np.sqrt(3.0)
 
@@ -429,25 +461,92 @@ def surrogate_form(eng, device, train_steps: int, run_steps: int, arith: dict,
         e.begin(0.0)
         return e
 
-    s = eng.Surrogate(seed=seed, cutoff=3.0, device=device)
-    t0 = time.perf_counter()
-    nsnap = 0
-    for k, T in enumerate((300.0, 700.0, 1100.0, 1500.0)):
-        pos, vel, L = system(T, seed + k, ncell=8)
-        e = engine(pos, vel, L)
-        for q in range(13 if k < 2 else 12):
-            e.step(8)
-            s.collect(e)
-            nsnap += 1
+    def rel(fa, fb):
+        return float(np.sqrt(((fa - fb) ** 2).sum(1).mean() / (fb ** 2).sum(1).mean()))
+
+    def states(T, sd, marks):
+        pos, vel, L = system(T, sd)
+        e = engine(pos, vel, L, eng.PREC_MIXED)
+        out, done = [], 0
+        for m in marks:
+            e.step(m - done)
+            done = m
+            out.append(e.download() + (L, m))
         e.close()
-    t_collect = time.perf_counter() - t0
+        return out
+
     t0 = time.perf_counter()
-    loss_e, loss_f = s.train_forces(train_steps, lr=2e-3, w_energy=0.1, w_force=1.0)
-    t_train = time.perf_counter() - t0
+    snaps = [x for k, T in enumerate(SUR_TEMPS) for x in states(T, seed + k, SUR_MARKS)]
+    t_traj = time.perf_counter() - t0
+    natoms = len(snaps[0][0])
+    heldout = []
+    for p, v, L, m in states(900.0, seed + 20, SUR_HELDOUT):
+        ef = engine(p, v, L)
+        heldout.append((m, ef, ef.compute_forces()[0]))
+
+    def collect(keep):
+        s = eng.Surrogate(seed=seed, cutoff=3.0, device=device)
+        t0 = time.perf_counter()
+        for j in keep:
+            p, v, L, _ = snaps[j]
+            e = engine(p, v, L)
+            s.collect(e)
+            e.close()
+        return s, time.perf_counter() - t0
+
+    def train(s, kind, hidden, nsnap, t_collect):
+        if kind == 1:
+            s.set_model(1, hidden)
+        else:
+            s.set_model(0)
+        t0 = time.perf_counter()
+        le = lf = None
+        for frac, lr in SUR_LR[kind]:
+            le, lf = s.train_forces(max(1, int(round(train_steps * frac))), lr=lr,
+                                    w_energy=0.1 if kind == 0 else 0.0, w_force=1.0)
+        t_train = time.perf_counter() - t0
+        errs = {m: rel(s.forces(ef)[0], fx) for m, ef, fx in heldout}
+        name = "energy network 32-64-64-1 (BF16 tcgen05)" if kind == 0 else \
+            f"direct-force head 32-{hidden}-{hidden}-32 (FP32)"
+        return {"model": name, "kind": kind, "hidden": 64 if kind == 0 else hidden,
+                "parameters": s.nparams if kind == 0 else len(s.head_params()),
+                "snapshots": nsnap, "environments": nsnap * natoms, "adam_steps": train_steps,
+                "loss_force": lf, "loss_energy": le if kind == 0 else None,
+                "heldout_force_rms_rel_by_step": errs,
+                "heldout_force_rms_rel_mean": float(np.mean(list(errs.values()))),
+                "collect_s": t_collect, "train_s": t_train}
+
+    full = list(range(len(snaps)))
+    s, t_collect = collect(full)
+    plan = [(0, 64), (1, 64)] + ([(1, 32), (1, 128)] if sweep else [])
+    models, chosen, saved = [], None, None
+    for kind, hidden in plan:
+        rec = train(s, kind, hidden, len(full), t_collect)
+        models.append(rec)
+        if chosen is None or rec["heldout_force_rms_rel_mean"] < \
+                chosen["heldout_force_rms_rel_mean"]:
+            chosen = rec
+            saved = (s.head_params(), s.head_scale()) if kind == 1 else None
+    # the chosen model back in place
+    if chosen["kind"] == 0:
+        s.set_model(0)
+    else:
+        s.set_model(1, chosen["hidden"])
+        s.head_params(saved[0])
+        s.head_scale(saved[1])
+    if sweep:
+        for stride in (4, 16):
+            keep = full[::stride]
+            sub, tc = collect(keep)
+            for kind in (0, 1):
+                models.append(train(sub, kind, 64, len(keep), tc))
+            sub.close()
+    for _, ef, _ in heldout:
+        ef.close()
     pos, vel, L = system(900.0, seed + 10)
     n = len(pos)
 
-    def run(threshold, precision=eng.PREC_FP64):
+    def run(threshold, steps, precision=eng.PREC_FP64, series=False):
         e = engine(pos, vel, L, precision)
         if threshold is not None:
             s.attach(e, threshold, 10)
@@ -455,9 +554,15 @@ def surrogate_form(eng, device, train_steps: int, run_steps: int, arith: dict,
         e.synchronize()
         th0 = e.thermo_now()
         ex0 = e.compute_forces()[1][3]
-        es0 = s.forces(e)[1] if threshold is not None else ex0
+        es0 = s.forces(e)[1]
+        errs = []
         e.set_timing(True)
-        e.step(run_steps)
+        if series:  # the check error after every check (one per 10 steps)
+            for _ in range(steps // 10):
+                e.step(10)
+                errs.append(eng.Surrogate.report(e)["last_error"])
+        else:
+            e.step(steps)
         e.synchronize()
         ms, _ = e.kernel_time(eng.KERNEL_STEP)
         mb_ms, mb_n = e.kernel_time(eng.KERNEL_MB)
@@ -468,65 +573,78 @@ def surrogate_form(eng, device, train_steps: int, run_steps: int, arith: dict,
         rep = eng.Surrogate.report(e) if threshold is not None else None
         p1, v1 = e.download()
         e.close()
-        # the drift is that of the energy whose gradient moved the atoms: the
-        # network's when it computed any step, else the exact kernel's
-        if threshold is None or not rep or rep["surrogate_steps"] == 0:
-            es0, es1 = ex0, en[3]
         # the exact FP64 forces at the final positions are the reference for every variant
         e64 = engine(p1, v1, L)
         fx, _ = e64.compute_forces()
         e64.close()
-
-        def rel(fa):
-            return float(np.sqrt(((fa - fx) ** 2).sum(1).mean() / (fx ** 2).sum(1).mean()))
-
+        used = threshold is not None and rep and rep["surrogate_steps"] > 0
         # the same precision with lists built at the final positions, as the
         # FP64 reference's are: the arithmetic's own error, without the list state
         same = None
         if precision != eng.PREC_FP64 and threshold is None:
             ef = engine(p1, v1, L, precision)
-            same = rel(ef.compute_forces()[0])
+            same = rel(ef.compute_forces()[0], fx)
             ef.close()
-        drift = ((th1["ek"] + es1) - (th0["ek"] + es0)) / n / run_steps * 1000.0
-        roof = None
+        per = 1000.0 / n / steps
+        out = {"md_steps": steps, "ms_per_step": ms / steps, "value": n * steps / (ms / 1e3),
+               "force_rms_rel_vs_exact": rel(fs if used else fk, fx),
+               "force_rms_rel_vs_exact_same_lists": same,
+               "network_force_rms_rel_vs_exact": rel(fs, fx),
+               "energy_drift_per_atom_per_1000_steps": ((th1["ek"] + en[3]) -
+                                                        (th0["ek"] + ex0)) * per,
+               "surrogate": rep}
+        if used and np.isfinite(es0):  # the energy network's own energy
+            out["network_energy_drift_per_atom_per_1000_steps"] = \
+                ((th1["ek"] + es1) - (th0["ek"] + es0)) * per
         if threshold is None and mb_n:
-            roof = bond_order_roofline(bond_order_counts(p1, L), mb_ms / mb_n / 1e3, arith,
-                                       precision == eng.PREC_FP64)
-        return {"ms_per_step": ms / run_steps, "value": n * run_steps / (ms / 1e3),
-                "roofline": roof,
-                "force_rms_rel_vs_exact_same_lists": same,
-                "force_rms_rel_vs_exact": rel(fs if threshold is not None and rep and
-                                              rep["surrogate_steps"] > 0 else fk),
-                "network_force_rms_rel_vs_exact": rel(fs),
-                "energy_drift_per_atom_per_1000_steps": drift, "surrogate": rep}
+            out["roofline"] = bond_order_roofline(bond_order_counts(p1, L), mb_ms / mb_n / 1e3,
+                                                  arith, precision == eng.PREC_FP64)
+        return out, np.array(errs)
 
-    exact = run(None)
-    exact32 = run(None, eng.PREC_MIXED)
+    exact, _ = run(None, fp64_steps)
+    exact32, _ = run(None, run_steps, eng.PREC_MIXED)
     # the surrogate runs beside the precision form: its error check and fallback
     # is the exact kernel of the context (FP32 pairs, FP64 Gear)
-    strict = run(1e-4, eng.PREC_MIXED)
-    loose = run(1.0, eng.PREC_MIXED)
+    strict, errs = run(1e-4, run_steps, eng.PREC_MIXED, series=True)
+    accept = {str(t): float((errs <= t).mean()) for t in SUR_LADDER}
+    tau = next((t for t in SUR_LADDER if accept[str(t)] >= 0.5), SUR_LADDER[-1])
+    strict["check_error_along_exact_trajectory"] = {
+        "min": float(errs.min()), "median": float(np.median(errs)), "max": float(errs.max()),
+        "by_1000_steps": [float(np.median(errs[k:k + 100])) for k in range(0, len(errs), 100)]}
+    at_best, _ = run(tau, run_steps, eng.PREC_MIXED)
+    at_best["threshold"] = tau
+    # the surrogate's own step: every check accepted
+    every, _ = run(1.0, 1000, eng.PREC_MIXED)
     s.close()
     return {
         "metric": "atom-steps/s of the bond-order system on 1 GB300", "unit": "atom-steps/s",
         "config": {"atoms": n, "lattice": "N diamond 16^3 cells, 1.5 A bonds, 0.02 A noise",
-                   "training": f"{nsnap} snapshots of 4,096-atom boxes along exact trajectories "
-                               f"at 300, 700, 1100, 1500 K (every 8 steps) = {nsnap * 4096} atomic "
-                               f"environments; force matching, {train_steps} Adam steps",
-                   "network": "32-64-64-1 tanh, BF16 weights on tcgen05, FP32 accumulation",
-                   "run": f"{run_steps} NVE steps at 900 K (dt 0.5 fs), FP64 Gear",
+                   "training": f"{len(snaps)} snapshots of {natoms}-atom trajectories from "
+                               f"{', '.join('%g' % t for t in SUR_TEMPS)} K over 10,000 steps "
+                               f"= {len(snaps) * natoms} atomic environments, exact FP64 "
+                               f"bond-order forces as labels; force matching, {train_steps} "
+                               "Adam steps; held-out states along a 900 K trajectory",
+                   "run": f"NVE at 900 K (dt 0.5 fs), FP64 Gear; surrogate runs {run_steps} "
+                          f"steps, exact FP64 {fp64_steps} steps",
                    "threshold_policy": "exact-kernel check every 10 steps (the context's "
                                        "precision: FP32 pairs for the surrogate runs)"},
-        "train": {"loss_energy": loss_e, "loss_force": loss_f, "collect_s": t_collect,
-                  "train_s": t_train},
+        "trajectories_s": t_traj,
+        "models": models,
+        "chosen_model": chosen["model"],
+        "acceptance_along_exact_trajectory": accept,
+        "best_accepted_threshold": tau,
         "exact": exact,
         "exact_precision_form": exact32,
         "surrogate_threshold_1e-4": strict,
-        "surrogate_accepting": loose,
-        "speedup_accepting_vs_exact": exact["ms_per_step"] / loose["ms_per_step"],
+        "surrogate_best_threshold": at_best,
+        "surrogate_every_step_1000_steps": every,
+        "speedup_best_threshold_vs_exact": exact["ms_per_step"] / at_best["ms_per_step"],
         "speedup_threshold_1e-4_vs_exact": exact["ms_per_step"] / strict["ms_per_step"],
         "speedup_precision_form_vs_exact": exact["ms_per_step"] / exact32["ms_per_step"],
-        "speedup_accepting_vs_precision_form": exact32["ms_per_step"] / loose["ms_per_step"],
+        "speedup_best_threshold_vs_precision_form":
+            exact32["ms_per_step"] / at_best["ms_per_step"],
+        "speedup_surrogate_step_vs_precision_form":
+            exact32["ms_per_step"] / every["ms_per_step"],
     }
 
 
@@ -748,7 +866,8 @@ def run_gb300(args, rank, world):
         line["forms"] = {"batched": batched_form(eng, device, args.batch_steps,
                                                   args.batch_loop_steps),
                          "surrogate": surrogate_form(eng, device, args.sur_train_steps,
-                                                     args.sur_run_steps, arith)}
+                                                     args.sur_run_steps, args.sur_fp64_steps,
+                                                     arith, args.sur_sweep)}
     if rank == 0 and world == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1
         csteps = args.cpu_md_steps
@@ -804,6 +923,37 @@ def run_case(args) -> int:
         e.close()
         print(json.dumps({"case": "bo32k", "atoms": 32768, "md_steps": args.steps,
                           "ms_per_step": ms / max(args.steps, 1)}))
+    if args.case == "sur32k":
+        # a briefly trained surrogate (two FP64 snapshots, 300 Adam steps; the
+        # model kind of --sur-kind) driving the 32,768-atom lattice: --steps MD
+        # steps inside a profiler range (ncu --profile-from-start off)
+        import ctypes
+        s = eng.Surrogate(seed=5, cutoff=3.0)
+        e = bond_order_lattice(eng, 900.0, 15, eng.PREC_FP64)
+        for _ in range(2):
+            e.step(20)
+            s.collect(e)
+        e.close()
+        if args.sur_kind == 1:
+            s.set_model(1, 64)
+        s.train_forces(300, lr=1e-3, w_energy=0.1, w_force=1.0)
+        e = bond_order_lattice(eng, 900.0, 15, eng.PREC_MIXED)
+        s.attach(e, 1.0, 10)
+        e.step(20)
+        e.synchronize()
+        drv = ctypes.CDLL("libcuda.so.1")
+        drv.cuProfilerStart()
+        e.set_timing(True)
+        e.step(args.steps)
+        e.synchronize()
+        drv.cuProfilerStop()
+        ms, _ = e.kernel_time(eng.KERNEL_STEP)
+        rep = eng.Surrogate.report(e)
+        e.close()
+        s.close()
+        print(json.dumps({"case": "sur32k", "atoms": 32768, "kind": args.sur_kind,
+                          "md_steps": args.steps, "ms_per_step": ms / max(args.steps, 1),
+                          "surrogate": rep}))
     return 0
 
 
@@ -836,11 +986,17 @@ def main():
     ap.add_argument("--batch-steps", type=int, default=5000)
     ap.add_argument("--batch-loop-steps", type=int, default=10)
     ap.add_argument("--sur-train-steps", type=int, default=20000)
-    ap.add_argument("--sur-run-steps", type=int, default=200)
-    ap.add_argument("--case", default=None, choices=["bo32k"],
+    ap.add_argument("--sur-run-steps", type=int, default=10000)
+    ap.add_argument("--sur-fp64-steps", type=int, default=400)
+    ap.add_argument("--sur-sweep", action="store_true",
+                    help="also train the head at H = 32, 128 and both kinds on less data")
+    ap.add_argument("--case", default=None, choices=["bo32k", "sur32k"],
                     help="a profiling case instead of the benchmark: bo32k runs the "
                          "32,768-atom bond-order lattice in the precision form for --steps "
-                         "MD steps and prints its step time")
+                         "MD steps and prints its step time; sur32k the same lattice driven "
+                         "by a briefly trained surrogate, the steps inside a profiler range")
+    ap.add_argument("--sur-kind", type=int, default=1, choices=[0, 1],
+                    help="sur32k: 0 the energy network, 1 the direct-force head (H = 64)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.case:

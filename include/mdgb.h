@@ -249,6 +249,7 @@ typedef struct md_surrogate_stats {
   long long checks;            /* exact-kernel checks of the network */
   long long rejected_checks;   /* checks whose error exceeded the threshold */
   double last_error;           /* relative RMS force error at the last check */
+  double max_error;            /* the largest of them since md_surrogate_attach */
 } md_surrogate_stats;
 md_status md_surrogate_create(int device, unsigned long long seed, float cutoff,
                               md_surrogate** out);
@@ -298,6 +299,32 @@ md_status md_surrogate_force_grad(md_surrogate* s, const float* x, const float* 
                                   float* grad);
 /* network output t (n) and dt/dx (n x 32) for normalised inputs x (n x 32) */
 md_status md_surrogate_net(md_surrogate* s, const float* x, int n, float* t, float* dtdx);
+/* Model kind, before training: 0 (default) the per-atom energy network above
+ * (BF16 tcgen05, forces from its gradient); 1 a direct-force head: a
+ * 32 -> hidden -> hidden -> 32 FP32 network (tanh; hidden 32, 64 or 128) whose
+ * outputs w_i, scaled by the output scale s_out and the descriptor
+ * normalisation istd, stand where dE_i/dG_i stands for the energy network:
+ * F_j = -sum_i (w_i s_out istd) . dG_i/dr_j.  Nothing makes these forces a
+ * gradient, so they can follow the reference's non-conservative bond-order
+ * forces; the head has no energy (md_surrogate_forces reports NaN).  It is
+ * trained by md_surrogate_train_forces (force matching; w_energy is
+ * ignored).  Its hidden weights start from the surrogate's seed, its output
+ * layer at zero. */
+md_status md_surrogate_set_model(md_surrogate* s, int kind, int hidden);
+/* s_out, the forces of one unit of head output: the force RMS of the
+ * training data over the force RMS that unit-variance outputs give on the
+ * first training configuration, measured at the first training after a
+ * normalisation (set = 0 reads it, 0 before then; set = 1 restores a saved
+ * value together with md_surrogate_head_params) */
+md_status md_surrogate_head_scale(md_surrogate* s, double* scale, int set);
+/* parameters of the direct-force head: W1 [h][32], b1 [h], W2 [h][h], b2 [h],
+ * W3 [32][h], b3 [32]; count must be md_surrogate_head_param_count(hidden) */
+int md_surrogate_head_param_count(int hidden);
+md_status md_surrogate_head_params(md_surrogate* s, float* params, int count, int set);
+/* parameter gradient of sum_i v_i . w(x_i) of the head (x, v: n x 32 host
+ * arrays), for the comparison with the CPU restatement */
+md_status md_surrogate_head_grad(md_surrogate* s, const float* x, const float* v, int n,
+                                 float* grad);
 
 /* Tensor-core self-test (no counterpart in the reference): c[128 x ncols] =
  * a[128 x kdim] * b[ncols x kdim]^T on tcgen05 with BF16 operands rounded to

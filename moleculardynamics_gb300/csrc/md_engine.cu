@@ -129,7 +129,7 @@ struct md_ctx {
   // force error, measured by the exact kernel every sur_every steps, stays
   // within sur_threshold; otherwise the exact kernel computes the forces
   md_surrogate* sur = nullptr;
-  double sur_threshold = 0.0, sur_err = -1.0;
+  double sur_threshold = 0.0, sur_err = -1.0, sur_err_max = -1.0;
   int sur_every = 10, sur_last_check = -1;
   bool sur_use = false;
   long long sur_steps = 0, sur_exact_steps = 0, sur_checks = 0, sur_rejects = 0;
@@ -376,6 +376,7 @@ md_status mb_forces_step(md_ctx* c, double* f3) {
     r = sur_rel_err(c->sur_fs, c->sur_fx, nmb, c->sur->scratch, &err, c->st);
     if (r) return cuda_fail(c, (cudaError_t)r, "surrogate check");
     c->sur_err = err;
+    c->sur_err_max = std::max(c->sur_err_max, err);
     c->sur_use = err <= c->sur_threshold;
     c->sur_last_check = c->t;
     c->sur_checks++;
@@ -1809,7 +1810,7 @@ md_status md_surrogate_attach(md_ctx* c, md_surrogate* s, double threshold, int 
   c->sur_every = check_every;
   c->sur_last_check = -1;
   c->sur_use = false;
-  c->sur_err = -1.0;
+  c->sur_err = c->sur_err_max = -1.0;
   c->sur_steps = c->sur_exact_steps = c->sur_checks = c->sur_rejects = 0;
   return MD_OK;
 }
@@ -1821,6 +1822,7 @@ md_status md_surrogate_report(const md_ctx* c, md_surrogate_stats* out) {
   out->checks = c->sur_checks;
   out->rejected_checks = c->sur_rejects;
   out->last_error = c->sur_err;
+  out->max_error = c->sur_err_max;
   return MD_OK;
 }
 
@@ -1908,6 +1910,43 @@ md_status md_surrogate_loss_grad(md_surrogate* s, const float* x, const float* t
                                  float* grad, double* loss) {
   if (!s || !x || !t || !grad || !loss || n < 1) return MD_BAD_ARGUMENT;
   return sur_loss_grad(*s, x, t, n, grad, loss, s->stream) ? MD_CUDA_ERROR : MD_OK;
+}
+
+md_status md_surrogate_set_model(md_surrogate* s, int kind, int hidden) {
+  if (!s) return MD_BAD_ARGUMENT;
+  int r = sur_set_model(*s, kind, hidden, s->stream);
+  if (r == -1) return MD_BAD_ARGUMENT;
+  return r ? MD_CUDA_ERROR : MD_OK;
+}
+
+int md_surrogate_head_param_count(int hidden) {
+  return hidden == 32 || hidden == 64 || hidden == 128 ? sur_fh_param_count(hidden) : -1;
+}
+
+md_status md_surrogate_head_params(md_surrogate* s, float* params, int count, int set) {
+  if (!s || !params) return MD_BAD_ARGUMENT;
+  int r = sur_fh_params(*s, params, count, set != 0, s->stream);
+  if (r == -1) return MD_BAD_ARGUMENT;
+  return r ? MD_CUDA_ERROR : MD_OK;
+}
+
+md_status md_surrogate_head_scale(md_surrogate* s, double* scale, int set) {
+  if (!s || !scale) return MD_BAD_ARGUMENT;
+  if (!set) {
+    *scale = s->fh_out;
+    return MD_OK;
+  }
+  if (!(*scale > 0.0) || !std::isfinite(*scale)) return MD_BAD_ARGUMENT;
+  s->fh_out = *scale;
+  return MD_OK;
+}
+
+md_status md_surrogate_head_grad(md_surrogate* s, const float* x, const float* v, int n,
+                                 float* grad) {
+  if (!s || !x || !v || !grad || n < 1) return MD_BAD_ARGUMENT;
+  int r = sur_fh_grad(*s, x, v, n, grad, s->stream);
+  if (r == -1) return MD_BAD_ARGUMENT;
+  return r ? MD_CUDA_ERROR : MD_OK;
 }
 
 md_status md_surrogate_net(md_surrogate* s, const float* x, int n, float* t, float* dtdx) {

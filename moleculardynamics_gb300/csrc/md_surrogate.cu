@@ -1185,15 +1185,355 @@ __global__ void k_collect(const float* __restrict__ Graw, const double* __restri
 inline int sblocks(long long n, int t) { return (int)((n + t - 1) / t); }
 
 bool attrs_set = false;
+// ---- the direct-force head: 32 -> H (tanh) -> H (tanh) -> 32, FP32 ----
+// The second model kind.  Its 32 outputs w_i per atom, scaled to gcoef_i =
+// w_i * s_out * istd (descriptor units; s_out = fh_out), take the place of the energy
+// network's dE_i/dG_i in k_sg_force: F_j = -sum_i gcoef_i . dG_i/dr_j.
+// Nothing makes gcoef a gradient, so the forces need not be conservative,
+// as the reference's bond-order forces are not.  FP32 on the CUDA cores: the
+// outputs multiply the descriptor derivatives directly, so BF16 weights would
+// bound the force error near 1e-3; at 8-33 K parameters and one thread per
+// atom the layers take tens of microseconds per 32,768 atoms.
+// Parameters: W1 [H][32], b1 [H], W2 [H][H], b2 [H], W3 [32][H], b3 [32].
+__host__ __device__ constexpr int fh_params(int H) { return H * 32 + H + H * H + H + 32 * H + 32; }
+
+// forward, one thread per atom (weights in shared memory, read as broadcasts):
+// gcoef (atom-major) and, for training, the input and hidden activations
+// feature-major (xT[d n + i], h1T[j n + i], h2T[j n + i])
+template <int H>
+__global__ void __launch_bounds__(128)
+    k_fh_forward(const float* __restrict__ X, int n, const float* __restrict__ P,
+                 const float* __restrict__ gscale, float* __restrict__ gcoef,
+                 float* __restrict__ xT, float* __restrict__ h1T, float* __restrict__ h2T) {
+  extern __shared__ float wsm[];
+  for (int k = threadIdx.x; k < fh_params(H); k += blockDim.x) wsm[k] = P[k];
+  __syncthreads();
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float *W1 = wsm, *b1 = W1 + H * 32, *W2 = b1 + H, *b2 = W2 + H * H, *W3 = b2 + H,
+              *b3 = W3 + 32 * H;
+  float x[32];
+#pragma unroll
+  for (int d = 0; d < 32; d++) {
+    x[d] = X[(size_t)i * 32 + d];
+    if (xT) xT[(size_t)d * n + i] = x[d];
+  }
+  float h1[H];
+#pragma unroll
+  for (int j = 0; j < H; j++) {
+    float a = b1[j];
+#pragma unroll
+    for (int d = 0; d < 32; d++) a = fmaf(W1[j * 32 + d], x[d], a);
+    h1[j] = tanhf(a);
+    if (h1T) h1T[(size_t)j * n + i] = h1[j];
+  }
+  float w[32];
+#pragma unroll
+  for (int d = 0; d < 32; d++) w[d] = b3[d];
+#pragma unroll 1
+  for (int j = 0; j < H; j++) {
+    float a = b2[j];
+#pragma unroll
+    for (int k = 0; k < H; k++) a = fmaf(W2[j * H + k], h1[k], a);
+    const float h = tanhf(a);
+    if (h2T) h2T[(size_t)j * n + i] = h;
+#pragma unroll
+    for (int d = 0; d < 32; d++) w[d] = fmaf(W3[d * H + j], h, w[d]);
+  }
+#pragma unroll
+  for (int d = 0; d < 32; d++) gcoef[(size_t)i * 32 + d] = gscale ? w[d] * gscale[d] : w[d];
+}
+
+// backward of sum_i v_i . w_i (v = dL/dw, atom-major): the output and hidden
+// deltas, feature-major (d3T[d n + i], d2T[j n + i], d1T[k n + i])
+template <int H>
+__global__ void __launch_bounds__(128)
+    k_fh_backward(const float* __restrict__ V, int n, const float* __restrict__ P,
+                  const float* __restrict__ h1T, const float* __restrict__ h2T,
+                  float* __restrict__ d1T, float* __restrict__ d2T, float* __restrict__ d3T) {
+  extern __shared__ float wsm[];
+  for (int k = threadIdx.x; k < fh_params(H); k += blockDim.x) wsm[k] = P[k];
+  __syncthreads();
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float *W2 = wsm + H * 32 + H, *W3 = W2 + H * H + H;
+  float d3[32];
+#pragma unroll
+  for (int d = 0; d < 32; d++) {
+    d3[d] = V[(size_t)i * 32 + d];
+    d3T[(size_t)d * n + i] = d3[d];
+  }
+  float d2[H];
+#pragma unroll
+  for (int j = 0; j < H; j++) {
+    float a = 0.f;
+#pragma unroll
+    for (int d = 0; d < 32; d++) a = fmaf(W3[d * H + j], d3[d], a);
+    const float h = h2T[(size_t)j * n + i];
+    d2[j] = a * (1.f - h * h);
+    d2T[(size_t)j * n + i] = d2[j];
+  }
+#pragma unroll 1
+  for (int k = 0; k < H; k++) {
+    float a = 0.f;
+#pragma unroll
+    for (int j = 0; j < H; j++) a = fmaf(W2[j * H + k], d2[j], a);
+    const float h = h1T[(size_t)k * n + i];
+    d1T[(size_t)k * n + i] = a * (1.f - h * h);
+  }
+}
+
+// G[j][k] += sum_i A[j][i] B[k][i] (A: J x n, B: K x n, feature-major) and,
+// when gb is given, gb[j] += sum_i A[j][i]: 32 x 32 output tiles per block
+// over a chunk of atoms, staged 64 atoms at a time, one atomic per output
+constexpr int kOutChunk = 1024;
+__global__ void __launch_bounds__(256)
+    k_fh_outer(const float* __restrict__ A, const float* __restrict__ B, int n, int J, int K,
+               float* __restrict__ G, float* __restrict__ gb) {
+  __shared__ float as[32][65], bs[32][65];
+  const int j0 = blockIdx.x * 32, k0 = blockIdx.y * 32, i0 = blockIdx.z * kOutChunk;
+  const int tid = threadIdx.x, tj = tid >> 3, tk = (tid & 7) * 4;  // 32 x (8 x 4)
+  float acc[4] = {0.f, 0.f, 0.f, 0.f}, bsum = 0.f;
+  const int i1 = min(n, i0 + kOutChunk);
+  for (int ib = i0; ib < i1; ib += 64) {
+    for (int e = tid; e < 32 * 64; e += 256) {
+      const int r = e >> 6, c = e & 63, ii = ib + c;
+      as[r][c] = (j0 + r < J && ii < i1) ? A[(size_t)(j0 + r) * n + ii] : 0.f;
+      bs[r][c] = (k0 + r < K && ii < i1) ? B[(size_t)(k0 + r) * n + ii] : 0.f;
+    }
+    __syncthreads();
+#pragma unroll 8
+    for (int c = 0; c < 64; c++) {
+      const float a = as[tj][c];
+      acc[0] = fmaf(a, bs[tk][c], acc[0]);
+      acc[1] = fmaf(a, bs[tk + 1][c], acc[1]);
+      acc[2] = fmaf(a, bs[tk + 2][c], acc[2]);
+      acc[3] = fmaf(a, bs[tk + 3][c], acc[3]);
+      if (gb && blockIdx.y == 0 && tk == 0) bsum += a;
+    }
+    __syncthreads();
+  }
+  if (j0 + tj < J) {
+#pragma unroll
+    for (int u = 0; u < 4; u++)
+      if (k0 + tk + u < K) atomicAdd(&G[(size_t)(j0 + tj) * K + k0 + tk + u], acc[u]);
+    if (gb && blockIdx.y == 0 && tk == 0) atomicAdd(&gb[j0 + tj], bsum);
+  }
+}
+
+// Adam over `count` parameters (the force head's; k_adam's rule)
+__global__ void k_adam_n(float* __restrict__ P, float* __restrict__ M, float* __restrict__ V,
+                         const float* __restrict__ G, int count, int step, float lr, float b1,
+                         float b2, float eps) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= count) return;
+  const float g = G[k];
+  const float m = b1 * M[k] + (1.f - b1) * g;
+  const float v = b2 * V[k] + (1.f - b2) * g * g;
+  M[k] = m;
+  V[k] = v;
+  const float mh = m / (1.f - powf(b1, (float)step));
+  const float vh = v / (1.f - powf(b2, (float)step));
+  P[k] -= lr * mh / (sqrtf(vh) + eps);
+}
+
+// gscale_d = F_rms istd_d: the head's outputs in units of the force scale
+__global__ void k_fh_gscale(const float* __restrict__ istd, float frms, float* __restrict__ gs) {
+  if (threadIdx.x < 32) gs[threadIdx.x] = frms * istd[threadIdx.x];
+}
+
+__global__ void k_fill_nan(double* p) { *p = __longlong_as_double(0x7FF8000000000000LL); }
+
+// probe outputs: w uniform on [-sqrt 3, sqrt 3] (unit variance, from a
+// splitmix64 hash of the index), written as coefficients w istd_d
+__global__ void k_fh_probe(float* __restrict__ gcoef, long long n32, const float* __restrict__ istd,
+                           unsigned long long seed) {
+  const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n32) return;
+  unsigned long long z = seed + 0x9E3779B97F4A7C15ULL * (unsigned long long)(k + 1);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+  z ^= z >> 31;
+  const float u = (float)(z >> 40) * (1.f / 16777216.f);  // [0, 1)
+  gcoef[k] = (2.f * u - 1.f) * 1.7320508f * istd[k & 31];
+}
+
+// acc[0] += sum_k F[k]^2
+__global__ void k_sumsq(const float* __restrict__ F, int n3, double* __restrict__ acc) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  double s = k < n3 ? (double)F[k] * F[k] : 0.0;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) atomicAdd(acc, s);
+}
+
 void set_attrs() {
   if (attrs_set) return;
   cudaFuncSetAttribute(k_net_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmInfer);
   cudaFuncSetAttribute(k_net_train, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmTrain);
   cudaFuncSetAttribute(k_net_train_force, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmForce);
+  cudaFuncSetAttribute(k_fh_forward<128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)sizeof(float) * fh_params(128));
+  cudaFuncSetAttribute(k_fh_backward<128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)sizeof(float) * fh_params(128));
   attrs_set = true;
 }
 
+double fh_out_scale(const Surrogate& s) {
+  if (s.fh_out > 0.0) return s.fh_out;
+  return sqrt(s.force_var > 0 ? s.force_var : 1.0);
+}
+
+// the direct-force head's launches for its width
+void fh_forward(const Surrogate& s, const float* X, int n, float* gcoef, bool keep,
+                cudaStream_t st) {
+  const int B = (n + 127) / 128;
+  const size_t sm = sizeof(float) * fh_params(s.fh_hidden);
+  float* xT = keep ? s.fh_xT : nullptr;
+  float* h1 = keep ? s.fh_h1T : nullptr;
+  float* h2 = keep ? s.fh_h2T : nullptr;
+  const float* gs = s.fh_gs;
+  if (s.fh_hidden == 32)
+    k_fh_forward<32><<<B, 128, sm, st>>>(X, n, s.FP_d, gs, gcoef, xT, h1, h2);
+  else if (s.fh_hidden == 64)
+    k_fh_forward<64><<<B, 128, sm, st>>>(X, n, s.FP_d, gs, gcoef, xT, h1, h2);
+  else
+    k_fh_forward<128><<<B, 128, sm, st>>>(X, n, s.FP_d, gs, gcoef, xT, h1, h2);
+}
+
+// FG += d(sum_i v_i . w_i)/dparams for the activations of the last kept forward
+void fh_backward(Surrogate& s, const float* V, int n, cudaStream_t st) {
+  const int H = s.fh_hidden, B = (n + 127) / 128;
+  const size_t sm = sizeof(float) * fh_params(H);
+  if (H == 32)
+    k_fh_backward<32><<<B, 128, sm, st>>>(V, n, s.FP_d, s.fh_h1T, s.fh_h2T, s.fh_d1T, s.fh_d2T,
+                                          s.fh_d3T);
+  else if (H == 64)
+    k_fh_backward<64><<<B, 128, sm, st>>>(V, n, s.FP_d, s.fh_h1T, s.fh_h2T, s.fh_d1T, s.fh_d2T,
+                                          s.fh_d3T);
+  else
+    k_fh_backward<128><<<B, 128, sm, st>>>(V, n, s.FP_d, s.fh_h1T, s.fh_h2T, s.fh_d1T,
+                                           s.fh_d2T, s.fh_d3T);
+  float* G = s.FG_d;
+  float *gW1 = G, *gb1 = gW1 + H * 32, *gW2 = gb1 + H, *gb2 = gW2 + H * H, *gW3 = gb2 + H,
+        *gb3 = gW3 + 32 * H;
+  const int nz = (n + kOutChunk - 1) / kOutChunk;
+  const int hb = (H + 31) / 32;
+  k_fh_outer<<<dim3(1, hb, nz), 256, 0, st>>>(s.fh_d3T, s.fh_h2T, n, 32, H, gW3, gb3);
+  k_fh_outer<<<dim3(hb, hb, nz), 256, 0, st>>>(s.fh_d2T, s.fh_h1T, n, H, H, gW2, gb2);
+  k_fh_outer<<<dim3(hb, 1, nz), 256, 0, st>>>(s.fh_d1T, s.fh_xT, n, H, 32, gW1, gb1);
+}
+
+cudaError_t fh_scratch(Surrogate& s, long long n) {
+  if (n <= s.fh_n) return cudaSuccess;
+  cudaError_t e;
+  const long long H = s.fh_hidden;
+  for (float** p : {&s.fh_h1T, &s.fh_h2T, &s.fh_d1T, &s.fh_d2T}) {
+    long long h = 0;
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+    if ((e = sur_grow(*p, h, H * n)) != cudaSuccess) return e;
+  }
+  for (float** p : {&s.fh_xT, &s.fh_d3T}) {
+    long long h = 0;
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+    if ((e = sur_grow(*p, h, 32 * n)) != cudaSuccess) return e;
+  }
+  s.fh_n = n;
+  return cudaSuccess;
+}
+
 }  // namespace
+
+int sur_fh_param_count(int hidden) { return fh_params(hidden); }
+
+int sur_set_model(Surrogate& s, int kind, int hidden, cudaStream_t st) {
+  if (kind == 0) {
+    s.kind = 0;
+    return 0;
+  }
+  if (kind != 1 || !(hidden == 32 || hidden == 64 || hidden == 128)) return -1;
+  set_attrs();
+  s.kind = 1;
+  if (hidden != s.fh_hidden) s.fh_n = 0;  // activations are per width
+  s.fh_hidden = hidden;
+  s.fh_np = fh_params(hidden);
+  cudaError_t e;
+  for (float** p : {&s.FP_d, &s.FM_d, &s.FV_d, &s.FG_d}) {
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+    long long h = 0;
+    if ((e = sur_grow(*p, h, s.fh_np)) != cudaSuccess) return e;
+  }
+  if (!s.fh_gs) {
+    long long h = 0;
+    if ((e = sur_grow(s.fh_gs, h, 32)) != cudaSuccess) return e;
+  }
+  // weights from the surrogate's seed (another stream of the LCG than the
+  // energy network's), zero biases
+  const int H = hidden;
+  std::vector<float> P(s.fh_np, 0.f);
+  unsigned long long x = (s.seed ^ 0x9E3779B97F4A7C15ULL) * 6364136223846793005ULL + 1;
+  auto uni = [&]() {
+    x = x * 6364136223846793005ULL + 1442695040888963407ULL;
+    return (float)((x >> 11) * (1.0 / 9007199254740992.0)) * 2.f - 1.f;
+  };
+  // hidden layers Xavier-uniform; output layer zero, so that training starts
+  // from zero forces (loss 1) rather than from forces many times F_rms
+  const float a1 = sqrtf(6.f / (32 + H)), a2 = sqrtf(6.f / (H + H));
+  for (int k = 0; k < H * 32; k++) P[k] = a1 * uni();
+  for (int k = 0; k < H * H; k++) P[H * 32 + H + k] = a2 * uni();
+  return sur_fh_params(s, P.data(), s.fh_np, true, st);
+}
+
+int sur_fh_params(Surrogate& s, float* P, int count, bool set, cudaStream_t st) {
+  if (s.kind != 1 || count != s.fh_np) return -1;
+  cudaError_t e;
+  if (set) {
+    if ((e = cudaMemcpyAsync(s.FP_d, P, sizeof(float) * count, cudaMemcpyHostToDevice, st)) !=
+        cudaSuccess)
+      return e;
+    cudaMemsetAsync(s.FM_d, 0, sizeof(float) * count, st);
+    cudaMemsetAsync(s.FV_d, 0, sizeof(float) * count, st);
+    s.fh_step = 0;
+  } else if ((e = cudaMemcpyAsync(P, s.FP_d, sizeof(float) * count, cudaMemcpyDeviceToHost,
+                                  st)) != cudaSuccess) {
+    return e;
+  }
+  return cudaStreamSynchronize(st);
+}
+
+int sur_fh_grad(Surrogate& s, const float* X, const float* V, int n, float* grad,
+                cudaStream_t st) {
+  if (s.kind != 1) return -1;
+  cudaError_t e;
+  float *dX = nullptr, *dV = nullptr, *dw = nullptr;
+  if ((e = fh_scratch(s, n)) != cudaSuccess) return e;
+  if ((e = cudaMalloc(&dX, sizeof(float) * 32 * n)) != cudaSuccess) return e;
+  if ((e = cudaMalloc(&dV, sizeof(float) * 32 * n)) != cudaSuccess ||
+      (e = cudaMalloc(&dw, sizeof(float) * 32 * n)) != cudaSuccess) {
+    cudaFree(dX);
+    if (dV) cudaFree(dV);
+    return e;
+  }
+  cudaMemcpyAsync(dX, X, sizeof(float) * 32 * n, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(dV, V, sizeof(float) * 32 * n, cudaMemcpyHostToDevice, st);
+  // raw outputs (no scaling) with the activations kept
+  const float* gs = s.fh_gs;
+  s.fh_gs = nullptr;
+  fh_forward(s, dX, n, dw, true, st);
+  s.fh_gs = const_cast<float*>(gs);
+  cudaMemsetAsync(s.FG_d, 0, sizeof(float) * s.fh_np, st);
+  fh_backward(s, dV, n, st);
+  cudaMemcpyAsync(grad, s.FG_d, sizeof(float) * s.fh_np, cudaMemcpyDeviceToHost, st);
+  e = cudaStreamSynchronize(st);
+  cudaFree(dX);
+  cudaFree(dV);
+  cudaFree(dw);
+  if (e != cudaSuccess) return e;
+  return (int)cudaGetLastError();
+}
 
 int sur_init(Surrogate& s, unsigned long long seed, cudaStream_t st) {
   cudaError_t e;
@@ -1376,6 +1716,7 @@ int sur_normalise(Surrogate& s, cudaStream_t st) {
   cudaMemcpyAsync(s.mean_d, mean, sizeof(mean), cudaMemcpyHostToDevice, st);
   cudaMemcpyAsync(s.istd_d, istd, sizeof(istd), cudaMemcpyHostToDevice, st);
   s.normalised = true;
+  s.fh_out = 0.0;  // measured again for the new normalisation
   return cudaStreamSynchronize(st);
 }
 }  // namespace
@@ -1476,6 +1817,17 @@ int sur_forces(Surrogate& s, const md_double4* pos, int n, const RowWalker& w, d
   int r = sur_descriptors(s, pos, n, w, true, d_status, st);
   if (r) return r;
   if (n == 0) return 0;
+  if (s.kind == 1) {
+    // the direct-force head: coefficients straight from the network; it
+    // models forces only, so the energy it reports is NaN
+    k_fh_gscale<<<1, 32, 0, st>>>(s.istd_d, (float)fh_out_scale(s), s.fh_gs);
+    fh_forward(s, s.X, n, s.gcoef, false, st);
+    cudaMemsetAsync(s.F32, 0, sizeof(float) * 3 * (size_t)n, st);
+    k_sg_force<<<sblocks(n, 4), 128, 0, st>>>(pos, n, s.sl, s.slen, w.g.box, s.P, s.gcoef, s.F32);
+    k_sg_store<<<sblocks(3LL * n, 256), 256, 0, st>>>(s.F32, f3, n, accumulate);
+    if (energy_dev) k_fill_nan<<<1, 1, 0, st>>>(energy_dev);
+    return (int)cudaGetLastError();
+  }
   k_net_infer<<<(n + 127) / 128, 128, kSmInfer, st>>>(s.X, n, net_of(s), s.t, s.dtdx, s.status_d);
   k_sg_scale<<<sblocks(n, 256), 256, 0, st>>>(s.t, s.dtdx, n, s.mu, s.sigma, s.istd_d, s.gcoef,
                                               s.eatom);
@@ -1552,7 +1904,75 @@ int sur_normalise_cfgs(Surrogate& s, cudaStream_t st) {
   cudaMemcpyAsync(s.mean_d, mean, sizeof(mean), cudaMemcpyHostToDevice, st);
   cudaMemcpyAsync(s.istd_d, istd, sizeof(istd), cudaMemcpyHostToDevice, st);
   s.normalised = true;
+  s.fh_out = 0.0;  // measured again for the new normalisation
   return cudaStreamSynchronize(st);
+}
+}  // namespace
+
+namespace {
+// Force matching of the direct-force head: per Adam step one stored
+// configuration, loss w_force mean(|F - F*|^2) / var_F, with
+//   dL/dw_i = -2 kappa s_out istd . sum_j (F_j - F*_j) . dG_i/dr_j
+// (s_out = fh_out, the force scale of one unit of output)
+// from the same transpose as the energy network's force term (k_sg_ctrans),
+// then the head's backward pass and Adam.
+int train_fh(Surrogate& s, int steps, float lr, int nmax, double* loss_e, double* loss_f,
+             cudaStream_t st) {
+  cudaError_t e;
+  if ((e = fh_scratch(s, nmax)) != cudaSuccess) return e;
+  const int ncfg = (int)s.cfgs.size();
+  if (s.fh_out <= 0.0) {
+    // the output scale: force RMS per component from unit-variance outputs
+    // on the first configuration
+    const SurConfig& c = s.cfgs[0];
+    k_fh_probe<<<sblocks(32LL * c.n, 256), 256, 0, st>>>(s.gcoef, 32LL * c.n, s.istd_d,
+                                                         s.seed);
+    cudaMemsetAsync(s.F32, 0, sizeof(float) * 3 * (size_t)c.n, st);
+    k_sg_force<<<sblocks(c.n, 4), 128, 0, st>>>(c.pos, c.n, c.sl, c.slen, c.box, s.P, s.gcoef,
+                                                s.F32);
+    cudaMemsetAsync(s.scratch, 0, sizeof(double), st);
+    k_sumsq<<<sblocks(3LL * c.n, 256), 256, 0, st>>>(s.F32, 3 * c.n, s.scratch);
+    double sq = 0;
+    cudaMemcpyAsync(&sq, s.scratch, sizeof(double), cudaMemcpyDeviceToHost, st);
+    if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
+    const double rms = sqrt(sq / (3.0 * c.n));
+    s.fh_out = rms > 0 ? sqrt(s.force_var) / rms : sqrt(s.force_var);
+  }
+  const float gsc = (float)s.fh_out;
+  k_fh_gscale<<<1, 32, 0, st>>>(s.istd_d, gsc, s.fh_gs);
+  double acc_f = 0;
+  int nacc = 0;
+  for (int it = 0; it < steps; it++) {
+    const SurConfig& c = s.cfgs[(it * 7919 + (int)(s.seed % 101)) % ncfg];
+    const int n = c.n;
+    fh_forward(s, c.X, n, s.gcoef, true, st);
+    cudaMemsetAsync(s.F32, 0, sizeof(float) * 3 * (size_t)n, st);
+    k_sg_force<<<sblocks(n, 4), 128, 0, st>>>(c.pos, n, c.sl, c.slen, c.box, s.P, s.gcoef,
+                                                s.F32);
+    cudaMemsetAsync(s.scratch, 0, sizeof(double) * 2, st);
+    k_fm_resid<<<sblocks(3LL * n, 256), 256, 0, st>>>(s.F32, c.fx, 3 * n, s.E3, s.scratch);
+    const float kappa = (float)(s.w_force / (3.0 * n * s.force_var));
+    k_sg_ctrans<<<sblocks(n, 4), 128, 0, st>>>(c.pos, n, c.sl, c.slen, c.box, s.P, s.E3,
+                                                 -2.f * kappa * gsc, s.istd_d, s.V);
+    cudaMemsetAsync(s.FG_d, 0, sizeof(float) * s.fh_np, st);
+    fh_backward(s, s.V, n, st);
+    s.fh_step++;
+    k_adam_n<<<sblocks(s.fh_np, 256), 256, 0, st>>>(s.FP_d, s.FM_d, s.FV_d, s.FG_d, s.fh_np,
+                                                    s.fh_step, lr, 0.9f, 0.999f, 1e-8f);
+    if (it >= steps - std::min(steps, 2 * ncfg)) {  // loss over the last pass
+      double lf[2];
+      cudaMemcpyAsync(lf, s.scratch, sizeof(double) * 2, cudaMemcpyDeviceToHost, st);
+      if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
+      acc_f += lf[0] / (3.0 * n * s.force_var);
+      nacc++;
+    }
+  }
+  if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
+  s.last_loss_e = 0.0;
+  s.last_loss_f = nacc ? acc_f / nacc : 0.0;
+  if (loss_e) *loss_e = 0.0;
+  if (loss_f) *loss_f = s.last_loss_f;
+  return (int)cudaGetLastError();
 }
 }  // namespace
 
@@ -1615,6 +2035,7 @@ int sur_train_fm(Surrogate& s, int steps, float lr, double* loss_e, double* loss
     if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
     s.n_iota = nmax;
   }
+  if (s.kind == 1) return train_fh(s, steps, lr, nmax, loss_e, loss_f, st);
   const NetDev w = net_of(s);
   double acc_e = 0, acc_f = 0;
   int nacc = 0;
@@ -1710,6 +2131,10 @@ md_surrogate::~md_surrogate() {
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (void* p : {(void*)iota_d, (void*)V, (void*)E3, (void*)pos32})
+    if (p) cudaFree(p);
+  for (void* p : {(void*)FP_d, (void*)FM_d, (void*)FV_d, (void*)FG_d, (void*)fh_gs,
+                  (void*)fh_xT, (void*)fh_h1T, (void*)fh_h2T, (void*)fh_d1T, (void*)fh_d2T,
+                  (void*)fh_d3T})
     if (p) cudaFree(p);
   for (mdgb::SurConfig& c : cfgs)
     for (void* p : {(void*)c.pos, (void*)c.sl, (void*)c.slen, (void*)c.fx, (void*)c.eatom,

@@ -82,6 +82,18 @@ struct md_surrogate {
   float *V = nullptr, *E3 = nullptr;  // per-atom force sensitivity, residuals
   long long n_fm = 0;
   double last_loss_e = 0.0, last_loss_f = 0.0;
+  // model kind: 0 the per-atom energy network (tensor cores), 1 the
+  // direct-force head (FP32, 32 -> fh_hidden -> fh_hidden -> 32)
+  int kind = 0;
+  int fh_hidden = 64, fh_np = 0, fh_step = 0;
+  float *FP_d = nullptr, *FM_d = nullptr, *FV_d = nullptr, *FG_d = nullptr, *fh_gs = nullptr;
+  float *fh_xT = nullptr, *fh_h1T = nullptr, *fh_h2T = nullptr;
+  float *fh_d1T = nullptr, *fh_d2T = nullptr, *fh_d3T = nullptr;
+  long long fh_n = 0;
+  // force units per unit head output: F_rms over the force RMS that
+  // outputs drawn with unit variance per component produce on the first
+  // training configuration (0 until measured: F_rms alone)
+  double fh_out = 0.0;
   ~md_surrogate();
 };
 
@@ -120,6 +132,15 @@ int sur_loss_grad(Surrogate& s, const float* X, const float* T, int n, float* gr
 int sur_net_eval(Surrogate& s, const float* X, int n, float* t, float* dtdx, cudaStream_t st);
 int sur_forces(Surrogate& s, const md_double4* pos, int n, const RowWalker& w, double* f3,
                int accumulate, double* energy_dev, int* d_status, cudaStream_t st);
+// model kind (0 energy network, 1 direct-force head with `hidden` units per
+// hidden layer: 32, 64 or 128); the head's weights start from the seed
+int sur_set_model(Surrogate& s, int kind, int hidden, cudaStream_t st);
+int sur_fh_param_count(int hidden);
+int sur_fh_params(Surrogate& s, float* P, int count, bool set, cudaStream_t st);
+// parameter gradient of sum_i v_i . w(x_i) of the direct-force head (host
+// arrays x, v: n x 32), for the comparison with the CPU restatement
+int sur_fh_grad(Surrogate& s, const float* X, const float* V, int n, float* grad,
+                cudaStream_t st);
 // relative RMS of a against b over n atoms (3 components)
 int sur_rel_err(const double* a, const double* b, int n, double* scratch, double* err,
                 cudaStream_t st);

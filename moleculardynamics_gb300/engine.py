@@ -74,7 +74,7 @@ class MdTuneResult(C.Structure):
 class MdSurrogateStats(C.Structure):
     _fields_ = [("surrogate_steps", C.c_longlong), ("exact_steps", C.c_longlong),
                 ("checks", C.c_longlong), ("rejected_checks", C.c_longlong),
-                ("last_error", C.c_double)]
+                ("last_error", C.c_double), ("max_error", C.c_double)]
 
 
 class ListSettings(C.Structure):
@@ -110,7 +110,8 @@ EXPORTS = ["md_create", "md_destroy", "md_status_string", "md_last_error", "md_u
            "md_surrogate_params", "md_surrogate_normalisation", "md_surrogate_loss_grad",
            "md_surrogate_net", "md_surrogate_train_forces", "md_surrogate_force_grad",
            "md_surrogate_desc_directional", "md_set_wait_limit", "md_measure_arith_peaks",
-           "md_device_sm_count"]
+           "md_device_sm_count", "md_surrogate_set_model", "md_surrogate_head_param_count",
+           "md_surrogate_head_params", "md_surrogate_head_grad", "md_surrogate_head_scale"]
 
 
 def load(path: str | None = None) -> C.CDLL:
@@ -172,6 +173,11 @@ def load(path: str | None = None) -> C.CDLL:
     L.md_surrogate_train_forces.argtypes = [C.c_void_p, C.c_int, C.c_float, C.c_float,
                                             C.c_float, P(C.c_double), P(C.c_double)]
     L.md_surrogate_force_grad.argtypes = [C.c_void_p, _fp, _fp, C.c_int, _fp]
+    L.md_surrogate_set_model.argtypes = [C.c_void_p, C.c_int, C.c_int]
+    L.md_surrogate_head_param_count.argtypes = [C.c_int]
+    L.md_surrogate_head_params.argtypes = [C.c_void_p, _fp, C.c_int, C.c_int]
+    L.md_surrogate_head_grad.argtypes = [C.c_void_p, _fp, _fp, C.c_int, _fp]
+    L.md_surrogate_head_scale.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.c_int]
     L.md_batch_create.argtypes = [P(MdConfig), C.c_int, _ip, _dp, P(C.c_void_p)]
     L.md_batch_size.argtypes = [C.c_void_p]
     L.md_batch_records.argtypes = [C.c_void_p, C.c_void_p, C.c_int]
@@ -402,6 +408,7 @@ class Surrogate:
             raise EngineError(s, "md_surrogate_create")
         self.h = h
         self.nparams = self.lib.md_surrogate_param_count()
+        self.kind, self.hidden = 0, 64
 
     def close(self):
         if getattr(self, "h", None):
@@ -450,6 +457,34 @@ class Surrogate:
         g = np.zeros(self.nparams, np.float32)
         self._ck(self.lib.md_surrogate_force_grad(self.h, x, v, len(x), g),
                  "md_surrogate_force_grad")
+        return g
+
+    def set_model(self, kind: int, hidden: int = 64):
+        """0: the per-atom energy network (tensor cores); 1: the direct-force
+        head with `hidden` units per hidden layer (32, 64 or 128)."""
+        self._ck(self.lib.md_surrogate_set_model(self.h, kind, hidden), "md_surrogate_set_model")
+        self.kind, self.hidden = kind, hidden
+
+    def head_params(self, new=None) -> np.ndarray:
+        n = self.lib.md_surrogate_head_param_count(self.hidden)
+        p = np.zeros(n, np.float32) if new is None else np.ascontiguousarray(new, np.float32)
+        self._ck(self.lib.md_surrogate_head_params(self.h, p, n, 0 if new is None else 1),
+                 "md_surrogate_head_params")
+        return p
+
+    def head_scale(self, new: float | None = None) -> float:
+        """s_out, the forces of one unit of head output (0 before training)."""
+        v = C.c_double(0.0 if new is None else new)
+        self._ck(self.lib.md_surrogate_head_scale(self.h, C.byref(v), 0 if new is None else 1),
+                 "md_surrogate_head_scale")
+        return v.value
+
+    def head_grad(self, x, v):
+        x = np.ascontiguousarray(x, np.float32)
+        v = np.ascontiguousarray(v, np.float32)
+        g = np.zeros(self.lib.md_surrogate_head_param_count(self.hidden), np.float32)
+        self._ck(self.lib.md_surrogate_head_grad(self.h, x, v, len(x), g),
+                 "md_surrogate_head_grad")
         return g
 
     def attach(self, e: "Engine", threshold: float, check_every: int = 10):

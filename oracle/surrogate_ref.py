@@ -20,7 +20,11 @@ mathematics plainly (numpy, float64) so the GPU kernels can be checked:
   everything else is FP32/FP64;
 * the training loss mean((t - y)^2) and its gradient with respect to the
   parameters, laid out as W1 [64][32], b1 [64], W2 [64][64], b2 [64],
-  w3 [64], b3.
+  w3 [64], b3;
+* the direct-force head, the second model kind: 32 -> H -> H -> 32 (tanh,
+  FP32 on the GPU), parameters W1 [H][32], b1 [H], W2 [H][H], b2 [H],
+  W3 [32][H], b3 [32]; its outputs w(x) and the parameter gradient of
+  sum_i v_i . w(x_i).
 """
 import numpy as np
 
@@ -170,3 +174,37 @@ def directional(p, x, v):
     hd1 = (1.0 - h1 ** 2) * (v @ W1.T)
     hd2 = (1.0 - h2 ** 2) * (hd1 @ W2.T)
     return float((hd2 @ w3).sum())
+
+
+def head_unpack(p, H):
+    p = np.asarray(p, np.float64)
+    o = 0
+    W1 = p[o:o + H * 32].reshape(H, 32); o += H * 32
+    b1 = p[o:o + H]; o += H
+    W2 = p[o:o + H * H].reshape(H, H); o += H * H
+    b2 = p[o:o + H]; o += H
+    W3 = p[o:o + 32 * H].reshape(32, H); o += 32 * H
+    b3 = p[o:o + 32]
+    return W1, b1, W2, b2, W3, b3
+
+
+def head_forward(p, x, H):
+    """w(x) of the direct-force head (n x 32)."""
+    W1, b1, W2, b2, W3, b3 = head_unpack(p, H)
+    h1 = np.tanh(np.asarray(x, np.float64) @ W1.T + b1)
+    h2 = np.tanh(h1 @ W2.T + b2)
+    return h2 @ W3.T + b3
+
+
+def head_grad(p, x, v, H):
+    """Parameter gradient of sum_i v_i . w(x_i), in the parameter layout."""
+    W1, b1, W2, b2, W3, b3 = head_unpack(p, H)
+    x = np.asarray(x, np.float64)
+    v = np.asarray(v, np.float64)
+    h1 = np.tanh(x @ W1.T + b1)
+    h2 = np.tanh(h1 @ W2.T + b2)
+    d3 = v
+    d2 = (d3 @ W3) * (1 - h2 * h2)
+    d1 = (d2 @ W2) * (1 - h1 * h1)
+    return np.concatenate([(d1.T @ x).ravel(), d1.sum(0), (d2.T @ h1).ravel(), d2.sum(0),
+                           (d3.T @ h2).ravel(), d3.sum(0)])

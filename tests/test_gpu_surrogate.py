@@ -148,6 +148,25 @@ def test_force_grad_vs_oracle(eng):
     assert g[6336] == 0.0
 
 
+@pytest.mark.parametrize("hidden", [32, 64, 128])
+def test_force_head_grad_vs_oracle(eng, hidden):
+    """The direct-force head (FP32 on the CUDA cores): its parameter gradient
+    of sum_i v_i . w(x_i) against the CPU restatement, for every width."""
+    from oracle import surrogate_ref as sref
+    rng = np.random.default_rng(21)
+    n_atoms = 300
+    with eng.Surrogate(seed=4, cutoff=MB_RC) as s:
+        s.set_model(1, hidden)
+        p = s.head_params()
+        p = s.head_params(p + rng.standard_normal(len(p)).astype(np.float32) * 0.05)
+        x = rng.standard_normal((n_atoms, 32)).astype(np.float32)
+        v = rng.standard_normal((n_atoms, 32)).astype(np.float32)
+        g = s.head_grad(x, v)
+    gr = sref.head_grad(p, x, v, hidden)
+    err = np.abs(g - gr).max() / np.abs(gr).max()
+    assert err < 1e-4, err
+
+
 def _train_surrogate(eng, s, temps=(300.0, 900.0, 1500.0), steps=3000):
     """Exact trajectories at several temperatures, then force matching."""
     for k, T in enumerate(temps):
@@ -208,3 +227,33 @@ def test_fallback_to_exact_kernel(eng):
     assert np.array_equal(got[0], ref[0]) and np.array_equal(got[1], ref[1])
     assert r0["surrogate_steps"] == 0 and r0["exact_steps"] == 25 and r0["rejected_checks"] == 5
     assert r1["surrogate_steps"] == 25 and r1["checks"] == 5 and r1["last_error"] > 0
+    assert r1["max_error"] >= r1["last_error"] and r0["max_error"] >= r0["last_error"] > 0
+
+
+def test_force_head_trains_and_drives_a_run(eng):
+    """The direct-force head, force-matched on the same trajectories as the
+    energy network, fits the exact bond-order forces at least as well (it is
+    not bound to a gradient field, and the exact forces are not one); its
+    energy is NaN, and behind the check it drives a run."""
+    pos, vel, L = nitrogen_diamond(4, temperature=600.0, seed=40, noise=0.02)
+    with eng.Surrogate(seed=11, cutoff=MB_RC) as s:
+        _train_surrogate(eng, s)
+        with _mb_engine(eng, pos, vel, L) as e:
+            e.step(30)
+            fx, _ = e.compute_forces()
+            fe, _ = s.forces(e)
+        s.set_model(1, 64)
+        assert s.head_scale() == 0.0
+        _, loss_f = s.train_forces(3000, lr=1e-3, w_energy=0.0, w_force=1.0)
+        assert s.head_scale() > 0.0
+        with _mb_engine(eng, pos, vel, L) as e:
+            e.step(30)
+            fh, eh = s.forces(e)
+            s.attach(e, threshold=1e9, check_every=5)
+            e.step(10)
+            r = s.report(e)
+    err_energy_model, err_head = rel_rms(fe, fx), rel_rms(fh, fx)
+    assert np.isfinite(loss_f) and loss_f < 0.5, loss_f
+    assert err_head < 0.7 and err_head <= 1.2 * err_energy_model, (err_head, err_energy_model)
+    assert np.isnan(eh)
+    assert r["surrogate_steps"] == 10 and r["last_error"] == pytest.approx(err_head, rel=0.5)

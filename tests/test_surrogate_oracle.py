@@ -1,6 +1,7 @@
 """The surrogate's CPU restatement checked against finite differences (no
 GPU): the force-matching gradient is the parameter gradient of
-sum_i v_i . dt/dx(x_i), and the energy-loss gradient that of mean((t-y)^2)."""
+sum_i v_i . dt/dx(x_i), the energy-loss gradient that of mean((t-y)^2), and
+the direct-force head's gradient that of sum_i v_i . w(x_i)."""
 import numpy as np
 
 from oracle import surrogate_ref as sref
@@ -47,4 +48,22 @@ def test_loss_grad_is_gradient_of_loss():
         dp = np.zeros_like(p)
         dp[k] = h
         fd = (loss(p + dp) - loss(p - dp)) / (2 * h)
+        assert abs(fd - g[k]) <= 1e-6 * max(1.0, abs(fd)), k
+
+
+def test_head_grad_is_gradient_of_projection():
+    rng = np.random.default_rng(3)
+    H = 32
+    n = 32 * H + H + H * H + H + 32 * H + 32
+    p = rng.standard_normal(n) * 0.3
+    x = rng.standard_normal((6, 32))
+    v = rng.standard_normal((6, 32))
+    g = sref.head_grad(p, x, v, H)
+    assert g.shape == (n,)
+    h = 1e-6
+    for k in rng.choice(n, 60, replace=False):
+        dp = np.zeros_like(p)
+        dp[k] = h
+        fd = ((sref.head_forward(p + dp, x, H) * v).sum()
+              - (sref.head_forward(p - dp, x, H) * v).sum()) / (2 * h)
         assert abs(fd - g[k]) <= 1e-6 * max(1.0, abs(fd)), k
