@@ -1,12 +1,9 @@
 // Configuration and results files of the reference, on the host.
 //
 // md_read_config follows common/ConfigParser.cpp:22-156 and
-// common/Loader.cpp:34-83: key=value lines, lines starting with "//" and
-// empty lines skipped, "//" comments cut from the end, keys upper-cased and
-// not trimmed, trailing blanks trimmed from values (except a value whose
-// only non-blank character is its first, ConfigParser.cpp:87), the first
-// occurrence of a key wins (unordered_map::insert), numbers read with
-// istream >> (bools as 0/1), and the 25 keys of Loader.cpp:49-82 mandatory.
+// common/Loader.cpp:34-83: key=value lines read by the rules R1-R6 below,
+// numbers read with istream >> (bools as 0/1), and the 25 keys of
+// Loader.cpp:49-82 mandatory.
 // md_write_results writes the .dat/.txt pair of common/Results.cpp:120-229
 // and the pair list of common/Results.cpp:88-118.
 #include <cctype>
@@ -33,45 +30,51 @@ std::string upper(std::string s) {
   return s;
 }
 
+// The reference's reading rules (common/ConfigParser.cpp:22-98), one by one:
+//  R1 lines as std::getline splits the file: a last line without '\n'
+//     counts, the empty segment after a final '\n' does not;
+//  R2 empty lines and lines that begin with "//" are skipped;
+//  R3 comments are cut at the LAST "//" again and again until none is left,
+//     so "a///b" keeps "a/";
+//  R4 the key is the text before the first '=', upper-cased and not
+//     trimmed; a line without '=' or with an empty key is an error that
+//     names how many key lines were read before it;
+//  R5 blanks (space, tab) are cut from the end of the value, unless the
+//     value is all blanks or its only non-blank character is its first;
+//  R6 the first line of a key wins.
+namespace rules {
+bool skipped(const std::string& l) { return l.empty() || l.compare(0, 2, "//") == 0; }  // R2
+std::string uncomment(std::string l) {                                                   // R3
+  for (size_t at; (at = l.rfind("//")) != std::string::npos;) l.erase(at);
+  return l;
+}
+std::string trim_value(const std::string& v) {  // R5
+  const size_t last = v.find_last_not_of(" \t");
+  return last == std::string::npos || last == 0 ? v : v.substr(0, last + 1);
+}
+}  // namespace rules
+
 bool parse_file(const char* path, Parsed& p) {
-  std::ifstream ifs(path, std::ifstream::in);
-  if (ifs.fail()) {
+  std::ifstream in(path);
+  if (!in) {
     p.err = "Error opening configuration file.";
     return false;
   }
-  int lineid = 0;
-  for (;;) {
-    std::string line;
-    std::getline(ifs, line);
-    if (ifs.eof() && line.empty()) break;
-    if (ifs.fail()) {
-      p.err = "Unable to read line from configuration file.";
+  int keys = 0;
+  for (std::string raw; std::getline(in, raw);) {  // R1
+    if (rules::skipped(raw)) continue;
+    const std::string line = rules::uncomment(raw);
+    const size_t eq = line.find('=');
+    if (eq == std::string::npos || eq == 0) {  // R4
+      p.err = "Error in configuration file!\nLine: " + std::to_string(keys);
       return false;
     }
-    if (!line.substr(0, 2).compare("//") || line.empty()) continue;
-    size_t pos;
-    while ((pos = line.rfind("//")) != std::string::npos) line = line.substr(0, pos);
-    pos = line.find("=");
-    if (pos == std::string::npos) {
-      p.err = "Error in configuration file!\nLine: " + std::to_string(lineid);
-      return false;
-    }
-    std::string key = line.substr(0, pos);
-    std::string value = line.substr(pos + 1);
-    if (key.empty()) {
-      p.err = "Error in configuration file!\nLine: " + std::to_string(lineid);
-      return false;
-    }
-    if (!value.empty()) {
-      int ipos = (int)value.size() - 1;
-      while (value[ipos] == ' ' || value[ipos] == '\t') {
-        ipos--;
-        if (ipos < 0) break;
-      }
-      if (ipos > 0 && ipos != (int)value.size() - 1) value = value.substr(0, ipos + 1);
-    }
-    p.kv.insert({upper(key), value});
-    lineid++;
+    p.kv.emplace(upper(line.substr(0, eq)), rules::trim_value(line.substr(eq + 1)));  // R6
+    keys++;
+  }
+  if (!in.eof()) {  // a read that failed before the end of the file
+    p.err = "Unable to read line from configuration file.";
+    return false;
   }
   return true;
 }

@@ -16,6 +16,7 @@ Every fixture is the reference's own output on a seeded input:
   walls       32 NG atoms thrown at the walls (vxcm 0.9, energy loss 0.5)
   quirk       an atom at +max|x| in cell `cells` (NeighborList.cpp:53,81,147)
   configs/    configuration files and the values readConfiguration returns
+              (alone: make_golden.py --configs-only)
   results     a .dat/.txt pair written by writeResults/tailResults
 """
 import json
@@ -57,12 +58,72 @@ def lj_case(R, pos, vel, rs, rc, steps, species_name):
                 run_thermo=run["thermo"], run_builds=run["builds"], species=species_name)
 
 
+def write_configs(R):
+    """Configuration files (common/ConfigParser.cpp semantics) and the values
+    the reference's readConfiguration returns for them."""
+    cfgdir = os.path.join(HERE, "configs")
+    os.makedirs(cfgdir, exist_ok=True)
+    base = {"Lennard Jones Particles": "864", "Many Body Particles": "0", "Timesteps": "1000",
+            "DT": "2", "Temperature": "94.4", "LennardJonesRS": "9.534",
+            "LennardJonesRCUT": "8.5125", "ManyBodyRS": "3.5", "ManyBodyRCUT": "3",
+            "Input": "input.txt", "Output": "output.txt", "Filename": "results",
+            "CUDA Blocks": "64", "Use Cuda": "0", "UseLennardJones": "1", "UseManyBody": "0",
+            "LennardJonesBPP": "0", "ManyBodyBPP": "0", "OutputTimesteps": "100", "Debug": "0",
+            "Fallback": "1", "VXCMFROM": "0", "VXCMTO": "0", "VXCMSTEP": "1", "EnergyLoss": "1",
+            "AnimationTimesteps": "-1", "AnimationData": "anim"}
+    cases = {
+        "plain": "".join(f"{k}={v}\n" for k, v in base.items()),
+        "comments_case_blanks": "// header comment\n\n" + "".join(
+            f"{k.lower() if i % 2 else k.upper()}={v}   // note\n" if k != "Input" else
+            f"{k}={v}\t \n" for i, (k, v) in enumerate(base.items())),
+        "duplicate_first_wins": "".join(f"{k}={v}\n" for k, v in base.items()) + "Timesteps=5\n",
+        "single_char_value_kept_blanks": "".join(
+            f"{k}={v}{'  ' if k == 'Debug' else ''}\n" for k, v in base.items()),
+        # "//" cut at its last occurrence again and again: "output.txt///c" -> "output.txt/"
+        "triple_slash_comment": "".join(
+            f"{k}={v}{'///c' if k == 'Output' else ''}\n" for k, v in base.items()),
+        # a value of blanks only keeps them
+        "blank_only_value": "".join(
+            f"{k}={'   ' if k == 'AnimationData' else v}\n" for k, v in base.items()),
+        # the last line has no newline
+        "last_line_without_newline": "\n".join(f"{k}={v}" for k, v in base.items()),
+    }
+    expect = {}
+    for name, text in cases.items():
+        path = os.path.join(cfgdir, name + ".cfg")
+        with open(path, "w") as fh:
+            fh.write(text)
+        ints = np.zeros(13, np.int32)
+        floats = np.zeros(10, np.float32)
+        import ctypes as C
+        strs = C.create_string_buffer(1024)
+        R.lib.ref_read_configuration(path.encode(), ints, floats, strs)
+        raw = strs.raw
+        expect[name] = dict(ints=ints.tolist(), floats=[float(x) for x in floats],
+                            strings=[raw[256 * k:256 * (k + 1)].split(b"\0")[0].decode()
+                                     for k in range(4)])
+    # files the reference rejects (missing key; line without '=')
+    with open(os.path.join(cfgdir, "bad_missing_key.cfg"), "w") as fh:
+        fh.write("".join(f"{k}={v}\n" for k, v in base.items() if k != "EnergyLoss"))
+    with open(os.path.join(cfgdir, "bad_no_equals.cfg"), "w") as fh:
+        fh.write("".join(f"{k}={v}\n" for k, v in base.items()) + "garbage line\n")
+    # keys are not trimmed: "Timesteps =5" is another key, and Timesteps is missing
+    with open(os.path.join(cfgdir, "bad_key_with_blank.cfg"), "w") as fh:
+        fh.write("".join(f"{k}{' ' if k == 'Timesteps' else ''}={v}\n"
+                         for k, v in base.items()))
+    with open(os.path.join(cfgdir, "expected.json"), "w") as fh:
+        json.dump(expect, fh, indent=1)
+
+
 def main():
     build_reference()
     R = load_reference("neon")
     RA = load_reference("argon")
     if R is None or RA is None:
         sys.exit("reference not built (sources missing?)")
+    if "--configs-only" in sys.argv:
+        write_configs(R)
+        return
     out = {}
     pos, vel, _ = lat.make_system("fcc", 3, 100.0, seed=11, a=4.3, species=2,
                                   mass_table="neon", noise=0.05)
@@ -123,47 +184,7 @@ def main():
             flat[f"{case}/{k}"] = np.asarray(v)
     np.savez_compressed(os.path.join(HERE, "reference_fixtures.npz"), **flat)
 
-    # configuration files (common/ConfigParser.cpp semantics)
-    cfgdir = os.path.join(HERE, "configs")
-    os.makedirs(cfgdir, exist_ok=True)
-    base = {"Lennard Jones Particles": "864", "Many Body Particles": "0", "Timesteps": "1000",
-            "DT": "2", "Temperature": "94.4", "LennardJonesRS": "9.534",
-            "LennardJonesRCUT": "8.5125", "ManyBodyRS": "3.5", "ManyBodyRCUT": "3",
-            "Input": "input.txt", "Output": "output.txt", "Filename": "results",
-            "CUDA Blocks": "64", "Use Cuda": "0", "UseLennardJones": "1", "UseManyBody": "0",
-            "LennardJonesBPP": "0", "ManyBodyBPP": "0", "OutputTimesteps": "100", "Debug": "0",
-            "Fallback": "1", "VXCMFROM": "0", "VXCMTO": "0", "VXCMSTEP": "1", "EnergyLoss": "1",
-            "AnimationTimesteps": "-1", "AnimationData": "anim"}
-    cases = {
-        "plain": "".join(f"{k}={v}\n" for k, v in base.items()),
-        "comments_case_blanks": "// header comment\n\n" + "".join(
-            f"{k.lower() if i % 2 else k.upper()}={v}   // note\n" if k != "Input" else
-            f"{k}={v}\t \n" for i, (k, v) in enumerate(base.items())),
-        "duplicate_first_wins": "".join(f"{k}={v}\n" for k, v in base.items()) + "Timesteps=5\n",
-        "single_char_value_kept_blanks": "".join(
-            f"{k}={v}{'  ' if k == 'Debug' else ''}\n" for k, v in base.items()),
-    }
-    expect = {}
-    for name, text in cases.items():
-        path = os.path.join(cfgdir, name + ".cfg")
-        with open(path, "w") as fh:
-            fh.write(text)
-        ints = np.zeros(13, np.int32)
-        floats = np.zeros(10, np.float32)
-        import ctypes as C
-        strs = C.create_string_buffer(1024)
-        R.lib.ref_read_configuration(path.encode(), ints, floats, strs)
-        raw = strs.raw
-        expect[name] = dict(ints=ints.tolist(), floats=[float(x) for x in floats],
-                            strings=[raw[256 * k:256 * (k + 1)].split(b"\0")[0].decode()
-                                     for k in range(4)])
-    # files the reference rejects (missing key; line without '=')
-    with open(os.path.join(cfgdir, "bad_missing_key.cfg"), "w") as fh:
-        fh.write("".join(f"{k}={v}\n" for k, v in base.items() if k != "EnergyLoss"))
-    with open(os.path.join(cfgdir, "bad_no_equals.cfg"), "w") as fh:
-        fh.write("".join(f"{k}={v}\n" for k, v in base.items()) + "garbage line\n")
-    with open(os.path.join(cfgdir, "expected.json"), "w") as fh:
-        json.dump(expect, fh, indent=1)
+    write_configs(R)
 
     # results writer
     rng = np.random.default_rng(21)

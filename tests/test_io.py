@@ -12,7 +12,8 @@ CFG = os.path.join(GOLD, "configs")
 
 
 @pytest.mark.parametrize("name", ["plain", "comments_case_blanks", "duplicate_first_wins",
-                                  "single_char_value_kept_blanks"])
+                                  "single_char_value_kept_blanks", "triple_slash_comment",
+                                  "blank_only_value", "last_line_without_newline"])
 def test_read_config_matches_reference(eng, name):
     exp = json.load(open(os.path.join(CFG, "expected.json")))[name]
     cfg, strings, extra = eng.read_config(os.path.join(CFG, name + ".cfg"))
@@ -28,11 +29,25 @@ def test_read_config_matches_reference(eng, name):
     assert (cfg.periodic, cfg.precision, cfg.species) == (0, 0, 0)
 
 
-@pytest.mark.parametrize("name", ["bad_missing_key", "bad_no_equals"])
+@pytest.mark.parametrize("name", ["bad_missing_key", "bad_no_equals", "bad_key_with_blank"])
 def test_bad_config_is_an_error_not_an_exit(eng, name):
     with pytest.raises(eng.EngineError) as ei:
         eng.read_config(os.path.join(CFG, name + ".cfg"))
     assert ei.value.status == 1  # MD_BAD_CONFIG
+
+
+def test_bad_line_names_the_key_lines_before_it(eng, tmp_path):
+    """ConfigParser.cpp:60-64: the line number in the message counts the
+    key lines read so far; comments and empty lines do not count."""
+    p = tmp_path / "c.cfg"
+    p.write_text("// c\n\nA=1\n\n// d\nB=2\nno equals here\n")
+    with pytest.raises(eng.EngineError) as ei:
+        eng.read_config(str(p))
+    assert "Line: 2" in str(ei.value)
+    p.write_text("A=1\n=2\n")
+    with pytest.raises(eng.EngineError) as ei:
+        eng.read_config(str(p))
+    assert "Line: 1" in str(ei.value)
 
 
 def test_extension_keys(eng, tmp_path):
