@@ -532,8 +532,8 @@ __global__ void __launch_bounds__(128)
 constexpr int kThirdMax = 64;
 struct ThirdSm {
   float x[kThirdMax], y[kThirdMax], z[kThirdMax];  // position at its image
-  float r[kThirdMax], fc[kThirdMax], dfc[kThirdMax];
-  float ux[kThirdMax], uy[kThirdMax], uz[kThirdMax];  // (r_i - r_m) / r_im
+  float r[kThirdMax], ir[kThirdMax], fc[kThirdMax], dfc[kThirdMax];  // r_im, 1 / r_im
+  float ux[kThirdMax], uy[kThirdMax], uz[kThirdMax];                // (r_i - r_m) / r_im
   int id[kThirdMax];                                  // atom, -1 for an NG atom
 };
 
@@ -569,20 +569,22 @@ __global__ void __launch_bounds__(128)
         int tm;
         PosT<T>::load(pos, posf, mp, xm, ym, zm, tm);
         PosT<T>::image(xm, ym, zm, em, g);
-        const T imx = xi - xm, imy = yi - ym, imz = zi - zm;
-        const T rim = md_sqrt(imx * imx + imy * imy + imz * imz);
-        T fci, dfci;
-        cutoff<T>(rim, fci, dfci);
+        const float imx = (float)(xi - xm), imy = (float)(yi - ym), imz = (float)(zi - zm);
+        const float r2 = imx * imx + imy * imy + imz * imz;
+        const float irim = rsqrtf(r2), rim = r2 * irim;
+        float fci, dfci;
+        cutoff<float>(rim, fci, dfci);
         TS.id[m] = tm == SP_NG ? -1 : mp;
         TS.x[m] = (float)xm;
         TS.y[m] = (float)ym;
         TS.z[m] = (float)zm;
-        TS.r[m] = (float)rim;
-        TS.fc[m] = (float)fci;
-        TS.dfc[m] = (float)dfci;
-        TS.ux[m] = (float)fdiv<T>(imx, rim);
-        TS.uy[m] = (float)fdiv<T>(imy, rim);
-        TS.uz[m] = (float)fdiv<T>(imz, rim);
+        TS.r[m] = rim;
+        TS.ir[m] = irim;
+        TS.fc[m] = fci;
+        TS.dfc[m] = dfci;
+        TS.ux[m] = imx * irim;
+        TS.uy[m] = imy * irim;
+        TS.uz[m] = imz * irim;
       }
       __syncwarp();
     }
@@ -599,7 +601,7 @@ __global__ void __launch_bounds__(128)
       if (tj == SP_NG || rij > cut_rijsq) {
         xsi_s[slot] = nanv;
         xsj_s[slot] = nanv;
-        va_s[slot] = 0;
+        if (!kFast) va_s[slot] = 0;
         continue;
       }
       rij = md_sqrt(rij);
@@ -620,7 +622,7 @@ __global__ void __launch_bounds__(128)
         T xsi = 0, xsj = 0;
         T dxsix = 0, dxsiy = 0, dxsiz = 0, dxsjx = 0, dxsjy = 0, dxsjz = 0;
         for (int m = 0; m < S; m++) {
-          T xm, ym, zm, rim, fci, dfci, drimx, drimy, drimz;
+          T xm, ym, zm, rim, inv_rim, fci, dfci, drimx, drimy, drimz;
           if (staged) {
             const int mp = TS.id[m];
             if (mp < 0 || mp == j) continue;
@@ -628,6 +630,7 @@ __global__ void __launch_bounds__(128)
             ym = TS.y[m];
             zm = TS.z[m];
             rim = TS.r[m];
+            inv_rim = TS.ir[m];
             fci = TS.fc[m];
             dfci = TS.dfc[m];
             drimx = TS.ux[m];
@@ -646,19 +649,27 @@ __global__ void __launch_bounds__(128)
             drimx = fdiv<T>(imx, rim);
             drimy = fdiv<T>(imy, rim);
             drimz = fdiv<T>(imz, rim);
+            inv_rim = fdiv<T>(1.0f, rim);
           }
           const T jmx = xj - xm, jmy = yj - ym, jmz = zj - zm;
-          const T rjm = md_sqrt(jmx * jmx + jmy * jmy + jmz * jmz);
+          T rjm, inv_rjm = 0;
+          if (kFast) {  // the distance and its reciprocal from one rsqrt
+            const float r2 = (float)(jmx * jmx + jmy * jmy + jmz * jmz);
+            const float ir = rsqrtf(r2);
+            inv_rjm = ir;
+            rjm = r2 * ir;
+          } else {
+            rjm = md_sqrt(jmx * jmx + jmy * jmy + jmz * jmz);
+          }
           T fcj, dfcj;
           cutoff<T>(rjm, fcj, dfcj);
           if (kFast && fci > 0) {
             // d cos / d r_i = drij (1/rim - cos/rij) + drim (1/rij - cos/rim):
             // the reference's quotient below, two scalars per triplet
-            const T inv_rim = fdiv<T>(1.0f, rim);
             const T num2 = rij * rij + rim * rim - rjm * rjm;
             const T icos = num2 * half_inv_rij * inv_rim;
             T gth, gpre;
-            angular<T>(icos, gth, gpre);
+            angular1<T>(icos, gth, gpre);
             xsi += fci * gth * E;
             const T fE = fci * E;
             const T cm = dfci * gth * E + fE * gpre * (inv_rij - icos * inv_rim);
@@ -685,11 +696,10 @@ __global__ void __launch_bounds__(128)
           }
           if (kFast && fcj > 0) {
             // d cos / d r_i = drij (1/rjm - cos/rij) - drim rim / (rij rjm)
-            const T inv_rjm = fdiv<T>(1.0f, rjm);
             const T num2 = rij * rij + rjm * rjm - rim * rim;
             const T jcos = num2 * half_inv_rij * inv_rjm;
             T gth, gpre;
-            angular<T>(jcos, gth, gpre);
+            angular1<T>(jcos, gth, gpre);
             xsj += fcj * gth * E;
             const T fE = fcj * E;
             const T cj = fE * (gpre * (inv_rjm - jcos * inv_rij) + (T)MD_LAMDA3 * gth);
@@ -723,10 +733,16 @@ __global__ void __launch_bounds__(128)
         dbx = 0.5f * (pbi * dxsix + pbj * dxsjx);
         dby = 0.5f * (pbi * dxsiy + pbj * dxsjy);
         dbz = 0.5f * (pbi * dxsiz + pbj * dxsjz);
+        if (kFast) {
+          // what the FP32 pass 2 needs of this pair: va E / (4 (1 + xi)^2) for
+          // either end (its force is -factor x the derivative of the angle terms)
+          xs_i = 0.25f * va * E * pbi;
+          xs_j = 0.25f * va * E * pbj;
+        }
       }
       xsi_s[slot] = xs_i;
       xsj_s[slot] = xs_j;
-      va_s[slot] = va;
+      if (!kFast) va_s[slot] = va;
       vander_waals<T>(vdw, dvdw, rij, get_r0v<T>(ti, tj));
       const T fij = dvr - bo * dva + dvdw;
       fx += fdiv<T>(fij * ijx, rij) - dbx * va;
@@ -772,8 +788,7 @@ __global__ void __launch_bounds__(128)
   const int warps = blockDim.x >> 5;
   const int k = blockIdx.x * warps + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
-  // FP32: the angle derivatives in a shorter, algebraically equal form
-  constexpr bool kFast = std::is_same<T, float>::value;
+  static_assert(std::is_same<T, double>::value, "FP32 pass 2 is k_mb_pass2f");
   double ev[1] = {0.0};
   if (k < n) {
     T xk, yk, zk;
@@ -796,7 +811,6 @@ __global__ void __launch_bounds__(128)
       T fci, dfci;
       cutoff<T>(rik, fci, dfci);
       const T drikx = fdiv<T>(ikx, rik), driky = fdiv<T>(iky, rik), drikz = fdiv<T>(ikz, rik);
-      const T inv_rik = fdiv<T>(1.0f, rik);
       const int Si = slen[ip];
       for (int sj = 0; sj < Si; sj++) {
         const size_t q = (size_t)sj * n + ip;
@@ -842,23 +856,8 @@ __global__ void __launch_bounds__(128)
         T fcj, dfcj;
         cutoff<T>(rjk, fcj, dfcj);
         const T E = md_exp((T)MD_LAMDA3 * (rij - re));
-        const T half_inv_rij = fdiv<T>(0.5f, rij), inv_rij = 2.0f * half_inv_rij;
-        const T inv_rjk = fdiv<T>(1.0f, rjk);
         T dbx = 0, dby = 0, dbz = 0;
-        if (kFast && fci > 0) {
-          // d cos / d r_k = drik (1/rij - cos/rik) - drjk rjk / (rij rik)
-          const T num2 = rij * rij + rik * rik - rjk * rjk;
-          const T icos = num2 * half_inv_rij * inv_rik;
-          T gth, gpre;
-          angular<T>(icos, gth, gpre);
-          const T p = fdiv<T>(1.0f, (1.0f + xs_i) * (1.0f + xs_i));
-          const T pE = 0.5f * p * E;
-          const T ck = pE * (dfci * gth + fci * gpre * (inv_rij - icos * inv_rik));
-          const T cj = -pE * fci * gpre * rjk * inv_rij * inv_rik;
-          dbx = fma(drikx, ck, fma(drjkx, cj, dbx));
-          dby = fma(driky, ck, fma(drjky, cj, dby));
-          dbz = fma(drikz, ck, fma(drjkz, cj, dbz));
-        } else if (fci > 0) {
+        if (fci > 0) {
           const T num2 = rij * rij + rik * rik - rjk * rjk;
           const T icos = fdiv<T>(num2, 2.0f * rij * rik);
           T gth, gpre;
@@ -872,20 +871,7 @@ __global__ void __launch_bounds__(128)
           dby += 0.5f * (p * (dfci * driky * gth * E + fci * (gpre * dcy) * E));
           dbz += 0.5f * (p * (dfci * drikz * gth * E + fci * (gpre * dcz) * E));
         }
-        if (kFast && fcj > 0) {
-          // d cos / d r_k = drjk (1/rij - cos/rjk) - drik rik / (rij rjk)
-          const T num2 = rij * rij + rjk * rjk - rik * rik;
-          const T jcos = num2 * half_inv_rij * inv_rjk;
-          T gth, gpre;
-          angular<T>(jcos, gth, gpre);
-          const T p = fdiv<T>(1.0f, (1.0f + xs_j) * (1.0f + xs_j));
-          const T pE = 0.5f * p * E;
-          const T cj = pE * (dfcj * gth + fcj * gpre * (inv_rij - jcos * inv_rjk));
-          const T ck = -pE * fcj * gpre * rik * inv_rij * inv_rjk;
-          dbx = fma(drjkx, cj, fma(drikx, ck, dbx));
-          dby = fma(drjky, cj, fma(driky, ck, dby));
-          dbz = fma(drjkz, cj, fma(drikz, ck, dbz));
-        } else if (fcj > 0) {
+        if (fcj > 0) {
           const T num2 = rij * rij + rjk * rjk - rik * rik;
           const T jcos = fdiv<T>(num2, 2.0f * rij * rjk);
           T gth, gpre;
@@ -906,6 +892,151 @@ __global__ void __launch_bounds__(128)
     }
     double sx = warp_sum((double)fx), sy = warp_sum((double)fy), sz = warp_sum((double)fz);
     int m = __reduce_add_sync(0xffffffffu, miss);
+    if (lane == 0) {
+      f3[3 * k] += sx;
+      f3[3 * k + 1] += sy;
+      f3[3 * k + 2] += sz;
+      if (m) atomicAdd(missing, m);
+      if (ENERGY) {
+        const md_double4 p = pos[k];
+        ev[0] = p.x * sx + p.y * sy + p.z * sz;
+      }
+    }
+  }
+  if (ENERGY) block_partial<1>(ev, epart);
+}
+
+
+// the part of pass 2 for one pair (i, j) of the warp's atom k: i at (xi, yi,
+// zi) with its k-side terms, j = entry sl[q]; adds -F_k to (fx, fy, fz)
+struct Pass2I {
+  float x, y, z, r, ir, fc, dfc, ux, uy, uz;
+  int id;
+};
+
+__device__ __forceinline__ void pass2_pair(const Pass2I& I, size_t q, int k, float xk, float yk,
+                                           float zk, const md_double4* pos, const float4* posf,
+                                           const uint32_t* sl, const Grid& g, const int* cell3,
+                                           const int* ref_rows, int ref_nls, int ref_nlargest,
+                                           float rc2, float cut_rijsq, const float* wi_s,
+                                           const float* wj_s, float& fx, float& fy, float& fz,
+                                           int& miss) {
+  const int jp = entry_index(sl[q]);
+  if (jp == k) return;
+  int im[3] = {0, 0, 0};
+  if (ref_rows) {
+    // caller-supplied rows (no periodic box): is jp in row k?
+    const int* row = ref_rows + (size_t)k * ref_nls;
+    bool found = false;
+    for (int q2 = 0; q2 < ref_nlargest && row[q2] != -1; q2++)
+      if (row[q2] == jp) {
+        found = true;
+        break;
+      }
+    if (!found) return;
+  } else if (!in_row(cell3, g, k, jp, im)) {
+    return;
+  }
+  // j at its image in k's row, as BondOrderFuncs.h:367-369 sees it
+  float xj, yj, zj;
+  int tj;
+  PosT<float>::load(pos, posf, jp, xj, yj, zj, tj);
+  if (im[0] | im[1] | im[2]) PosT<float>::image3(xj, yj, zj, im[0], im[1], im[2], g);
+  const float ijx = I.x - xj, ijy = I.y - yj, ijz = I.z - zj;
+  const float r2ij = ijx * ijx + ijy * ijy + ijz * ijz;
+  if (r2ij >= rc2 || r2ij > cut_rijsq) return;
+  const float wi = wi_s[q], wj = wj_s[q];
+  if (wi != wi || tj == SP_NG) {
+    miss++;
+    return;
+  }
+  const float irij = rsqrtf(r2ij), rij = r2ij * irij, half_irij = 0.5f * irij;
+  const float jkx = xj - xk, jky = yj - yk, jkz = zj - zk;
+  const float r2jk = jkx * jkx + jky * jky + jkz * jkz;
+  const float irjk = rsqrtf(r2jk), rjk = r2jk * irjk;
+  const float drjkx = -jkx * irjk, drjky = -jky * irjk, drjkz = -jkz * irjk;
+  float fcj, dfcj;
+  cutoff<float>(rjk, fcj, dfcj);
+  float ck = 0.f, cj = 0.f;  // coefficients of d_ik and d_jk in -F_k
+  if (I.fc > 0.f) {
+    // d cos / d r_k = drik (1/rij - cos/rik) - drjk rjk / (rij rik)
+    const float icos = (rij * rij + I.r * I.r - rjk * rjk) * half_irij * I.ir;
+    float gth, gpre;
+    angular1<float>(icos, gth, gpre);
+    ck = wi * (I.dfc * gth + I.fc * gpre * (irij - icos * I.ir));
+    cj = -wi * I.fc * gpre * rjk * irij * I.ir;
+  }
+  if (fcj > 0.f) {
+    // d cos / d r_k = drjk (1/rij - cos/rjk) - drik rik / (rij rjk)
+    const float jcos = (rij * rij + rjk * rjk - I.r * I.r) * half_irij * irjk;
+    float gth, gpre;
+    angular1<float>(jcos, gth, gpre);
+    cj = fmaf(wj, dfcj * gth + fcj * gpre * (irij - jcos * irjk), cj);
+    ck = fmaf(-wj * fcj * gpre, I.r * irij * irjk, ck);
+  }
+  fx -= fmaf(I.ux, ck, drjkx * cj);
+  fy -= fmaf(I.uy, ck, drjky * cj);
+  fz -= fmaf(I.uz, ck, drjkz * cj);
+}
+
+__device__ __forceinline__ Pass2I pass2_entry(uint32_t ei, float xk, float yk, float zk,
+                                              const md_double4* pos, const float4* posf,
+                                              const Grid& g) {
+  Pass2I I;
+  I.id = entry_index(ei);
+  int ti;
+  PosT<float>::load(pos, posf, I.id, I.x, I.y, I.z, ti);
+  PosT<float>::image(I.x, I.y, I.z, ei, g);
+  const float ikx = xk - I.x, iky = yk - I.y, ikz = zk - I.z;
+  const float r2 = ikx * ikx + iky * iky + ikz * ikz;
+  I.ir = rsqrtf(r2);
+  I.r = r2 * I.ir;
+  cutoff<float>(I.r, I.fc, I.dfc);
+  I.ux = ikx * I.ir;
+  I.uy = iky * I.ir;
+  I.uz = ikz * I.ir;
+  return I;
+}
+
+// Pass 2 in FP32 (BondOrderFuncs.h:148-237 bondOrder2 for every pair i-j
+// with k as third body), one entry i of k's short list per lane as in the
+// FP64 kernel.  Per pair, pass 1 left va E / (4 (1 + xi_ij)^2) and
+// va E / (4 (1 + xi_ji)^2) in the slot, so the exponential and the two
+// quotients of the reference's per-triplet expression are not evaluated
+// again here; NaN marks a slot pass 1 did not evaluate (its va is 0: counted
+// as missing, no force).  Distances come with their reciprocals from one
+// rsqrt.  (Spreading the (i, j) pairs of k over all 32 lanes through a prefix
+// of the row lengths was measured slower, 348 against 249 us on 32,768
+// atoms: lanes of one i read 32 different lines of the slot arrays, where
+// lanes of neighbouring i, stored side by side, share sectors.)
+template <bool ENERGY>
+__global__ void __launch_bounds__(128)
+    k_mb_pass2f(const md_double4* __restrict__ pos, const float4* __restrict__ posf,
+                double* __restrict__ f3, int n, const uint32_t* __restrict__ sl,
+                const int* __restrict__ slen, Grid g, const int* __restrict__ cell3,
+                const int* __restrict__ ref_rows, int ref_nls, int ref_nlargest,
+                double rcutsq, const float* __restrict__ wi_s, const float* __restrict__ wj_s,
+                int* __restrict__ missing, double* __restrict__ epart) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int k = blockIdx.x * 4 + warp;
+  double ev[1] = {0.0};
+  if (k < n) {
+    float xk, yk, zk;
+    int tk;
+    PosT<float>::load(pos, posf, k, xk, yk, zk, tk);
+    const int Sk = slen[k];
+    const float rc2 = (float)rcutsq, cut_rijsq = (float)MD_CUTOFF_RIJSQ;
+    float fx = 0.f, fy = 0.f, fz = 0.f;
+    int miss = 0;
+    for (int s = lane; s < Sk; s += 32) {
+      const Pass2I I = pass2_entry(sl[(size_t)s * n + k], xk, yk, zk, pos, posf, g);
+      const int Si = slen[I.id];
+      for (int sj = 0; sj < Si; sj++)
+        pass2_pair(I, (size_t)sj * n + I.id, k, xk, yk, zk, pos, posf, sl, g, cell3, ref_rows,
+                   ref_nls, ref_nlargest, rc2, cut_rijsq, wi_s, wj_s, fx, fy, fz, miss);
+    }
+    const double sx = warp_sum((double)fx), sy = warp_sum((double)fy), sz = warp_sum((double)fz);
+    const int m = __reduce_add_sync(0xffffffffu, miss);
     if (lane == 0) {
       f3[3 * k] += sx;
       f3[3 * k + 1] += sy;
@@ -964,6 +1095,19 @@ void launch_lj(const ForceArgs& a, bool fp32, bool energy, cudaStream_t st) {
 int lj_blocks(int n) { return nblk(n, 128); }
 int mb_blocks(int n) { return nblk(n, 4); }
 
+template <typename T, bool ENERGY>
+static void launch_pass2(const MbArgs& a, int B, T* xsi, T* xsj, T* va, cudaStream_t st) {
+  double* ep = ENERGY ? a.epart2 : nullptr;
+  if constexpr (std::is_same<T, float>::value)
+    k_mb_pass2f<ENERGY><<<B, 128, 0, st>>>(a.pos, a.posf, a.f3, a.n, a.sl, a.slen, a.grid,
+                                           a.cell3, a.ref_rows, a.ref_nls, a.ref_nlargest,
+                                           a.rcutsq, xsi, xsj, a.missing, ep);
+  else
+    k_mb_pass2<T, ENERGY><<<B, 128, 0, st>>>(a.pos, a.posf, a.f3, a.n, a.sl, a.slen, a.grid,
+                                             a.cell3, a.ref_rows, a.ref_nls, a.ref_nlargest,
+                                             a.rcutsq, xsi, xsj, va, a.missing, ep);
+}
+
 template <typename T>
 static void launch_mb_t(const MbArgs& a, bool energy, cudaStream_t st) {
   if (a.n <= 0) return;
@@ -976,15 +1120,11 @@ static void launch_mb_t(const MbArgs& a, bool energy, cudaStream_t st) {
   if (energy) {
     k_mb_pass1<T, true><<<B, 128, 0, st>>>(a.pos, a.posf, a.f3, a.n, a.sl, a.slen, a.grid,
                                            a.ljexist, xsi, xsj, va, a.epart1, a.eatom);
-    k_mb_pass2<T, true><<<B, 128, 0, st>>>(a.pos, a.posf, a.f3, a.n, a.sl, a.slen, a.grid,
-                                           a.cell3, a.ref_rows, a.ref_nls, a.ref_nlargest, a.rcutsq, xsi, xsj, va,
-                                           a.missing, a.epart2);
+    launch_pass2<T, true>(a, B, xsi, xsj, va, st);
   } else {
     k_mb_pass1<T, false><<<B, 128, 0, st>>>(a.pos, a.posf, a.f3, a.n, a.sl, a.slen, a.grid,
                                             a.ljexist, xsi, xsj, va, nullptr, nullptr);
-    k_mb_pass2<T, false><<<B, 128, 0, st>>>(a.pos, a.posf, a.f3, a.n, a.sl, a.slen, a.grid,
-                                            a.cell3, a.ref_rows, a.ref_nls, a.ref_nlargest, a.rcutsq, xsi, xsj,
-                                            va, a.missing, nullptr);
+    launch_pass2<T, false>(a, B, xsi, xsj, va, st);
   }
 }
 

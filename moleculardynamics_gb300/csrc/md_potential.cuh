@@ -93,6 +93,16 @@ __device__ __forceinline__ void angular(T costhe, T& g, T& gpre) {
   gpre = -fdiv<T>(MD_C, q * q) * 2.0f * hc;
 }
 
+// the same with one reciprocal, for the FP32 forms (the FP64 path keeps the
+// reference's two quotients)
+template <typename T>
+__device__ __forceinline__ void angular1(T costhe, T& g, T& gpre) {
+  const T hc = MD_H - costhe;
+  const T iq = fdiv<T>(1.0f, MD_D + hc * hc);
+  g = 1.0f + MD_C / MD_D - MD_C * iq;
+  gpre = -MD_C * iq * iq * 2.0f * hc;
+}
+
 // LennardJones.h:65-86: parameters of an NG pair, selected by the other type
 __device__ __forceinline__ int lj_select(int ti, int tj) { return ti == SP_NG ? tj : ti; }
 

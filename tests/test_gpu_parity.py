@@ -266,6 +266,32 @@ def test_precision_form_bond_order(eng):
     assert rel_rms(out[eng.PREC_MIXED], out[eng.PREC_FP64]) < 1e-4
 
 
+@pytest.mark.parametrize("mixed_o,steps", [(False, 0), (True, 0), (False, 300)])
+def test_precision_form_bond_order_periodic(eng, mixed_o, steps):
+    """The FP32 bond-order passes against FP64 at the same positions, lists built
+    at those positions: periodic diamond (N, or N and O), on the lattice and
+    after 300 FP64 steps at 900 K, when the structure has left the lattice."""
+    pos, vel, L = nitrogen_diamond(4, temperature=900.0, seed=31, mixed_o=mixed_o)
+    n = len(pos)
+    kw = dict(n_mb=n, use_lj=0, use_mb=1, mb_rs=MB_RS, mb_rcut=MB_RC, dt=0.5, periodic=1,
+              box=L, species=0)
+    if steps:
+        with _engine(eng, precision=eng.PREC_FP64, **kw) as e:
+            e.upload(pos, vel)
+            e.begin(0.0)
+            e.step(steps)
+            pos, vel = e.download()
+    out, miss = {}, {}
+    for prec in (eng.PREC_FP64, eng.PREC_MIXED):
+        with _engine(eng, precision=prec, **kw) as e:
+            e.upload(pos, vel)
+            e.begin(0.0)
+            out[prec] = e.compute_forces()[0]
+            miss[prec] = e.stats()["missing_xi"]
+    assert rel_rms(out[eng.PREC_MIXED], out[eng.PREC_FP64]) < 1e-4
+    assert miss[eng.PREC_MIXED] == miss[eng.PREC_FP64]
+
+
 def test_reference_signature_layer(eng, oracle):
     """mdgb_* (the functions a drop-in Device.cpp forwards to) against the oracle."""
     sh = eng.Shim(species=eng.SPECIES_NEON)
