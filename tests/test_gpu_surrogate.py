@@ -246,9 +246,19 @@ def test_force_head_trains_and_drives_a_run(eng):
         assert s.head_scale() == 0.0
         _, loss_f = s.train_forces(3000, lr=1e-3, w_energy=0.0, w_force=1.0)
         assert s.head_scale() > 0.0
+        saved = (s.head_params(), s.head_scale(), s.normalisation())
         with _mb_engine(eng, pos, vel, L) as e:
             e.step(30)
             fh, eh = s.forces(e)
+            # a head saved and restored into another surrogate gives the same
+            # forces (up to the order of the FP32 atomics of the force assembly)
+            with eng.Surrogate(seed=99, cutoff=MB_RC) as s2:
+                mean, istd, mu, sigma = saved[2]
+                s2.normalisation(mean, istd, mu, sigma)
+                s2.set_model(1, 64)
+                s2.head_params(saved[0])
+                s2.head_scale(saved[1])
+                fh2, _ = s2.forces(e)
             s.attach(e, threshold=1e9, check_every=5)
             e.step(10)
             r = s.report(e)
@@ -256,4 +266,5 @@ def test_force_head_trains_and_drives_a_run(eng):
     assert np.isfinite(loss_f) and loss_f < 0.5, loss_f
     assert err_head < 0.7 and err_head <= 1.2 * err_energy_model, (err_head, err_energy_model)
     assert np.isnan(eh)
+    assert rel_rms(fh2, fh) < 1e-6
     assert r["surrogate_steps"] == 10 and r["last_error"] == pytest.approx(err_head, rel=0.5)
