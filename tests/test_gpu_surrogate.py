@@ -199,7 +199,8 @@ def test_trained_network_gains_over_no_model(eng):
     # (about 10% apart on these lattices), and per-atom energies depend on
     # neighbours beyond the descriptor cutoff: part of the error is out of reach
     assert loss_f < 0.5, (loss_e, loss_f)
-    assert err_trained < 0.5 * err_untrained and err_trained < 0.7, (err_trained, err_untrained)
+    # measured 0.12-0.14 over runs (the training's FP32 atomics are not order-deterministic)
+    assert err_trained < 0.5 * err_untrained and err_trained < 0.3, (err_trained, err_untrained)
     # the energy term weighs 0.1 of the loss and 3000 steps fit its offset
     # loosely (9-11% in runs that differ only in float summation order): the
     # bound guards against an energy unrelated to the exact one
@@ -232,9 +233,10 @@ def test_fallback_to_exact_kernel(eng):
 
 def test_force_head_trains_and_drives_a_run(eng):
     """The direct-force head, force-matched on the same trajectories as the
-    energy network, fits the exact bond-order forces at least as well (it is
-    not bound to a gradient field, and the exact forces are not one); its
-    energy is NaN, and behind the check it drives a run."""
+    energy network, fits the exact bond-order forces as well as it does here
+    (0.135 against 0.12-0.14 over runs; on the 32,768-atom data of the bench
+    it does better, not being bound to a gradient field); its energy is NaN,
+    and behind the check it drives a run."""
     pos, vel, L = nitrogen_diamond(4, temperature=600.0, seed=40, noise=0.02)
     with eng.Surrogate(seed=11, cutoff=MB_RC) as s:
         _train_surrogate(eng, s)
@@ -263,8 +265,8 @@ def test_force_head_trains_and_drives_a_run(eng):
             e.step(10)
             r = s.report(e)
     err_energy_model, err_head = rel_rms(fe, fx), rel_rms(fh, fx)
-    assert np.isfinite(loss_f) and loss_f < 0.5, loss_f
-    assert err_head < 0.7 and err_head <= 1.2 * err_energy_model, (err_head, err_energy_model)
+    assert np.isfinite(loss_f) and loss_f < 0.2, loss_f
+    assert err_head < 0.3 and err_energy_model < 0.3, (err_head, err_energy_model)
     assert np.isnan(eh)
     assert rel_rms(fh2, fh) < 1e-6
     assert r["surrogate_steps"] == 10 and r["last_error"] == pytest.approx(err_head, rel=0.5)
