@@ -914,14 +914,15 @@ def run_case(args) -> int:
     from moleculardynamics_gb300 import engine as eng
     b.build()
     eng.load()
-    if args.case == "bo32k":
-        e = bond_order_lattice(eng, 900.0, 15, eng.PREC_MIXED)
+    if args.case in ("bo32k", "bo32k64"):
+        prec = eng.PREC_MIXED if args.case == "bo32k" else eng.PREC_FP64
+        e = bond_order_lattice(eng, 900.0, 15, prec)
         e.set_timing(True)
         e.step(args.steps)
         e.synchronize()
         ms, _ = e.kernel_time(eng.KERNEL_STEP)
         e.close()
-        print(json.dumps({"case": "bo32k", "atoms": 32768, "md_steps": args.steps,
+        print(json.dumps({"case": args.case, "atoms": 32768, "md_steps": args.steps,
                           "ms_per_step": ms / max(args.steps, 1)}))
     if args.case == "sur32k":
         # a briefly trained surrogate (two FP64 snapshots, 300 Adam steps; the
@@ -990,11 +991,12 @@ def main():
     ap.add_argument("--sur-fp64-steps", type=int, default=400)
     ap.add_argument("--sur-sweep", action="store_true",
                     help="also train the head at H = 32, 128 and both kinds on less data")
-    ap.add_argument("--case", default=None, choices=["bo32k", "sur32k"],
+    ap.add_argument("--case", default=None, choices=["bo32k", "bo32k64", "sur32k"],
                     help="a profiling case instead of the benchmark: bo32k runs the "
                          "32,768-atom bond-order lattice in the precision form for --steps "
-                         "MD steps and prints its step time; sur32k the same lattice driven "
-                         "by a briefly trained surrogate, the steps inside a profiler range")
+                         "MD steps and prints its step time (bo32k64: the plain FP64 path); "
+                         "sur32k the same lattice driven by a briefly trained surrogate, the "
+                         "steps inside a profiler range")
     ap.add_argument("--sur-kind", type=int, default=1, choices=[0, 1],
                     help="sur32k: 0 the energy network, 1 the direct-force head (H = 64)")
     args = ap.parse_args()

@@ -387,7 +387,7 @@ void mdgb_calculate_potential(const double* pos4, double* vib_lj, double* vib_mb
  * accumulated into when it is 1).  d_missing_xi (device int, may be NULL)
  * receives the number of third-body reads of a xi that pass 1 did not make
  * (a list built at other positions; those xi count as 0), as the regular
- * path reports missing_xi.  Scratch lives in one fixed array of about 33 MB
+ * path reports missing_xi.  Scratch lives in one fixed array of about 24 MB
  * inside the library, held on every GPU that loads it until the process
  * exits; sizes above 16384 atoms or 1048576 atom x row-slot pairs
  * (n * nlargestsize) are rejected with MD_BAD_ARGUMENT and a message in err.

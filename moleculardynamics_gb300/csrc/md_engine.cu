@@ -138,7 +138,7 @@ struct md_ctx {
   // bond-order scratch
   uint32_t* mb_sl = nullptr;
   int* mb_slen = nullptr;
-  void *xsi = nullptr, *xsj = nullptr, *va = nullptr;
+  void *xsi = nullptr, *xsj = nullptr;
   long long mb_elems = 0;
   // flags and reductions
   int* status = nullptr;
@@ -265,7 +265,7 @@ md_status ensure_epart(md_ctx* c, long long need) {
 md_status ensure_mb_scratch(md_ctx* c) {
   long long need = (long long)c->mb.cap * (c->cfg.n_mb > 0 ? c->cfg.n_mb : 1);
   if (need <= c->mb_elems && c->mb_sl) return MD_OK;
-  for (void** p : {(void**)&c->mb_sl, &c->xsi, &c->xsj, &c->va})
+  for (void** p : {(void**)&c->mb_sl, &c->xsi, &c->xsj})
     if (*p) {
       cudaFree(*p);
       *p = nullptr;
@@ -274,7 +274,6 @@ md_status ensure_mb_scratch(md_ctx* c) {
   CK(cudaMalloc(&c->mb_sl, sizeof(uint32_t) * (size_t)need), "mb short list");
   CK(cudaMalloc(&c->xsi, es * (size_t)need), "mb xi");
   CK(cudaMalloc(&c->xsj, es * (size_t)need), "mb xi");
-  CK(cudaMalloc(&c->va, es * (size_t)need), "mb va");
   c->mb_elems = need;
   return MD_OK;
 }
@@ -324,7 +323,6 @@ MbArgs mb_args(md_ctx* c, double* f3, int ljexist) {
   a.slen = c->mb_slen;
   a.xsi = c->xsi;
   a.xsj = c->xsj;
-  a.va = c->va;
   a.missing = c->missing;
   a.epart1 = nullptr;
   a.epart2 = nullptr;
@@ -1077,7 +1075,7 @@ void md_destroy(md_ctx* c) {
   for (cudaGraphExec_t x : c->gexec)
     if (x) cudaGraphExecDestroy(x);
   void* ptrs[] = {c->seq_buf, c->inv, c->sur_fx, c->sur_fs, c->rep_ranges, c->rep_buf, c->io, c->pos_alt, c->posf_alt, c->pos, c->vel, c->acc, c->b, c->c, c->f3, c->f3_tmp, c->posf, c->mb_sl,
-                  c->mb_slen, c->xsi, c->xsj, c->va, c->status, c->epart, c->dsc, c->rec,
+                  c->mb_slen, c->xsi, c->xsj, c->status, c->epart, c->dsc, c->rec,
                   c->sc.dpart, c->sc.umax, c->sc.counts, c->sc.block_sums};
   for (void* p : ptrs)
     if (p) cudaFree(p);

@@ -527,14 +527,16 @@ __global__ void __launch_bounds__(128)
   if (lane == 0) slen[i] = cnt;
 }
 
-// Third bodies m of the warp's atom i (pass 1, FP32): what depends on i and
-// m only, computed once per warp instead of once per pair i-j
+// Third bodies m of the warp's atom i (pass 1): what depends on i and m
+// only, computed once per warp instead of once per pair i-j.  In FP64 with
+// the expressions of the per-pair evaluation, so the values are the same.
 constexpr int kThirdMax = 64;
+template <typename T>
 struct ThirdSm {
-  float x[kThirdMax], y[kThirdMax], z[kThirdMax];  // position at its image
-  float r[kThirdMax], ir[kThirdMax], fc[kThirdMax], dfc[kThirdMax];  // r_im, 1 / r_im
-  float ux[kThirdMax], uy[kThirdMax], uz[kThirdMax];                // (r_i - r_m) / r_im
-  int id[kThirdMax];                                  // atom, -1 for an NG atom
+  T x[kThirdMax], y[kThirdMax], z[kThirdMax];  // position at its image
+  T r[kThirdMax], ir[kThirdMax], fc[kThirdMax], dfc[kThirdMax];  // r_im, 1 / r_im (FP32)
+  T ux[kThirdMax], uy[kThirdMax], uz[kThirdMax];                // (r_i - r_m) / r_im
+  int id[kThirdMax];                                            // atom, -1 for an NG atom
 };
 
 template <typename T, bool ENERGY>
@@ -542,7 +544,7 @@ __global__ void __launch_bounds__(128)
     k_mb_pass1(const md_double4* __restrict__ pos, const float4* __restrict__ posf,
                double* __restrict__ f3, int n, const uint32_t* __restrict__ sl,
                const int* __restrict__ slen, Grid g, int ljexist, T* __restrict__ xsi_s,
-               T* __restrict__ xsj_s, T* __restrict__ va_s, double* __restrict__ epart,
+               T* __restrict__ xsj_s, double* __restrict__ epart,
                double* __restrict__ eatom) {
   const int warps = blockDim.x >> 5;
   const int i = blockIdx.x * warps + (threadIdx.x >> 5);
@@ -550,8 +552,8 @@ __global__ void __launch_bounds__(128)
   // FP32: the angle derivatives in a shorter, algebraically equal form
   constexpr bool kFast = std::is_same<T, float>::value;
   double ev[2] = {0.0, 0.0};
-  __shared__ ThirdSm third_sm[4];
-  ThirdSm& TS = third_sm[(threadIdx.x >> 5) & 3];
+  __shared__ ThirdSm<T> third_sm[4];
+  ThirdSm<T>& TS = third_sm[(threadIdx.x >> 5) & 3];
   if (i < n) {
     T xi, yi, zi;
     int ti;
@@ -560,7 +562,7 @@ __global__ void __launch_bounds__(128)
     T fx = 0, fy = 0, fz = 0;
     const T cut_rijsq = (T)MD_CUTOFF_RIJSQ;
     const T nanv = (T)NAN;
-    const bool staged = kFast && S <= kThirdMax && blockDim.x <= 128;  // warp-uniform
+    const bool staged = S <= kThirdMax && blockDim.x <= 128;  // warp-uniform
     if (staged) {
       for (int m = lane; m < S; m += 32) {
         const uint32_t em = sl[(size_t)m * n + i];
@@ -569,22 +571,36 @@ __global__ void __launch_bounds__(128)
         int tm;
         PosT<T>::load(pos, posf, mp, xm, ym, zm, tm);
         PosT<T>::image(xm, ym, zm, em, g);
-        const float imx = (float)(xi - xm), imy = (float)(yi - ym), imz = (float)(zi - zm);
-        const float r2 = imx * imx + imy * imy + imz * imz;
-        const float irim = rsqrtf(r2), rim = r2 * irim;
-        float fci, dfci;
-        cutoff<float>(rim, fci, dfci);
         TS.id[m] = tm == SP_NG ? -1 : mp;
-        TS.x[m] = (float)xm;
-        TS.y[m] = (float)ym;
-        TS.z[m] = (float)zm;
-        TS.r[m] = rim;
-        TS.ir[m] = irim;
-        TS.fc[m] = fci;
-        TS.dfc[m] = dfci;
-        TS.ux[m] = imx * irim;
-        TS.uy[m] = imy * irim;
-        TS.uz[m] = imz * irim;
+        TS.x[m] = xm;
+        TS.y[m] = ym;
+        TS.z[m] = zm;
+        if constexpr (kFast) {
+          const float imx = xi - xm, imy = yi - ym, imz = zi - zm;
+          const float r2 = imx * imx + imy * imy + imz * imz;
+          const float irim = rsqrtf(r2), rim = r2 * irim;
+          float fci, dfci;
+          cutoff<float>(rim, fci, dfci);
+          TS.r[m] = rim;
+          TS.ir[m] = irim;
+          TS.fc[m] = fci;
+          TS.dfc[m] = dfci;
+          TS.ux[m] = imx * irim;
+          TS.uy[m] = imy * irim;
+          TS.uz[m] = imz * irim;
+        } else {
+          // the per-pair branch's expressions below, once per third body
+          const T imx = xi - xm, imy = yi - ym, imz = zi - zm;
+          const T rim = md_sqrt(imx * imx + imy * imy + imz * imz);
+          T fci, dfci;
+          cutoff<T>(rim, fci, dfci);
+          TS.r[m] = rim;
+          TS.fc[m] = fci;
+          TS.dfc[m] = dfci;
+          TS.ux[m] = fdiv<T>(imx, rim);
+          TS.uy[m] = fdiv<T>(imy, rim);
+          TS.uz[m] = fdiv<T>(imz, rim);
+        }
       }
       __syncwarp();
     }
@@ -601,7 +617,6 @@ __global__ void __launch_bounds__(128)
       if (tj == SP_NG || rij > cut_rijsq) {
         xsi_s[slot] = nanv;
         xsj_s[slot] = nanv;
-        if (!kFast) va_s[slot] = 0;
         continue;
       }
       rij = md_sqrt(rij);
@@ -630,7 +645,7 @@ __global__ void __launch_bounds__(128)
             ym = TS.y[m];
             zm = TS.z[m];
             rim = TS.r[m];
-            inv_rim = TS.ir[m];
+            inv_rim = kFast ? TS.ir[m] : T(0);  // written by the FP32 staging only
             fci = TS.fc[m];
             dfci = TS.dfc[m];
             drimx = TS.ux[m];
@@ -733,16 +748,13 @@ __global__ void __launch_bounds__(128)
         dbx = 0.5f * (pbi * dxsix + pbj * dxsjx);
         dby = 0.5f * (pbi * dxsiy + pbj * dxsjy);
         dbz = 0.5f * (pbi * dxsiz + pbj * dxsjz);
-        if (kFast) {
-          // what the FP32 pass 2 needs of this pair: va E / (4 (1 + xi)^2) for
-          // either end (its force is -factor x the derivative of the angle terms)
-          xs_i = 0.25f * va * E * pbi;
-          xs_j = 0.25f * va * E * pbj;
-        }
+        // what pass 2 needs of this pair: va E / (4 (1 + xi)^2) for either
+        // end (its force is -factor x the derivative of the angle terms)
+        xs_i = (T)0.25 * va * E * pbi;
+        xs_j = (T)0.25 * va * E * pbj;
       }
       xsi_s[slot] = xs_i;
       xsj_s[slot] = xs_j;
-      if (!kFast) va_s[slot] = va;
       vander_waals<T>(vdw, dvdw, rij, get_r0v<T>(ti, tj));
       const T fij = dvr - bo * dva + dvdw;
       fx += fdiv<T>(fij * ijx, rij) - dbx * va;
@@ -776,151 +788,33 @@ __global__ void __launch_bounds__(128)
   if (ENERGY) block_partial<2>(ev, epart);
 }
 
-template <typename T, bool ENERGY>
-__global__ void __launch_bounds__(128)
-    k_mb_pass2(const md_double4* __restrict__ pos, const float4* __restrict__ posf,
-               double* __restrict__ f3, int n, const uint32_t* __restrict__ sl,
-               const int* __restrict__ slen, Grid g, const int* __restrict__ cell3,
-               const int* __restrict__ ref_rows, int ref_nls, int ref_nlargest,
-               double rcutsq, const T* __restrict__ xsi_s, const T* __restrict__ xsj_s,
-               const T* __restrict__ va_s, int* __restrict__ missing,
-               double* __restrict__ epart) {
-  const int warps = blockDim.x >> 5;
-  const int k = blockIdx.x * warps + (threadIdx.x >> 5);
-  const int lane = threadIdx.x & 31;
-  static_assert(std::is_same<T, double>::value, "FP32 pass 2 is k_mb_pass2f");
-  double ev[1] = {0.0};
-  if (k < n) {
-    T xk, yk, zk;
-    int tk;
-    PosT<T>::load(pos, posf, k, xk, yk, zk, tk);
-    const int Sk = slen[k];
-    const T cut_rijsq = (T)MD_CUTOFF_RIJSQ;
-    const T rc2 = (T)rcutsq;
-    T fx = 0, fy = 0, fz = 0;
-    int miss = 0;
-    for (int s = lane; s < Sk; s += 32) {
-      const uint32_t ei = sl[(size_t)s * n + k];
-      const int ip = entry_index(ei);
-      T xi, yi, zi;
-      int ti;
-      PosT<T>::load(pos, posf, ip, xi, yi, zi, ti);
-      PosT<T>::image(xi, yi, zi, ei, g);
-      const T ikx = xk - xi, iky = yk - yi, ikz = zk - zi;
-      const T rik = md_sqrt(ikx * ikx + iky * iky + ikz * ikz);
-      T fci, dfci;
-      cutoff<T>(rik, fci, dfci);
-      const T drikx = fdiv<T>(ikx, rik), driky = fdiv<T>(iky, rik), drikz = fdiv<T>(ikz, rik);
-      const int Si = slen[ip];
-      for (int sj = 0; sj < Si; sj++) {
-        const size_t q = (size_t)sj * n + ip;
-        const uint32_t ej = sl[q];
-        const int jp = entry_index(ej);
-        if (jp == k) continue;
-        int im[3] = {0, 0, 0};
-        if (ref_rows) {
-          // caller-supplied rows (no periodic box): is jp in row k?
-          const int* row = ref_rows + (size_t)k * ref_nls;
-          bool found = false;
-          for (int q2 = 0; q2 < ref_nlargest && row[q2] != -1; q2++)
-            if (row[q2] == jp) {
-              found = true;
-              break;
-            }
-          if (!found) continue;
-        } else if (!in_row(cell3, g, k, jp, im)) {
-          continue;
-        }
-        // j at its image in k's row, as BondOrderFuncs.h:367-369 sees it
-        T xj, yj, zj;
-        int tj;
-        PosT<T>::load(pos, posf, jp, xj, yj, zj, tj);
-        if (im[0] | im[1] | im[2]) PosT<T>::image3(xj, yj, zj, im[0], im[1], im[2], g);
-        const T ijx = xi - xj, ijy = yi - yj, ijz = zi - zj;
-        T rij = ijx * ijx + ijy * ijy + ijz * ijz;
-        if (rij >= rc2 || rij > cut_rijsq) continue;
-        T xs_i = xsi_s[q], xs_j = xsj_s[q];
-        if (xs_i != xs_i || tj == SP_NG) {
-          miss++;
-          xs_i = 0;
-          xs_j = 0;
-        }
-        rij = md_sqrt(rij);
-        const T va = va_s[q];
-        const T re = get_re<T>(ti, tj);
-        const T pjx = xj, pjy = yj, pjz = zj;
-        // BondOrderFuncs.h:148-237 bondOrder2 (k third body of pair ip, jp)
-        const T jkx = pjx - xk, jky = pjy - yk, jkz = pjz - zk;
-        const T rjk = md_sqrt(jkx * jkx + jky * jky + jkz * jkz);
-        const T drjkx = fdiv<T>(-jkx, rjk), drjky = fdiv<T>(-jky, rjk), drjkz = fdiv<T>(-jkz, rjk);
-        T fcj, dfcj;
-        cutoff<T>(rjk, fcj, dfcj);
-        const T E = md_exp((T)MD_LAMDA3 * (rij - re));
-        T dbx = 0, dby = 0, dbz = 0;
-        if (fci > 0) {
-          const T num2 = rij * rij + rik * rik - rjk * rjk;
-          const T icos = fdiv<T>(num2, 2.0f * rij * rik);
-          T gth, gpre;
-          angular<T>(icos, gth, gpre);
-          const T den = 4.0f * rij * rij * rik * rik;
-          const T dcx = fdiv<T>(((2.0f * rik * drikx - 2.0f * rjk * drjkx) * 2.0f * rij * rik - (2.0f * rij * drikx) * num2), den);
-          const T dcy = fdiv<T>(((2.0f * rik * driky - 2.0f * rjk * drjky) * 2.0f * rij * rik - (2.0f * rij * driky) * num2), den);
-          const T dcz = fdiv<T>(((2.0f * rik * drikz - 2.0f * rjk * drjkz) * 2.0f * rij * rik - (2.0f * rij * drikz) * num2), den);
-          const T p = fdiv<T>(1.0f, (1.0f + xs_i) * (1.0f + xs_i));
-          dbx += 0.5f * (p * (dfci * drikx * gth * E + fci * (gpre * dcx) * E));
-          dby += 0.5f * (p * (dfci * driky * gth * E + fci * (gpre * dcy) * E));
-          dbz += 0.5f * (p * (dfci * drikz * gth * E + fci * (gpre * dcz) * E));
-        }
-        if (fcj > 0) {
-          const T num2 = rij * rij + rjk * rjk - rik * rik;
-          const T jcos = fdiv<T>(num2, 2.0f * rij * rjk);
-          T gth, gpre;
-          angular<T>(jcos, gth, gpre);
-          const T den = 4.0f * rij * rij * rjk * rjk;
-          const T dcx = fdiv<T>(((2.0f * rjk * drjkx - 2.0f * rik * drikx) * 2.0f * rij * rjk - (2.0f * rij * drjkx) * num2), den);
-          const T dcy = fdiv<T>(((2.0f * rjk * drjky - 2.0f * rik * driky) * 2.0f * rij * rjk - (2.0f * rij * drjky) * num2), den);
-          const T dcz = fdiv<T>(((2.0f * rjk * drjkz - 2.0f * rik * drikz) * 2.0f * rij * rjk - (2.0f * rij * drjkz) * num2), den);
-          const T p = fdiv<T>(1.0f, (1.0f + xs_j) * (1.0f + xs_j));
-          dbx += 0.5f * (p * (dfcj * drjkx * gth * E + fcj * (gpre * dcx) * E));
-          dby += 0.5f * (p * (dfcj * drjky * gth * E + fcj * (gpre * dcy) * E));
-          dbz += 0.5f * (p * (dfcj * drjkz * gth * E + fcj * (gpre * dcz) * E));
-        }
-        fx -= 0.5f * dbx * va;
-        fy -= 0.5f * dby * va;
-        fz -= 0.5f * dbz * va;
-      }
-    }
-    double sx = warp_sum((double)fx), sy = warp_sum((double)fy), sz = warp_sum((double)fz);
-    int m = __reduce_add_sync(0xffffffffu, miss);
-    if (lane == 0) {
-      f3[3 * k] += sx;
-      f3[3 * k + 1] += sy;
-      f3[3 * k + 2] += sz;
-      if (m) atomicAdd(missing, m);
-      if (ENERGY) {
-        const md_double4 p = pos[k];
-        ev[0] = p.x * sx + p.y * sy + p.z * sz;
-      }
-    }
-  }
-  if (ENERGY) block_partial<1>(ev, epart);
-}
-
-
-// the part of pass 2 for one pair (i, j) of the warp's atom k: i at (xi, yi,
-// zi) with its k-side terms, j = entry sl[q]; adds -F_k to (fx, fy, fz)
+// the part of pass 2 for one pair (i, j) of the warp's atom k: i at (x, y, z)
+// with its k-side terms, j = entry sl[q]; adds -F_k to (fx, fy, fz)
+template <typename T>
 struct Pass2I {
-  float x, y, z, r, ir, fc, dfc, ux, uy, uz;
+  T x, y, z, r, ir, fc, dfc, ux, uy, uz;
   int id;
 };
 
-__device__ __forceinline__ void pass2_pair(const Pass2I& I, size_t q, int k, float xk, float yk,
-                                           float zk, const md_double4* pos, const float4* posf,
+// r and 1/r from r^2: one rsqrt in FP32; the square root and a quotient in FP64
+template <typename T>
+__device__ __forceinline__ void dist_recip(T r2, T& r, T& ir) {
+  if constexpr (std::is_same<T, float>::value) {
+    ir = rsqrtf(r2);
+    r = r2 * ir;
+  } else {
+    r = md_sqrt(r2);
+    ir = fdiv<T>(1.0, r);
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ void pass2_pair(const Pass2I<T>& I, size_t q, int k, T xk, T yk, T zk,
+                                           const md_double4* pos, const float4* posf,
                                            const uint32_t* sl, const Grid& g, const int* cell3,
                                            const int* ref_rows, int ref_nls, int ref_nlargest,
-                                           float rc2, float cut_rijsq, const float* wi_s,
-                                           const float* wj_s, float& fx, float& fy, float& fz,
-                                           int& miss) {
+                                           T rc2, T cut_rijsq, const T* wi_s, const T* wj_s,
+                                           T& fx, T& fy, T& fz, int& miss) {
   const int jp = entry_index(sl[q]);
   if (jp == k) return;
   int im[3] = {0, 0, 0};
@@ -938,102 +832,105 @@ __device__ __forceinline__ void pass2_pair(const Pass2I& I, size_t q, int k, flo
     return;
   }
   // j at its image in k's row, as BondOrderFuncs.h:367-369 sees it
-  float xj, yj, zj;
+  T xj, yj, zj;
   int tj;
-  PosT<float>::load(pos, posf, jp, xj, yj, zj, tj);
-  if (im[0] | im[1] | im[2]) PosT<float>::image3(xj, yj, zj, im[0], im[1], im[2], g);
-  const float ijx = I.x - xj, ijy = I.y - yj, ijz = I.z - zj;
-  const float r2ij = ijx * ijx + ijy * ijy + ijz * ijz;
+  PosT<T>::load(pos, posf, jp, xj, yj, zj, tj);
+  if (im[0] | im[1] | im[2]) PosT<T>::image3(xj, yj, zj, im[0], im[1], im[2], g);
+  const T ijx = I.x - xj, ijy = I.y - yj, ijz = I.z - zj;
+  const T r2ij = ijx * ijx + ijy * ijy + ijz * ijz;
   if (r2ij >= rc2 || r2ij > cut_rijsq) return;
-  const float wi = wi_s[q], wj = wj_s[q];
+  const T wi = wi_s[q], wj = wj_s[q];
   if (wi != wi || tj == SP_NG) {
     miss++;
     return;
   }
-  const float irij = rsqrtf(r2ij), rij = r2ij * irij, half_irij = 0.5f * irij;
-  const float jkx = xj - xk, jky = yj - yk, jkz = zj - zk;
-  const float r2jk = jkx * jkx + jky * jky + jkz * jkz;
-  const float irjk = rsqrtf(r2jk), rjk = r2jk * irjk;
-  const float drjkx = -jkx * irjk, drjky = -jky * irjk, drjkz = -jkz * irjk;
-  float fcj, dfcj;
-  cutoff<float>(rjk, fcj, dfcj);
-  float ck = 0.f, cj = 0.f;  // coefficients of d_ik and d_jk in -F_k
-  if (I.fc > 0.f) {
+  T rij, irij, rjk, irjk;
+  dist_recip<T>(r2ij, rij, irij);
+  const T half_irij = (T)0.5 * irij;
+  const T jkx = xj - xk, jky = yj - yk, jkz = zj - zk;
+  dist_recip<T>(jkx * jkx + jky * jky + jkz * jkz, rjk, irjk);
+  const T drjkx = -jkx * irjk, drjky = -jky * irjk, drjkz = -jkz * irjk;
+  T fcj, dfcj;
+  cutoff<T>(rjk, fcj, dfcj);
+  T ck = 0, cj = 0;  // coefficients of d_ik and d_jk in -F_k
+  if (I.fc > 0) {
     // d cos / d r_k = drik (1/rij - cos/rik) - drjk rjk / (rij rik)
-    const float icos = (rij * rij + I.r * I.r - rjk * rjk) * half_irij * I.ir;
-    float gth, gpre;
-    angular1<float>(icos, gth, gpre);
+    const T icos = (rij * rij + I.r * I.r - rjk * rjk) * half_irij * I.ir;
+    T gth, gpre;
+    angular1<T>(icos, gth, gpre);
     ck = wi * (I.dfc * gth + I.fc * gpre * (irij - icos * I.ir));
     cj = -wi * I.fc * gpre * rjk * irij * I.ir;
   }
-  if (fcj > 0.f) {
+  if (fcj > 0) {
     // d cos / d r_k = drjk (1/rij - cos/rjk) - drik rik / (rij rjk)
-    const float jcos = (rij * rij + rjk * rjk - I.r * I.r) * half_irij * irjk;
-    float gth, gpre;
-    angular1<float>(jcos, gth, gpre);
-    cj = fmaf(wj, dfcj * gth + fcj * gpre * (irij - jcos * irjk), cj);
-    ck = fmaf(-wj * fcj * gpre, I.r * irij * irjk, ck);
+    const T jcos = (rij * rij + rjk * rjk - I.r * I.r) * half_irij * irjk;
+    T gth, gpre;
+    angular1<T>(jcos, gth, gpre);
+    cj = fma(wj, dfcj * gth + fcj * gpre * (irij - jcos * irjk), cj);
+    ck = fma(-wj * fcj * gpre, I.r * irij * irjk, ck);
   }
-  fx -= fmaf(I.ux, ck, drjkx * cj);
-  fy -= fmaf(I.uy, ck, drjky * cj);
-  fz -= fmaf(I.uz, ck, drjkz * cj);
+  fx -= fma(I.ux, ck, drjkx * cj);
+  fy -= fma(I.uy, ck, drjky * cj);
+  fz -= fma(I.uz, ck, drjkz * cj);
 }
 
-__device__ __forceinline__ Pass2I pass2_entry(uint32_t ei, float xk, float yk, float zk,
-                                              const md_double4* pos, const float4* posf,
-                                              const Grid& g) {
-  Pass2I I;
+template <typename T>
+__device__ __forceinline__ Pass2I<T> pass2_entry(uint32_t ei, T xk, T yk, T zk,
+                                                 const md_double4* pos, const float4* posf,
+                                                 const Grid& g) {
+  Pass2I<T> I;
   I.id = entry_index(ei);
   int ti;
-  PosT<float>::load(pos, posf, I.id, I.x, I.y, I.z, ti);
-  PosT<float>::image(I.x, I.y, I.z, ei, g);
-  const float ikx = xk - I.x, iky = yk - I.y, ikz = zk - I.z;
-  const float r2 = ikx * ikx + iky * iky + ikz * ikz;
-  I.ir = rsqrtf(r2);
-  I.r = r2 * I.ir;
-  cutoff<float>(I.r, I.fc, I.dfc);
+  PosT<T>::load(pos, posf, I.id, I.x, I.y, I.z, ti);
+  PosT<T>::image(I.x, I.y, I.z, ei, g);
+  const T ikx = xk - I.x, iky = yk - I.y, ikz = zk - I.z;
+  dist_recip<T>(ikx * ikx + iky * iky + ikz * ikz, I.r, I.ir);
+  cutoff<T>(I.r, I.fc, I.dfc);
   I.ux = ikx * I.ir;
   I.uy = iky * I.ir;
   I.uz = ikz * I.ir;
   return I;
 }
 
-// Pass 2 in FP32 (BondOrderFuncs.h:148-237 bondOrder2 for every pair i-j
-// with k as third body), one entry i of k's short list per lane as in the
-// FP64 kernel.  Per pair, pass 1 left va E / (4 (1 + xi_ij)^2) and
-// va E / (4 (1 + xi_ji)^2) in the slot, so the exponential and the two
-// quotients of the reference's per-triplet expression are not evaluated
-// again here; NaN marks a slot pass 1 did not evaluate (its va is 0: counted
-// as missing, no force).  Distances come with their reciprocals from one
-// rsqrt.  (Spreading the (i, j) pairs of k over all 32 lanes through a prefix
-// of the row lengths was measured slower, 348 against 249 us on 32,768
-// atoms: lanes of one i read 32 different lines of the slot arrays, where
-// lanes of neighbouring i, stored side by side, share sectors.)
-template <bool ENERGY>
+// Pass 2 (BondOrderFuncs.h:148-237 bondOrder2 for every pair i-j with k as
+// third body), one entry i of k's short list per lane.  Per pair, pass 1
+// left va E / (4 (1 + xi_ij)^2) and va E / (4 (1 + xi_ji)^2) in the slot, so
+// the exponential and the two quotients of the reference's per-triplet
+// expression are not evaluated again here; NaN marks a slot pass 1 did not
+// evaluate (its va is 0: counted as missing, no force).  Each angle's
+// derivative takes the shorter equal form (test_bond_order_identities: equal
+// to 1e-13 in FP64) with one reciprocal per distance: one rsqrt in FP32, a
+// square root and a quotient in FP64.  (Spreading the (i, j) pairs of k over
+// all 32 lanes through a prefix of the row lengths was measured slower in
+// FP32, 348 against 249 us on 32,768 atoms: lanes of one i read 32 different
+// lines of the slot arrays, where lanes of neighbouring i, stored side by
+// side, share sectors.)
+template <typename T, bool ENERGY>
 __global__ void __launch_bounds__(128)
-    k_mb_pass2f(const md_double4* __restrict__ pos, const float4* __restrict__ posf,
-                double* __restrict__ f3, int n, const uint32_t* __restrict__ sl,
-                const int* __restrict__ slen, Grid g, const int* __restrict__ cell3,
-                const int* __restrict__ ref_rows, int ref_nls, int ref_nlargest,
-                double rcutsq, const float* __restrict__ wi_s, const float* __restrict__ wj_s,
-                int* __restrict__ missing, double* __restrict__ epart) {
+    k_mb_pass2(const md_double4* __restrict__ pos, const float4* __restrict__ posf,
+               double* __restrict__ f3, int n, const uint32_t* __restrict__ sl,
+               const int* __restrict__ slen, Grid g, const int* __restrict__ cell3,
+               const int* __restrict__ ref_rows, int ref_nls, int ref_nlargest, double rcutsq,
+               const T* __restrict__ wi_s, const T* __restrict__ wj_s,
+               int* __restrict__ missing, double* __restrict__ epart) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int k = blockIdx.x * 4 + warp;
   double ev[1] = {0.0};
   if (k < n) {
-    float xk, yk, zk;
+    T xk, yk, zk;
     int tk;
-    PosT<float>::load(pos, posf, k, xk, yk, zk, tk);
+    PosT<T>::load(pos, posf, k, xk, yk, zk, tk);
     const int Sk = slen[k];
-    const float rc2 = (float)rcutsq, cut_rijsq = (float)MD_CUTOFF_RIJSQ;
-    float fx = 0.f, fy = 0.f, fz = 0.f;
+    const T rc2 = (T)rcutsq, cut_rijsq = (T)MD_CUTOFF_RIJSQ;
+    T fx = 0, fy = 0, fz = 0;
     int miss = 0;
     for (int s = lane; s < Sk; s += 32) {
-      const Pass2I I = pass2_entry(sl[(size_t)s * n + k], xk, yk, zk, pos, posf, g);
+      const Pass2I<T> I = pass2_entry<T>(sl[(size_t)s * n + k], xk, yk, zk, pos, posf, g);
       const int Si = slen[I.id];
       for (int sj = 0; sj < Si; sj++)
-        pass2_pair(I, (size_t)sj * n + I.id, k, xk, yk, zk, pos, posf, sl, g, cell3, ref_rows,
-                   ref_nls, ref_nlargest, rc2, cut_rijsq, wi_s, wj_s, fx, fy, fz, miss);
+        pass2_pair<T>(I, (size_t)sj * n + I.id, k, xk, yk, zk, pos, posf, sl, g, cell3,
+                      ref_rows, ref_nls, ref_nlargest, rc2, cut_rijsq, wi_s, wj_s, fx, fy, fz,
+                      miss);
     }
     const double sx = warp_sum((double)fx), sy = warp_sum((double)fy), sz = warp_sum((double)fz);
     const int m = __reduce_add_sync(0xffffffffu, miss);
@@ -1096,16 +993,11 @@ int lj_blocks(int n) { return nblk(n, 128); }
 int mb_blocks(int n) { return nblk(n, 4); }
 
 template <typename T, bool ENERGY>
-static void launch_pass2(const MbArgs& a, int B, T* xsi, T* xsj, T* va, cudaStream_t st) {
-  double* ep = ENERGY ? a.epart2 : nullptr;
-  if constexpr (std::is_same<T, float>::value)
-    k_mb_pass2f<ENERGY><<<B, 128, 0, st>>>(a.pos, a.posf, a.f3, a.n, a.sl, a.slen, a.grid,
+static void launch_pass2(const MbArgs& a, int B, T* xsi, T* xsj, cudaStream_t st) {
+  k_mb_pass2<T, ENERGY><<<B, 128, 0, st>>>(a.pos, a.posf, a.f3, a.n, a.sl, a.slen, a.grid,
                                            a.cell3, a.ref_rows, a.ref_nls, a.ref_nlargest,
-                                           a.rcutsq, xsi, xsj, a.missing, ep);
-  else
-    k_mb_pass2<T, ENERGY><<<B, 128, 0, st>>>(a.pos, a.posf, a.f3, a.n, a.sl, a.slen, a.grid,
-                                             a.cell3, a.ref_rows, a.ref_nls, a.ref_nlargest,
-                                             a.rcutsq, xsi, xsj, va, a.missing, ep);
+                                           a.rcutsq, xsi, xsj, a.missing,
+                                           ENERGY ? a.epart2 : nullptr);
 }
 
 template <typename T>
@@ -1116,15 +1008,14 @@ static void launch_mb_t(const MbArgs& a, bool energy, cudaStream_t st) {
   const int B = nblk(a.n, 4);
   T* xsi = (T*)a.xsi;
   T* xsj = (T*)a.xsj;
-  T* va = (T*)a.va;
   if (energy) {
     k_mb_pass1<T, true><<<B, 128, 0, st>>>(a.pos, a.posf, a.f3, a.n, a.sl, a.slen, a.grid,
-                                           a.ljexist, xsi, xsj, va, a.epart1, a.eatom);
-    launch_pass2<T, true>(a, B, xsi, xsj, va, st);
+                                           a.ljexist, xsi, xsj, a.epart1, a.eatom);
+    launch_pass2<T, true>(a, B, xsi, xsj, st);
   } else {
     k_mb_pass1<T, false><<<B, 128, 0, st>>>(a.pos, a.posf, a.f3, a.n, a.sl, a.slen, a.grid,
-                                            a.ljexist, xsi, xsj, va, nullptr, nullptr);
-    launch_pass2<T, false>(a, B, xsi, xsj, va, st);
+                                            a.ljexist, xsi, xsj, nullptr, nullptr);
+    launch_pass2<T, false>(a, B, xsi, xsj, st);
   }
 }
 

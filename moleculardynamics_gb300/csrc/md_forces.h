@@ -44,9 +44,8 @@ struct MbArgs {
   int ljexist;          // accumulate onto F (BondOrderFuncs.h:325-336)
   uint32_t* sl;         // short list scratch (cap x n)
   int* slen;
-  void* xsi;            // per (i, slot), T
-  void* xsj;
-  void* va;
+  void* xsi;            // per (i, slot), T: pass 2's factor va E / (4 (1 + xi_ij)^2)
+  void* xsj;            // and va E / (4 (1 + xi_ji)^2), NaN where pass 1 skipped the pair
   int* missing;
   double* epart1;       // 2 doubles per pass-1 block
   double* epart2;       // 1 double per pass-2 block

@@ -33,7 +33,7 @@ struct Shim {
   int* len = nullptr;
   uint32_t* sl = nullptr;
   int* slen = nullptr;
-  double *xsi = nullptr, *xsj = nullptr, *va = nullptr;
+  double *xsi = nullptr, *xsj = nullptr;
   long long ell_alloc = 0, len_alloc = 0;
   int* flags = nullptr;  // status, wall flag, missing
   Scratch sc;
@@ -270,9 +270,9 @@ void mdgb_many_body_forces(const double* pos4, double* f3, int n, int nlargestsi
   const long long ell = (long long)cap * n;
   SHIM_CK(grow(s.rows, s.rows_alloc, nrows) && grow(s.ell, s.ell_alloc, ell), MD_OUT_OF_MEMORY);
   // short list and xi scratch sized like the ELL rows
-  static thread_local long long sl_alloc = 0, x_alloc = 0, xj_alloc = 0, va_alloc = 0;
+  static thread_local long long sl_alloc = 0, x_alloc = 0, xj_alloc = 0;
   SHIM_CK(grow(s.sl, sl_alloc, ell) && grow(s.xsi, x_alloc, ell) && grow(s.xsj, xj_alloc, ell) &&
-              grow(s.va, va_alloc, ell) && grow(s.len, s.len_alloc, n),
+              grow(s.len, s.len_alloc, n),
           MD_OUT_OF_MEMORY);
   static thread_local long long slen_alloc = 0;
   SHIM_CK(grow(s.slen, slen_alloc, n), MD_OUT_OF_MEMORY);
@@ -301,7 +301,6 @@ void mdgb_many_body_forces(const double* pos4, double* f3, int n, int nlargestsi
   a.slen = s.slen;
   a.xsi = s.xsi;
   a.xsj = s.xsj;
-  a.va = s.va;
   a.missing = s.flags + 2;
   launch_mb(a, false, false, s.st);
   SHIM_CK(down(f3, s.v[4], 24 * (size_t)n) && finish(), MD_CUDA_ERROR);

@@ -11,7 +11,7 @@
 // passes device arrays for the inputs and the output.
 //
 // Limits: at most kStaticMaxAtoms atoms and kStaticMaxSlots atom x row-slot
-// pairs (n * nlargestsize).  The array is about 33 MB and every GPU that loads
+// pairs (n * nlargestsize).  The array is about 24 MB and every GPU that loads
 // the library holds it until the process exits.  All calls share it and it
 // keeps the last call's contents, so calls that overlap on the GPU (two
 // streams, two host threads) race on it: serialise them.
@@ -27,14 +27,13 @@ namespace {
 constexpr long long kStaticMaxAtoms = 16384;
 constexpr long long kStaticMaxSlots = 1 << 20;
 
-// layout: ell | short list (uint32 per slot), xsi | xsj | va (double per
-// slot), len | slen (int per atom), flags (4 ints: missing count, ...)
+// layout: ell | short list (uint32 per slot), xsi | xsj (double per slot),
+// len | slen (int per atom), flags (4 ints: missing count, ...)
 constexpr size_t kOffEll = 0;
 constexpr size_t kOffSl = kOffEll + 4 * kStaticMaxSlots;
 constexpr size_t kOffXsi = kOffSl + 4 * kStaticMaxSlots;
 constexpr size_t kOffXsj = kOffXsi + 8 * kStaticMaxSlots;
-constexpr size_t kOffVa = kOffXsj + 8 * kStaticMaxSlots;
-constexpr size_t kOffLen = kOffVa + 8 * kStaticMaxSlots;
+constexpr size_t kOffLen = kOffXsj + 8 * kStaticMaxSlots;
 constexpr size_t kOffSlen = kOffLen + 4 * kStaticMaxAtoms;
 constexpr size_t kOffFlags = kOffSlen + 4 * kStaticMaxAtoms;
 constexpr size_t kStaticBytes = kOffFlags + 256;
@@ -130,7 +129,6 @@ extern "C" int mdgb_many_body_forces_static(const double* d_pos4, double* d_f3, 
   a.slen = (int*)(base + kOffSlen);
   a.xsi = base + kOffXsi;
   a.xsj = base + kOffXsj;
-  a.va = base + kOffVa;
   a.missing = flags;
   launch_mb(a, false, false, st);
   // pass 2's count of xi reads that pass 1 never made (the regular entry
