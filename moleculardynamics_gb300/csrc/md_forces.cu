@@ -595,6 +595,7 @@ __global__ void __launch_bounds__(128)
           T fci, dfci;
           cutoff<T>(rim, fci, dfci);
           TS.r[m] = rim;
+          TS.ir[m] = fdiv<T>(1.0, rim);
           TS.fc[m] = fci;
           TS.dfc[m] = dfci;
           TS.ux[m] = fdiv<T>(imx, rim);
@@ -645,7 +646,7 @@ __global__ void __launch_bounds__(128)
             ym = TS.y[m];
             zm = TS.z[m];
             rim = TS.r[m];
-            inv_rim = kFast ? TS.ir[m] : T(0);  // written by the FP32 staging only
+            inv_rim = TS.ir[m];
             fci = TS.fc[m];
             dfci = TS.dfc[m];
             drimx = TS.ux[m];
@@ -675,12 +676,13 @@ __global__ void __launch_bounds__(128)
             rjm = r2 * ir;
           } else {
             rjm = md_sqrt(jmx * jmx + jmy * jmy + jmz * jmz);
+            inv_rjm = fdiv<T>(1.0, rjm);
           }
           T fcj, dfcj;
           cutoff<T>(rjm, fcj, dfcj);
-          if (kFast && fci > 0) {
-            // d cos / d r_i = drij (1/rim - cos/rij) + drim (1/rij - cos/rim):
-            // the reference's quotient below, two scalars per triplet
+          if (fci > 0) {
+            // d cos / d r_i = drij (1/rim - cos/rij) + drim (1/rij - cos/rim): the
+            // reference's quotient per component (BondOrderFuncs.h) in two scalars
             const T num2 = rij * rij + rim * rim - rjm * rjm;
             const T icos = num2 * half_inv_rij * inv_rim;
             T gth, gpre;
@@ -692,24 +694,8 @@ __global__ void __launch_bounds__(128)
             dxsix = fma(drimx, cm, fma(drijx, cj, dxsix));
             dxsiy = fma(drimy, cm, fma(drijy, cj, dxsiy));
             dxsiz = fma(drimz, cm, fma(drijz, cj, dxsiz));
-          } else if (fci > 0) {
-            const T num2 = rij * rij + rim * rim - rjm * rjm;
-            const T icos = fdiv<T>(num2, 2.0f * rij * rim);
-            T gth, gpre;
-            angular<T>(icos, gth, gpre);
-            xsi += fci * gth * E;
-            const T den = 4.0f * rij * rij * rim * rim;
-            const T dcx = fdiv<T>(((2.0f * rij * drijx + 2.0f * rim * drimx) * 2.0f * rij * rim -
-                           (2.0f * rim * drijx + 2.0f * rij * drimx) * num2), den);
-            const T dcy = fdiv<T>(((2.0f * rij * drijy + 2.0f * rim * drimy) * 2.0f * rij * rim -
-                           (2.0f * rim * drijy + 2.0f * rij * drimy) * num2), den);
-            const T dcz = fdiv<T>(((2.0f * rij * drijz + 2.0f * rim * drimz) * 2.0f * rij * rim -
-                           (2.0f * rim * drijz + 2.0f * rij * drimz) * num2), den);
-            dxsix += dfci * drimx * gth * E + fci * (gpre * dcx) * E + fci * gth * MD_LAMDA3 * E * drijx;
-            dxsiy += dfci * drimy * gth * E + fci * (gpre * dcy) * E + fci * gth * MD_LAMDA3 * E * drijy;
-            dxsiz += dfci * drimz * gth * E + fci * (gpre * dcz) * E + fci * gth * MD_LAMDA3 * E * drijz;
           }
-          if (kFast && fcj > 0) {
+          if (fcj > 0) {
             // d cos / d r_i = drij (1/rjm - cos/rij) - drim rim / (rij rjm)
             const T num2 = rij * rij + rjm * rjm - rim * rim;
             const T jcos = num2 * half_inv_rij * inv_rjm;
@@ -722,22 +708,6 @@ __global__ void __launch_bounds__(128)
             dxsjx = fma(drijx, cj, fma(drimx, cm, dxsjx));
             dxsjy = fma(drijy, cj, fma(drimy, cm, dxsjy));
             dxsjz = fma(drijz, cj, fma(drimz, cm, dxsjz));
-          } else if (fcj > 0) {
-            const T num2 = rij * rij + rjm * rjm - rim * rim;
-            const T jcos = fdiv<T>(num2, 2.0f * rij * rjm);
-            T gth, gpre;
-            angular<T>(jcos, gth, gpre);
-            xsj += fcj * gth * E;
-            const T den = 4.0f * rij * rij * rjm * rjm;
-            const T dcx = fdiv<T>(((2.0f * rij * drijx - 2.0f * rim * drimx) * 2.0f * rij * rjm -
-                           2.0f * rjm * drijx * num2), den);
-            const T dcy = fdiv<T>(((2.0f * rij * drijy - 2.0f * rim * drimy) * 2.0f * rij * rjm -
-                           2.0f * rjm * drijy * num2), den);
-            const T dcz = fdiv<T>(((2.0f * rij * drijz - 2.0f * rim * drimz) * 2.0f * rij * rjm -
-                           2.0f * rjm * drijz * num2), den);
-            dxsjx += fcj * ((gpre * dcx) * E + MD_LAMDA3 * E * drijx * gth);
-            dxsjy += fcj * ((gpre * dcy) * E + MD_LAMDA3 * E * drijy * gth);
-            dxsjz += fcj * ((gpre * dcz) * E + MD_LAMDA3 * E * drijz * gth);
           }
         }
         xs_i = xsi;
