@@ -77,6 +77,13 @@ __global__ void __launch_bounds__(128)
     const int ti = (int)pi.w;
     const double box = w.g.box;
     double fx = 0.0, fy = 0.0, fz = 0.0;
+    // the species-pair constants of LennardJones.h:12-30, once per thread
+    double sq[3], cn[3];
+#pragma unroll
+    for (int t = 0; t < 3; t++) {
+      sq[t] = lj_sigsq(sp.sig[t]);
+      cn[t] = lj_con(sp.eps[t], sq[t]);
+    }
     auto visit = [&](int j, int ix, int iy, int iz, bool img) {
       const md_double4 pj = pos[j];
       double xj = pj.x, yj = pj.y, zj = pj.z;
@@ -92,7 +99,9 @@ __global__ void __launch_bounds__(128)
       if (tj == SP_NG || ti == SP_NG) {
         const int sel = lj_select(ti, tj);
         const double sig = sp.sig[sel], eps = sp.eps[sel];
-        const double fij = lj_pair_exact(fx, fy, fz, __dsqrt_rn(r2), ijx, ijy, ijz, sig, eps);
+        const double sigsq = sel == 0 ? sq[0] : (sel == 1 ? sq[1] : sq[2]);
+        const double con = sel == 0 ? cn[0] : (sel == 1 ? cn[1] : cn[2]);
+        const double fij = lj_pair_exact_c(fx, fy, fz, __dsqrt_rn(r2), ijx, ijy, ijz, sigsq, con);
         if (ENERGY) {
           // common/DebugCalculations.cpp:199-201 per ordered pair, restricted
           // to the force's pairs; shifted by its value at the cutoff

@@ -459,7 +459,11 @@ int list_build(NeighborList& nl, md_double4* pos, int n, const Grid& g, int comp
   double rc = rcut;
   nl.trip_dist = compact ? 0.5 * ((double)rv - rc) - (double)margin : 1e300;
   nl.rv2_keep = rv2;
-  if (!nl.skin && (e = cudaMalloc(&nl.skin, sizeof(int) * 4)) != cudaSuccess) return e;
+  if (!nl.skin) {
+    if ((e = cudaMalloc(&nl.skin, sizeof(int) * 4)) != cudaSuccess) return e;
+    // [3], the trip count, is cleared by its reader after each build: zero it once here
+    cudaMemsetAsync(nl.skin, 0, sizeof(int) * 4, st);
+  }
   cudaMemsetAsync(nl.skin, 0, sizeof(int) * 3, st);
   return (int)cudaGetLastError();
 }

@@ -108,11 +108,11 @@ __device__ __forceinline__ int lj_select(int ti, int tj) { return ti == SP_NG ? 
 
 // LennardJones.h:12-30 in FP64 with every rounding of the reference
 // (no FMA contraction): adds r_ij * f_ij to (fx, fy, fz) and returns f_ij.
-__device__ __forceinline__ double lj_pair_exact(double& fx, double& fy, double& fz,
-                                                double dist, double ijx, double ijy,
-                                                double ijz, double sig, double eps) {
-  double sigsq = xmul(sig, sig);
-  double con = xdiv(xmul(24.0, eps), sigsq);
+// sigsq = sig * sig and con = 24 eps / sigsq depend on the species pair only:
+// a caller that evaluates them once with these operations gets the same bits
+__device__ __forceinline__ double lj_pair_exact_c(double& fx, double& fy, double& fz,
+                                                  double dist, double ijx, double ijy,
+                                                  double ijz, double sigsq, double con) {
   double dist2 = xdiv(xmul(dist, dist), sigsq);
   double dist4 = xmul(dist2, dist2);
   double dist8 = xmul(dist4, dist4);
@@ -125,6 +125,18 @@ __device__ __forceinline__ double lj_pair_exact(double& fx, double& fy, double& 
   fy = xadd(fy, xmul(ijy, fij));
   fz = xadd(fz, xmul(ijz, fij));
   return fij;
+}
+
+__device__ __forceinline__ double lj_sigsq(double sig) { return xmul(sig, sig); }
+__device__ __forceinline__ double lj_con(double eps, double sigsq) {
+  return xdiv(xmul(24.0, eps), sigsq);
+}
+
+__device__ __forceinline__ double lj_pair_exact(double& fx, double& fy, double& fz,
+                                                double dist, double ijx, double ijy,
+                                                double ijz, double sig, double eps) {
+  const double sigsq = lj_sigsq(sig);
+  return lj_pair_exact_c(fx, fy, fz, dist, ijx, ijy, ijz, sigsq, lj_con(eps, sigsq));
 }
 
 }  // namespace mdgb
