@@ -557,10 +557,14 @@ def surrogate_form(eng, device, train_steps: int, run_steps: int, fp64_steps: in
         es0 = s.forces(e)[1]
         errs = []
         e.set_timing(True)
-        if series:  # the check error after every check (one per 10 steps)
+        if series:  # the check error after every check (one per 10 steps);
+            # a check declined for descriptors outside the training range fails
+            declined = 0
             for _ in range(steps // 10):
                 e.step(10)
-                errs.append(eng.Surrogate.report(e)["last_error"])
+                rep = eng.Surrogate.report(e)
+                errs.append(np.inf if rep["declined_steps"] > declined else rep["last_error"])
+                declined = rep["declined_steps"]
         else:
             e.step(steps)
         e.synchronize()
@@ -608,8 +612,11 @@ def surrogate_form(eng, device, train_steps: int, run_steps: int, fp64_steps: in
     strict, errs = run(1e-4, run_steps, eng.PREC_MIXED, series=True)
     accept = {str(t): float((errs <= t).mean()) for t in SUR_LADDER}
     tau = next((t for t in SUR_LADDER if accept[str(t)] >= 0.5), SUR_LADDER[-1])
+    fin = errs[np.isfinite(errs)]
     strict["check_error_along_exact_trajectory"] = {
-        "min": float(errs.min()), "median": float(np.median(errs)), "max": float(errs.max()),
+        "declined_checks": int((~np.isfinite(errs)).sum()),
+        "min": float(fin.min()) if len(fin) else None,
+        "median": float(np.median(errs)), "max": float(fin.max()) if len(fin) else None,
         "by_1000_steps": [float(np.median(errs[k:k + 100])) for k in range(0, len(errs), 100)]}
     at_best, _ = run(tau, run_steps, eng.PREC_MIXED)
     at_best["threshold"] = tau
@@ -627,7 +634,9 @@ def surrogate_form(eng, device, train_steps: int, run_steps: int, fp64_steps: in
                    "run": f"NVE at 900 K (dt 0.5 fs), FP64 Gear; surrogate runs {run_steps} "
                           f"steps, exact FP64 {fp64_steps} steps",
                    "threshold_policy": "exact-kernel check every 10 steps (the context's "
-                                       "precision: FP32 pairs for the surrogate runs)"},
+                                       "precision: FP32 pairs for the surrogate runs); a "
+                                       "step with any atom's descriptors outside the training "
+                                       "range (widened by a tenth) takes the exact forces"},
         "trajectories_s": t_traj,
         "models": models,
         "chosen_model": chosen["model"],

@@ -250,6 +250,8 @@ typedef struct md_surrogate_stats {
   long long rejected_checks;   /* checks whose error exceeded the threshold */
   double last_error;           /* relative RMS force error at the last check */
   double max_error;            /* the largest of them since md_surrogate_attach */
+  long long declined_steps;    /* steps (checks included) on which some atom's descriptors
+                                  lay outside the training data's range: exact forces */
 } md_surrogate_stats;
 md_status md_surrogate_create(int device, unsigned long long seed, float cutoff,
                               md_surrogate** out);
@@ -317,6 +319,13 @@ md_status md_surrogate_set_model(md_surrogate* s, int kind, int hidden);
  * normalisation (set = 0 reads it, 0 before then; set = 1 restores a saved
  * value together with md_surrogate_head_params) */
 md_status md_surrogate_head_scale(md_surrogate* s, double* scale, int set);
+/* The descriptor range the attached surrogate accepts (32 normalised lower
+ * and upper bounds).  md_surrogate_train_forces sets it to the range of the
+ * stored configurations, widened by a tenth of each span; while it is set, a
+ * step on which any atom's descriptors fall outside it takes the exact
+ * kernel's forces, and a check on such a step fails.  set = 0 reads it
+ * (MD_BAD_ARGUMENT before any training), set = 1 restores a saved one. */
+md_status md_surrogate_range(md_surrogate* s, float* lo32, float* hi32, int set);
 /* parameters of the direct-force head: W1 [h][32], b1 [h], W2 [h][h], b2 [h],
  * W3 [32][h], b3 [32]; count must be md_surrogate_head_param_count(hidden) */
 int md_surrogate_head_param_count(int hidden);

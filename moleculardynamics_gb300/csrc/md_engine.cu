@@ -133,6 +133,7 @@ struct md_ctx {
   int sur_every = 10, sur_last_check = -1;
   bool sur_use = false;
   long long sur_steps = 0, sur_exact_steps = 0, sur_checks = 0, sur_rejects = 0;
+  long long sur_declined = 0;  // steps whose descriptors left the training range
   double *sur_fx = nullptr, *sur_fs = nullptr;  // check buffers (3 doubles per many-body atom)
   long long graph_windows = 0;
   // bond-order scratch
@@ -366,28 +367,37 @@ md_status mb_forces_step(md_ctx* c, double* f3) {
   if (c->t - c->sur_last_check >= c->sur_every || c->sur_last_check < 0 || c->t < c->sur_last_check) {
     MbArgs a = mb_args(c, c->sur_fx, 0);
     launch_mb(a, c->mixed(), false, c->st);
+    bool declined = false;
     int r = sur_forces(*c->sur, c->pos, nmb, make_walker(c->mb), c->sur_fs, 0, nullptr, c->status,
-                       c->st);
+                       c->st, &declined);
     if (r) return r == -1 ? fail(c, MD_BAD_ARGUMENT, "surrogate not trained")
                           : cuda_fail(c, (cudaError_t)r, "surrogate forces");
-    double err = 0;
-    r = sur_rel_err(c->sur_fs, c->sur_fx, nmb, c->sur->scratch, &err, c->st);
-    if (r) return cuda_fail(c, (cudaError_t)r, "surrogate check");
-    c->sur_err = err;
-    c->sur_err_max = std::max(c->sur_err_max, err);
+    // an atom outside the training data's descriptor range fails the check
+    double err = INFINITY;
+    if (!declined) {
+      r = sur_rel_err(c->sur_fs, c->sur_fx, nmb, c->sur->scratch, &err, c->st);
+      if (r) return cuda_fail(c, (cudaError_t)r, "surrogate check");
+      c->sur_err = err;
+      c->sur_err_max = std::max(c->sur_err_max, err);
+    } else {
+      c->sur_declined++;
+    }
     c->sur_use = err <= c->sur_threshold;
     c->sur_last_check = c->t;
     c->sur_checks++;
     if (!c->sur_use) c->sur_rejects++;
     c->stats.launches += 12;
   }
+  bool declined = false;
   if (c->sur_use) {
     int r = sur_forces(*c->sur, c->pos, nmb, make_walker(c->mb), f3, acc, nullptr, c->status,
-                       c->st);
+                       c->st, &declined);
     if (r) return cuda_fail(c, (cudaError_t)r, "surrogate forces");
-    c->sur_steps++;
     c->stats.launches += 7;
-  } else {
+    if (declined) c->sur_declined++;
+    else c->sur_steps++;
+  }
+  if (!c->sur_use || declined) {
     launch_mb(mb_args(c, f3, acc), c->mixed(), false, c->st);
     c->sur_exact_steps++;
     c->stats.launches += 3;
@@ -1809,7 +1819,7 @@ md_status md_surrogate_attach(md_ctx* c, md_surrogate* s, double threshold, int 
   c->sur_last_check = -1;
   c->sur_use = false;
   c->sur_err = c->sur_err_max = -1.0;
-  c->sur_steps = c->sur_exact_steps = c->sur_checks = c->sur_rejects = 0;
+  c->sur_steps = c->sur_exact_steps = c->sur_checks = c->sur_rejects = c->sur_declined = 0;
   return MD_OK;
 }
 
@@ -1821,6 +1831,7 @@ md_status md_surrogate_report(const md_ctx* c, md_surrogate_stats* out) {
   out->rejected_checks = c->sur_rejects;
   out->last_error = c->sur_err;
   out->max_error = c->sur_err_max;
+  out->declined_steps = c->sur_declined;
   return MD_OK;
 }
 
@@ -1937,6 +1948,16 @@ md_status md_surrogate_head_scale(md_surrogate* s, double* scale, int set) {
   if (!(*scale > 0.0) || !std::isfinite(*scale)) return MD_BAD_ARGUMENT;
   s->fh_out = *scale;
   return MD_OK;
+}
+
+md_status md_surrogate_range(md_surrogate* s, float* lo32, float* hi32, int set) {
+  if (!s || !lo32 || !hi32) return MD_BAD_ARGUMENT;
+  if (set)
+    for (int f = 0; f < 32; f++)
+      if (!(lo32[f] <= hi32[f])) return MD_BAD_ARGUMENT;
+  int r = sur_range(*s, lo32, hi32, set != 0, s->stream);
+  if (r == -1) return MD_BAD_ARGUMENT;
+  return r ? MD_CUDA_ERROR : MD_OK;
 }
 
 md_status md_surrogate_head_grad(md_surrogate* s, const float* x, const float* v, int n,

@@ -6,6 +6,7 @@
 // energies of the exact method, and the tensor-core self-test.
 #include <cuda_bf16.h>
 
+#include <climits>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -1344,6 +1345,43 @@ __global__ void k_fh_gscale(const float* __restrict__ istd, float frms, float* _
 
 __global__ void k_fill_nan(double* p) { *p = __longlong_as_double(0x7FF8000000000000LL); }
 
+// floats as ints with the same order (negative values: the 31 low bits flipped)
+__device__ __forceinline__ int ord_key(float f) {
+  const int b = __float_as_int(f);
+  return b >= 0 ? b : b ^ 0x7FFFFFFF;
+}
+
+// per-feature minimum and maximum of X (n32 = 32 n values, atom-major) as
+// ordered keys; the grid's stride is a multiple of 32, so a thread keeps
+// one feature
+__global__ void k_feat_range(const float* __restrict__ X, long long n32, int* __restrict__ lo,
+                             int* __restrict__ hi) {
+  const int f = threadIdx.x & 31;
+  int kl = INT_MAX, kh = INT_MIN;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < n32;
+       e += (long long)gridDim.x * blockDim.x) {
+    const int k = ord_key(X[e]);
+    kl = min(kl, k);
+    kh = max(kh, k);
+  }
+  atomicMin(&lo[f], kl);
+  atomicMax(&hi[f], kh);
+}
+
+// flag = 1 when a value of X lies outside [lo_f, hi_f] of its feature (or is NaN)
+__global__ void k_range_check(const float* __restrict__ X, long long n32,
+                              const float* __restrict__ lo, const float* __restrict__ hi,
+                              int* __restrict__ flag) {
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  bool out = false;
+  if (e < n32) {
+    const float x = X[e];
+    const int f = (int)(e & 31);
+    out = !(x >= lo[f] && x <= hi[f]);
+  }
+  if (__any_sync(0xffffffffu, out) && (threadIdx.x & 31) == 0) atomicOr(flag, 1);
+}
+
 // probe outputs: w uniform on [-sqrt 3, sqrt 3] (unit variance, from a
 // splitmix64 hash of the index), written as coefficients w istd_d
 __global__ void k_fh_probe(float* __restrict__ gcoef, long long n32, const float* __restrict__ istd,
@@ -1811,12 +1849,30 @@ int sur_net_eval(Surrogate& s, const float* X, int n, float* t, float* dtdx, cud
 // bond-order forces (into f3, added when accumulate) and per-atom energies
 // of atoms [0, n) from the network; energy_dev (optional) gets their sum
 int sur_forces(Surrogate& s, const md_double4* pos, int n, const RowWalker& w, double* f3,
-               int accumulate, double* energy_dev, int* d_status, cudaStream_t st) {
+               int accumulate, double* energy_dev, int* d_status, cudaStream_t st,
+               bool* declined) {
   if (!s.normalised) return -1;
   set_attrs();
   int r = sur_descriptors(s, pos, n, w, true, d_status, st);
   if (r) return r;
   if (n == 0) return 0;
+  if (declined) {
+    *declined = false;
+    if (s.have_range) {
+      // outside the training data's descriptor range the model is not used
+      cudaMemsetAsync(s.oor_d, 0, sizeof(int), st);
+      k_range_check<<<sblocks(32LL * n, 256), 256, 0, st>>>(s.X, 32LL * n, s.xlo_d, s.xhi_d,
+                                                            s.oor_d);
+      int flag = 0;
+      cudaError_t e = cudaMemcpyAsync(&flag, s.oor_d, sizeof(int), cudaMemcpyDeviceToHost, st);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+      if (e != cudaSuccess) return e;
+      if (flag) {
+        *declined = true;
+        return 0;
+      }
+    }
+  }
   if (s.kind == 1) {
     // the direct-force head: coefficients straight from the network; it
     // models forces only, so the energy it reports is NaN
@@ -1976,6 +2032,74 @@ int train_fh(Surrogate& s, int steps, float lr, int nmax, double* loss_e, double
 }
 }  // namespace
 
+namespace {
+// the descriptor range of the stored configurations (normalised), widened
+// by range_margin of each feature's span
+int fm_range(Surrogate& s, cudaStream_t st) {
+  cudaError_t e;
+  long long h = 0;
+  if (!s.xlo_d) {
+    if ((e = sur_grow(s.xlo_d, h, 32)) != cudaSuccess) return e;
+    h = 0;
+    if ((e = sur_grow(s.xhi_d, h, 32)) != cudaSuccess) return e;
+    h = 0;
+    if ((e = sur_grow(s.oor_d, h, 4)) != cudaSuccess) return e;
+  }
+  int init[64];
+  for (int f = 0; f < 32; f++) {
+    init[f] = INT_MAX;
+    init[32 + f] = INT_MIN;
+  }
+  // the ordered keys are kept in xlo_d and xhi_d until they are decoded below
+  int* klo = reinterpret_cast<int*>(s.xlo_d);
+  int* khi = reinterpret_cast<int*>(s.xhi_d);
+  cudaMemcpyAsync(klo, init, sizeof(int) * 32, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(khi, init + 32, sizeof(int) * 32, cudaMemcpyHostToDevice, st);
+  for (const SurConfig& c : s.cfgs)
+    if (c.X && c.n > 0) k_feat_range<<<304, 256, 0, st>>>(c.X, 32LL * c.n, klo, khi);
+  int keys[64];
+  cudaMemcpyAsync(keys, klo, sizeof(int) * 32, cudaMemcpyDeviceToHost, st);
+  cudaMemcpyAsync(keys + 32, khi, sizeof(int) * 32, cudaMemcpyDeviceToHost, st);
+  if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
+  float lo[32], hi[32];
+  for (int f = 0; f < 32; f++) {
+    auto val = [](int k) {
+      const int b = k >= 0 ? k : k ^ 0x7FFFFFFF;
+      float v;
+      std::memcpy(&v, &b, sizeof(v));
+      return v;
+    };
+    const float a = val(keys[f]), b = val(keys[32 + f]), span = b - a;
+    lo[f] = a - s.range_margin * span;
+    hi[f] = b + s.range_margin * span;
+  }
+  return sur_range(s, lo, hi, true, st);
+}
+}  // namespace
+
+int sur_range(Surrogate& s, float* lo, float* hi, bool set, cudaStream_t st) {
+  cudaError_t e;
+  if (set) {
+    long long h = 0;
+    if (!s.xlo_d) {
+      if ((e = sur_grow(s.xlo_d, h, 32)) != cudaSuccess) return e;
+      h = 0;
+      if ((e = sur_grow(s.xhi_d, h, 32)) != cudaSuccess) return e;
+      h = 0;
+      if ((e = sur_grow(s.oor_d, h, 4)) != cudaSuccess) return e;
+    }
+    cudaMemcpyAsync(s.xlo_d, lo, sizeof(float) * 32, cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(s.xhi_d, hi, sizeof(float) * 32, cudaMemcpyHostToDevice, st);
+    if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
+    s.have_range = true;
+    return 0;
+  }
+  if (!s.have_range) return -1;
+  cudaMemcpyAsync(lo, s.xlo_d, sizeof(float) * 32, cudaMemcpyDeviceToHost, st);
+  cudaMemcpyAsync(hi, s.xhi_d, sizeof(float) * 32, cudaMemcpyDeviceToHost, st);
+  return cudaStreamSynchronize(st);
+}
+
 int sur_train_fm(Surrogate& s, int steps, float lr, double* loss_e, double* loss_f,
                  cudaStream_t st) {
   if (s.cfgs.empty()) return -1;
@@ -2035,6 +2159,7 @@ int sur_train_fm(Surrogate& s, int steps, float lr, double* loss_e, double* loss
     if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
     s.n_iota = nmax;
   }
+  if ((e = (cudaError_t)fm_range(s, st)) != cudaSuccess) return e;
   if (s.kind == 1) return train_fh(s, steps, lr, nmax, loss_e, loss_f, st);
   const NetDev w = net_of(s);
   double acc_e = 0, acc_f = 0;
@@ -2131,6 +2256,8 @@ md_surrogate::~md_surrogate() {
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (void* p : {(void*)iota_d, (void*)V, (void*)E3, (void*)pos32})
+    if (p) cudaFree(p);
+  for (void* p : {(void*)xlo_d, (void*)xhi_d, (void*)oor_d})
     if (p) cudaFree(p);
   for (void* p : {(void*)FP_d, (void*)FM_d, (void*)FV_d, (void*)FG_d, (void*)fh_gs,
                   (void*)fh_xT, (void*)fh_h1T, (void*)fh_h2T, (void*)fh_d1T, (void*)fh_d2T,

@@ -94,6 +94,13 @@ struct md_surrogate {
   // outputs drawn with unit variance per component produce on the first
   // training configuration (0 until measured: F_rms alone)
   double fh_out = 0.0;
+  // the descriptor range of the force-matching data (normalised units,
+  // widened by range_margin of each span): a guarded force call declines
+  // a configuration with any atom outside it
+  float *xlo_d = nullptr, *xhi_d = nullptr;  // 32 each
+  int* oor_d = nullptr;                      // out-of-range flag of the last guarded call
+  bool have_range = false;
+  float range_margin = 0.1f;
   ~md_surrogate();
 };
 
@@ -130,8 +137,13 @@ int sur_force_grad(Surrogate& s, const float* X, const float* V, int n, float* g
 int sur_loss_grad(Surrogate& s, const float* X, const float* T, int n, float* grad,
                   double* loss, cudaStream_t st);
 int sur_net_eval(Surrogate& s, const float* X, int n, float* t, float* dtdx, cudaStream_t st);
+// declined (optional): with a descriptor range known, set when an atom's
+// descriptors fall outside it; the forces are then not computed
 int sur_forces(Surrogate& s, const md_double4* pos, int n, const RowWalker& w, double* f3,
-               int accumulate, double* energy_dev, int* d_status, cudaStream_t st);
+               int accumulate, double* energy_dev, int* d_status, cudaStream_t st,
+               bool* declined = nullptr);
+// the accepted descriptor range (normalised units): read, or set (and use)
+int sur_range(Surrogate& s, float* lo, float* hi, bool set, cudaStream_t st);
 // model kind (0 energy network, 1 direct-force head with `hidden` units per
 // hidden layer: 32, 64 or 128); the head's weights start from the seed
 int sur_set_model(Surrogate& s, int kind, int hidden, cudaStream_t st);

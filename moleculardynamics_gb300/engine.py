@@ -74,7 +74,8 @@ class MdTuneResult(C.Structure):
 class MdSurrogateStats(C.Structure):
     _fields_ = [("surrogate_steps", C.c_longlong), ("exact_steps", C.c_longlong),
                 ("checks", C.c_longlong), ("rejected_checks", C.c_longlong),
-                ("last_error", C.c_double), ("max_error", C.c_double)]
+                ("last_error", C.c_double), ("max_error", C.c_double),
+                ("declined_steps", C.c_longlong)]
 
 
 class ListSettings(C.Structure):
@@ -111,7 +112,8 @@ EXPORTS = ["md_create", "md_destroy", "md_status_string", "md_last_error", "md_u
            "md_surrogate_net", "md_surrogate_train_forces", "md_surrogate_force_grad",
            "md_surrogate_desc_directional", "md_set_wait_limit", "md_measure_arith_peaks",
            "md_device_sm_count", "md_surrogate_set_model", "md_surrogate_head_param_count",
-           "md_surrogate_head_params", "md_surrogate_head_grad", "md_surrogate_head_scale"]
+           "md_surrogate_head_params", "md_surrogate_head_grad", "md_surrogate_head_scale",
+           "md_surrogate_range"]
 
 
 def load(path: str | None = None) -> C.CDLL:
@@ -178,6 +180,7 @@ def load(path: str | None = None) -> C.CDLL:
     L.md_surrogate_head_params.argtypes = [C.c_void_p, _fp, C.c_int, C.c_int]
     L.md_surrogate_head_grad.argtypes = [C.c_void_p, _fp, _fp, C.c_int, _fp]
     L.md_surrogate_head_scale.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.c_int]
+    L.md_surrogate_range.argtypes = [C.c_void_p, _fp, _fp, C.c_int]
     L.md_batch_create.argtypes = [P(MdConfig), C.c_int, _ip, _dp, P(C.c_void_p)]
     L.md_batch_size.argtypes = [C.c_void_p]
     L.md_batch_records.argtypes = [C.c_void_p, C.c_void_p, C.c_int]
@@ -478,6 +481,16 @@ class Surrogate:
         self._ck(self.lib.md_surrogate_head_scale(self.h, C.byref(v), 0 if new is None else 1),
                  "md_surrogate_head_scale")
         return v.value
+
+    def descriptor_range(self, lo=None, hi=None):
+        """The accepted descriptor range (32 lower, 32 upper bounds): read, or set."""
+        if lo is None:
+            lo, hi = np.zeros(32, np.float32), np.zeros(32, np.float32)
+            self._ck(self.lib.md_surrogate_range(self.h, lo, hi, 0), "md_surrogate_range")
+            return lo, hi
+        lo = np.ascontiguousarray(lo, np.float32)
+        hi = np.ascontiguousarray(hi, np.float32)
+        self._ck(self.lib.md_surrogate_range(self.h, lo, hi, 1), "md_surrogate_range")
 
     def head_grad(self, x, v):
         x = np.ascontiguousarray(x, np.float32)

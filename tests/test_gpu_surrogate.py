@@ -213,6 +213,9 @@ def test_fallback_to_exact_kernel(eng):
     pos, vel, L = nitrogen_diamond(4, temperature=300.0, seed=50, noise=0.02)
     with eng.Surrogate(seed=13, cutoff=MB_RC) as s:
         _train_surrogate(eng, s, temps=(300.0,), steps=500)
+        # the threshold alone: the descriptor-range guard (its own test below)
+        # would decline the steps that leave this narrow training set
+        s.descriptor_range(np.full(32, -1e30), np.full(32, 1e30))
         with _mb_engine(eng, pos, vel, L) as e:
             e.step(25)
             ref = e.download()
@@ -270,3 +273,34 @@ def test_force_head_trains_and_drives_a_run(eng):
     assert np.isnan(eh)
     assert rel_rms(fh2, fh) < 1e-6
     assert r["surrogate_steps"] == 10 and r["last_error"] == pytest.approx(err_head, rel=0.5)
+
+
+def test_descriptors_outside_the_training_range_take_the_exact_forces(eng):
+    """Training sets the accepted descriptor range; a lattice compressed from
+    1.5 to 1.2 A bonds lies outside it, so every check fails, no step uses the
+    network and the run equals the exact one bit for bit, while a run at the
+    training density declines nothing."""
+    from moleculardynamics_gb300 import lattice as lat
+    a = 4 * 1.2 / np.sqrt(3.0)
+    cpos, cvel, cL = lat.make_system("diamond", 4, 300.0, seed=60, a=a, noise=0.02,
+                                     species=lat.SPECIES_N, mass_table="neon")
+    pos, vel, L = nitrogen_diamond(4, temperature=600.0, seed=61, noise=0.02)
+    with eng.Surrogate(seed=17, cutoff=MB_RC) as s:
+        _train_surrogate(eng, s, temps=(300.0, 900.0), steps=500)
+        lo, hi = s.descriptor_range()
+        with _mb_engine(eng, cpos, cvel, cL) as e:
+            e.step(10)
+            ref = e.download()
+        with _mb_engine(eng, cpos, cvel, cL) as e:
+            s.attach(e, threshold=1e9, check_every=5)
+            e.step(10)
+            got = e.download()
+            rc = s.report(e)
+        with _mb_engine(eng, pos, vel, L) as e:
+            s.attach(e, threshold=1e9, check_every=5)
+            e.step(10)
+            rn = s.report(e)
+    assert lo.shape == (32,) and np.all(lo < hi)
+    assert rc["surrogate_steps"] == 0 and rc["declined_steps"] == rc["checks"] == 2
+    assert np.array_equal(got[0], ref[0]) and np.array_equal(got[1], ref[1])
+    assert rn["declined_steps"] == 0 and rn["surrogate_steps"] == 10
