@@ -14,6 +14,8 @@ Committed: the configuration file, the input state (dropin_input.npz; the
 Input text file is written from it by input_text below), the .dat/.txt
 pair of every pass, and SHA-256 digests of the Output file and of the .anm
 animation of every pass (manifest.json).
+With --bond-order: the bond-order case of tests/golden/dropin_bo/
+(main_bond_order below).
 """
 import hashlib
 import json
@@ -87,5 +89,41 @@ def main():
     print("wrote", OUT)
 
 
+def main_bond_order():
+    """tests/golden/dropin_bo/: the bond-order half.  The unmodified cpumd
+    with the reference's own constants (oracle/_ref/cpumd_neon) on 64 N and O
+    atoms (dropin_bo.cfg).  The bond-order forces use exp and tanh, whose
+    CUDA and libm results differ in the last bits, so the comparison is
+    numerical: the run's Output, .dat and .txt are committed whole."""
+    from moleculardynamics_gb300 import lattice as lat
+    from oracle.oracle import REF_DIR
+    exe = os.path.join(REF_DIR, "cpumd_neon")
+    if not os.path.exists(exe):
+        sys.exit("oracle/_ref/cpumd_neon not built (run oracle/build_ref.sh)")
+    out = os.path.join(HERE, "dropin_bo")
+    cfg = "dropin_bo.cfg"
+    a = 4 * 1.5 / np.sqrt(3.0)
+    pos, vel, _ = lat.make_system("diamond", 2, 300.0, seed=64, a=a, noise=0.02,
+                                  species=lat.SPECIES_N, mass_table="neon")
+    pos[::2, 3] = lat.SPECIES_O
+    np.savez(os.path.join(out, "dropin_input.npz"), pos=pos, vel=vel)
+    names = ["results(vxcm-0).dat", "results(vxcm-0).txt", "output.txt"]
+    with tempfile.TemporaryDirectory() as d:
+        shutil.copy(os.path.join(out, cfg), d)
+        with open(os.path.join(d, "input.txt"), "w") as f:
+            f.write(input_text(pos, vel))
+        r = subprocess.run([exe, cfg], cwd=d, capture_output=True, text=True)
+        if r.returncode != 0:
+            sys.exit(r.stdout + r.stderr)
+        for name in names:
+            shutil.copy(os.path.join(d, name), os.path.join(out, name))
+    with open(os.path.join(out, "manifest.json"), "w") as f:
+        json.dump({"config": cfg, "files": names}, f, indent=1, sort_keys=True)
+    print("wrote", out)
+
+
 if __name__ == "__main__":
-    main()
+    if "--bond-order" in sys.argv:
+        main_bond_order()
+    else:
+        main()

@@ -59,3 +59,49 @@ def test_mdgb_run_writes_the_reference_files(eng, tmp_path):
         assert got == want, name
     for name, digest in man["sha256"].items():
         assert _sha(tmp_path / name) == digest, name
+
+
+def _tokens_close(want: str, got: str, rtol: float = 2e-7):
+    """Equal token by token: numbers within rtol (the last printed digit),
+    everything else exactly."""
+    tw, tg = want.split(), got.split()
+    assert len(tw) == len(tg)
+    for a, b in zip(tw, tg):
+        try:
+            x, y = float(a), float(b)
+        except ValueError:
+            assert a == b
+            continue
+        assert abs(x - y) <= rtol * max(abs(x), 1e-30) or a == b, (a, b)
+
+
+def test_mdgb_run_bond_order_matches_the_reference(eng, tmp_path):
+    """The bond-order half (tests/golden/dropin_bo, made by the unmodified
+    cpumd with the reference's constants): 64 N and O atoms in the
+    reference's walls, 200 steps.  The reference's exp and tanh (libm) and
+    CUDA's differ in the last bits, so the records' doubles (.dat) are
+    compared within 1e-10 (measured 3e-13); the .dat header, the printed
+    records, the N-O pair list and the final state (.txt, Output) match to
+    their printed digits."""
+    from moleculardynamics_gb300 import build
+    from golden.make_dropin_golden import input_text
+    gold = os.path.join(HERE, "golden", "dropin_bo")
+    with open(os.path.join(gold, "manifest.json")) as f:
+        man = json.load(f)
+    data = np.load(os.path.join(gold, "dropin_input.npz"))
+    shutil.copy(os.path.join(gold, man["config"]), tmp_path)
+    (tmp_path / "input.txt").write_text(input_text(data["pos"], data["vel"]))
+    r = subprocess.run([build.RUN, man["config"]], cwd=tmp_path, capture_output=True,
+                       text=True, timeout=600)
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
+    # .dat: header (particles, steps, dt, flags, rs/rcut, vxcm: 26 bytes) exact
+    want = open(os.path.join(gold, "results(vxcm-0).dat"), "rb").read()
+    got = (tmp_path / "results(vxcm-0).dat").read_bytes()
+    assert got[:26] == want[:26] and len(got) == len(want)
+    rw = np.frombuffer(want[26:], np.float64).reshape(-1, 11)
+    rg = np.frombuffer(got[26:], np.float64).reshape(-1, 11)
+    assert np.all(np.abs(rg - rw) <= 1e-10 * np.maximum(np.abs(rw), 1e-12))
+    _tokens_close(_mask_time(open(os.path.join(gold, "results(vxcm-0).txt"), "rb").read()).decode(),
+                  _mask_time((tmp_path / "results(vxcm-0).txt").read_bytes()).decode())
+    _tokens_close(open(os.path.join(gold, "output.txt")).read(),
+                  (tmp_path / "output.txt").read_text())
