@@ -14,8 +14,8 @@ Committed: the configuration file, the input state (dropin_input.npz; the
 Input text file is written from it by input_text below), the .dat/.txt
 pair of every pass, and SHA-256 digests of the Output file and of the .anm
 animation of every pass (manifest.json).
-With --bond-order: the bond-order case of tests/golden/dropin_bo/
-(main_bond_order below).
+With --bond-order: the bond-order and mixed cases of tests/golden/dropin_bo/
+and tests/golden/dropin_mixed/ (main_bond_order below).
 """
 import hashlib
 import json
@@ -89,23 +89,17 @@ def main():
     print("wrote", OUT)
 
 
-def main_bond_order():
-    """tests/golden/dropin_bo/: the bond-order half.  The unmodified cpumd
-    with the reference's own constants (oracle/_ref/cpumd_neon) on 64 N and O
-    atoms (dropin_bo.cfg).  The bond-order forces use exp and tanh, whose
-    CUDA and libm results differ in the last bits, so the comparison is
-    numerical: the run's Output, .dat and .txt are committed whole."""
-    from moleculardynamics_gb300 import lattice as lat
+def bond_order_case(name: str, cfg: str, pos, vel):
+    """tests/golden/<name>/: the unmodified cpumd with the reference's own
+    constants (oracle/_ref/cpumd_neon) on cfg.  The bond-order forces use exp
+    and tanh, whose CUDA and libm results differ in the last bits, so the
+    comparison is numerical: the run's Output, .dat and .txt are committed
+    whole."""
     from oracle.oracle import REF_DIR
     exe = os.path.join(REF_DIR, "cpumd_neon")
     if not os.path.exists(exe):
         sys.exit("oracle/_ref/cpumd_neon not built (run oracle/build_ref.sh)")
-    out = os.path.join(HERE, "dropin_bo")
-    cfg = "dropin_bo.cfg"
-    a = 4 * 1.5 / np.sqrt(3.0)
-    pos, vel, _ = lat.make_system("diamond", 2, 300.0, seed=64, a=a, noise=0.02,
-                                  species=lat.SPECIES_N, mass_table="neon")
-    pos[::2, 3] = lat.SPECIES_O
+    out = os.path.join(HERE, name)
     np.savez(os.path.join(out, "dropin_input.npz"), pos=pos, vel=vel)
     names = ["results(vxcm-0).dat", "results(vxcm-0).txt", "output.txt"]
     with tempfile.TemporaryDirectory() as d:
@@ -115,11 +109,29 @@ def main_bond_order():
         r = subprocess.run([exe, cfg], cwd=d, capture_output=True, text=True)
         if r.returncode != 0:
             sys.exit(r.stdout + r.stderr)
-        for name in names:
-            shutil.copy(os.path.join(d, name), os.path.join(out, name))
+        for fname in names:
+            shutil.copy(os.path.join(d, fname), os.path.join(out, fname))
     with open(os.path.join(out, "manifest.json"), "w") as f:
         json.dump({"config": cfg, "files": names}, f, indent=1, sort_keys=True)
     print("wrote", out)
+
+
+def main_bond_order():
+    """dropin_bo: 64 N and O atoms alternating on a 2^3 diamond (1.5 A bonds,
+    0.02 A noise, 300 K); dropin_mixed: the same block beside 108 neon atoms
+    (FCC 3^3 at 6.0 A, 100 K, 22 A away), LJ and bond order together."""
+    from moleculardynamics_gb300 import lattice as lat
+    a = 4 * 1.5 / np.sqrt(3.0)
+    pos, vel, _ = lat.make_system("diamond", 2, 300.0, seed=64, a=a, noise=0.02,
+                                  species=lat.SPECIES_N, mass_table="neon")
+    pos[::2, 3] = lat.SPECIES_O
+    bond_order_case("dropin_bo", "dropin_bo.cfg", pos, vel)
+    p2, v2, _ = lat.make_system("fcc", 3, 100.0, seed=65, a=6.0, species=lat.SPECIES_NG,
+                                mass_table="neon")
+    p2[:, :3] += np.array([22.0, 0.0, 0.0])
+    bond_order_case("dropin_mixed", "dropin_mixed.cfg",
+                    np.ascontiguousarray(np.concatenate([pos, p2])),
+                    np.ascontiguousarray(np.concatenate([vel, v2])))
 
 
 if __name__ == "__main__":

@@ -75,17 +75,19 @@ def _tokens_close(want: str, got: str, rtol: float = 2e-7):
         assert abs(x - y) <= rtol * max(abs(x), 1e-30) or a == b, (a, b)
 
 
-def test_mdgb_run_bond_order_matches_the_reference(eng, tmp_path):
-    """The bond-order half (tests/golden/dropin_bo, made by the unmodified
-    cpumd with the reference's constants): 64 N and O atoms in the
-    reference's walls, 200 steps.  The reference's exp and tanh (libm) and
-    CUDA's differ in the last bits, so the records' doubles (.dat) are
-    compared within 1e-10 (measured 3e-13); the .dat header, the printed
-    records, the N-O pair list and the final state (.txt, Output) match to
-    their printed digits."""
+@pytest.mark.parametrize("case", ["dropin_bo", "dropin_mixed"])
+def test_mdgb_run_bond_order_matches_the_reference(eng, tmp_path, case):
+    """The bond-order half, alone (dropin_bo: 64 N and O atoms) and beside
+    108 neon atoms with LJ on (dropin_mixed), in the reference's walls for 200
+    steps; fixtures made by the unmodified cpumd with the reference's
+    constants.  The reference's exp and tanh (libm) and CUDA's differ in the
+    last bits, so the records' doubles (.dat) are compared within 1e-10
+    (measured 3e-13 for dropin_bo); the .dat header, the printed records, the
+    N-O pair list and the final state (.txt, Output) match to their printed
+    digits."""
     from moleculardynamics_gb300 import build
     from golden.make_dropin_golden import input_text
-    gold = os.path.join(HERE, "golden", "dropin_bo")
+    gold = os.path.join(HERE, "golden", case)
     with open(os.path.join(gold, "manifest.json")) as f:
         man = json.load(f)
     data = np.load(os.path.join(gold, "dropin_input.npz"))
@@ -94,12 +96,14 @@ def test_mdgb_run_bond_order_matches_the_reference(eng, tmp_path):
     r = subprocess.run([build.RUN, man["config"]], cwd=tmp_path, capture_output=True,
                        text=True, timeout=600)
     assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
-    # .dat: header (particles, steps, dt, flags, rs/rcut, vxcm: 26 bytes) exact
+    # .dat: the header (particles, steps, dt, two flags each with rs and rcut
+    # when set, vxcm) exact, then records of 11 doubles
     want = open(os.path.join(gold, "results(vxcm-0).dat"), "rb").read()
     got = (tmp_path / "results(vxcm-0).dat").read_bytes()
-    assert got[:26] == want[:26] and len(got) == len(want)
-    rw = np.frombuffer(want[26:], np.float64).reshape(-1, 11)
-    rg = np.frombuffer(got[26:], np.float64).reshape(-1, 11)
+    head = len(want) - 88 * ((len(want) - 14) // 88)
+    assert got[:head] == want[:head] and len(got) == len(want)
+    rw = np.frombuffer(want[head:], np.float64).reshape(-1, 11)
+    rg = np.frombuffer(got[head:], np.float64).reshape(-1, 11)
     assert np.all(np.abs(rg - rw) <= 1e-10 * np.maximum(np.abs(rw), 1e-12))
     _tokens_close(_mask_time(open(os.path.join(gold, "results(vxcm-0).txt"), "rb").read()).decode(),
                   _mask_time((tmp_path / "results(vxcm-0).txt").read_bytes()).decode())
