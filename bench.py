@@ -622,6 +622,14 @@ def surrogate_form(eng, device, train_steps: int, run_steps: int, fp64_steps: in
     at_best["threshold"] = tau
     # the surrogate's own step: every check accepted
     every, _ = run(1.0, 1000, eng.PREC_MIXED)
+    # the other model kind at the same threshold: the energy network's forces
+    # are a gradient (conservative), the head's are not
+    other = None
+    if chosen["kind"] == 1:
+        s.set_model(0)
+        other, _ = run(tau, run_steps, eng.PREC_MIXED)
+        other["model"] = next(m["model"] for m in models if m["kind"] == 0)
+        other["threshold"] = tau
     s.close()
     return {
         "metric": "atom-steps/s of the bond-order system on 1 GB300", "unit": "atom-steps/s",
@@ -647,6 +655,7 @@ def surrogate_form(eng, device, train_steps: int, run_steps: int, fp64_steps: in
         "surrogate_threshold_1e-4": strict,
         "surrogate_best_threshold": at_best,
         "surrogate_every_step_1000_steps": every,
+        "surrogate_best_threshold_energy_network": other,
         "speedup_best_threshold_vs_exact": exact["ms_per_step"] / at_best["ms_per_step"],
         "speedup_threshold_1e-4_vs_exact": exact["ms_per_step"] / strict["ms_per_step"],
         "speedup_precision_form_vs_exact": exact["ms_per_step"] / exact32["ms_per_step"],

@@ -135,6 +135,9 @@ struct md_ctx {
   long long sur_steps = 0, sur_exact_steps = 0, sur_checks = 0, sur_rejects = 0;
   long long sur_declined = 0;  // steps whose descriptors left the training range
   double *sur_fx = nullptr, *sur_fs = nullptr;  // check buffers (3 doubles per many-body atom)
+  // device: [0] this step's "surrogate declined, exact forces" flag, [1] the
+  // declined steps between checks (read by md_surrogate_report)
+  int* sur_flags = nullptr;
   long long graph_windows = 0;
   // bond-order scratch
   uint32_t* mb_sl = nullptr;
@@ -388,16 +391,18 @@ md_status mb_forces_step(md_ctx* c, double* f3) {
     if (!c->sur_use) c->sur_rejects++;
     c->stats.launches += 12;
   }
-  bool declined = false;
   if (c->sur_use) {
+    // no host wait: the store of the network's forces and the exact kernels
+    // that take the step instead both read the device flag of the range check
     int r = sur_forces(*c->sur, c->pos, nmb, make_walker(c->mb), f3, acc, nullptr, c->status,
-                       c->st, &declined);
+                       c->st, nullptr, c->sur_flags, c->sur_flags + 1);
     if (r) return cuda_fail(c, (cudaError_t)r, "surrogate forces");
-    c->stats.launches += 7;
-    if (declined) c->sur_declined++;
-    else c->sur_steps++;
-  }
-  if (!c->sur_use || declined) {
+    MbArgs a = mb_args(c, f3, acc);
+    a.run_if = c->sur_flags;
+    launch_mb(a, c->mixed(), false, c->st);
+    c->stats.launches += 10;
+    c->sur_steps++;
+  } else {
     launch_mb(mb_args(c, f3, acc), c->mixed(), false, c->st);
     c->sur_exact_steps++;
     c->stats.launches += 3;
@@ -1084,7 +1089,7 @@ void md_destroy(md_ctx* c) {
   cluster_free(c->cl);
   for (cudaGraphExec_t x : c->gexec)
     if (x) cudaGraphExecDestroy(x);
-  void* ptrs[] = {c->seq_buf, c->inv, c->sur_fx, c->sur_fs, c->rep_ranges, c->rep_buf, c->io, c->pos_alt, c->posf_alt, c->pos, c->vel, c->acc, c->b, c->c, c->f3, c->f3_tmp, c->posf, c->mb_sl,
+  void* ptrs[] = {c->sur_flags, c->seq_buf, c->inv, c->sur_fx, c->sur_fs, c->rep_ranges, c->rep_buf, c->io, c->pos_alt, c->posf_alt, c->pos, c->vel, c->acc, c->b, c->c, c->f3, c->f3_tmp, c->posf, c->mb_sl,
                   c->mb_slen, c->xsi, c->xsj, c->status, c->epart, c->dsc, c->rec,
                   c->sc.dpart, c->sc.umax, c->sc.counts, c->sc.block_sums};
   for (void* p : ptrs)
@@ -1812,7 +1817,9 @@ md_status md_surrogate_attach(md_ctx* c, md_surrogate* s, double threshold, int 
     const size_t B = sizeof(double) * 3 * (size_t)c->cfg.n_mb;
     CK(cudaMalloc(&c->sur_fx, B), "surrogate check buffers");
     CK(cudaMalloc(&c->sur_fs, B), "surrogate check buffers");
+    CK(cudaMalloc(&c->sur_flags, sizeof(int) * 2), "surrogate flags");
   }
+  if (c->sur_flags) CK(cudaMemsetAsync(c->sur_flags, 0, sizeof(int) * 2, c->st), "surrogate flags");
   c->sur = s;
   c->sur_threshold = threshold;
   c->sur_every = check_every;
@@ -1825,13 +1832,20 @@ md_status md_surrogate_attach(md_ctx* c, md_surrogate* s, double threshold, int 
 
 md_status md_surrogate_report(const md_ctx* c, md_surrogate_stats* out) {
   if (!c || !out) return MD_BAD_ARGUMENT;
-  out->surrogate_steps = c->sur_steps;
-  out->exact_steps = c->sur_exact_steps;
+  // steps the network was meant to take but declined on the device
+  int d[2] = {0, 0};
+  if (c->sur_flags) {
+    if (cudaStreamSynchronize(c->st) != cudaSuccess ||
+        cudaMemcpy(d, c->sur_flags, sizeof(d), cudaMemcpyDeviceToHost) != cudaSuccess)
+      return MD_CUDA_ERROR;
+  }
+  out->surrogate_steps = c->sur_steps - d[1];
+  out->exact_steps = c->sur_exact_steps + d[1];
   out->checks = c->sur_checks;
   out->rejected_checks = c->sur_rejects;
   out->last_error = c->sur_err;
   out->max_error = c->sur_err_max;
-  out->declined_steps = c->sur_declined;
+  out->declined_steps = c->sur_declined + d[1];
   return MD_OK;
 }
 

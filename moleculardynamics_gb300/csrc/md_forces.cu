@@ -490,7 +490,9 @@ template <typename T>
 __global__ void __launch_bounds__(128)
     k_mb_short(const md_double4* __restrict__ pos, const float4* __restrict__ posf, int n,
                int ld, const uint32_t* __restrict__ list, const int* __restrict__ len, Grid g,
-               double rcutsq, uint32_t* __restrict__ sl, int* __restrict__ slen) {
+               double rcutsq, uint32_t* __restrict__ sl, int* __restrict__ slen,
+               const int* __restrict__ run_if) {
+  if (run_if && *run_if == 0) return;  // the whole launch: a gated call with nothing to do
   // one warp per atom, lanes over its row: the kept entries in row order
   // (ballot prefix), 32 candidates tested at a time
   const int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
@@ -554,7 +556,8 @@ __global__ void __launch_bounds__(128)
                double* __restrict__ f3, int n, const uint32_t* __restrict__ sl,
                const int* __restrict__ slen, Grid g, int ljexist, T* __restrict__ xsi_s,
                T* __restrict__ xsj_s, double* __restrict__ epart,
-               double* __restrict__ eatom) {
+               double* __restrict__ eatom, const int* __restrict__ run_if) {
+  if (!ENERGY && run_if && *run_if == 0) return;
   const int warps = blockDim.x >> 5;
   const int i = blockIdx.x * warps + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
@@ -891,7 +894,9 @@ __global__ void __launch_bounds__(128)
                const int* __restrict__ slen, Grid g, const int* __restrict__ cell3,
                const int* __restrict__ ref_rows, int ref_nls, int ref_nlargest, double rcutsq,
                const T* __restrict__ wi_s, const T* __restrict__ wj_s,
-               int* __restrict__ missing, double* __restrict__ epart) {
+               int* __restrict__ missing, double* __restrict__ epart,
+               const int* __restrict__ run_if) {
+  if (!ENERGY && run_if && *run_if == 0) return;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int k = blockIdx.x * 4 + warp;
   double ev[1] = {0.0};
@@ -976,24 +981,24 @@ static void launch_pass2(const MbArgs& a, int B, T* xsi, T* xsj, cudaStream_t st
   k_mb_pass2<T, ENERGY><<<B, 128, 0, st>>>(a.pos, a.posf, a.f3, a.n, a.sl, a.slen, a.grid,
                                            a.cell3, a.ref_rows, a.ref_nls, a.ref_nlargest,
                                            a.rcutsq, xsi, xsj, a.missing,
-                                           ENERGY ? a.epart2 : nullptr);
+                                           ENERGY ? a.epart2 : nullptr, a.run_if);
 }
 
 template <typename T>
 static void launch_mb_t(const MbArgs& a, bool energy, cudaStream_t st) {
   if (a.n <= 0) return;
   k_mb_short<T><<<nblk(a.n, 4), 128, 0, st>>>(a.pos, a.posf, a.n, a.ld, a.list, a.len, a.grid,
-                                              a.rcutsq, a.sl, a.slen);
+                                              a.rcutsq, a.sl, a.slen, energy ? nullptr : a.run_if);
   const int B = nblk(a.n, 4);
   T* xsi = (T*)a.xsi;
   T* xsj = (T*)a.xsj;
   if (energy) {
     k_mb_pass1<T, true><<<B, 128, 0, st>>>(a.pos, a.posf, a.f3, a.n, a.sl, a.slen, a.grid,
-                                           a.ljexist, xsi, xsj, a.epart1, a.eatom);
+                                           a.ljexist, xsi, xsj, a.epart1, a.eatom, nullptr);
     launch_pass2<T, true>(a, B, xsi, xsj, st);
   } else {
     k_mb_pass1<T, false><<<B, 128, 0, st>>>(a.pos, a.posf, a.f3, a.n, a.sl, a.slen, a.grid,
-                                            a.ljexist, xsi, xsj, nullptr, nullptr);
+                                            a.ljexist, xsi, xsj, nullptr, nullptr, a.run_if);
     launch_pass2<T, false>(a, B, xsi, xsj, st);
   }
 }

@@ -47,6 +47,7 @@ struct MbArgs {
   void* xsi;            // per (i, slot), T: pass 2's factor va E / (4 (1 + xi_ij)^2)
   void* xsj;            // and va E / (4 (1 + xi_ji)^2), NaN where pass 1 skipped the pair
   int* missing;
+  const int* run_if = nullptr;  // force launches only: return at once unless *run_if != 0
   double* epart1;       // 2 doubles per pass-1 block
   double* epart2;       // 1 double per pass-2 block
   double* eatom = nullptr;  // energy launches: per-atom energy (sum over j of half the pair)

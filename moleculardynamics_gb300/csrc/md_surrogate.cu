@@ -468,9 +468,16 @@ __global__ void k_sg_pos32(const md_double4* __restrict__ pos, int n, float4* __
   out[i] = make_float4((float)p.x, (float)p.y, (float)p.z, 0.f);
 }
 
+// skip (optional, device): when set, the forces are not stored and
+// skipped (device, optional) counts the call once
 __global__ void k_sg_store(const float* __restrict__ F32, double* __restrict__ f3, int n,
-                           int accumulate) {
+                           int accumulate, const int* __restrict__ skip,
+                           int* __restrict__ skipped) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (skip && *skip) {
+    if (k == 0 && skipped) atomicAdd(skipped, 1);
+    return;
+  }
   if (k >= 3 * n) return;
   f3[k] = accumulate ? f3[k] + (double)F32[k] : (double)F32[k];
 }
@@ -1850,13 +1857,23 @@ int sur_net_eval(Surrogate& s, const float* X, int n, float* t, float* dtdx, cud
 // of atoms [0, n) from the network; energy_dev (optional) gets their sum
 int sur_forces(Surrogate& s, const md_double4* pos, int n, const RowWalker& w, double* f3,
                int accumulate, double* energy_dev, int* d_status, cudaStream_t st,
-               bool* declined) {
+               bool* declined, int* run_exact, int* declined_count) {
   if (!s.normalised) return -1;
   set_attrs();
   int r = sur_descriptors(s, pos, n, w, true, d_status, st);
   if (r) return r;
   if (n == 0) return 0;
-  if (declined) {
+  const int* skip = nullptr;
+  if (run_exact) {
+    // the decision stays on the device: the store below and the caller's
+    // exact kernels read the flag
+    cudaMemsetAsync(run_exact, 0, sizeof(int), st);
+    if (s.have_range) {
+      k_range_check<<<sblocks(32LL * n, 256), 256, 0, st>>>(s.X, 32LL * n, s.xlo_d, s.xhi_d,
+                                                            run_exact);
+      skip = run_exact;
+    }
+  } else if (declined) {
     *declined = false;
     if (s.have_range) {
       // outside the training data's descriptor range the model is not used
@@ -1880,7 +1897,8 @@ int sur_forces(Surrogate& s, const md_double4* pos, int n, const RowWalker& w, d
     fh_forward(s, s.X, n, s.gcoef, false, st);
     cudaMemsetAsync(s.F32, 0, sizeof(float) * 3 * (size_t)n, st);
     k_sg_force<<<sblocks(n, 4), 128, 0, st>>>(pos, n, s.sl, s.slen, w.g.box, s.P, s.gcoef, s.F32);
-    k_sg_store<<<sblocks(3LL * n, 256), 256, 0, st>>>(s.F32, f3, n, accumulate);
+    k_sg_store<<<sblocks(3LL * n, 256), 256, 0, st>>>(s.F32, f3, n, accumulate, skip,
+                                                      declined_count);
     if (energy_dev) k_fill_nan<<<1, 1, 0, st>>>(energy_dev);
     return (int)cudaGetLastError();
   }
@@ -1889,7 +1907,8 @@ int sur_forces(Surrogate& s, const md_double4* pos, int n, const RowWalker& w, d
                                               s.eatom);
   cudaMemsetAsync(s.F32, 0, sizeof(float) * 3 * (size_t)n, st);
   k_sg_force<<<sblocks(n, 4), 128, 0, st>>>(pos, n, s.sl, s.slen, w.g.box, s.P, s.gcoef, s.F32);
-  k_sg_store<<<sblocks(3LL * n, 256), 256, 0, st>>>(s.F32, f3, n, accumulate);
+  k_sg_store<<<sblocks(3LL * n, 256), 256, 0, st>>>(s.F32, f3, n, accumulate, skip,
+                                                    declined_count);
   if (energy_dev) k_sum_d<<<1, 256, 0, st>>>(s.eatom, n, energy_dev);
   return (int)cudaGetLastError();
 }

@@ -137,11 +137,16 @@ int sur_force_grad(Surrogate& s, const float* X, const float* V, int n, float* g
 int sur_loss_grad(Surrogate& s, const float* X, const float* T, int n, float* grad,
                   double* loss, cudaStream_t st);
 int sur_net_eval(Surrogate& s, const float* X, int n, float* t, float* dtdx, cudaStream_t st);
-// declined (optional): with a descriptor range known, set when an atom's
-// descriptors fall outside it; the forces are then not computed
+// With a descriptor range known, a configuration with an atom's descriptors
+// outside it is declined: declined (host, optional) is then set and no forces
+// are computed; or, without a host wait, run_exact (device flag, optional) is
+// set to 1 (0 otherwise), f3 is left as it was and declined_count (device,
+// optional) counts the declined calls, so that exact kernels gated on
+// run_exact take the step.
 int sur_forces(Surrogate& s, const md_double4* pos, int n, const RowWalker& w, double* f3,
                int accumulate, double* energy_dev, int* d_status, cudaStream_t st,
-               bool* declined = nullptr);
+               bool* declined = nullptr, int* run_exact = nullptr,
+               int* declined_count = nullptr);
 // the accepted descriptor range (normalised units): read, or set (and use)
 int sur_range(Surrogate& s, float* lo, float* hi, bool set, cudaStream_t st);
 // model kind (0 energy network, 1 direct-force head with `hidden` units per

@@ -304,3 +304,32 @@ def test_descriptors_outside_the_training_range_take_the_exact_forces(eng):
     assert rc["surrogate_steps"] == 0 and rc["declined_steps"] == rc["checks"] == 2
     assert np.array_equal(got[0], ref[0]) and np.array_equal(got[1], ref[1])
     assert rn["declined_steps"] == 0 and rn["surrogate_steps"] == 10
+
+
+def test_steps_declined_between_checks_take_the_exact_forces(eng):
+    """Between checks the decision stays on the device: with the range
+    narrowed after a passing check, every later step is declined there and the
+    gated exact kernels take it; the run then follows the exact one that
+    branches off after the same first step."""
+    pos, vel, L = nitrogen_diamond(4, temperature=600.0, seed=62, noise=0.02)
+    with eng.Surrogate(seed=19, cutoff=MB_RC) as s:
+        _train_surrogate(eng, s, temps=(300.0, 900.0), steps=500)
+        wide = s.descriptor_range()
+        with _mb_engine(eng, pos, vel, L) as e:
+            s.attach(e, threshold=1e9, check_every=100)
+            e.step(1)
+            s.descriptor_range(np.zeros(32), np.zeros(32) + 1e-6)
+            e.step(9)
+            got = e.download()
+            r = s.report(e)
+        s.descriptor_range(*wide)
+        with _mb_engine(eng, pos, vel, L) as e:
+            s.attach(e, threshold=1e9, check_every=100)
+            e.step(1)
+            eng.Surrogate.detach(e)
+            e.step(9)
+            ref = e.download()
+    assert r["checks"] == 1 and r["surrogate_steps"] == 1
+    assert r["declined_steps"] == 9 and r["exact_steps"] == 9
+    # the first step's network forces sum FP32 atomics in any order
+    assert rel_rms(got[0][:, :3], ref[0][:, :3]) < 1e-9 and rel_rms(got[1], ref[1]) < 1e-6
