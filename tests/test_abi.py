@@ -90,3 +90,23 @@ def test_library_links_only_cuda_runtime(eng):
     out = subprocess.run(["ldd", eng.LIB_PATH], capture_output=True, text=True).stdout
     assert "libcudart" in out or "cudart" in out
     assert "torch" not in out and "python" not in out
+
+
+def test_surrogate_model_calls_reject_bad_arguments(eng):
+    """The head, scale and range entry points check their arguments before
+    touching a device: a NULL surrogate or NULL arrays are MD_BAD_ARGUMENT."""
+    import ctypes as C
+    import numpy as np
+    lib = eng.load()
+    assert [lib.md_surrogate_head_param_count(h) for h in (32, 64, 128)] == [
+        h * 32 + h + h * h + h + 32 * h + 32 for h in (32, 64, 128)]
+    assert lib.md_surrogate_head_param_count(48) == -1
+    p = np.zeros(8, np.float32)
+    assert lib.md_surrogate_set_model(None, 1, 64) == 6
+    assert lib.md_surrogate_head_params(None, p, 8, 0) == 6
+    d = C.c_double(1.0)
+    assert lib.md_surrogate_head_scale(None, C.byref(d), 1) == 6
+    lo, hi = np.zeros(32, np.float32), np.ones(32, np.float32)
+    assert lib.md_surrogate_range(None, lo, hi, 1) == 6
+    x = np.zeros(32, np.float32)
+    assert lib.md_surrogate_head_grad(None, x, x, 1, p) == 6
