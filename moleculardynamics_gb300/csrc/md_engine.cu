@@ -133,7 +133,9 @@ struct md_ctx {
   int sur_every = 10, sur_last_check = -1;
   bool sur_use = false;
   long long sur_steps = 0, sur_exact_steps = 0, sur_checks = 0, sur_rejects = 0;
-  long long sur_declined = 0;  // steps whose descriptors left the training range
+  // checks declined for descriptors outside the training range (steps
+  // declined between checks are counted on the device, sur_flags[1])
+  long long sur_declined = 0;
   double *sur_fx = nullptr, *sur_fs = nullptr;  // check buffers (3 doubles per many-body atom)
   // device: [0] this step's "surrogate declined, exact forces" flag, [1] the
   // declined steps between checks (read by md_surrogate_report)

@@ -561,7 +561,8 @@ __global__ void __launch_bounds__(128)
   const int warps = blockDim.x >> 5;
   const int i = blockIdx.x * warps + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
-  // FP32: the angle derivatives in a shorter, algebraically equal form
+  // FP32: hardware rsqrt for distances and their reciprocals, and the
+  // third bodies' terms staged in FP32 (FP64: exact roots and quotients)
   constexpr bool kFast = std::is_same<T, float>::value;
   double ev[2] = {0.0, 0.0};
   __shared__ ThirdSm<T> third_sm[4];
@@ -681,7 +682,7 @@ __global__ void __launch_bounds__(128)
           }
           const T jmx = xj - xm, jmy = yj - ym, jmz = zj - zm;
           T rjm, inv_rjm = 0;
-          if (kFast) {  // the distance and its reciprocal from one rsqrt
+          if constexpr (kFast) {  // the distance and its reciprocal from one rsqrt
             const float r2 = (float)(jmx * jmx + jmy * jmy + jmz * jmz);
             const float ir = rsqrtf(r2);
             inv_rjm = ir;
