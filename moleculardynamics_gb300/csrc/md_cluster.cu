@@ -1453,8 +1453,11 @@ __device__ __noinline__ LeanSum lean_minimg(const SegShared& sh, const float4* s
   return s;
 }
 
+// 72 registers (7 blocks of 128 threads per SM): fewer spills than at 64
+// registers and 8 blocks, which paid more than the eighth block did; blocks
+// of up to 224 threads stay launchable for the autotuner.
 template <int GEAR>
-__global__ void __launch_bounds__(256, 4) k_lj_lean(const ClStep a) {
+__global__ void __launch_bounds__(224, 4) k_lj_lean(const ClStep a) {
   extern __shared__ __align__(128) unsigned char dyn[];
   float4* st = reinterpret_cast<float4*>(dyn);
   const int tid = threadIdx.x;
@@ -1989,6 +1992,39 @@ int cluster_build(ClusterList& cl, const std::vector<ClusterReplica>& reps_in, f
   cl.built = true;
   cl.version++;
   return (int)cudaGetLastError();
+}
+
+int cluster_occupancy_cap(int threads, int row_loads, bool all_ng) {
+  // the kernel and row-tile bytes the fused every-step launch below uses
+  const bool block_tiles = row_loads == 1 || row_loads == 4;
+  const size_t tiles =
+      block_tiles ? (row_loads == 4 ? 3 : 2) * kClusterTileSlots * (size_t)(threads + 8) *
+                        sizeof(uint16_t)
+                  : (row_loads == 3 ? (size_t)(threads / 32) * 2 * kWarpTileBytes : 0);
+  const void* kern;
+  if (row_loads == 2 && all_ng)
+    kern = (const void*)k_lj_lean<1>;
+  else if (block_tiles)
+    kern = all_ng ? (const void*)k_lj_cl<false, true, 1, 0> : (const void*)k_lj_cl<false, false, 1, 0>;
+  else if (row_loads == 3)
+    kern = all_ng ? (const void*)k_lj_cl<false, true, 1, 2> : (const void*)k_lj_cl<false, false, 1, 2>;
+  else
+    kern = all_ng ? (const void*)k_lj_cl<false, true, 1, 1> : (const void*)k_lj_cl<false, false, 1, 1>;
+  auto blocks = [&](int staged) {
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, threads,
+                                                      tiles + stage_bytes(staged)) != cudaSuccess)
+      nb = 0;
+    return nb;
+  };
+  const int nb0 = blocks(1);
+  if (nb0 < 1) return kClusterMaxStaged;
+  int lo = 1, hi = kClusterMaxStaged;  // the largest stage with nb0 blocks per SM
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) / 2;
+    if (blocks(mid) >= nb0) lo = mid; else hi = mid - 1;
+  }
+  return lo;
 }
 
 void launch_lj_cluster(const ClusterForceArgs& f, bool energy, cudaStream_t st) {

@@ -154,6 +154,11 @@ void launch_scatter_host(const double* src, double* host, const int* inv, int n,
 // flag |= 1 when some atom is not of the NG species
 void launch_species_check(const md_double4* pos, int n, int* flag, cudaStream_t st);
 int cluster_blocks(const ClusterList& cl);
+// Largest stage cap (staged atoms per segment) at which the fused every-step
+// launch of `threads`-thread blocks on row scheme `row_loads` keeps the
+// blocks per SM that its registers allow (the kernels' shared-memory limits
+// must have been raised: any cluster_build does it).
+int cluster_occupancy_cap(int threads, int row_loads, bool all_ng);
 
 // Reference-layout rows (common/NeighborList.cpp:119-177) of atoms in their
 // original numbering: out[o * nlistsize + k], -1 padded; images as

@@ -550,8 +550,10 @@ struct ThirdSm {
   int id[kThirdMax];                                            // atom, -1 for an NG atom
 };
 
+// FP32: 64 registers without spills, 8 blocks per SM instead of 7 (FP64
+// instances keep their registers: a bound there spills)
 template <typename T, bool ENERGY>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(128, sizeof(T) == 4 ? 8 : 0)
     k_mb_pass1(const md_double4* __restrict__ pos, const float4* __restrict__ posf,
                double* __restrict__ f3, int n, const uint32_t* __restrict__ sl,
                const int* __restrict__ slen, Grid g, int ljexist, T* __restrict__ xsi_s,
@@ -888,8 +890,10 @@ __device__ __forceinline__ Pass2I<T> pass2_entry(uint32_t ei, T xk, T yk, T zk,
 // FP32, 348 against 249 us on 32,768 atoms: lanes of one i read 32 different
 // lines of the slot arrays, where lanes of neighbouring i, stored side by
 // side, share sectors.)
+// FP32: 40 registers, 12 blocks per SM instead of 10 (FP64 instances keep
+// their registers)
 template <typename T, bool ENERGY>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(128, sizeof(T) == 4 ? 12 : 0)
     k_mb_pass2(const md_double4* __restrict__ pos, const float4* __restrict__ posf,
                double* __restrict__ f3, int n, const uint32_t* __restrict__ sl,
                const int* __restrict__ slen, Grid g, const int* __restrict__ cell3,
