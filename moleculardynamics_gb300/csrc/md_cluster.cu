@@ -806,6 +806,10 @@ struct ClStep {
   int nbuf;  // row tiles in flight in the block-tile scheme (2 or 3)
   int wait_limit;  // polls of a bounded mbarrier wait
   int grouped;     // rows grouped by eight slots, byte offsets (row_slot)
+  // the lean kernel's cutoff band (rc_lo, rc_hi, rc_mid, rc_half) and LJ
+  // factors (P, Q), computed on the host with k_lj_cl's float expressions:
+  // as kernel parameters they need no registers in the pair loop
+  float lean_c[6];
 };
 
 // FP32 LJ force, persistent: each block takes segments from a shared
@@ -1472,17 +1476,12 @@ __global__ void __launch_bounds__(224, 4) k_lj_lean(const ClStep a) {
   __syncthreads();
   const bool tripped = s_trip != 0;
   LeanConst k;
-  {
-    const float rc2 = (float)a.rcutsq;
-    k.rc_lo = rc2 * (1.0f - 1e-5f);
-    k.rc_hi = rc2 * (1.0f + 1e-5f);
-    k.rc_mid = 0.5f * (k.rc_lo + k.rc_hi);
-    k.rc_half = 0.5f * (k.rc_hi - k.rc_lo) * 1.001f;
-    const float s2 = a.sp.sig[2] * a.sp.sig[2], c24 = 24.0f * a.sp.eps[2];
-    const float q6 = s2 * s2 * s2;
-    k.lj_q = c24 * q6;
-    k.lj_p = 2.0f * c24 * q6 * q6;
-  }
+  k.rc_lo = a.lean_c[0];
+  k.rc_hi = a.lean_c[1];
+  k.rc_mid = a.lean_c[2];
+  k.rc_half = a.lean_c[3];
+  k.lj_p = a.lean_c[4];
+  k.lj_q = a.lean_c[5];
   uint32_t phase = 0u;
   bool trip_next = false;
   for (;;) {
@@ -2061,6 +2060,18 @@ void launch_lj_cluster(const ClusterForceArgs& f, bool energy, cudaStream_t st) 
   a.status = f.status;
   if (f.gear) a.g = *f.gear;
   else memset(&a.g, 0, sizeof(a.g));
+  {
+    const float rc2 = (float)f.rcutsq;
+    const float lo = rc2 * (1.0f - 1e-5f), hi = rc2 * (1.0f + 1e-5f);
+    const float s2 = f.sp.sig[2] * f.sp.sig[2], c24 = 24.0f * f.sp.eps[2];
+    const float q6 = s2 * s2 * s2;
+    a.lean_c[0] = lo;
+    a.lean_c[1] = hi;
+    a.lean_c[2] = 0.5f * (lo + hi);
+    a.lean_c[3] = 0.5f * (hi - lo) * 1.001f;
+    a.lean_c[4] = 2.0f * c24 * q6 * q6;
+    a.lean_c[5] = c24 * q6;
+  }
   a.nbuf = nbuf;
   a.wait_limit = f.wait_limit;
   a.grouped = cl.grouped;
