@@ -179,7 +179,9 @@ md_status md_kernel_time(const md_ctx* ctx, int kernel, double* total_ms, long l
  * launches of the kernel the steps use (the fused force + Gear kernel in the
  * precision form, on a scratch copy of the Gear state) on the current state
  * for each candidate block size, staged-atom cap per segment and row-load
- * scheme, keeps the fastest and rebuilds the list with it.  Forces do not
+ * scheme, keeps the fastest and rebuilds the list with it.  The caps tried
+ * are 1152, 1536 and, per block size and scheme, the largest at which the
+ * kernel keeps the blocks per SM that its registers allow.  Forces do not
  * depend on the choice (same pairs, same order).  No-op for the other
  * kernels.  Call after md_begin, best on a thermalised state: on a perfect
  * lattice every row has the same length, which favours other tilings. */
