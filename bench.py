@@ -942,6 +942,43 @@ def run_case(args) -> int:
         e.close()
         print(json.dumps({"case": args.case, "atoms": 32768, "md_steps": args.steps,
                           "ms_per_step": ms / max(args.steps, 1)}))
+    if args.case == "batch":
+        # the batched form's ensemble (256 replicas, 1,868,538 atoms), tuned
+        # after 300 steps, then --steps MD steps inside a profiler range with
+        # the step split into its kernels and the list builds and skin trips
+        import ctypes
+        from moleculardynamics_gb300 import lattice as lat
+        pos, vel, natoms, boxes, _ = lat.make_batch(256, 256, 32000, 60.0, 150.0, seed=4096)
+        cfg = eng.make_config(dt=2.0, lj_rs=2.8 * SIGMA, lj_rcut=2.5 * SIGMA, periodic=1,
+                              precision=eng.PREC_MIXED, species=eng.SPECIES_ARGON)
+        b = eng.Batch(cfg, natoms, boxes)
+        b.upload(pos, vel)
+        b.begin(0.0)
+        b.step(200)
+        tune = b.autotune(2)
+        b.step(100)
+        b.synchronize()
+        s0 = b.stats()
+        drv = ctypes.CDLL("libcuda.so.1")
+        drv.cuProfilerStart()
+        b.set_timing(True)
+        b.step(args.steps)
+        b.synchronize()
+        drv.cuProfilerStop()
+        s1 = b.stats()
+        split = {}
+        for name, k in (("step", eng.KERNEL_STEP), ("fused", eng.KERNEL_FUSED),
+                        ("fused_correct", eng.KERNEL_FUSED_CORRECT), ("predict", eng.KERNEL_PREDICT),
+                        ("list", eng.KERNEL_LIST)):
+            ms, cnt = b.kernel_time(k)
+            split[name] = {"ms": ms, "launches": cnt}
+        b.close()
+        print(json.dumps({"case": "batch", "atoms": int(natoms.sum()), "md_steps": args.steps,
+                          "ms_per_step": split["step"]["ms"] / max(args.steps, 1),
+                          "kernels": split, "autotune": tune,
+                          "list_builds": s1["list_builds"] - s0["list_builds"],
+                          "skin_trips": s1["list_trips"] - s0["list_trips"],
+                          "segments": s1["cluster_segments"], "max_staged": s1["cluster_max_staged"]}))
     if args.case == "sur32k":
         # a briefly trained surrogate (two FP64 snapshots, 300 Adam steps; the
         # model kind of --sur-kind) driving the 32,768-atom lattice: --steps MD
@@ -1009,12 +1046,13 @@ def main():
     ap.add_argument("--sur-fp64-steps", type=int, default=400)
     ap.add_argument("--sur-sweep", action="store_true",
                     help="also train the head at H = 32, 128 and both kinds on less data")
-    ap.add_argument("--case", default=None, choices=["bo32k", "bo32k64", "sur32k"],
+    ap.add_argument("--case", default=None, choices=["bo32k", "bo32k64", "sur32k", "batch"],
                     help="a profiling case instead of the benchmark: bo32k runs the "
                          "32,768-atom bond-order lattice in the precision form for --steps "
                          "MD steps and prints its step time (bo32k64: the plain FP64 path); "
                          "sur32k the same lattice driven by a briefly trained surrogate, the "
-                         "steps inside a profiler range")
+                         "steps inside a profiler range; batch the batched form's 256-replica "
+                         "ensemble, the steps inside a profiler range")
     ap.add_argument("--sur-kind", type=int, default=1, choices=[0, 1],
                     help="sur32k: 0 the energy network, 1 the direct-force head (H = 64)")
     args = ap.parse_args()
